@@ -1,0 +1,476 @@
+// Device side of the method-of-lines hot path: problem view, tap selection,
+// boundary rows, derivative terms and the register-machine interpreter of the
+// pointwise programs.  Templated on the state type T (double, or float for the
+// Float32-state variant).
+//
+// GB300 note: sm_103a executes FP64 at 1/64 of its FP32 rate, so every kernel in
+// this library is bound by the FP64 pipe long before HBM.  Integer work (tap
+// selection, interpreter dispatch, index wrapping) issues on other pipes and is
+// effectively free next to one warp-wide DFMA; the design therefore spends
+// integer instructions to save FP64 ones (host-hoisted coordinate terms, shared
+// reciprocals in WENO, Markstein division by 3).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "molgpu.h"
+
+namespace mol {
+
+template <class T>
+struct DevBC {
+    int kind, prog, op, pad;
+    T a, b, g;
+};
+
+// Everything a kernel needs to evaluate f(du, u, p, t) of one problem instance.
+// Passed by value (kernel parameter space / constant bank); arrays live in HBM.
+template <class T>
+struct DevProb {
+    int ndim, nfields, nparams, cell_prog;
+    int n[3];        // grid points per dim (1 for unused dims)
+    int lo[3], up[3];
+    int ni[3];       // interior extents
+    int permask[MOL_MAX_FIELDS];  // bit d set: field periodic along d
+    long long ncell; // interior cells per field
+    const T* coords[3];
+    const DevBC<T>* bc;           // [field][dim][side]
+    const mol_op1d* ops;
+    const T* w;
+    const mol_term* terms;
+    const mol_instr* code;
+    const int* progs;             // (start, len) pairs
+    const T* consts;
+    const T* aux;
+    const long long* aux_off;     // naux + 1 offsets into aux
+    int naux;
+};
+
+__device__ __forceinline__ int wrap_periodic(int i, int l) {
+    // _wrapperiodic (interface_boundary.jl:33-42): u[1] == u[l]
+    return i <= 1 ? i + (l - 1) : (i > l ? i - (l - 1) : i);
+}
+
+template <class T>
+__device__ __forceinline__ long long flat_interior(const DevProb<T>& P, int i0, int i1, int i2) {
+    return (long long)(i0 - 1 - P.lo[0]) +
+           (long long)P.ni[0] * ((long long)(i1 - 1 - P.lo[1]) + (long long)P.ni[1] * (long long)(i2 - 1 - P.lo[2]));
+}
+
+// Interior-or-zero load (no boundary row evaluation): used inside boundary rows.
+template <class T>
+__device__ __forceinline__ T load_interior(const DevProb<T>& P, const T* u, int f, const int* I) {
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) in &= (I[d] > P.lo[d]) & (I[d] <= P.n[d] - P.up[d]);
+    if (!in) return T(0);
+    return u[(long long)f * P.ncell + flat_interior(P, I[0], I[1], I[2])];
+}
+
+// Small straight-line program used by boundary rows (a, b, g may depend on t, x, p).
+template <class T>
+__device__ T run_bc_prog(const DevProb<T>& P, int prog, int out_index, const int* I, T t, const T* p) {
+    T r[16];
+    const int start = P.progs[2 * prog], len = P.progs[2 * prog + 1];
+    T res = T(0);
+    for (int pc = start; pc < start + len; ++pc) {
+        const mol_instr in = P.code[pc];
+        const int dst = in.dst & 15;
+        switch (in.op) {
+            case MOL_OP_CONST: r[dst] = P.consts[in.imm]; break;
+            case MOL_OP_PARAM: r[dst] = p[in.imm]; break;
+            case MOL_OP_COORD: r[dst] = P.coords[in.imm][I[in.imm] - 1]; break;
+            case MOL_OP_TIME: r[dst] = t; break;
+            case MOL_OP_ADD: r[dst] = r[in.a & 15] + r[in.b & 15]; break;
+            case MOL_OP_SUB: r[dst] = r[in.a & 15] - r[in.b & 15]; break;
+            case MOL_OP_MUL: r[dst] = r[in.a & 15] * r[in.b & 15]; break;
+            case MOL_OP_DIV: r[dst] = r[in.a & 15] / r[in.b & 15]; break;
+            case MOL_OP_NEG: r[dst] = -r[in.a & 15]; break;
+            case MOL_OP_OUT: if (in.imm == out_index) res = r[in.a & 15]; break;
+            default: break;
+        }
+    }
+    return res;
+}
+
+// Value of field f at full-grid point I (1-based), resolving boundary rows:
+// unknowns are read directly, a point outside the interior in exactly one
+// dimension is an observed boundary value (Robin/Neumann/Dirichlet row,
+// generate_bc_eqs.jl:238-328, solved for the boundary point), a point outside
+// in two or more dimensions is a corner row (~ 0, generate_bc_eqs.jl:396-459).
+template <class T>
+__device__ __noinline__ T bc_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t, const T* p);
+
+template <class T>
+__device__ __forceinline__ T load_pt(const DevProb<T>& P, const T* u, int f, int i0, int i1, int i2, T t, const T* p) {
+    int I[3] = {i0, i1, i2};
+    int nout = 0, dout = 0, side = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (I[d] <= P.lo[d]) {
+            if ((P.permask[f] >> d) & 1) { I[d] = wrap_periodic(I[d], P.n[d]); continue; }
+            ++nout; dout = d; side = 0;
+        } else if (I[d] > P.n[d] - P.up[d]) {
+            ++nout; dout = d; side = 1;
+        }
+    }
+    if (nout == 0) return u[(long long)f * P.ncell + flat_interior(P, I[0], I[1], I[2])];
+    if (nout > 1) return T(0);
+    return bc_value(P, u, f, I, dout, side, t, p);
+}
+
+template <class T>
+__device__ __noinline__ T bc_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t, const T* p) {
+    // boundary rows exist only on the boundary points themselves
+    if ((side == 0 && I[dout] != 1) || (side == 1 && I[dout] != P.n[dout])) return T(0);
+    const DevBC<T> B = P.bc[(f * 3 + dout) * 2 + side];
+    if (B.kind != MOL_BC_ROBIN) return T(0);
+    T a = B.a, b = B.b, g = B.g;
+    if (B.prog >= 0) {
+        a = run_bc_prog(P, B.prog, 0, I, t, p);
+        b = run_bc_prog(P, B.prog, 1, I, t, p);
+        g = run_bc_prog(P, B.prog, 2, I, t, p);
+    }
+    if (b == T(0)) return g / a;
+    const mol_op1d op = P.ops[B.op];
+    const int n = P.n[dout];
+    const T* w = side == 0 ? P.w + op.w_lo : P.w + op.w_hi;  // centered table at the last point
+    const int first = side == 0 ? 1 : n - op.bLhi + 1;
+    const int cnt = side == 0 ? op.bLlo : op.bLhi;
+    const int kb = side == 0 ? 0 : cnt - 1;
+    T acc = T(0);
+    bool started = false;
+    int J[3] = {I[0], I[1], I[2]};
+    for (int k = 0; k < cnt; ++k) {
+        if (k == kb) continue;
+        J[dout] = first + k;
+        const T term = w[k] * load_interior(P, u, f, J);
+        acc = started ? acc + term : term;
+        started = true;
+    }
+    return (g - b * acc) / (a + b * w[kb]);
+}
+
+struct TapSel {
+    long long woff;
+    int first, cnt;
+    bool wrap;
+};
+
+// Tap selection of one 1-D operator at position i of a line of `len` points.
+__device__ __forceinline__ TapSel select_taps(const mol_op1d& op, int i, int len, bool per) {
+    TapSel s;
+    if (!per && i <= op.nlo) {
+        s.woff = op.w_lo + (long long)(i - 1) * op.bLlo; s.first = 1; s.cnt = op.bLlo; s.wrap = false;
+    } else if (!per && i > len - op.nhi) {
+        s.woff = op.w_hi + (long long)(len - i - op.hi_base) * op.bLhi; s.first = len - op.bLhi + 1;
+        s.cnt = op.bLhi; s.wrap = false;
+    } else {
+        s.woff = op.w_int; s.first = i + op.omin; s.cnt = op.L; s.wrap = per;
+    }
+    return s;
+}
+
+// sum_k w_k u[tap_k] along dimension d (centered_difference.jl:5-30, upwind_difference.jl:1-28).
+template <class T>
+__device__ T apply_op(const DevProb<T>& P, const mol_op1d& op, const T* u, int f, int d, const int* I,
+                      T t, const T* p) {
+    const bool per = (P.permask[f] >> d) & 1;
+    const TapSel s = select_taps(op, I[d], P.n[d], per);
+    int J[3] = {I[0], I[1], I[2]};
+    T acc = T(0);
+    for (int k = 0; k < s.cnt; ++k) {
+        int tp = s.first + k;
+        if (s.wrap) tp = wrap_periodic(tp, P.n[d]);
+        J[d] = tp;
+        const T v = load_pt(P, u, f, J[0], J[1], J[2], t, p);
+        acc = k == 0 ? P.w[s.woff] * v : fma(P.w[s.woff + k], v, acc);
+    }
+    return acc;
+}
+
+// Mixed derivative: tensor product of two first-derivative centered stencils
+// (2nd_order_mixed_deriv.jl:5-22), both wrapped.
+template <class T>
+__device__ T apply_mixed(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, T t, const T* p) {
+    const int f = tm.field, d1 = tm.dim, d2 = tm.dim2;
+    const mol_op1d o1 = P.ops[tm.op], o2 = P.ops[tm.op2];
+    const bool p1 = (P.permask[f] >> d1) & 1, p2 = (P.permask[f] >> d2) & 1;
+    const TapSel s1 = select_taps(o1, I[d1], P.n[d1], p1);
+    const TapSel s2 = select_taps(o2, I[d2], P.n[d2], p2);
+    int J[3] = {I[0], I[1], I[2]};
+    T acc = T(0);
+    bool started = false;
+    for (int a = 0; a < s1.cnt; ++a) {
+        const T wa = P.w[s1.woff + a];
+        if (wa == T(0)) continue;  // zero taps drop out of the symbolic sum
+        int ta = s1.first + a;
+        if (s1.wrap) ta = wrap_periodic(ta, P.n[d1]);
+        J[d1] = ta;
+        for (int b = 0; b < s2.cnt; ++b) {
+            const T wb = P.w[s2.woff + b];
+            if (wb == T(0)) continue;
+            int tb = s2.first + b;
+            if (s2.wrap) tb = wrap_periodic(tb, P.n[d2]);
+            J[d2] = tb;
+            const T v = load_pt(P, u, f, J[0], J[1], J[2], t, p);
+            const T ww = wa * wb;
+            acc = started ? fma(ww, v, acc) : ww * v;
+            started = true;
+        }
+    }
+    return acc;
+}
+
+// Jiang-Shu WENO5 node derivative (WENO.jl:6-57), periodic taps i-2..i+2.
+// Algebraically identical to the reference; the six nonlinear weights share
+// one reciprocal of each (eps + beta)^2 and one reciprocal of each weight sum,
+// which replaces 12 FP64 divisions by 5.
+template <class T>
+__device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps, T inv_dx) {
+    const T c13_12 = T(13) / T(12);
+    const T a1 = u0 - T(2) * up1 + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
+    const T a2 = um1 - T(2) * u0 + up1, b2 = um1 - up1;
+    const T a3 = um2 - T(2) * um1 + u0, b3 = um2 - T(4) * um1 + T(3) * u0;
+    const T beta1 = fma(c13_12 * a1, a1, T(0.25) * (b1 * b1));
+    const T beta2 = fma(c13_12 * a2, a2, T(0.25) * (b2 * b2));
+    const T beta3 = fma(c13_12 * a3, a3, T(0.25) * (b3 * b3));
+    const T e1 = eps + beta1, e2 = eps + beta2, e3 = eps + beta3;
+    const T q1 = T(1) / (e1 * e1), q2 = T(1) / (e2 * e2), q3 = T(1) / (e3 * e3);
+    // minus side: gamma = (1/10, 3/5, 3/10); plus side: gamma = (3/10, 3/5, 1/10)
+    const T wm1 = T(0.1) * q1, wm2 = T(0.6) * q2, wm3 = T(0.3) * q3;
+    const T wp1 = T(0.3) * q1, wp2 = T(0.6) * q2, wp3 = T(0.1) * q3;
+    const T sixth = T(1) / T(6);
+    const T hm1 = (T(11) * u0 - T(7) * up1 + T(2) * up2) * sixth;
+    const T hm2 = (T(5) * u0 - up1 + T(2) * um1) * sixth;
+    const T hm3 = (T(2) * u0 + T(5) * um1 - um2) * sixth;
+    const T hp1 = (T(2) * u0 + T(5) * up1 - up2) * sixth;
+    const T hp2 = (T(5) * u0 + T(2) * up1 - um1) * sixth;
+    const T hp3 = (T(11) * u0 - T(7) * um1 + T(2) * um2) * sixth;
+    const T hp = fma(wp1, hp1, fma(wp2, hp2, wp3 * hp3)) / (wp1 + wp2 + wp3);
+    const T hm = fma(wm1, hm1, fma(wm2, hm2, wm3 * hm3)) / (wm1 + wm2 + wm3);
+    return (hp - hm) * inv_dx;
+}
+
+template <class T>
+__device__ T apply_weno(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, T t, const T* p) {
+    const int f = tm.field, d = tm.dim, n = P.n[d];
+    int J[3] = {I[0], I[1], I[2]};
+    T v[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        J[d] = wrap_periodic(I[d] - 2 + k, n);
+        v[k] = load_pt(P, u, f, J[0], J[1], J[2], t, p);
+    }
+    return weno5_point<T>(v[0], v[1], v[2], v[3], v[4], T(tm.eps), T(1.0 / tm.dx));
+}
+
+template <class T>
+__device__ __forceinline__ T apply_fn(int fn, T x) {
+    switch (fn) {
+        case MOL_FN_SIN: return sin(x);
+        case MOL_FN_COS: return cos(x);
+        case MOL_FN_TAN: return tan(x);
+        case MOL_FN_EXP: return exp(x);
+        case MOL_FN_LOG: return log(x);
+        case MOL_FN_SQRT: return sqrt(x);
+        case MOL_FN_ABS: return fabs(x);
+        case MOL_FN_TANH: return tanh(x);
+        case MOL_FN_SINH: return sinh(x);
+        case MOL_FN_COSH: return cosh(x);
+        case MOL_FN_ATAN: return atan(x);
+        default: return x;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ T apply_cmp(int c, T a, T b) {
+    bool r;
+    switch (c) {
+        case MOL_CMP_LE: r = a <= b; break;
+        case MOL_CMP_LT: r = a < b; break;
+        case MOL_CMP_GE: r = a >= b; break;
+        case MOL_CMP_GT: r = a > b; break;
+        default: r = a == b; break;
+    }
+    return r ? T(1) : T(0);
+}
+
+template <class T>
+__device__ __forceinline__ T powi(T x, int n) {
+    if (n == 2) return x * x;
+    if (n == 3) return x * x * x;
+    if (n == 1) return x;
+    if (n == 0) return T(1);
+    if (n == -1) return T(1) / x;
+    if (n == -2) return T(1) / (x * x);
+    return pow(x, T(n));
+}
+
+// Face value a(x_{I+1/2}, u~) * (D_inner u)_{I+1/2} of a nonlinear Laplacian term
+// (nonlinear_laplacian.jl:28-103): u~ and x~ by the half-offset interpolation
+// table, the inner derivative by the half-offset first-derivative table.
+template <class T>
+__device__ __noinline__ T nonlinlap_face(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, int Ih,
+                            T t, const T* p) {
+    const int f = tm.field, d = tm.dim, n = P.n[d];
+    const bool per = (P.permask[f] >> d) & 1;
+    int J[3] = {I[0], I[1], I[2]};
+    // inner derivative at the half point
+    const mol_op1d oin = P.ops[tm.op2];
+    const TapSel si = select_taps(oin, Ih, n, per);
+    T du = T(0);
+    for (int k = 0; k < si.cnt; ++k) {
+        int tp = si.first + k;
+        if (per) tp = wrap_periodic(tp, n);
+        J[d] = tp;
+        const T v = load_pt(P, u, f, J[0], J[1], J[2], t, p);
+        du = k == 0 ? P.w[si.woff] * v : fma(P.w[si.woff + k], v, du);
+    }
+    if (tm.prog < 0) return du;
+    // face program: a(x~, u~, p)
+    const mol_op1d oip = P.ops[tm.op3];
+    const TapSel sp = select_taps(oip, Ih, n, per);
+    T r[MOL_MAX_REGS];
+    T a = T(1);
+    const int start = P.progs[2 * tm.prog], len = P.progs[2 * tm.prog + 1];
+    for (int pc = start; pc < start + len; ++pc) {
+        const mol_instr in = P.code[pc];
+        T& R = r[in.dst];
+        switch (in.op) {
+            case MOL_OP_CONST: R = P.consts[in.imm]; break;
+            case MOL_OP_PARAM: R = p[in.imm]; break;
+            case MOL_OP_TIME: R = t; break;
+            case MOL_OP_FIELD: {
+                T acc = T(0);
+                for (int k = 0; k < sp.cnt; ++k) {
+                    int tp = sp.first + k;
+                    if (per) tp = wrap_periodic(tp, n);
+                    J[d] = tp;
+                    const T v = load_pt(P, u, in.imm, J[0], J[1], J[2], t, p);
+                    acc = k == 0 ? P.w[sp.woff] * v : fma(P.w[sp.woff + k], v, acc);
+                }
+                R = acc;
+                break;
+            }
+            case MOL_OP_AUX: {
+                // face array: extent n[d]+1 along d (index Ih), full-grid extents elsewhere
+                const int ax = tm.aux0 + in.imm;
+                long long e0 = P.n[0] + (d == 0), e1 = P.n[1] + (d == 1);
+                long long j0 = d == 0 ? Ih : I[0] - 1, j1 = d == 1 ? Ih : I[1] - 1, j2 = d == 2 ? Ih : I[2] - 1;
+                R = P.aux[P.aux_off[ax] + j0 + e0 * (j1 + e1 * j2)];
+                break;
+            }
+            case MOL_OP_ADD: R = r[in.a] + r[in.b]; break;
+            case MOL_OP_SUB: R = r[in.a] - r[in.b]; break;
+            case MOL_OP_MUL: R = r[in.a] * r[in.b]; break;
+            case MOL_OP_DIV: R = r[in.a] / r[in.b]; break;
+            case MOL_OP_NEG: R = -r[in.a]; break;
+            case MOL_OP_POWI: R = powi(r[in.a], in.imm); break;
+            case MOL_OP_POW: R = pow(r[in.a], r[in.b]); break;
+            case MOL_OP_FN: R = apply_fn(in.imm, r[in.a]); break;
+            case MOL_OP_CMP: R = apply_cmp(in.imm, r[in.a], r[in.b]); break;
+            case MOL_OP_IFELSE: R = r[in.a] != T(0) ? r[in.b] : r[in.c]; break;
+            case MOL_OP_OUT: a = r[in.a]; break;
+            default: break;
+        }
+    }
+    return a * du;
+}
+
+template <class T>
+__device__ T apply_nonlinlap(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, T t, const T* p) {
+    const int f = tm.field, d = tm.dim, n = P.n[d];
+    const bool per = (P.permask[f] >> d) & 1;
+    const mol_op1d oo = P.ops[tm.op];
+    // outer half-offset stencil at II - 1 on a line clipped to n - 1 points; taps are half points
+    const TapSel so = select_taps(oo, I[d] - 1, n - 1, per);
+    T acc = T(0);
+    bool started = false;
+    for (int k = 0; k < so.cnt; ++k) {
+        const T wo = P.w[so.woff + k];
+        if (wo == T(0)) continue;  // zero outer weights drop out of the symbolic sum
+        const int Ih = so.first + k;  // not wrapped: the face program wraps its own taps
+        const T F = nonlinlap_face(P, tm, u, I, Ih, t, p);
+        acc = started ? fma(wo, F, acc) : wo * F;
+        started = true;
+    }
+    return acc;
+}
+
+template <class T>
+__device__ __noinline__ T eval_term(const DevProb<T>& P, int k, const T* u, const int* I, T t, const T* p) {
+    const mol_term tm = P.terms[k];
+    switch (tm.kind) {
+        case MOL_TERM_LINEAR: return apply_op(P, P.ops[tm.op], u, tm.field, tm.dim, I, t, p);
+        case MOL_TERM_MIXED: return apply_mixed(P, tm, u, I, t, p);
+        case MOL_TERM_WENO: return apply_weno(P, tm, u, I, t, p);
+        case MOL_TERM_NONLINLAP: return apply_nonlinlap(P, tm, u, I, t, p);
+        default: return T(0);
+    }
+}
+
+// Full-grid index of interior cell `c` (flat, first dimension fastest).
+template <class T>
+__device__ __forceinline__ void cell_index(const DevProb<T>& P, long long c, int* I) {
+    const long long c0 = c % P.ni[0];
+    const long long r = c / P.ni[0];
+    const long long c1 = r % P.ni[1];
+    const long long c2 = r / P.ni[1];
+    I[0] = (int)c0 + 1 + P.lo[0];
+    I[1] = (int)c1 + 1 + P.lo[1];
+    I[2] = (int)c2 + 1 + P.lo[2];
+}
+
+// The cell program: one OUT per field.  `out` receives du for every field.
+template <class T>
+__device__ __noinline__ void eval_cell(const DevProb<T>& P, const T* u, long long c, const int* I, T t, const T* p, T* out) {
+    T r[MOL_MAX_REGS];
+    const int start = P.progs[2 * P.cell_prog], len = P.progs[2 * P.cell_prog + 1];
+    for (int pc = start; pc < start + len; ++pc) {
+        const mol_instr in = P.code[pc];
+        T& R = r[in.dst];
+        switch (in.op) {
+            case MOL_OP_CONST: R = P.consts[in.imm]; break;
+            case MOL_OP_PARAM: R = p[in.imm]; break;
+            case MOL_OP_FIELD: R = u[(long long)in.imm * P.ncell + c]; break;
+            case MOL_OP_AUX: R = P.aux[P.aux_off[in.imm] + c]; break;
+            case MOL_OP_COORD: R = P.coords[in.imm][I[in.imm] - 1]; break;
+            case MOL_OP_TIME: R = t; break;
+            case MOL_OP_TERM: R = eval_term(P, in.imm, u, I, t, p); break;
+            case MOL_OP_UPWIND: {
+                // rhs term kappa*Dx^d(u) is (-kappa)*Dx^d(u) on the cardinalised lhs; the reference
+                // takes the backward (windmap[2]) stencil when that coefficient is > 0.
+                const T kap = r[in.a];
+                R = kap < T(0) ? kap * eval_term(P, in.b, u, I, t, p) : kap * eval_term(P, in.c, u, I, t, p);
+                break;
+            }
+            case MOL_OP_ADD: R = r[in.a] + r[in.b]; break;
+            case MOL_OP_SUB: R = r[in.a] - r[in.b]; break;
+            case MOL_OP_MUL: R = r[in.a] * r[in.b]; break;
+            case MOL_OP_DIV: R = r[in.a] / r[in.b]; break;
+            case MOL_OP_NEG: R = -r[in.a]; break;
+            case MOL_OP_POWI: R = powi(r[in.a], in.imm); break;
+            case MOL_OP_POW: R = pow(r[in.a], r[in.b]); break;
+            case MOL_OP_FN: R = apply_fn(in.imm, r[in.a]); break;
+            case MOL_OP_CMP: R = apply_cmp(in.imm, r[in.a], r[in.b]); break;
+            case MOL_OP_IFELSE: R = r[in.a] != T(0) ? r[in.b] : r[in.c]; break;
+            case MOL_OP_OUT: out[in.imm] = r[in.a]; break;
+            default: break;
+        }
+    }
+}
+
+// Correctly rounded x/3 with one multiply and two FMAs (Markstein's theorem:
+// with c = RN(1/3) and q0 within an ulp of x/3, q0 + (x - 3 q0) c rounds to
+// RN(x/3)); replaces the FP64 division in SSPRK33's last stage.
+__device__ __forceinline__ double div3(double x) {
+    const double c = 0.33333333333333331483;  // RN(1/3)
+    const double q0 = x * c;
+    const double r = fma(-q0, 3.0, x);
+    return fma(r, c, q0);
+}
+__device__ __forceinline__ float div3(float x) { return x / 3.0f; }
+
+}  // namespace mol

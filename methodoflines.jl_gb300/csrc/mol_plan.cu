@@ -1,0 +1,1028 @@
+// libmolgpu: plan creation, f!(du,u,p,t), fixed-step SSPRK33 and adaptive Tsit5.
+//
+// Replaces, at runtime, the ModelingToolkit-compiled ODEFunction that
+// MethodOfLines.jl builds in src/MOL_discretization.jl:171-201 and the
+// OrdinaryDiffEq steppers that call it (benchmark/weno/suite.jl:283-295).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mol_device.cuh"
+#include "mol_plan.h"
+
+namespace mol {
+
+std::atomic<long long> g_launches{0};
+
+int set_err(mol_plan* plan, int code, const std::string& msg) {
+    if (plan) plan->err = msg;
+    return code;
+}
+
+int cuda_check(mol_plan* plan, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return MOL_OK;
+    cudaGetLastError();
+    return set_err(plan, e == cudaErrorMemoryAllocation ? MOL_ERR_OOM : MOL_ERR_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int plan_alloc(mol_plan* plan, void** ptr, size_t bytes) {
+    *ptr = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) return cuda_check(plan, e, "cudaMalloc");
+    plan->allocs.push_back(*ptr);
+    return MOL_OK;
+}
+
+int plan_grid(const mol_plan* plan) { return plan->nblocks; }
+
+template <class T>
+int ensure_ws(mol_plan* plan, int count) {
+    T** ws = workspace<T>(plan);
+    for (int i = 0; i < count; ++i) {
+        if (!ws[i]) {
+            void* p;
+            int st = plan_alloc(plan, &p, sizeof(T) * (size_t)plan->nunk);
+            if (st) return st;
+            ws[i] = (T*)p;
+        }
+    }
+    return MOL_OK;
+}
+template int ensure_ws<double>(mol_plan*, int);
+template int ensure_ws<float>(mol_plan*, int);
+
+// allocate one workspace slot only (host staging buffers)
+template <class T>
+static int ensure_slot(mol_plan* plan, int slot) {
+    T** ws = workspace<T>(plan);
+    if (ws[slot]) return MOL_OK;
+    void* p;
+    int st = plan_alloc(plan, &p, sizeof(T) * (size_t)plan->nunk);
+    if (st) return st;
+    ws[slot] = (T*)p;
+    return MOL_OK;
+}
+
+constexpr int kThreads = 256;
+
+// ----------------------------------------------------------------------------
+// kernels
+// ----------------------------------------------------------------------------
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_rhs(DevProb<T> P, const T* __restrict__ u, T* __restrict__ du,
+                                                  const T* __restrict__ p, double t) {
+    T out[MOL_MAX_FIELDS];
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        eval_cell(P, u, c, I, T(t), p, out);
+        for (int f = 0; f < P.nfields; ++f) du[(long long)f * P.ncell + c] = out[f];
+    }
+}
+
+// One SSPRK33 stage with OrdinaryDiffEq's evaluation order fused as the epilogue:
+//   stage 1: u1 = u0 + dt*f(u0, t)
+//   stage 2: u2 = (3*u0 + u1 + dt*f(u1, t+dt)) / 4
+//   stage 3: u  = (u0 + 2*u2 + 2*dt*f(u2, t+dt/2)) / 3,  then t += dt
+template <class T, int STAGE>
+__global__ void __launch_bounds__(kThreads) k_ssprk(DevProb<T> P, const T* __restrict__ uin, const T* u0,
+                                                    T* uout, const T* __restrict__ p, SolverState* S, double dt) {
+    const double t0 = S->t;
+    const double ts = STAGE == 1 ? t0 : (STAGE == 2 ? t0 + dt : t0 + dt / 2);
+    const T dtT = T(dt);
+    const T dt2 = T(2 * dt);
+    T out[MOL_MAX_FIELDS];
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        eval_cell(P, uin, c, I, T(ts), p, out);
+        for (int f = 0; f < P.nfields; ++f) {
+            const long long g = (long long)f * P.ncell + c;
+            const T k = out[f];
+            T r;
+            if (STAGE == 1) {
+                r = u0[g] + dtT * k;
+            } else if (STAGE == 2) {
+                const T s = T(3) * u0[g] + uin[g];
+                r = (s + dtT * k) * T(0.25);
+            } else {
+                const T s = u0[g] + T(2) * uin[g];
+                r = div3(s + dt2 * k);
+            }
+            uout[g] = r;
+        }
+    }
+    if (STAGE == 3) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const unsigned v = atomicAdd(&S->blocks_done, 1u);
+            if (v == gridDim.x - 1) {
+                S->t = t0 + dt;
+                S->blocks_done = 0;
+                __threadfence();
+            }
+        }
+    }
+}
+
+// Tsitouras (2011) 5(4) pair, the tableau OrdinaryDiffEq's Tsit5 implements.
+__constant__ double c_tsit_c[8] = {0.0, 0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0};
+
+// Stage i (2..7): k_i = f(y_i, t + c_i dt); epilogue writes y_{i+1} = u + sum_j (dt a_{i+1,j}) k_j.
+// Stage 7 instead accumulates the scaled error sum_j (dt btilde_j) k_j and the last
+// block runs the PI controller.
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_tsit_stage(DevProb<T> P, int stage, const T* __restrict__ y,
+                                                         T* ynext, const T* __restrict__ u, T* const* k,
+                                                         const T* __restrict__ p, SolverState* S,
+                                                         double* partials) {
+    if (S->done) return;
+    const double t = S->t + c_tsit_c[stage] * S->dt;
+    T out[MOL_MAX_FIELDS];
+    double errsq = 0.0;
+    const double abstol = S->abstol, reltol = S->reltol;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        eval_cell(P, y, c, I, T(t), p, out);
+        for (int f = 0; f < P.nfields; ++f) {
+            const long long g = (long long)f * P.ncell + c;
+            k[stage - 1][g] = out[f];
+            if (stage < 7) {
+                T acc = u[g];
+                for (int j = 1; j <= stage; ++j) {
+                    const T kj = j == stage ? out[f] : k[j - 1][g];
+                    acc = fma(T(S->dta[stage + 1][j]), kj, acc);
+                }
+                ynext[g] = acc;
+            } else {
+                T e = T(0);
+                for (int j = 1; j <= 7; ++j) {
+                    const T kj = j == 7 ? out[f] : k[j - 1][g];
+                    e = fma(T(S->dtb[j]), kj, e);
+                }
+                const double un = (double)y[g];
+                const double uo = (double)u[g];
+                const double sc = abstol + fmax(fabs(uo), fabs(un)) * reltol;
+                const double r = (double)e / sc;
+                errsq = fma(r, r, errsq);
+            }
+        }
+    }
+    if (stage < 7) return;
+    // deterministic block reduction of the error sum
+    __shared__ double red[kThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = errsq;
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) s += red[w];
+        partials[blockIdx.x] = s;
+        __threadfence();
+        const unsigned v = atomicAdd(&S->blocks_done, 1u);
+        last = (v == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double s = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[b];
+    S->blocks_done = 0;
+    const double N = (double)P.ncell * P.nfields;
+    const double EEst = sqrt(s / N);
+    S->EEst = EEst;
+    S->nf += 6;
+    S->iter += 1;
+    if (!isfinite(EEst)) {
+        S->status = MOL_ERR_NONFINITE;
+        S->done = 1;
+        S->accepted = 0;
+        return;
+    }
+    // PI controller (beta1 = 7/50, beta2 = 2/25, qmin = 1/5, qmax = 10, gamma = 9/10)
+    const double beta1 = 0.14, beta2 = 0.08, qmin = 0.2, qmax = 10.0, gamma = 0.9, qoldinit = 1e-4;
+    const double q11 = pow(EEst, beta1);
+    double dt = S->dt, dtnew;
+    if (EEst <= 1.0) {
+        double q = q11 / pow(S->qold, beta2);
+        q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gamma));
+        S->t = S->t + dt;
+        S->qold = fmax(EEst, qoldinit);
+        dtnew = dt / q;
+        S->naccept += 1;
+        S->accepted = 1;
+        if (S->t >= S->t1) S->done = 1;
+    } else {
+        const double q = fmin(1.0 / qmin, q11 / gamma);
+        dtnew = dt / q;
+        S->nreject += 1;
+        S->accepted = 0;
+    }
+    if (!S->done) {
+        if (S->t + dtnew > S->t1) dtnew = S->t1 - S->t;
+        if (!(dtnew > S->dtmin) && S->t < S->t1) {
+            S->status = MOL_ERR_DTMIN;
+            S->done = 1;
+        }
+        if (S->iter >= S->maxiters) {
+            S->status = MOL_ERR_MAXITERS;
+            S->done = 1;
+        }
+    }
+    S->dt = dtnew;
+    __threadfence();
+}
+
+// Row updates of the controller's dt-scaled tableau; one thread.
+__device__ void tsit_scale(SolverState* S) {
+    const double A[8][8] = {
+        {0}, {0},
+        {0, 0.161},
+        {0, -0.008480655492356989, 0.335480655492357},
+        {0, 2.897153057105493, -6.359448489975075, 4.3622954328695815},
+        {0, 5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525},
+        {0, 5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383},
+        {0, 0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081,
+         2.324710524099774}};
+    const double B[8] = {0, -0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+                         -0.1447110071732629, 0.5823571654525552, -0.45808210592918697, 0.015151515151515152};
+    const double dt = S->dt;
+    for (int i = 0; i < 8; ++i)
+        for (int j = 0; j < 8; ++j) S->dta[i][j] = dt * A[i][j];
+    for (int j = 0; j < 8; ++j) S->dtb[j] = dt * B[j];
+}
+
+// After the controller: commit an accepted step (u <- y7, k1 <- k7), rescale the
+// tableau for the new dt and form y2 = u + dt a21 k1 for the next attempt.
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_tsit_commit(DevProb<T> P, T* u, T* k1, const T* k7, const T* y7,
+                                                          T* y2, SolverState* S, int first) {
+    const bool acc = !first && S->accepted;
+    const bool done = S->done;
+    __shared__ double a21;
+    if (threadIdx.x == 0) {
+        double dt = S->dt;
+        a21 = dt * 0.161;
+    }
+    __syncthreads();
+    const long long n = P.ncell * P.nfields;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        T uu, kk;
+        if (acc) {
+            uu = y7[g];
+            kk = k7[g];
+            u[g] = uu;
+            k1[g] = kk;
+        } else {
+            uu = u[g];
+            kk = k1[g];
+        }
+        if (!done) y2[g] = fma(T(a21), kk, uu);
+    }
+    // the tableau is rescaled by the last block once everyone has read S->dt
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned v = atomicAdd(&S->blocks_done, 1u);
+        if (v == gridDim.x - 1) {
+            tsit_scale(S);
+            S->blocks_done = 0;
+            __threadfence();
+        }
+    }
+}
+
+// Sums for Hairer's initial step: sums[0] = sum (u/sk)^2, sums[1] = sum (f/sk)^2,
+// sums[2] = sum ((f1-f0)/sk)^2 with sk = abstol + |u0| reltol.
+template <class T>
+__global__ void k_init_norms(long long n, const T* u0, const T* f0, const T* f1, double abstol, double reltol,
+                             double* partials) {
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        const double sk = abstol + fabs((double)u0[g]) * reltol;
+        const double a = (double)u0[g] / sk, b = (double)f0[g] / sk;
+        s0 += a * a;
+        s1 += b * b;
+        if (f1) {
+            const double c = ((double)f1[g] - (double)f0[g]) / sk;
+            s2 += c * c;
+        }
+    }
+    __shared__ double red[3][kThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = s0;
+        red[1][threadIdx.x >> 5] = s1;
+        red[2][threadIdx.x >> 5] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0, c = 0;
+        for (int w = 0; w < kThreads / 32; ++w) { a += red[0][w]; b += red[1][w]; c += red[2][w]; }
+        partials[3 * blockIdx.x + 0] = a;
+        partials[3 * blockIdx.x + 1] = b;
+        partials[3 * blockIdx.x + 2] = c;
+    }
+}
+
+template <class T>
+__global__ void k_axpy(long long n, T* y, const T* x, const T* f, double h) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
+        y[g] = fma(T(h), f[g], x[g]);
+}
+
+__global__ void k_tsit_init_state(SolverState* S, double t0, double t1, double dt, double abstol, double reltol,
+                                  long long maxiters) {
+    S->t = t0;
+    S->t1 = t1;
+    S->dt = dt;
+    S->abstol = abstol;
+    S->reltol = reltol;
+    S->qold = 1e-4;
+    S->EEst = 0;
+    S->dtmin = 1e-14 * fmax(fabs(t0), fabs(t1)) + 1e-300;
+    S->naccept = S->nreject = 0;
+    S->nf = 0;
+    S->iter = 0;
+    S->maxiters = maxiters;
+    S->done = (t0 >= t1);
+    S->status = 0;
+    S->accepted = 0;
+    S->blocks_done = 0;
+    tsit_scale(S);
+}
+
+__global__ void k_set_time(SolverState* S, double t) {
+    S->t = t;
+    S->blocks_done = 0;
+    S->done = 0;
+    S->status = 0;
+}
+
+// ----------------------------------------------------------------------------
+// launch helpers
+// ----------------------------------------------------------------------------
+
+template <class T>
+int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t) {
+    k_rhs<T><<<plan->nblocks, kThreads, 0, plan->stream>>>(prob<T>(plan), u, du, p, t);
+    ++g_launches;
+    return cuda_check(plan, cudaGetLastError(), "k_rhs launch");
+}
+template int launch_rhs<double>(mol_plan*, double*, const double*, const double*, double);
+template int launch_rhs<float>(mol_plan*, float*, const float*, const float*, double);
+
+template <class T>
+int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt) {
+    const DevProb<T>& P = prob<T>(plan);
+    k_ssprk<T, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt);
+    k_ssprk<T, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt);
+    k_ssprk<T, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, u, p, plan->d_state, dt);
+    g_launches += 3;
+    return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
+}
+template int launch_ssprk_step<double>(mol_plan*, double*, double*, double*, const double*, double);
+template int launch_ssprk_step<float>(mol_plan*, float*, float*, float*, const float*, double);
+
+}  // namespace mol
+
+using namespace mol;
+
+// ----------------------------------------------------------------------------
+// descriptor validation
+// ----------------------------------------------------------------------------
+
+static int validate_prog(mol_plan* plan, const mol_problem_desc* d, int prog, int kind, int nregs,
+                         long long aux_need_cell, const mol_term* term) {
+    if (prog < 0 || prog >= d->nprogs) return set_err(plan, MOL_ERR_INVALID, "program index out of range");
+    const int start = d->prog_ranges[2 * prog], len = d->prog_ranges[2 * prog + 1];
+    if (start < 0 || len < 0 || start + len > d->ninstr) return set_err(plan, MOL_ERR_INVALID, "program range out of bounds");
+    for (int pc = start; pc < start + len; ++pc) {
+        const mol_instr& in = d->code[pc];
+        const bool bc_are_terms = in.op == MOL_OP_UPWIND;
+        if (in.dst >= nregs || in.a >= nregs || (!bc_are_terms && (in.b >= nregs || in.c >= nregs)))
+            return set_err(plan, MOL_ERR_INVALID, "register index out of range");
+        switch (in.op) {
+            case MOL_OP_CONST:
+                if (in.imm < 0 || in.imm >= d->nconsts) return set_err(plan, MOL_ERR_INVALID, "constant index");
+                break;
+            case MOL_OP_PARAM:
+                if (in.imm < 0 || in.imm >= d->nparams) return set_err(plan, MOL_ERR_INVALID, "parameter index");
+                break;
+            case MOL_OP_FIELD:
+                if (kind == 2) return set_err(plan, MOL_ERR_INVALID, "FIELD in a boundary program");
+                if (in.imm < 0 || in.imm >= d->nfields) return set_err(plan, MOL_ERR_INVALID, "field index");
+                break;
+            case MOL_OP_AUX: {
+                if (kind == 2) return set_err(plan, MOL_ERR_INVALID, "AUX in a boundary program");
+                const int ax = kind == 1 ? term->aux0 + in.imm : in.imm;
+                if (ax < 0 || ax >= d->naux) return set_err(plan, MOL_ERR_INVALID, "aux index");
+                long long need = aux_need_cell;
+                if (kind == 1) {
+                    need = 1;
+                    for (int q = 0; q < 3; ++q)
+                        need *= (q < d->ndim ? d->npts[q] : 1) + (q == term->dim ? 1 : 0);
+                }
+                if (d->aux_len[ax] < need) return set_err(plan, MOL_ERR_INVALID, "aux array too short");
+                break;
+            }
+            case MOL_OP_COORD:
+                if (kind == 1) return set_err(plan, MOL_ERR_INVALID, "COORD in a face program (hoist it)");
+                if (in.imm < 0 || in.imm >= d->ndim) return set_err(plan, MOL_ERR_INVALID, "coordinate index");
+                break;
+            case MOL_OP_TIME: break;
+            case MOL_OP_TERM:
+                if (kind != 0 || in.imm < 0 || in.imm >= d->nterms) return set_err(plan, MOL_ERR_INVALID, "term index");
+                break;
+            case MOL_OP_UPWIND:
+                if (kind != 0 || in.b >= d->nterms || in.c >= d->nterms) return set_err(plan, MOL_ERR_INVALID, "upwind terms");
+                break;
+            case MOL_OP_ADD: case MOL_OP_SUB: case MOL_OP_MUL: case MOL_OP_DIV: case MOL_OP_NEG:
+            case MOL_OP_POWI: case MOL_OP_POW: case MOL_OP_IFELSE:
+                if (kind == 2 && (in.op == MOL_OP_POWI || in.op == MOL_OP_POW || in.op == MOL_OP_IFELSE))
+                    return set_err(plan, MOL_ERR_UNSUPPORTED, "boundary programs support + - * / only");
+                break;
+            case MOL_OP_FN:
+                if (kind == 2 || in.imm < 0 || in.imm > MOL_FN_ATAN) return set_err(plan, MOL_ERR_INVALID, "function id");
+                break;
+            case MOL_OP_CMP:
+                if (kind == 2 || in.imm < 0 || in.imm > MOL_CMP_EQ) return set_err(plan, MOL_ERR_INVALID, "comparison id");
+                break;
+            case MOL_OP_OUT:
+                if (kind == 0 && (in.imm < 0 || in.imm >= d->nfields)) return set_err(plan, MOL_ERR_INVALID, "output index");
+                if (kind == 2 && (in.imm < 0 || in.imm > 2)) return set_err(plan, MOL_ERR_INVALID, "output index");
+                break;
+            default:
+                return set_err(plan, MOL_ERR_INVALID, "unknown opcode");
+        }
+    }
+    return MOL_OK;
+}
+
+static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
+    if (!d) return set_err(plan, MOL_ERR_INVALID, "null descriptor");
+    if (d->abi_version != MOL_ABI_VERSION) return set_err(plan, MOL_ERR_INVALID, "ABI version mismatch");
+    if (d->ndim < 1 || d->ndim > MOL_MAX_DIMS) return set_err(plan, MOL_ERR_INVALID, "ndim must be 1..3");
+    if (d->nfields < 1 || d->nfields > MOL_MAX_FIELDS) return set_err(plan, MOL_ERR_INVALID, "nfields must be 1..8");
+    if (d->nparams < 0 || (d->nparams > 0 && !d->params)) return set_err(plan, MOL_ERR_INVALID, "parameters");
+    for (int q = 0; q < d->ndim; ++q) {
+        if (d->npts[q] < 1 || d->npts[q] > (1ll << 30)) return set_err(plan, MOL_ERR_INVALID, "npts out of range");
+        if (d->lower[q] < 0 || d->upper[q] < 0 || d->npts[q] - d->lower[q] - d->upper[q] < 1)
+            return set_err(plan, MOL_ERR_INVALID, "empty interior");
+        if (!d->coords[q]) return set_err(plan, MOL_ERR_INVALID, "missing coordinates");
+    }
+    if (d->nops < 0 || (d->nops && !d->ops)) return set_err(plan, MOL_ERR_INVALID, "ops");
+    for (int i = 0; i < d->nops; ++i) {
+        const mol_op1d& o = d->ops[i];
+        if (o.L < 0 || o.nlo < 0 || o.nhi < 0 || o.bLlo < 0 || o.bLhi < 0 || o.hi_base < 0 || o.hi_base > 1)
+            return set_err(plan, MOL_ERR_INVALID, "operator sizes");
+        if (o.w_int < 0 || o.w_int + o.L > d->nweights || o.w_lo < 0 ||
+            o.w_lo + (long long)o.nlo * o.bLlo > d->nweights || o.w_hi < 0 ||
+            o.w_hi + (long long)o.nhi * o.bLhi > d->nweights)
+            return set_err(plan, MOL_ERR_INVALID, "operator weights out of the pool");
+    }
+    if (d->nterms < 0 || (d->nterms && !d->terms)) return set_err(plan, MOL_ERR_INVALID, "terms");
+    for (int k = 0; k < d->nterms; ++k) {
+        const mol_term& t = d->terms[k];
+        if (t.field < 0 || t.field >= d->nfields || t.dim < 0 || t.dim >= d->ndim)
+            return set_err(plan, MOL_ERR_INVALID, "term field/dim");
+        auto opok = [&](int o) { return o >= 0 && o < d->nops; };
+        switch (t.kind) {
+            case MOL_TERM_LINEAR: if (!opok(t.op)) return set_err(plan, MOL_ERR_INVALID, "term op"); break;
+            case MOL_TERM_MIXED:
+                if (!opok(t.op) || !opok(t.op2) || t.dim2 < 0 || t.dim2 >= d->ndim || t.dim2 == t.dim)
+                    return set_err(plan, MOL_ERR_INVALID, "mixed term");
+                break;
+            case MOL_TERM_WENO:
+                if (!(t.dx > 0)) return set_err(plan, MOL_ERR_INVALID, "weno dx");
+                for (int f = 0; f < d->nfields; ++f) (void)f;
+                if (d->bc[t.field][t.dim][0].kind != MOL_BC_PERIODIC)
+                    return set_err(plan, MOL_ERR_UNSUPPORTED,
+                                   "WENO on a non-periodic dimension needs the nonuniform boundary stencils (not built)");
+                if (d->npts[t.dim] - 1 < 5) return set_err(plan, MOL_ERR_INVALID, "WENO needs at least 6 grid points to wrap");
+                break;
+            case MOL_TERM_NONLINLAP:
+                if (!opok(t.op) || !opok(t.op2) || !opok(t.op3)) return set_err(plan, MOL_ERR_INVALID, "nonlinlap ops");
+                if (t.prog >= 0) {
+                    int st = validate_prog(plan, d, t.prog, 1, MOL_MAX_REGS, 0, &t);
+                    if (st) return st;
+                }
+                break;
+            default: return set_err(plan, MOL_ERR_INVALID, "unknown term kind");
+        }
+    }
+    if (!d->code || !d->prog_ranges) return set_err(plan, MOL_ERR_INVALID, "programs");
+    long long ncell = 1;
+    for (int q = 0; q < d->ndim; ++q) ncell *= d->npts[q] - d->lower[q] - d->upper[q];
+    int st = validate_prog(plan, d, d->cell_prog, 0, MOL_MAX_REGS, ncell, nullptr);
+    if (st) return st;
+    for (int f = 0; f < d->nfields; ++f)
+        for (int q = 0; q < d->ndim; ++q) {
+            const bool per = d->bc[f][q][0].kind == MOL_BC_PERIODIC;
+            if (per && d->lower[q] != 1) return set_err(plan, MOL_ERR_INVALID, "periodic dims clip exactly the low point");
+            for (int s = 0; s < 2; ++s) {
+                const mol_bc& b = d->bc[f][q][s];
+                if (b.kind == MOL_BC_ROBIN) {
+                    if (b.op < 0 || b.op >= d->nops) return set_err(plan, MOL_ERR_INVALID, "bc operator");
+                    const mol_op1d& o = d->ops[b.op];
+                    if ((s == 0 && (o.nlo < 1 || o.bLlo < 1)) || (s == 1 && (o.nhi < 1 || o.bLhi < 1)))
+                        return set_err(plan, MOL_ERR_INVALID, "bc operator lacks a boundary table");
+                    if (b.prog >= 0) {
+                        st = validate_prog(plan, d, b.prog, 2, 16, 0, nullptr);
+                        if (st) return st;
+                    }
+                } else if (b.kind != MOL_BC_NONE && b.kind != MOL_BC_PERIODIC) {
+                    return set_err(plan, MOL_ERR_INVALID, "bc kind");
+                }
+            }
+        }
+    return MOL_OK;
+}
+
+template <class T>
+static int upload(mol_plan* plan, void** dst, const double* src, long long n) {
+    std::vector<T> tmp((size_t)std::max<long long>(n, 1));
+    for (long long i = 0; i < n; ++i) tmp[(size_t)i] = (T)src[i];
+    int st = plan_alloc(plan, dst, sizeof(T) * tmp.size());
+    if (st) return st;
+    return cuda_check(plan, cudaMemcpy(*dst, tmp.data(), sizeof(T) * (size_t)n, cudaMemcpyHostToDevice), "upload");
+}
+
+template <class T>
+static int build_prec(mol_plan* plan, const mol_problem_desc* d, PlanArrays& A, DevProb<T>& P) {
+    int st;
+    if ((st = upload<T>(plan, &A.w, d->weights, d->nweights))) return st;
+    if ((st = upload<T>(plan, &A.consts, d->consts, d->nconsts))) return st;
+    std::vector<double> aux((size_t)std::max<long long>(plan->aux_total, 1));
+    for (int i = 0; i < d->naux; ++i)
+        std::memcpy(aux.data() + plan->aux_off_host[i], d->aux[i], sizeof(double) * (size_t)d->aux_len[i]);
+    if ((st = upload<T>(plan, &A.aux, aux.data(), plan->aux_total))) return st;
+    for (int q = 0; q < 3; ++q) {
+        if (q < d->ndim) {
+            if ((st = upload<T>(plan, &A.coords[q], d->coords[q], d->npts[q]))) return st;
+        } else {
+            double one = 0.0;
+            if ((st = upload<T>(plan, &A.coords[q], &one, 1))) return st;
+        }
+    }
+    std::vector<DevBC<T>> bc(MOL_MAX_FIELDS * 3 * 2);
+    for (int f = 0; f < MOL_MAX_FIELDS; ++f)
+        for (int q = 0; q < 3; ++q)
+            for (int s = 0; s < 2; ++s) {
+                DevBC<T> b{};
+                if (f < d->nfields && q < d->ndim) {
+                    const mol_bc& src = d->bc[f][q][s];
+                    b.kind = src.kind;
+                    b.prog = src.prog;
+                    b.op = src.op;
+                    b.a = (T)src.a;
+                    b.b = (T)src.b;
+                    b.g = (T)src.g;
+                }
+                bc[(f * 3 + q) * 2 + s] = b;
+            }
+    if ((st = plan_alloc(plan, &A.bc, sizeof(DevBC<T>) * bc.size()))) return st;
+    if ((st = cuda_check(plan, cudaMemcpy(A.bc, bc.data(), sizeof(DevBC<T>) * bc.size(), cudaMemcpyHostToDevice), "bc")))
+        return st;
+    if ((st = upload<T>(plan, &A.params, d->params, d->nparams))) return st;
+    P.ndim = d->ndim;
+    P.nfields = d->nfields;
+    P.nparams = d->nparams;
+    P.cell_prog = d->cell_prog;
+    for (int q = 0; q < 3; ++q) {
+        P.n[q] = q < d->ndim ? (int)d->npts[q] : 1;
+        P.lo[q] = q < d->ndim ? d->lower[q] : 0;
+        P.up[q] = q < d->ndim ? d->upper[q] : 0;
+        P.ni[q] = P.n[q] - P.lo[q] - P.up[q];
+        P.coords[q] = (const T*)A.coords[q];
+    }
+    for (int f = 0; f < MOL_MAX_FIELDS; ++f) {
+        int m = 0;
+        if (f < d->nfields)
+            for (int q = 0; q < d->ndim; ++q)
+                if (d->bc[f][q][0].kind == MOL_BC_PERIODIC) m |= 1 << q;
+        P.permask[f] = m;
+    }
+    P.ncell = plan->ncell;
+    P.bc = (const DevBC<T>*)A.bc;
+    P.ops = plan->d_ops;
+    P.w = (const T*)A.w;
+    P.terms = plan->d_terms;
+    P.code = plan->d_code;
+    P.progs = plan->d_progs;
+    P.consts = (const T*)A.consts;
+    P.aux = (const T*)A.aux;
+    P.aux_off = plan->d_aux_off;
+    P.naux = d->naux;
+    return MOL_OK;
+}
+
+static int copy_struct(mol_plan* plan, void** dst, const void* src, size_t bytes) {
+    int st = plan_alloc(plan, dst, bytes);
+    if (st) return st;
+    if (bytes == 0) return MOL_OK;
+    return cuda_check(plan, cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice), "descriptor copy");
+}
+
+// ----------------------------------------------------------------------------
+// C ABI
+// ----------------------------------------------------------------------------
+
+extern "C" {
+
+int mol_version(void) { return MOL_ABI_VERSION * 10000 + 100; }
+
+const char* mol_status_string(int s) {
+    switch (s) {
+        case MOL_OK: return "ok";
+        case MOL_ERR_INVALID: return "invalid descriptor or argument";
+        case MOL_ERR_OOM: return "device out of memory";
+        case MOL_ERR_NONFINITE: return "non-finite state";
+        case MOL_ERR_TIMEOUT: return "device wait timed out";
+        case MOL_ERR_CUDA: return "CUDA error";
+        case MOL_ERR_UNSUPPORTED: return "unsupported discretization";
+        case MOL_ERR_MAXITERS: return "maximum iterations reached";
+        case MOL_ERR_DTMIN: return "step size underflow";
+        default: return "unknown status";
+    }
+}
+
+int64_t mol_launch_count(void) { return g_launches.load(); }
+
+const char* mol_last_error(const mol_plan* plan) { return plan ? plan->err.c_str() : "null plan"; }
+
+int64_t mol_plan_n_unknowns(const mol_plan* plan) { return plan ? plan->nunk : -1; }
+
+int mol_plan_set_stream(mol_plan* plan, void* stream) {
+    if (!plan) return MOL_ERR_INVALID;
+    if (plan->own_stream && plan->stream) cudaStreamDestroy(plan->stream);
+    plan->own_stream = false;
+    plan->stream = (cudaStream_t)stream;
+    if (plan->g_ssp64) { cudaGraphExecDestroy(plan->g_ssp64); plan->g_ssp64 = nullptr; }
+    if (plan->g_ssp32) { cudaGraphExecDestroy(plan->g_ssp32); plan->g_ssp32 = nullptr; }
+    return MOL_OK;
+}
+
+int mol_plan_destroy(mol_plan* plan) {
+    if (!plan) return MOL_ERR_INVALID;
+    cudaSetDevice(plan->dev);
+    if (plan->stream) cudaStreamSynchronize(plan->stream);
+    if (plan->g_ssp64) cudaGraphExecDestroy(plan->g_ssp64);
+    if (plan->g_ssp32) cudaGraphExecDestroy(plan->g_ssp32);
+    for (void* p : plan->allocs) cudaFree(p);
+    if (plan->own_stream && plan->stream) cudaStreamDestroy(plan->stream);
+    delete plan;
+    return MOL_OK;
+}
+
+int mol_plan_create(const mol_problem_desc* d, mol_plan** out) {
+    if (!out) return MOL_ERR_INVALID;
+    *out = nullptr;
+    mol_plan* plan = new mol_plan();
+    int st = validate_desc(plan, d);
+    if (st) {
+        *out = plan;  // caller may read mol_last_error, then destroy
+        return st;
+    }
+    cudaGetDevice(&plan->dev);
+    plan->desc = *d;
+    plan->nfields = d->nfields;
+    plan->nparams = d->nparams;
+    plan->naux = d->naux;
+    long long ncell = 1;
+    for (int q = 0; q < d->ndim; ++q) ncell *= d->npts[q] - d->lower[q] - d->upper[q];
+    plan->ncell = ncell;
+    plan->nunk = ncell * d->nfields;
+    plan->aux_off_host.resize(d->naux + 1);
+    long long off = 0;
+    for (int i = 0; i < d->naux; ++i) {
+        plan->aux_off_host[i] = off;
+        off += d->aux_len[i];
+    }
+    plan->aux_off_host[d->naux] = off;
+    plan->aux_total = off;
+    plan->params_host.assign(d->params, d->params + d->nparams);
+    auto fail = [&](int code) {
+        *out = plan;
+        return code;
+    };
+    if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->stream, cudaStreamNonBlocking), "stream"))) return fail(st);
+    plan->own_stream = true;
+    if ((st = copy_struct(plan, (void**)&plan->d_ops, d->ops, sizeof(mol_op1d) * d->nops))) return fail(st);
+    if ((st = copy_struct(plan, (void**)&plan->d_terms, d->terms, sizeof(mol_term) * d->nterms))) return fail(st);
+    if ((st = copy_struct(plan, (void**)&plan->d_code, d->code, sizeof(mol_instr) * d->ninstr))) return fail(st);
+    if ((st = copy_struct(plan, (void**)&plan->d_progs, d->prog_ranges, sizeof(int) * 2 * d->nprogs))) return fail(st);
+    if ((st = copy_struct(plan, (void**)&plan->d_aux_off, plan->aux_off_host.data(), sizeof(long long) * (d->naux + 1))))
+        return fail(st);
+    if ((st = build_prec<double>(plan, d, plan->a64, plan->P64))) return fail(st);
+    if ((st = build_prec<float>(plan, d, plan->a32, plan->P32))) return fail(st);
+    if ((st = plan_alloc(plan, (void**)&plan->d_state, sizeof(SolverState)))) return fail(st);
+    cudaMemset(plan->d_state, 0, sizeof(SolverState));
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->dev);
+    long long want = (ncell + kThreads - 1) / kThreads;
+    plan->nblocks = (int)std::max<long long>(1, std::min<long long>(want, (long long)sms * 8));
+    if ((st = plan_alloc(plan, (void**)&plan->d_partials, sizeof(double) * 3 * plan->nblocks))) return fail(st);
+    *out = plan;
+    return MOL_OK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------------------
+// host/device staging
+// ----------------------------------------------------------------------------
+
+namespace {
+
+template <class T>
+struct Staged {
+    T* ptr = nullptr;
+    bool host = false;
+};
+
+template <class T>
+int stage_in(mol_plan* plan, const T* src, int slot, Staged<T>& s, bool copy) {
+    if (is_device_ptr(src)) {
+        s.ptr = const_cast<T*>(src);
+        s.host = false;
+        return MOL_OK;
+    }
+    int st = ensure_slot<T>(plan, slot);
+    if (st) return st;
+    s.ptr = workspace<T>(plan)[slot];
+    s.host = true;
+    if (copy)
+        return cuda_check(plan, cudaMemcpyAsync(s.ptr, src, sizeof(T) * (size_t)plan->nunk, cudaMemcpyHostToDevice,
+                                                plan->stream), "H2D");
+    return MOL_OK;
+}
+
+template <class T>
+const T* params_ptr(mol_plan* plan, const T* p, int* st) {
+    *st = MOL_OK;
+    PlanArrays& A = std::is_same<T, double>::value ? plan->a64 : plan->a32;
+    if (!p) return (const T*)A.params;
+    if (is_device_ptr(p)) return p;
+    *st = cuda_check(plan, cudaMemcpyAsync(A.params, p, sizeof(T) * (size_t)std::max(plan->nparams, 0),
+                                           cudaMemcpyHostToDevice, plan->stream), "params H2D");
+    return (const T*)A.params;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <class T>
+int rhs_impl(mol_plan* plan, T* du, const T* u, const T* p, double t) {
+    if (!plan || !du || !u) return MOL_ERR_INVALID;
+    DeviceGuard g(plan->dev);
+    int st;
+    // slots 10 and 11 stage host buffers for f!
+    Staged<T> su, sdu;
+    if ((st = stage_in<T>(plan, u, 10, su, true))) return st;
+    if ((st = stage_in<T>(plan, du, 11, sdu, false))) return st;
+    const T* pp = params_ptr<T>(plan, p, &st);
+    if (st) return st;
+    if ((st = launch_rhs<T>(plan, sdu.ptr, su.ptr, pp, t))) return st;
+    if (sdu.host) {
+        if ((st = cuda_check(plan, cudaMemcpyAsync(du, sdu.ptr, sizeof(T) * (size_t)plan->nunk, cudaMemcpyDeviceToHost,
+                                                   plan->stream), "D2H")))
+            return st;
+        return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+    }
+    return MOL_OK;
+}
+
+template <class T>
+int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t nsteps) {
+    if (!plan || !u || nsteps < 0 || !std::isfinite(dt) || !std::isfinite(t0)) return MOL_ERR_INVALID;
+    DeviceGuard g(plan->dev);
+    int st;
+    if ((st = ensure_ws<T>(plan, 3))) return st;
+    T** ws = workspace<T>(plan);
+    Staged<T> su;
+    const bool host = !is_device_ptr(u);
+    T* ud = host ? ws[0] : u;
+    if (host && (st = cuda_check(plan, cudaMemcpyAsync(ud, u, sizeof(T) * (size_t)plan->nunk, cudaMemcpyHostToDevice,
+                                                       plan->stream), "H2D")))
+        return st;
+    const T* pp = params_ptr<T>(plan, p, &st);
+    if (st) return st;
+    k_set_time<<<1, 1, 0, plan->stream>>>(plan->d_state, t0);
+    ++g_launches;
+    T* u1 = ws[1];
+    T* u2 = ws[2];
+    // chunks of `chunk` steps replayed as one CUDA graph; the tail is launched directly
+    const int chunk = plan->g_chunk;
+    const bool is64 = std::is_same<T, double>::value;
+    cudaGraphExec_t& gx = is64 ? plan->g_ssp64 : plan->g_ssp32;
+    double& gdt = is64 ? plan->g_ssp64_dt : plan->g_ssp32_dt;
+    const void*& gp = is64 ? plan->g_ssp64_p : plan->g_ssp32_p;
+    const void*& gpp = is64 ? plan->g_ssp64_pp : plan->g_ssp32_pp;
+    int64_t done = 0;
+    if (nsteps >= chunk) {
+        // the state buffer, parameter pointer and dt are baked into the captured graph
+        if (gx && (gdt != dt || gp != (const void*)ud || gpp != (const void*)pp)) {
+            cudaGraphExecDestroy(gx);
+            gx = nullptr;
+        }
+        if (!gx) {
+            cudaGraph_t graph;
+            if ((st = cuda_check(plan, cudaStreamBeginCapture(plan->stream, cudaStreamCaptureModeThreadLocal),
+                                 "capture")))
+                return st;
+            const long long before = g_launches.load();
+            for (int s = 0; s < chunk; ++s) launch_ssprk_step<T>(plan, ud, u1, u2, pp, dt);
+            g_launches = before;
+            if ((st = cuda_check(plan, cudaStreamEndCapture(plan->stream, &graph), "end capture"))) return st;
+            st = cuda_check(plan, cudaGraphInstantiate(&gx, graph, 0), "instantiate");
+            cudaGraphDestroy(graph);
+            if (st) return st;
+            gdt = dt;
+            gp = (const void*)ud;
+            gpp = (const void*)pp;
+        }
+        for (; done + chunk <= nsteps; done += chunk) {
+            if ((st = cuda_check(plan, cudaGraphLaunch(gx, plan->stream), "graph launch"))) return st;
+            g_launches += 3 * chunk;
+        }
+    }
+    for (; done < nsteps; ++done)
+        if ((st = launch_ssprk_step<T>(plan, ud, u1, u2, pp, dt))) return st;
+    if (host) {
+        if ((st = cuda_check(plan, cudaMemcpyAsync(u, ud, sizeof(T) * (size_t)plan->nunk, cudaMemcpyDeviceToHost,
+                                                   plan->stream), "D2H")))
+            return st;
+        return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+    }
+    return cuda_check(plan, cudaGetLastError(), "ssprk33");
+}
+
+}  // namespace
+
+extern "C" {
+
+int mol_rhs(mol_plan* plan, double* du, const double* u, const double* p, double t) {
+    return rhs_impl<double>(plan, du, u, p, t);
+}
+int mol_rhs_f32state(mol_plan* plan, float* du, const float* u, const float* p, double t) {
+    return rhs_impl<float>(plan, du, u, p, t);
+}
+int mol_step_ssprk33(mol_plan* plan, double* u, const double* p, double t0, double dt, int64_t nsteps) {
+    return ssprk_impl<double>(plan, u, p, t0, dt, nsteps);
+}
+int mol_step_ssprk33_f32state(mol_plan* plan, float* u, const float* p, double t0, double dt, int64_t nsteps) {
+    return ssprk_impl<float>(plan, u, p, t0, dt, nsteps);
+}
+
+int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, double t1, double abstol, double reltol,
+                    double dt0, int64_t maxiters, mol_stats* stats) {
+    if (!plan || !u || !(t1 >= t0) || !(abstol > 0) || !(reltol >= 0)) return MOL_ERR_INVALID;
+    DeviceGuard g(plan->dev);
+    int st;
+    // slots: 0 u, 1..7 k1..k7, 8 ybuf0, 9 ybuf1
+    if ((st = ensure_ws<double>(plan, 10))) return st;
+    double** ws = plan->ws64;
+    const bool host = !is_device_ptr(u);
+    double* ud = host ? ws[0] : u;
+    if (host && (st = cuda_check(plan, cudaMemcpyAsync(ud, u, sizeof(double) * (size_t)plan->nunk,
+                                                       cudaMemcpyHostToDevice, plan->stream), "H2D")))
+        return st;
+    const double* pp = params_ptr<double>(plan, p, &st);
+    if (st) return st;
+    double** d_k = nullptr;
+    {
+        void* tmp;
+        if ((st = plan_alloc(plan, &tmp, sizeof(double*) * 7))) return st;
+        d_k = (double**)tmp;
+        double* hk[7];
+        for (int i = 0; i < 7; ++i) hk[i] = ws[1 + i];
+        if ((st = cuda_check(plan, cudaMemcpyAsync(d_k, hk, sizeof(hk), cudaMemcpyHostToDevice, plan->stream), "k ptrs")))
+            return st;
+    }
+    const long long n = plan->nunk;
+    double* k1 = ws[1];
+    double* k7 = ws[7];
+    double* yb0 = ws[8];
+    double* yb1 = ws[9];
+    const int nb = plan->nblocks;
+    // k1 = f(u0, t0)
+    if ((st = launch_rhs<double>(plan, k1, ud, pp, t0))) return st;
+    double dt = dt0;
+    if (!(dt > 0)) {
+        // Hairer's initial step (the heuristic OrdinaryDiffEq's ode_determine_initdt follows)
+        std::vector<double> hp(3 * nb);
+        k_init_norms<double><<<nb, kThreads, 0, plan->stream>>>(n, ud, k1, nullptr, abstol, reltol, plan->d_partials);
+        ++g_launches;
+        cudaMemcpyAsync(hp.data(), plan->d_partials, sizeof(double) * 3 * nb, cudaMemcpyDeviceToHost, plan->stream);
+        if ((st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "init norms"))) return st;
+        double s0 = 0, s1 = 0;
+        for (int b = 0; b < nb; ++b) { s0 += hp[3 * b]; s1 += hp[3 * b + 1]; }
+        const double d0 = std::sqrt(s0 / n), d1 = std::sqrt(s1 / n);
+        double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
+        h0 = std::min(h0, t1 - t0);
+        k_axpy<double><<<nb, kThreads, 0, plan->stream>>>(n, yb1, ud, k1, h0);
+        ++g_launches;
+        if ((st = launch_rhs<double>(plan, yb0, yb1, pp, t0 + h0))) return st;
+        k_init_norms<double><<<nb, kThreads, 0, plan->stream>>>(n, ud, k1, yb0, abstol, reltol, plan->d_partials);
+        ++g_launches;
+        cudaMemcpyAsync(hp.data(), plan->d_partials, sizeof(double) * 3 * nb, cudaMemcpyDeviceToHost, plan->stream);
+        if ((st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "init norms"))) return st;
+        double s2 = 0;
+        for (int b = 0; b < nb; ++b) s2 += hp[3 * b + 2];
+        const double d2 = std::sqrt(s2 / n) / h0;
+        const double m = std::max(d1, d2);
+        const double h1 = m <= 1e-15 ? std::max(1e-6, h0 * 1e-3) : std::pow(0.01 / m, 1.0 / 5.0);
+        dt = std::min(std::min(100 * h0, h1), t1 - t0);
+    }
+    if (maxiters <= 0) maxiters = 100000000;
+    k_tsit_init_state<<<1, 1, 0, plan->stream>>>(plan->d_state, t0, t1, dt, abstol, reltol, maxiters);
+    ++g_launches;
+    k_tsit_commit<double><<<nb, kThreads, 0, plan->stream>>>(plan->P64, ud, k1, k7, yb1, yb0, plan->d_state, 1);
+    ++g_launches;
+    // one attempt = stages 2..7 + commit; M attempts per captured graph
+    auto attempt = [&]() {
+        for (int s = 2; s <= 7; ++s) {
+            const double* yin = (s % 2 == 0) ? yb0 : yb1;
+            double* yout = (s % 2 == 0) ? yb1 : yb0;
+            k_tsit_stage<double><<<nb, kThreads, 0, plan->stream>>>(plan->P64, s, yin, yout, ud, d_k, pp,
+                                                                    plan->d_state, plan->d_partials);
+        }
+        k_tsit_commit<double><<<nb, kThreads, 0, plan->stream>>>(plan->P64, ud, k1, k7, yb1, yb0, plan->d_state, 0);
+    };
+    const int M = 32;
+    cudaGraph_t graph;
+    cudaGraphExec_t gx = nullptr;
+    if ((st = cuda_check(plan, cudaStreamBeginCapture(plan->stream, cudaStreamCaptureModeThreadLocal), "capture")))
+        return st;
+    for (int i = 0; i < M; ++i) attempt();
+    if ((st = cuda_check(plan, cudaStreamEndCapture(plan->stream, &graph), "end capture"))) return st;
+    st = cuda_check(plan, cudaGraphInstantiate(&gx, graph, 0), "instantiate");
+    cudaGraphDestroy(graph);
+    if (st) return st;
+    SolverState hs;
+    for (;;) {
+        if ((st = cuda_check(plan, cudaGraphLaunch(gx, plan->stream), "graph launch"))) break;
+        g_launches += 7 * M;
+        cudaMemcpyAsync(&hs, plan->d_state, sizeof(SolverState), cudaMemcpyDeviceToHost, plan->stream);
+        if ((st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "tsit5 sync"))) break;
+        if (hs.done) break;
+    }
+    cudaGraphExecDestroy(gx);
+    if (st) return st;
+    if (stats) {
+        stats->naccept = hs.naccept;
+        stats->nreject = hs.nreject;
+        stats->nf = hs.nf + 1;
+        stats->t = hs.t;
+        stats->dt = hs.dt;
+    }
+    if (host) {
+        if ((st = cuda_check(plan, cudaMemcpyAsync(u, ud, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost,
+                                                   plan->stream), "D2H")))
+            return st;
+        if ((st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync"))) return st;
+    }
+    if (hs.status) return set_err(plan, hs.status, "tsit5 stopped early");
+    return MOL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+// Host-side plan shared by the translation units of libmolgpu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "mol_device.cuh"
+#include "molgpu.h"
+
+namespace mol {
+
+extern std::atomic<long long> g_launches;
+
+// Device-resident integrator state; kernels read t/dt from here so a captured
+// CUDA graph can be replayed step after step.
+struct SolverState {
+    double t, dt, t1, abstol, reltol;
+    double qold, EEst, dtmin;
+    double dta[8][8];   // dt * a_ij of the Tsit5 tableau (row = stage index)
+    double dtb[8];      // dt * btilde_j
+    double sums[4];     // norms of the initial-step heuristic
+    long long naccept, nreject, nf, iter, maxiters;
+    int done, status, accepted, pad;
+    unsigned int blocks_done, pad2;
+};
+
+struct PlanArrays {
+    // per-precision copies of everything the kernels read
+    void* w = nullptr;
+    void* consts = nullptr;
+    void* aux = nullptr;
+    void* coords[3] = {nullptr, nullptr, nullptr};
+    void* bc = nullptr;
+    void* params = nullptr;
+};
+
+struct mol_plan_impl;
+
+}  // namespace mol
+
+struct mol_plan {
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    mol_problem_desc desc{};          // scalar fields only (pointers not retained)
+    long long nunk = 0, ncell = 0;
+    int nfields = 0, nparams = 0, naux = 0;
+    long long aux_total = 0;
+    std::vector<long long> aux_off_host;
+    std::vector<double> params_host;
+    // structure arrays (precision independent)
+    mol_op1d* d_ops = nullptr;
+    mol_term* d_terms = nullptr;
+    mol_instr* d_code = nullptr;
+    int* d_progs = nullptr;
+    long long* d_aux_off = nullptr;
+    mol::PlanArrays a64, a32;
+    mol::DevProb<double> P64{};
+    mol::DevProb<float> P32{};
+    // workspaces
+    std::vector<void*> allocs;
+    double* ws64[12] = {nullptr};
+    float* ws32[12] = {nullptr};
+    mol::SolverState* d_state = nullptr;
+    double* d_partials = nullptr;
+    int nblocks = 0;
+    // adjoint workspaces
+    double* adj[16] = {nullptr};
+    double* d_snap = nullptr;
+    long long nsnap_alloc = 0;
+    double* d_lam_p_partials = nullptr;
+    // cached CUDA graphs for fixed-step SSPRK33 chunks
+    cudaGraphExec_t g_ssp64 = nullptr, g_ssp32 = nullptr;
+    double g_ssp64_dt = 0, g_ssp32_dt = 0;
+    const void* g_ssp64_p = nullptr;
+    const void* g_ssp32_p = nullptr;
+    const void* g_ssp64_pp = nullptr;
+    const void* g_ssp32_pp = nullptr;
+    int g_chunk = 16;
+};
+
+namespace mol {
+
+int set_err(mol_plan* plan, int code, const std::string& msg);
+int cuda_check(mol_plan* plan, cudaError_t e, const char* what);
+bool is_device_ptr(const void* p);
+int plan_alloc(mol_plan* plan, void** ptr, size_t bytes);
+int plan_grid(const mol_plan* plan);
+
+template <class T>
+DevProb<T>& prob(mol_plan* plan);
+template <>
+inline DevProb<double>& prob<double>(mol_plan* plan) { return plan->P64; }
+template <>
+inline DevProb<float>& prob<float>(mol_plan* plan) { return plan->P32; }
+
+template <class T>
+T** workspace(mol_plan* plan);
+template <>
+inline double** workspace<double>(mol_plan* plan) { return plan->ws64; }
+template <>
+inline float** workspace<float>(mol_plan* plan) { return plan->ws32; }
+
+template <class T>
+int ensure_ws(mol_plan* plan, int count);
+
+// launch helpers implemented in mol_plan.cu
+template <class T>
+int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t);
+template <class T>
+int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt);
+
+}  // namespace mol

@@ -1,0 +1,216 @@
+"""User-facing API mirroring MethodOfLines.jl / SciMLBase for the GPU hot path.
+
+    disc = MOLFiniteDifference({x: dx, y: dy}, t, approx_order=2)
+    prob = discretize(pdesys, disc)            # ODEProblem whose f calls mol_rhs
+    prob.f(du, u, p, t)                        # the generated f!(du, u, p, t)
+    sol = solve(prob, SSPRK33(), dt=1e-4)      # on-device stepping (mol_step_ssprk33)
+    sol = solve(prob, Tsit5(), abstol=1e-10, reltol=1e-10)
+
+Arrays may be numpy (host) or any object exposing ``data_ptr()`` on the GPU
+(e.g. a torch CUDA tensor); the library detects which and stages host arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+from .lowering import Descriptor, Lowered, lower
+from .symbolic import IV, PDESystem
+
+
+class UpwindScheme:
+    """``UpwindScheme(order=1)`` (src/interface/scheme_types.jl:8-16)."""
+
+    def __init__(self, order: int = 1):
+        self.order = int(order)
+
+    def spec(self):
+        return ("upwind", self.order)
+
+
+class WENOScheme:
+    """``WENOScheme(; epsilon=1e-6)`` (src/discretization/schemes/WENO/WENO.jl:72-89)."""
+
+    def __init__(self, epsilon: float = 1e-6):
+        self.epsilon = float(epsilon)
+
+    def spec(self):
+        return ("weno", self.epsilon)
+
+
+class MOLFiniteDifference:
+    """``MOLFiniteDifference(dxs, time; approx_order, advection_scheme, grid_align, ...)``
+    (src/interface/MOLFiniteDifference.jl:31-76).  Only the options the GPU path honours are kept."""
+
+    def __init__(self, dxs, time: Optional[IV] = None, approx_order: int = 2, advection_scheme=None,
+                 grid_align: str = "center", **kwargs):
+        self.dxs = {(k.name if isinstance(k, IV) else k): v for k, v in dict(dxs).items()}
+        self.time = time
+        self.approx_order = int(approx_order)
+        self.advection_scheme = advection_scheme if advection_scheme is not None else UpwindScheme()
+        self.grid_align = grid_align
+        self.kwargs = kwargs
+
+
+def _ptr(a):
+    """(pointer, is_float32) of a numpy array or a CUDA tensor-like object."""
+    if a is None:
+        return None, None
+    if hasattr(a, "data_ptr"):
+        dt = str(getattr(a, "dtype", ""))
+        return C.c_void_p(a.data_ptr()), ("float32" in dt)
+    arr = a
+    if not (arr.flags["C_CONTIGUOUS"]):
+        raise ValueError("arrays must be contiguous")
+    return C.c_void_p(arr.ctypes.data), arr.dtype == np.float32
+
+
+class Plan:
+    """Owner of one ``mol_plan``: the compiled GPU right-hand side and its steppers."""
+
+    def __init__(self, lowered: Lowered):
+        self.lowered = lowered
+        self.desc = Descriptor(lowered)
+        h = C.c_void_p()
+        st = L.lib().mol_plan_create(C.byref(self.desc.desc), C.byref(h))
+        self._h = h
+        if st != 0:
+            msg = (L.lib().mol_last_error(h) or b"").decode() if h.value else ""
+            if h.value:
+                L.lib().mol_plan_destroy(h)
+            self._h = None
+            raise L.MolError(st, msg)
+        self.n = int(L.lib().mol_plan_n_unknowns(h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().mol_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_handle: int):
+        L.check(L.lib().mol_plan_set_stream(self._h, C.c_void_p(stream_handle)), self._h)
+
+    def rhs(self, du, u, p=None, t: float = 0.0):
+        """f!(du, u, p, t)."""
+        pd, f32 = _ptr(du)
+        pu, _ = _ptr(u)
+        pp, _ = _ptr(p)
+        fn = L.lib().mol_rhs_f32state if f32 else L.lib().mol_rhs
+        L.check(fn(self._h, pd, pu, pp, float(t)), self._h)
+        return du
+
+    def step_ssprk33(self, u, dt: float, nsteps: int, t0: float = 0.0, p=None):
+        pu, f32 = _ptr(u)
+        pp, _ = _ptr(p)
+        fn = L.lib().mol_step_ssprk33_f32state if f32 else L.lib().mol_step_ssprk33
+        L.check(fn(self._h, pu, pp, float(t0), float(dt), int(nsteps)), self._h)
+        return u
+
+    def solve_tsit5(self, u, t0: float, t1: float, abstol: float, reltol: float, p=None, dt0: float = 0.0,
+                    maxiters: int = 0):
+        pu, _ = _ptr(u)
+        pp, _ = _ptr(p)
+        stats = L.mol_stats()
+        L.check(L.lib().mol_solve_tsit5(self._h, pu, pp, float(t0), float(t1), float(abstol), float(reltol),
+                                        float(dt0), int(maxiters), C.byref(stats)), self._h)
+        return {"naccept": stats.naccept, "nreject": stats.nreject, "nf": stats.nf, "t": stats.t, "dt": stats.dt}
+
+    def vjp(self, lam, u, p=None, t: float = 0.0, lam_u=None, lam_p=None, lam_aux=None):
+        L.check(L.lib().mol_rhs_vjp(self._h, _ptr(lam)[0], _ptr(u)[0], _ptr(p)[0], float(t), _ptr(lam_u)[0],
+                                    _ptr(lam_p)[0], _ptr(lam_aux)[0]), self._h)
+
+    def adjoint_ssprk33(self, u0, dt: float, nsteps: int, target, t0: float = 0.0, p=None, nsnap: int = 64,
+                        loss_kind: int = L.LOSS_MISFIT, uT=None, dLdu0=None, dLdp=None, dLdaux=None):
+        loss = np.zeros(1)
+        nfw = C.c_int64(0)
+        L.check(L.lib().mol_adjoint_ssprk33(self._h, _ptr(u0)[0], _ptr(p)[0], float(t0), float(dt), int(nsteps),
+                                            int(nsnap), int(loss_kind), _ptr(target)[0], _ptr(uT)[0],
+                                            _ptr(loss)[0], _ptr(dLdu0)[0], _ptr(dLdp)[0], _ptr(dLdaux)[0],
+                                            C.byref(nfw)), self._h)
+        return float(loss[0]), int(nfw.value)
+
+    @property
+    def aux_sizes(self):
+        return [a.size for a in self.lowered.aux]
+
+
+class ODEFunction:
+    """The ODEFunction whose in-place call is the GPU RHS (src/MOL_discretization.jl:171-201)."""
+
+    def __init__(self, plan: Plan):
+        self.plan = plan
+
+    def __call__(self, du, u, p, t):
+        self.plan.rhs(du, u, p, t)
+        return None
+
+
+@dataclass
+class ODEProblem:
+    f: ODEFunction
+    u0: np.ndarray
+    tspan: tuple
+    p: np.ndarray
+    lowered: Lowered
+
+    @property
+    def plan(self) -> Plan:
+        return self.f.plan
+
+
+def discretize(pdesys: PDESystem, disc: MOLFiniteDifference, tspan=None) -> ODEProblem:
+    """``discretize(pdesys, MOLFiniteDifference(...))`` returning a GPU-backed ODEProblem."""
+    spec = pdesys.to_spec(disc)
+    lw = lower(spec)
+    plan = Plan(lw)
+    if tspan is None:
+        tname = spec["time"]
+        tspan = tuple(spec["domain"][tname]) if tname in spec["domain"] else (0.0, 1.0)
+    u0 = lw.u0 if lw.u0 is not None else np.zeros(lw.n_unknowns)
+    return ODEProblem(ODEFunction(plan), u0.copy(), tuple(tspan), lw.param_values.copy(), lw)
+
+
+class SSPRK33:
+    """Shu-Osher SSPRK33 (OrdinaryDiffEqSSPRK), fixed step on the device."""
+
+
+class Tsit5:
+    """Tsitouras 5(4) with the PI controller, adaptive on the device."""
+
+
+@dataclass
+class Solution:
+    u: np.ndarray
+    t: float
+    stats: dict
+
+
+def solve(prob: ODEProblem, alg, dt: Optional[float] = None, abstol: float = 1e-6, reltol: float = 1e-3,
+          adaptive: Optional[bool] = None, u0=None, p=None) -> Solution:
+    u = np.array(prob.u0 if u0 is None else u0, dtype=np.float64, copy=True)
+    t0, t1 = float(prob.tspan[0]), float(prob.tspan[1])
+    p = prob.p if p is None else np.ascontiguousarray(p, dtype=np.float64)
+    if isinstance(alg, SSPRK33) or alg is SSPRK33:
+        if dt is None:
+            raise ValueError("SSPRK33 needs dt")
+        n = int(round((t1 - t0) / dt))
+        prob.plan.step_ssprk33(u, dt, n, t0=t0, p=p)
+        return Solution(u, t0 + n * dt, {"nsteps": n})
+    if isinstance(alg, Tsit5) or alg is Tsit5:
+        stats = prob.plan.solve_tsit5(u, t0, t1, abstol, reltol, p=p, dt0=dt or 0.0)
+        return Solution(u, stats["t"], stats)
+    raise ValueError(f"unsupported algorithm {alg}")

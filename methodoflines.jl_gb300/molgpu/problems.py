@@ -1,0 +1,198 @@
+"""The benchmark problem families, written against the MethodOfLines-style API.
+
+Each builder returns ``(pdesys, disc, extras)``; ``extras`` carries the seeded
+synthetic inputs (targets, step sizes) the workloads use.  All random inputs
+come from ``numpy.random.Generator(PCG64(seed))`` in Float64.
+
+1. heat1d        u_t = D u_xx on [0,1], Dirichlet 0, u0 = sin(pi x)
+2. brusselator   2-D periodic Brusselator with the reference test's forcing
+                 (test/Brusselator/brusselator_eq.jl:8-58)
+3. burgers       u_t = -u u_x + nu u_xx, periodic, WENO5 (Convection_WENO tests)
+4. nonlinear_diffusion   u_t = div(u^2 grad u) + k u (1-u), Neumann 0 (ensemble member)
+5. adr3d         u_t = div(K grad u) + 0.3 u_xy - c.grad u - lambda u^2, periodic x,y, Dirichlet z
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .api import MOLFiniteDifference, UpwindScheme, WENOScheme
+from .symbolic import (Differential, Eq, Field, Interval, IV, Param, PDESystem, cos, exp, register, sin)
+
+
+def _rng(seed):
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def heat1d(n: int = 101, D: float = 1.0):
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dxx = Differential(t), Differential(x) ** 2
+    Dp = Param("D", D)
+    eq = Eq(Dt(u(x, t)), Dp * Dxx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), sin(math.pi * x)), Eq(u(0.0, t), 0.0), Eq(u(1.0, t), 0.0)]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 0.1)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [Dp])
+    disc = MOLFiniteDifference({x: n}, t, approx_order=2)
+    return sys, disc, {}
+
+
+def brusselator(N: int = 256, forcing: bool = True, t_end: float = 11.5):
+    """dx = dy = 1/N on [0,1]^2, periodic: N unknowns per dimension and field."""
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u, v = Field("u"), Field("v")
+    Dt = Differential(t)
+    Dxx, Dyy = Differential(x) ** 2, Differential(y) ** 2
+    alpha = Param("alpha", 10.0)
+
+    def lap(w):
+        return Dxx(w) + Dyy(w)
+
+    U, V = u(x, y, t), v(x, y, t)
+    f = ((((x - 0.3) ** 2 + (y - 0.6) ** 2) <= 0.1 ** 2) * (t >= 1.1)) * 5.0
+    rhs_u = 1.0 + V * U ** 2 - 4.4 * U + alpha * lap(U)
+    if forcing:
+        rhs_u = rhs_u + f
+    eqs = [Eq(Dt(U), rhs_u), Eq(Dt(V), 3.4 * U - V * U ** 2 + alpha * lap(V))]
+    bcs = [
+        Eq(u(x, y, 0.0), 22 * (y * (1 - y)) ** 1.5),
+        Eq(u(0.0, y, t), u(1.0, y, t)),
+        Eq(u(x, 0.0, t), u(x, 1.0, t)),
+        Eq(v(x, y, 0.0), 27 * (x * (1 - x)) ** 1.5),
+        Eq(v(0.0, y, t), v(1.0, y, t)),
+        Eq(v(x, 0.0, t), v(x, 1.0, t)),
+    ]
+    sys = PDESystem(eqs, bcs, [(x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0)), (t, Interval(0.0, t_end))],
+                    [x, y, t], [U, V], [alpha])
+    disc = MOLFiniteDifference({x: 1.0 / N, y: 1.0 / N}, t, approx_order=2)
+    dx = 1.0 / N
+    return sys, disc, {"dt_ssprk": dx * dx / (8 * 10.0)}
+
+
+def burgers_ic_coeffs(seed: int = 1):
+    r = _rng(seed)
+    ks = np.arange(1, 9)
+    a = r.normal(0.0, 1.0 / ks)
+    phi = r.uniform(0.0, 2 * math.pi, size=8)
+    return ks, a, phi
+
+
+def burgers(npts: int = 65537, nu: float = 1e-3, seed: int = 1, target_seed: int = 2):
+    """Periodic [0, 2 pi], `npts` grid points (npts - 1 unknowns), WENO5 convection."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dxx = Differential(t), Differential(x), Differential(x) ** 2
+    nup = Param("nu", nu)
+    U = u(x, t)
+    eq = Eq(Dt(U), -U * Dx(U) + nup * Dxx(U))
+    ks, a, phi = burgers_ic_coeffs(seed)
+    ic = None
+    for k, ak, pk in zip(ks, a, phi):
+        term = float(ak) * sin(float(k) * x + float(pk))
+        ic = term if ic is None else ic + term
+    L = 2 * math.pi
+    bcs = [Eq(u(x, 0.0), ic), Eq(u(0.0, t), u(L, t))]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, L))], [t, x], [U], [nup])
+    disc = MOLFiniteDifference({x: npts}, t, approx_order=2, advection_scheme=WENOScheme(1e-6))
+    # seeded target for the adjoint misfit
+    kt, at, pt = burgers_ic_coeffs(target_seed)
+    dx = L / (npts - 1)
+    xs = np.arange(1, npts) * dx
+    target = sum(float(ak) * np.sin(float(k) * xs + float(pk)) for k, ak, pk in zip(kt, at, pt))
+    u0 = sum(float(ak) * np.sin(float(k) * xs + float(pk)) for k, ak, pk in zip(ks, a, phi))
+    dt = 0.4 / (np.max(np.abs(u0)) / dx + 2 * nu / dx ** 2)
+    return sys, disc, {"target": target, "dt": float(dt)}
+
+
+def random_fourier_2d(seed: int, nmodes: int = 16, kmax: int = 4):
+    """Unit-variance sum of nmodes cosines with integer wavenumbers |k| <= kmax."""
+    r = _rng(seed)
+    kx = r.integers(-kmax, kmax + 1, size=nmodes)
+    ky = r.integers(-kmax, kmax + 1, size=nmodes)
+    zero = (kx == 0) & (ky == 0)
+    kx[zero] = 1
+    c = r.normal(size=nmodes)
+    ph = r.uniform(0, 2 * math.pi, size=nmodes)
+    scale = 1.0 / math.sqrt(0.5 * float(np.sum(c * c)))
+    return kx, ky, c * scale, ph
+
+
+def nonlinear_diffusion(n: int, k: float, seed: int):
+    """One ensemble member: n x n grid points on the unit square, Neumann 0 on every face."""
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dy = Differential(t), Differential(x), Differential(y)
+    kp = Param("k", k)
+    U = u(x, y, t)
+    eq = Eq(Dt(U), Dx(U ** 2 * Dx(U)) + Dy(U ** 2 * Dy(U)) + kp * U * (1 - U))
+    kx, ky, c, ph = random_fourier_2d(seed)
+    g = None
+    for a, b, cc, p in zip(kx, ky, c, ph):
+        term = float(cc) * cos(2 * math.pi * float(a) * x + 2 * math.pi * float(b) * y + float(p))
+        g = term if g is None else g + term
+    bcs = [Eq(u(x, y, 0.0), 0.5 + 0.1 * g),
+           Eq(Dx(u(0.0, y, t)), 0.0), Eq(Dx(u(1.0, y, t)), 0.0),
+           Eq(Dy(u(x, 0.0, t)), 0.0), Eq(Dy(u(x, 1.0, t)), 0.0)]
+    sys = PDESystem([eq], bcs, [(x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0)), (t, Interval(0.0, 1.0))],
+                    [x, y, t], [U], [kp])
+    disc = MOLFiniteDifference({x: n, y: n}, t, approx_order=2)
+    return sys, disc, {}
+
+
+def ensemble_members(count: int = 4096, seed_n: int = 7, seed_k: int = 8, nmin: int = 32, nmax: int = 512):
+    """(n_i, k_i, ic seed) of the ensemble: n log-uniform on [nmin, nmax], k uniform on [0, 2]."""
+    rn = _rng(seed_n)
+    rk = _rng(seed_k)
+    ns = np.rint(np.exp(rn.uniform(math.log(nmin), math.log(nmax), size=count))).astype(int)
+    ks = rk.uniform(0.0, 2.0, size=count)
+    return [(int(ns[i]), float(ks[i]), 1000 + i) for i in range(count)]
+
+
+def _kfield_modes(seed: int = 11, nmodes: int = 64, ell: float = 0.1):
+    r = _rng(seed)
+    kap = r.normal(0.0, 1.0 / ell, size=(nmodes, 3))
+    kx = np.rint(kap[:, 0] / (2 * math.pi))
+    ky = np.rint(kap[:, 1] / (2 * math.pi))
+    kz = kap[:, 2]
+    ph = r.uniform(0, 2 * math.pi, size=nmodes)
+    return kx, ky, kz, ph
+
+
+def make_kfield(seed: int = 11, sigma: float = 1.0, mean: float = 0.01):
+    """Log-normal diffusivity K = mean * exp(sigma g - sigma^2/2); g unit-variance random Fourier field."""
+    kx, ky, kz, ph = _kfield_modes(seed)
+    amp = math.sqrt(2.0 / len(kx))
+
+    def K(X, Y, Z):
+        g = np.zeros(np.broadcast(X, Y, Z).shape)
+        for a, b, c, p in zip(kx, ky, kz, ph):
+            g = g + amp * np.cos(2 * math.pi * a * X + 2 * math.pi * b * Y + c * Z + p)
+        return mean * np.exp(sigma * g - 0.5 * sigma * sigma)
+    return K
+
+
+def adr3d(N: int = 256, nz_pts: int = 258, seed_k: int = 11, target_seed: int = 12):
+    """256^3 unknowns by default: x, y periodic (N+1 points), z Dirichlet (nz_pts points, nz_pts-2 interior)."""
+    x, y, z, t = IV("x"), IV("y"), IV("z"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dy, Dz = Differential(t), Differential(x), Differential(y), Differential(z)
+    Kfun = make_kfield(seed_k)
+    K = register("K", Kfun)
+    U = u(x, y, z, t)
+    lam = Param("lambda", 0.5)
+    eq = Eq(Dt(U), Dx(K(x, y, z) * Dx(U)) + Dy(K(x, y, z) * Dy(U)) + Dz(K(x, y, z) * Dz(U))
+            + 0.3 * Dx(Dy(U)) - 1.0 * Dx(U) - 0.5 * Dy(U) - lam * U ** 2)
+    r2 = (x - 0.3) ** 2 + (y - 0.5) ** 2 + (z - 0.5) ** 2
+    ic = exp(-1.0 * r2 / (2 * 0.05 ** 2))
+    bcs = [Eq(u(x, y, z, 0.0), ic), Eq(u(0.0, y, z, t), u(1.0, y, z, t)), Eq(u(x, 0.0, z, t), u(x, 1.0, z, t)),
+           Eq(u(x, y, 0.0, t), 0.0), Eq(u(x, y, 1.0, t), 0.0)]
+    sys = PDESystem([eq], bcs, [(x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0)), (z, Interval(0.0, 1.0)),
+                                (t, Interval(0.0, 1.0))], [x, y, z, t], [U], [lam])
+    disc = MOLFiniteDifference({x: 1.0 / N, y: 1.0 / N, z: nz_pts}, t, approx_order=2,
+                               advection_scheme=UpwindScheme(1))
+    dx = 1.0 / N
+    dz = 1.0 / (nz_pts - 1)
+    kmax = 0.01 * math.exp(1.0 * 3 * math.sqrt(1.0) - 0.5)  # generous bound of the field
+    dt = 0.4 / (1.5 / dx + 2 * (3 * kmax + 0.3) / min(dx, dz) ** 2)
+    rt = _rng(target_seed)
+    return sys, disc, {"dt": float(dt), "target_seed": target_seed, "K": Kfun, "rng_target": rt}

@@ -1,0 +1,144 @@
+"""Finite-difference weight tables of the discretisation front end.
+
+The reference computes every table with Fornberg's algorithm
+(``src/discretization/schemes/fornberg_calculate_weights.jl:20-65``) and the
+DerivativeOperator constructors (``centered_diff_weights.jl:4-75``,
+``upwind_diff_weights.jl:4-91``, ``half_offset_weights.jl:4-70``).  The same
+Float64 operations, in the same order, are performed here, so the tables are
+bit-identical to the reference's; the GPU kernels receive them in the
+descriptor's weight pool.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from fractions import Fraction
+from typing import List, Sequence, Tuple
+
+
+def fornberg(m: int, z: float, nodes: Sequence[float]) -> List[float]:
+    """Weights of the m-th derivative at z on `nodes`, sum-to-zero corrected (m > 0)."""
+    n = len(nodes)
+    if not m < n:
+        raise ValueError("Not enough points for the requested order.")
+    xs = [float(v) for v in nodes]
+    z = float(z)
+    tab = [[0.0] * (m + 1) for _ in range(n)]
+    tab[0][0] = 1.0
+    c1 = 1.0
+    c4 = xs[0] - z
+    for i in range(1, n):
+        top = min(i, m)
+        c2 = 1.0
+        c5 = c4
+        c4 = xs[i] - z
+        row_prev = tab[i - 1]
+        for j in range(i):
+            c3 = xs[i] - xs[j]
+            c2 *= c3
+            if j == i - 1:
+                row = tab[i]
+                for s in range(top, 0, -1):
+                    row[s] = c1 * (s * row_prev[s - 1] - c5 * row_prev[s]) / c2
+                row[0] = -c1 * c5 * row_prev[0] / c2
+            rj = tab[j]
+            for s in range(top, 0, -1):
+                rj[s] = (c4 * rj[s] - s * rj[s - 1]) / c3
+            rj[0] = c4 * rj[0] / c3
+        c1 = c2
+    w = [r[m] for r in tab]
+    if m != 0:
+        total = w[0]
+        for v in w[1:]:
+            total = total + v       # Julia's sum of a short vector: left fold
+        w[n // 2] -= total
+    return w
+
+
+def julia_pow(x: float, d: int) -> float:
+    """``x^d`` for a runtime Int exponent as Julia evaluates it for d <= 3 (else correctly rounded)."""
+    if d == 0:
+        return 1.0
+    if d == 1:
+        return x
+    if d == 2:
+        return x * x
+    if d == 3:
+        return x * x * x
+    return float(Fraction(x) ** d)
+
+
+@dataclass
+class Operator:
+    """A DerivativeOperator in the descriptor's form (see ``mol_op1d``)."""
+    L: int
+    omin: int
+    interior: List[float]
+    low: List[List[float]]
+    high: List[List[float]]
+    bLlo: int
+    bLhi: int
+    hi_base: int = 0
+
+    @property
+    def nlo(self):
+        return len(self.low)
+
+    @property
+    def nhi(self):
+        return len(self.high)
+
+
+def centered(d: int, p: int, dx: float) -> Operator:
+    L = d + p - 1 + (d + p) % 2
+    bl = d + p
+    h = L // 2
+    s = 1.0 / julia_pow(dx, d)
+    inner = [s * w for w in fornberg(d, 0.0, range(-h, h + 1))]
+    low = [[s * w for w in fornberg(d, float(x0), range(bl))] for x0 in range(h)]
+    sg = -1.0 if d % 2 else 1.0
+    high = [[sg * w for w in lw[::-1]] for lw in low]
+    return Operator(L, -h, inner, low, high, bl, bl, 0)
+
+
+def upwind(d: int, p: int, dx: float, offside: int) -> Operator:
+    L = d + p
+    bl = d + p
+    s = 1.0 / julia_pow(dx, d)
+    inner = [s * w for w in fornberg(d, 0.0, [float(k - offside) for k in range(L)])]
+    low = [[s * w for w in fornberg(d, float(x0), [float(k) for k in range(bl)])] for x0 in range(offside)]
+    nhi = L - 1 - offside
+    neg = -1.0 / dx
+    hs = julia_pow(neg, d) if d <= 3 else float(Fraction(neg) ** d)
+    hx = [-float(k) for k in range(bl)]
+    high = [[hs * w for w in fornberg(d, -float(k), hx)] for k in range(nhi)][::-1]
+    return Operator(L, -offside, inner, low, high, bl, bl, 0)
+
+
+def half_centered(d: int, p: int, dx: float) -> Operator:
+    L = p + 2 * (d // 2) + (p % 2)
+    bl = d + p
+    e = L // 2
+    s = 1.0 / julia_pow(dx, d)
+    inner = [s * w for w in fornberg(d, 0.5, range(1 - e, e + 1))]
+    low = [[s * w for w in fornberg(d, 1.5 + k, range(1, bl + 1))] for k in range(e)]
+    sg = -1.0 if d % 2 else 1.0
+    high = [[sg * w for w in lw[::-1]] for lw in low]
+    return Operator(L, 1 - e, inner, low, high, bl, bl, 1)
+
+
+def select(op: Operator, i: int, length: int, periodic: bool) -> Tuple[List[float], List[int]]:
+    """(weights, unwrapped taps) of `op` at 1-based position i on a line of `length` points."""
+    if not periodic and i <= op.nlo:
+        return op.low[i - 1], list(range(1, op.bLlo + 1))
+    if not periodic and i > length - op.nhi:
+        return op.high[length - i - op.hi_base], list(range(length - op.bLhi + 1, length + 1))
+    return op.interior, list(range(i + op.omin, i + op.omin + op.L))
+
+
+def wrap(i: int, l: int) -> int:
+    """Periodic index wrap, u[1] == u[l] (interface_boundary.jl:33-42)."""
+    if i <= 1:
+        return i + (l - 1)
+    if i > l:
+        return i - (l - 1)
+    return i

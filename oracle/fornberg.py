@@ -1,0 +1,175 @@
+"""Oracle restatement of MethodOfLines.jl's finite-difference weight tables.
+
+Every function reproduces the reference's Float64 operation order so that the
+weights come out bit-identical (Python floats are IEEE binary64 and Python does
+not contract multiply-adds, exactly like Julia without ``@fastmath``).
+
+Test infrastructure only: imported by tests and the CPU baseline, never by the
+product package.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from fractions import Fraction
+from typing import List, Sequence
+
+
+def calculate_weights(order: int, x0: float, x: Sequence[float]) -> List[float]:
+    """Fornberg (1988) weights, ``src/discretization/schemes/fornberg_calculate_weights.jl:20-65``.
+
+    Integer node coordinates are converted exactly (Julia promotes ``Int`` to
+    ``Float64`` inside the same expressions).  The sum-to-zero correction of the
+    middle weight (``:62-65``) is applied for ``order != 0``; the sum is a
+    left-to-right fold, which is what Julia's ``sum`` does below 16 elements.
+    """
+    N = len(x)
+    assert order < N, "Not enough points for the requested order."
+    M = order
+    x = [float(v) for v in x]
+    x0 = float(x0)
+    c1 = 1.0
+    c4 = x[0] - x0
+    C = [[0.0] * (M + 1) for _ in range(N)]
+    C[0][0] = 1.0
+    for i in range(1, N):            # Julia i in 1:N-1, i1 = i+1 -> python row i
+        mn = min(i, M)
+        c2 = 1.0
+        c5 = c4
+        c4 = x[i] - x0
+        for j in range(0, i):        # Julia j in 0:i-1, j1 = j+1 -> python row j
+            c3 = x[i] - x[j]
+            c2 *= c3
+            if j == i - 1:
+                for s in range(mn, 0, -1):
+                    C[i][s] = c1 * (s * C[i - 1][s - 1] - c5 * C[i - 1][s]) / c2
+                C[i][0] = -c1 * c5 * C[i - 1][0] / c2
+            for s in range(mn, 0, -1):
+                C[j][s] = (c4 * C[j][s] - s * C[j][s - 1]) / c3
+            C[j][0] = c4 * C[j][0] / c3
+        c1 = c2
+    out = [C[k][M] for k in range(N)]
+    if order != 0:
+        if N < 16:
+            acc = out[0] + out[1] if N >= 2 else out[0]
+            for k in range(2, N):
+                acc = acc + out[k]
+        else:  # pragma: no cover - stencils here are short
+            acc = _pairwise_sum(out)
+        out[N // 2] -= acc
+    return out
+
+
+def _pairwise_sum(v):
+    if len(v) <= 16:
+        acc = v[0]
+        for a in v[1:]:
+            acc = acc + a
+        return acc
+    h = len(v) // 2
+    return _pairwise_sum(v[:h]) + _pairwise_sum(v[h:])
+
+
+def dx_pow(dx: float, d: int) -> float:
+    """``dx^d`` as Julia's ``^(::Float64, ::Int)`` gives it for d <= 3.
+
+    d = 2 is the correctly rounded square (Julia's compensated power returns
+    fl(dx*dx)), d = 3 is ``dx*dx*dx`` (Julia's explicit n == 3 branch).  For
+    d >= 4 the correctly rounded power is returned; Julia's compensated
+    power-by-squaring agrees in the overwhelming majority of cases but this is
+    not pinned.
+    """
+    if d == 0:
+        return 1.0
+    if d == 1:
+        return dx
+    if d == 2:
+        return dx * dx
+    if d == 3:
+        return dx * dx * dx
+    return float(Fraction(dx) ** d)
+
+
+@dataclass
+class DerivativeOperator:
+    """Field subset of ``src/discretization/derivative_operator.jl:1-15``."""
+    derivative_order: int
+    approximation_order: int
+    dx: float
+    stencil_length: int
+    stencil_coefs: List[float]
+    boundary_stencil_length: int
+    boundary_point_count: int
+    low_boundary_coefs: List[List[float]]
+    high_boundary_coefs: List[List[float]]
+    offside: int = 0
+    kind: str = "centered"
+
+
+def _scale(s: float, w):
+    return [s * v for v in w]
+
+
+def complete_centered_difference(d: int, p: int, dx: float) -> DerivativeOperator:
+    """``CompleteCenteredDifference``, ``centered_difference/centered_diff_weights.jl:4-75``."""
+    assert p > 1
+    L = d + p - 1 + (d + p) % 2
+    bL = d + p
+    half = L // 2
+    dummy_x = list(range(-half, half + 1))
+    left_x = list(range(0, bL))
+    bpc = half
+    spots = left_x[:half]
+    s = 1.0 / dx_pow(dx, d)
+    stencil = _scale(s, calculate_weights(d, 0.0, dummy_x))
+    low = [_scale(s, calculate_weights(d, 1.0 * x0, left_x)) for x0 in spots]
+    sign = -1.0 if d % 2 else 1.0
+    high = [[v * sign for v in reversed(w)] for w in low]
+    return DerivativeOperator(d, p, dx, L, stencil, bL, bpc, low, high, 0, "centered")
+
+
+def complete_upwind_difference(d: int, p: int, dx: float, offside: int = 0) -> DerivativeOperator:
+    """``CompleteUpwindDifference``, ``upwind_difference/upwind_diff_weights.jl:4-91``."""
+    assert offside > -1
+    L = d + p
+    bL = d + p
+    nlo = offside
+    nhi = L - 1 - offside
+    dummy_x = [float(k) for k in range(-offside, L - offside)]
+    s = 1.0 / dx_pow(dx, d)
+    stencil = _scale(s, calculate_weights(d, 0.0, dummy_x))
+    low_x = [float(k) for k in range(0, bL)]
+    low = [_scale(s, calculate_weights(d, float(x0), low_x)) for x0 in range(0, nlo)]
+    high_x = [-float(k) for k in range(0, bL)]
+    neg = -1.0 / dx
+    hs = 1.0
+    if d == 1:
+        hs = neg
+    elif d == 2:
+        hs = neg * neg
+    elif d == 3:
+        hs = neg * neg * neg
+    elif d > 3:
+        hs = float(Fraction(neg) ** d)
+    _high = [_scale(hs, calculate_weights(d, -float(k), high_x)) for k in range(0, nhi)]
+    high = list(reversed(_high))
+    # upwind operators report the high point count as boundary_point_count
+    return DerivativeOperator(d, p, dx, L, stencil, bL, nhi, low, high, offside, "upwind")
+
+
+def complete_half_centered_difference(d: int, p: int, dx: float) -> DerivativeOperator:
+    """``CompleteHalfCenteredDifference``, ``half_offset_weights.jl:4-70``."""
+    assert p > 1
+    L = p + 2 * (d // 2) + (p % 2)
+    bL = d + p
+    endpoint = L // 2
+    dummy_x = list(range(1 - endpoint, endpoint + 1))
+    left_x = list(range(1, bL + 1))
+    bpc = L // 2
+    xoffset = [1.5 + k for k in range(bpc)]
+    spots = xoffset[:L // 2]
+    s = 1.0 / dx_pow(dx, d)
+    stencil = _scale(s, calculate_weights(d, 0.5, dummy_x))
+    low = [_scale(s, calculate_weights(d, off, left_x)) for off in spots]
+    sign = -1.0 if d % 2 else 1.0
+    high = [[v * sign for v in reversed(w)] for w in low]
+    return DerivativeOperator(d, p, dx, L, stencil, bL, bpc, low, high, 0, "half")

@@ -1,0 +1,161 @@
+"""GPU parity: libmolgpu against the oracle, through the C ABI.
+
+Bars (the benchmark spec): RHS within 1e-12 relative (norm-wise) of the reference's
+discretisation; fixed-step SSPRK33 trajectories within 1e-10 relative.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from molgpu import Plan, lower, problems
+from oracle.integrators import ssprk33, tsit5
+from oracle.mol_oracle import OracleProblem
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-12
+TRAJ_TOL = 1e-10
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _setup(name, **kw):
+    sys_, disc, ex = getattr(problems, name)(**kw)
+    spec = sys_.to_spec(disc)
+    lw = lower(spec)
+    return Plan(lw), OracleProblem(spec), lw, ex
+
+
+CASES = [
+    ("heat1d", dict(n=101)),
+    ("heat1d", dict(n=7)),
+    ("brusselator", dict(N=8)),
+    ("brusselator", dict(N=64)),
+    ("brusselator", dict(N=256)),
+    ("burgers", dict(npts=65)),
+    ("burgers", dict(npts=65537)),
+    ("nonlinear_diffusion", dict(n=9, k=1.3, seed=1000)),
+    ("nonlinear_diffusion", dict(n=33, k=0.4, seed=1001)),
+    ("nonlinear_diffusion", dict(n=4, k=0.4, seed=1002)),
+    ("adr3d", dict(N=8, nz_pts=10)),
+    ("adr3d", dict(N=32, nz_pts=34)),
+]
+
+
+@pytest.mark.parametrize("name,kw", CASES)
+def test_rhs_parity(gpu_lib, name, kw):
+    plan, orc, lw, _ = _setup(name, **kw)
+    rng = np.random.default_rng(11)
+    u = lw.u0 * (1 + 0.05 * rng.standard_normal(lw.n_unknowns)) + 0.01 * rng.standard_normal(lw.n_unknowns)
+    for t in (0.0, 1.7):
+        du = np.zeros(lw.n_unknowns)
+        plan.rhs(du, u, None, t)
+        ref = orc.rhs(u, t)
+        assert _rel(du, ref) < RHS_TOL, (name, t, _rel(du, ref))
+
+
+def test_rhs_parameters_runtime(gpu_lib):
+    """p passed at call time (the ODEProblem's parameter vector) overrides the defaults."""
+    plan, orc, lw, _ = _setup("brusselator", N=32)
+    u = lw.u0.copy()
+    p = np.array([3.5])
+    du = np.zeros(lw.n_unknowns)
+    plan.rhs(du, u, p, 0.2)
+    assert _rel(du, orc.rhs(u, 0.2, p)) < RHS_TOL
+
+
+TRAJ = [
+    ("brusselator", dict(N=32), 40, None),
+    ("burgers", dict(npts=257), 60, None),
+    ("nonlinear_diffusion", dict(n=17, k=1.1, seed=1003), 40, 1e-5),
+    ("adr3d", dict(N=12, nz_pts=14), 20, None),
+    ("heat1d", dict(n=21), 50, 1e-5),
+]
+
+
+@pytest.mark.parametrize("name,kw,nsteps,dt", TRAJ)
+def test_ssprk33_trajectory(gpu_lib, name, kw, nsteps, dt):
+    plan, orc, lw, ex = _setup(name, **kw)
+    if dt is None:
+        dt = ex.get("dt", ex.get("dt_ssprk", 1e-5))
+    u = lw.u0.copy()
+    plan.step_ssprk33(u, dt, nsteps, t0=1.0)
+    ref, _ = ssprk33(lambda v, t: orc.rhs(v, t), lw.u0, 1.0, dt, nsteps)
+    assert _rel(u, ref) < TRAJ_TOL, _rel(u, ref)
+
+
+def test_ssprk33_graph_chunks_and_tail(gpu_lib):
+    """Steps replayed as captured CUDA graphs (chunks of 16) plus a directly launched tail."""
+    plan, orc, lw, ex = _setup("brusselator", N=16)
+    dt = ex["dt_ssprk"]
+    a = lw.u0.copy()
+    plan.step_ssprk33(a, dt, 37, t0=1.05)
+    b = lw.u0.copy()
+    for k in range(37):
+        plan.step_ssprk33(b, dt, 1, t0=1.05 + k * dt)
+    ref, _ = ssprk33(lambda v, t: orc.rhs(v, t), lw.u0, 1.05, dt, 37)
+    assert _rel(a, ref) < TRAJ_TOL
+    assert _rel(a, b) < 1e-13
+
+
+def test_tsit5_heat_exact(gpu_lib):
+    """Config 1: u0 = sin(pi x) decays exactly as exp(lam t) in the semi-discrete system."""
+    plan, orc, lw, _ = _setup("heat1d", n=101)
+    u = lw.u0.copy()
+    st = plan.solve_tsit5(u, 0.0, 0.1, 1e-10, 1e-10)
+    dx = 0.01
+    lam = -(4 / dx ** 2) * math.sin(math.pi * dx / 2) ** 2
+    assert abs(st["t"] - 0.1) < 1e-15
+    assert np.max(np.abs(u - math.exp(lam * 0.1) * lw.u0)) < 1e-9
+    ref, rst = tsit5(lambda v, t: orc.rhs(v, t), lw.u0, 0.0, 0.1, 1e-10, 1e-10)
+    assert _rel(u, ref) < 1e-9
+    assert abs(st["naccept"] - rst["naccept"]) <= 2
+
+
+def test_tsit5_brusselator_short(gpu_lib):
+    plan, orc, lw, _ = _setup("brusselator", N=16)
+    u = lw.u0.copy()
+    st = plan.solve_tsit5(u, 0.0, 1.5, 1e-8, 1e-8)
+    ref, rst = tsit5(lambda v, t: orc.rhs(v, t), lw.u0, 0.0, 1.5, 1e-8, 1e-8)
+    assert _rel(u, ref) < 1e-7
+    assert st["naccept"] > 10
+
+
+def test_f32state_error_reported(gpu_lib):
+    """Float32-state variant: same program in FP32; error against FP64 stays at FP32 level."""
+    plan, orc, lw, ex = _setup("brusselator", N=64)
+    u64 = lw.u0.copy()
+    du64 = np.zeros_like(u64)
+    plan.rhs(du64, u64, None, 0.3)
+    u32 = u64.astype(np.float32)
+    du32 = np.zeros_like(u32)
+    plan.rhs(du32, u32, None, 0.3)
+    assert _rel(du32.astype(np.float64), du64) < 1e-4
+    dt = ex["dt_ssprk"]
+    a = u64.copy()
+    plan.step_ssprk33(a, dt, 20, t0=0.0)
+    b = u32.copy()
+    plan.step_ssprk33(b, dt, 20, t0=0.0)
+    assert _rel(b.astype(np.float64), a) < 1e-5
+
+
+def test_device_pointers_match_host(gpu_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    plan, orc, lw, ex = _setup("burgers", npts=1025)
+    u = torch.tensor(lw.u0, device="cuda")
+    du = torch.zeros_like(u)
+    plan.rhs(du, u, None, 0.0)
+    torch.cuda.synchronize()
+    host = np.zeros(lw.n_unknowns)
+    plan.rhs(host, lw.u0, None, 0.0)
+    assert np.array_equal(du.cpu().numpy(), host)
+    plan.step_ssprk33(u, ex["dt"], 33, t0=0.0)
+    torch.cuda.synchronize()
+    h = lw.u0.copy()
+    plan.step_ssprk33(h, ex["dt"], 33, t0=0.0)
+    assert np.array_equal(u.cpu().numpy(), h)
