@@ -108,8 +108,10 @@ __device__ __forceinline__ T load_pt(const DevProb<T>& P, const T* u, int f, int
     int nout = 0, dout = 0, side = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
+        if ((P.permask[f] >> d) & 1) I[d] = wrap_periodic(I[d], P.n[d]);
+        // anything still outside the interior (including a tap that one wrap did not bring
+        // back) resolves through the boundary rows below and is never dereferenced
         if (I[d] <= P.lo[d]) {
-            if ((P.permask[f] >> d) & 1) { I[d] = wrap_periodic(I[d], P.n[d]); continue; }
             ++nout; dout = d; side = 0;
         } else if (I[d] > P.n[d] - P.up[d]) {
             ++nout; dout = d; side = 1;
@@ -162,9 +164,12 @@ struct TapSel {
 __device__ __forceinline__ TapSel select_taps(const mol_op1d& op, int i, int len, bool per) {
     TapSel s;
     if (!per && i <= op.nlo) {
-        s.woff = op.w_lo + (long long)(i - 1) * op.bLlo; s.first = 1; s.cnt = op.bLlo; s.wrap = false;
+        const int ti = i < 1 ? 0 : i - 1;  // positions below 1 only occur in malformed descriptors
+        s.woff = op.w_lo + (long long)ti * op.bLlo; s.first = 1; s.cnt = op.bLlo; s.wrap = false;
     } else if (!per && i > len - op.nhi) {
-        s.woff = op.w_hi + (long long)(len - i - op.hi_base) * op.bLhi; s.first = len - op.bLhi + 1;
+        int ti = len - i - op.hi_base;
+        ti = ti < 0 ? 0 : ti;
+        s.woff = op.w_hi + (long long)ti * op.bLhi; s.first = len - op.bLhi + 1;
         s.cnt = op.bLhi; s.wrap = false;
     } else {
         s.woff = op.w_int; s.first = i + op.omin; s.cnt = op.L; s.wrap = per;
@@ -357,6 +362,7 @@ __device__ __noinline__ T nonlinlap_face(const DevProb<T>& P, const mol_term& tm
             case MOL_OP_AUX: {
                 // face array: extent n[d]+1 along d (index Ih), full-grid extents elsewhere
                 const int ax = tm.aux0 + in.imm;
+                Ih = Ih < 0 ? 0 : (Ih > P.n[d] ? P.n[d] : Ih);
                 long long e0 = P.n[0] + (d == 0), e1 = P.n[1] + (d == 1);
                 long long j0 = d == 0 ? Ih : I[0] - 1, j1 = d == 1 ? Ih : I[1] - 1, j2 = d == 2 ? Ih : I[2] - 1;
                 R = P.aux[P.aux_off[ax] + j0 + e0 * (j1 + e1 * j2)];

@@ -35,10 +35,9 @@ class DescInterp:
         I = list(I)
         out = []
         for d in range(3):
+            if self.per[f][d]:
+                I[d] = wrap(I[d], self.n[d])
             if I[d] <= self.lo[d]:
-                if self.per[f][d]:
-                    I[d] = wrap(I[d], self.n[d])
-                    continue
                 out.append((d, 0))
             elif I[d] > self.n[d] - self.up[d]:
                 out.append((d, 1))
