@@ -26,7 +26,18 @@
 #ifndef MOLGPU_H
 #define MOLGPU_H
 
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
+#else
+/* runtime compilation (NVRTC) of the generated right-hand side sees this header too */
+typedef signed char int8_t;
+typedef short int16_t;
+typedef int int32_t;
+typedef long long int64_t;
+typedef unsigned short uint16_t;
+typedef unsigned int uint32_t;
+typedef unsigned long long uint64_t;
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -178,11 +189,22 @@ const char* mol_status_string(int status);
  * Copies the descriptor and every array it points to. */
 int mol_plan_create(const mol_problem_desc* desc, mol_plan** out);
 int mol_plan_destroy(mol_plan* plan);
+/* generate_code(pdesys, disc) (src/MOL_discretization.jl:208-217): the CUDA source the
+ * library generates for this problem structure; needs no device.  `needed` receives
+ * the buffer size including the terminating NUL. */
+int mol_generate_code(const mol_problem_desc* desc, char* buf, int64_t bufsize, int64_t* needed);
+/* Generates and compiles (NVRTC, sm_103a) without loading; needs no device.  `log`
+ * receives the compiler log on failure. */
+int mol_codegen_compile_check(const mol_problem_desc* desc, char* log, int64_t logsize);
 const char* mol_last_error(const mol_plan* plan);
 int mol_plan_set_stream(mol_plan* plan, void* cuda_stream);
 int64_t mol_plan_n_unknowns(const mol_plan* plan);
 /* Kernel launches issued by this process so far (all plans). */
 int64_t mol_launch_count(void);
+/* 1 when the plan runs the generated (NVRTC-compiled) right-hand side, 0 for the
+ * register-machine interpreter; the source text (or the reason it is off). */
+int mol_plan_uses_codegen(const mol_plan* plan);
+const char* mol_plan_codegen_source(const mol_plan* plan);
 
 /* ------------------------------------------------------------------------ */
 /* Hot path                                                                  */

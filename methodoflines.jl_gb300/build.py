@@ -36,17 +36,40 @@ def _stale(obj: str, src: str) -> bool:
     if not os.path.exists(obj):
         return True
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    deps.append(os.path.join(BUILD_DIR, "mol_embedded.inc"))
     deps.append(os.path.join(ROOT, "include", "molgpu.h"))
     t = os.path.getmtime(obj)
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+EMBED = ["molgpu.h", "mol_device.cuh", "mol_vjp.cuh", "mol_kernels.cuh"]
+
+
+def _embed() -> None:
+    """Write the device headers as C string literals: NVRTC compiles the generated code against them."""
+    texts = []
+    for name in EMBED:
+        path = os.path.join(ROOT, "include", name) if name == "molgpu.h" else os.path.join(CSRC, name)
+        txt = open(path).read()
+        if ")MOLRAW\"" in txt:
+            raise RuntimeError("raw-string delimiter found in " + name)
+        texts.append(txt)
+    body = "static const char* const kEmbedNames[] = {" + ", ".join('"%s"' % n for n in EMBED) + "};\n"
+    body += "static const char* const kEmbedTexts[] = {\n" + ",\n".join('R"MOLRAW(' + t + ')MOLRAW"' for t in texts)
+    body += "};\n"
+    out = os.path.join(BUILD_DIR, "mol_embedded.inc")
+    if not os.path.exists(out) or open(out).read() != body:
+        with open(out, "w") as fh:
+            fh.write(body)
+
+
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(BUILD_DIR, exist_ok=True)
+    _embed()
     cc = nvcc()
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"),
-                     "-I" + CSRC]
+                     "-I" + CSRC, "-I" + BUILD_DIR]
     objs = []
     jobs = []
     for src in sources():
@@ -68,7 +91,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             list(ex.map(run, jobs))
     if force or jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"] * 0)
+        run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"])
         os.replace(tmp, LIB)
     return LIB
 

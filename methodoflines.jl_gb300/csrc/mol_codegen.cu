@@ -1,0 +1,908 @@
+// Generated right-hand side: the GPU counterpart of the straight-line f! that
+// ModelingToolkit compiles for a discretised system (src/MOL_discretization.jl:171-201).
+//
+// From a validated descriptor the library writes CUDA C++ for one problem
+// *structure*: the pointwise program becomes SSA statements, every derivative
+// term becomes a function with an interior fast path (compile-time tap offsets,
+// direct strided loads, structural zero weights dropped) and the generic
+// boundary path (tap tables, wrap, observed boundary rows), and the reverse
+// sweep of the same statements gives the vector-Jacobian product.  Grid sizes,
+// weights, parameters and aux arrays stay runtime data, so one compiled module
+// serves every grid size of a structure (and every member of an ensemble).
+// The module is compiled with NVRTC for sm_103a and loaded through the CUDA
+// runtime's library API; the hand-written kernel templates of mol_kernels.cuh
+// are instantiated with the generated cell.
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "mol_codegen.h"
+
+#include "mol_embedded.inc"  // kEmbedNames / kEmbedTexts: the device headers, embedded at build time
+
+namespace mol {
+
+namespace {
+
+std::string lit(double v) {
+    if (!std::isfinite(v)) return "";
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "T(%a)", v);
+    return buf;
+}
+
+struct Emitter {
+    std::ostringstream o;
+    template <class X>
+    Emitter& operator<<(const X& x) {
+        o << x;
+        return *this;
+    }
+};
+
+std::string v(int pc) { return "v" + std::to_string(pc); }
+std::string a(int pc) { return "a" + std::to_string(pc); }
+
+// Register program -> SSA: for each instruction the SSA ids of its register operands.
+struct SSA {
+    std::vector<mol_instr> ins;
+    std::vector<int> ia, ib, ic;
+    bool ok = true;
+};
+
+SSA to_ssa(const mol_problem_desc* d, int prog) {
+    SSA s;
+    const int start = d->prog_ranges[2 * prog], len = d->prog_ranges[2 * prog + 1];
+    std::vector<int> last(MOL_MAX_REGS, -1);
+    for (int pc = 0; pc < len; ++pc) {
+        const mol_instr in = d->code[start + pc];
+        s.ins.push_back(in);
+        auto rd = [&](int r) { return (r >= 0 && r < MOL_MAX_REGS) ? last[r] : -1; };
+        int A = -1, B = -1, C = -1;
+        switch (in.op) {
+            case MOL_OP_NEG: case MOL_OP_POWI: case MOL_OP_FN: case MOL_OP_OUT: case MOL_OP_UPWIND:
+                A = rd(in.a);
+                break;
+            case MOL_OP_ADD: case MOL_OP_SUB: case MOL_OP_MUL: case MOL_OP_DIV: case MOL_OP_POW: case MOL_OP_CMP:
+                A = rd(in.a);
+                B = rd(in.b);
+                break;
+            case MOL_OP_IFELSE:
+                A = rd(in.a);
+                B = rd(in.b);
+                C = rd(in.c);
+                break;
+            default:
+                break;
+        }
+        if ((A == -2) || (B == -2) || (C == -2)) s.ok = false;
+        s.ia.push_back(A);
+        s.ib.push_back(B);
+        s.ic.push_back(C);
+        if (in.op != MOL_OP_OUT) last[in.dst] = pc;
+    }
+    return s;
+}
+
+// How leaves of a program are read and how their adjoints are written.
+struct Leaves {
+    // forward expressions
+    virtual std::string field(int f) const = 0;
+    virtual std::string aux(int k) const = 0;
+    virtual std::string coord(int d) const = 0;
+    virtual std::string term(int k) const = 0;
+    // reverse statements (adjoint value given as expression `g`)
+    virtual std::string field_adj(int f, const std::string& g) const = 0;
+    virtual std::string aux_adj(int k, const std::string& g) const = 0;
+    virtual std::string term_adj(int k, const std::string& g) const = 0;
+    virtual ~Leaves() {}
+};
+
+std::string fn_expr(int fn, const std::string& x) {
+    static const char* names[] = {"sin", "cos", "tan", "exp", "log", "sqrt", "fabs", "tanh", "sinh", "cosh", "atan"};
+    return std::string(names[fn]) + "(" + x + ")";
+}
+
+// d fn(x)/dx given x and r = fn(x)
+std::string fn_deriv(int fn, const std::string& x, const std::string& r) {
+    switch (fn) {
+        case MOL_FN_SIN: return "cos(" + x + ")";
+        case MOL_FN_COS: return "(-sin(" + x + "))";
+        case MOL_FN_TAN: return "(T(1) + " + r + " * " + r + ")";
+        case MOL_FN_EXP: return r;
+        case MOL_FN_LOG: return "(T(1) / " + x + ")";
+        case MOL_FN_SQRT: return "(T(0.5) / " + r + ")";
+        case MOL_FN_ABS: return "((" + x + ") < T(0) ? T(-1) : T(1))";
+        case MOL_FN_TANH: return "(T(1) - " + r + " * " + r + ")";
+        case MOL_FN_SINH: return "cosh(" + x + ")";
+        case MOL_FN_COSH: return "sinh(" + x + ")";
+        case MOL_FN_ATAN: return "(T(1) / (T(1) + " + x + " * " + x + "))";
+    }
+    return "T(0)";
+}
+
+// Forward statements of an SSA program; `outs` receives the OUT assignments.
+void emit_forward(Emitter& e, const mol_problem_desc* d, const SSA& s, const Leaves& L, const std::string& pre,
+                  std::vector<std::pair<int, int>>* outs, bool keep_terms) {
+    for (size_t pc = 0; pc < s.ins.size(); ++pc) {
+        const mol_instr& in = s.ins[pc];
+        const std::string V = pre + v((int)pc);
+        const std::string A = s.ia[pc] >= 0 ? pre + v(s.ia[pc]) : "";
+        const std::string B = s.ib[pc] >= 0 ? pre + v(s.ib[pc]) : "";
+        const std::string C = s.ic[pc] >= 0 ? pre + v(s.ic[pc]) : "";
+        switch (in.op) {
+            case MOL_OP_CONST: {
+                std::string l = lit(d->consts[in.imm]);
+                if (l.empty()) l = "P.consts[" + std::to_string(in.imm) + "]";
+                e << "    const T " << V << " = " << l << ";\n";
+                break;
+            }
+            case MOL_OP_PARAM: e << "    const T " << V << " = p[" << in.imm << "];\n"; break;
+            case MOL_OP_FIELD: e << "    const T " << V << " = " << L.field(in.imm) << ";\n"; break;
+            case MOL_OP_AUX: e << "    const T " << V << " = " << L.aux(in.imm) << ";\n"; break;
+            case MOL_OP_COORD: e << "    const T " << V << " = " << L.coord(in.imm) << ";\n"; break;
+            case MOL_OP_TIME: e << "    const T " << V << " = t;\n"; break;
+            case MOL_OP_TERM: e << "    const T " << V << " = " << L.term(in.imm) << ";\n"; break;
+            case MOL_OP_UPWIND:
+                e << "    const T " << pre << "tv" << pc << " = (" << A << " < T(0)) ? " << L.term(in.b) << " : "
+                  << L.term(in.c) << ";\n";
+                e << "    const T " << V << " = " << A << " * " << pre << "tv" << pc << ";\n";
+                break;
+            case MOL_OP_ADD: e << "    const T " << V << " = " << A << " + " << B << ";\n"; break;
+            case MOL_OP_SUB: e << "    const T " << V << " = " << A << " - " << B << ";\n"; break;
+            case MOL_OP_MUL: e << "    const T " << V << " = " << A << " * " << B << ";\n"; break;
+            case MOL_OP_DIV: e << "    const T " << V << " = " << A << " / " << B << ";\n"; break;
+            case MOL_OP_NEG: e << "    const T " << V << " = -" << A << ";\n"; break;
+            case MOL_OP_POWI:
+                if (in.imm == 2) e << "    const T " << V << " = " << A << " * " << A << ";\n";
+                else if (in.imm == 3) e << "    const T " << V << " = " << A << " * " << A << " * " << A << ";\n";
+                else if (in.imm == 1) e << "    const T " << V << " = " << A << ";\n";
+                else if (in.imm == 0) e << "    const T " << V << " = T(1);\n";
+                else e << "    const T " << V << " = powi(" << A << ", " << in.imm << ");\n";
+                break;
+            case MOL_OP_POW: e << "    const T " << V << " = pow(" << A << ", " << B << ");\n"; break;
+            case MOL_OP_FN: e << "    const T " << V << " = " << fn_expr(in.imm, A) << ";\n"; break;
+            case MOL_OP_CMP: {
+                static const char* ops[] = {"<=", "<", ">=", ">", "=="};
+                e << "    const T " << V << " = (" << A << " " << ops[in.imm] << " " << B << ") ? T(1) : T(0);\n";
+                break;
+            }
+            case MOL_OP_IFELSE:
+                e << "    const T " << V << " = (" << A << " != T(0)) ? " << B << " : " << C << ";\n";
+                break;
+            case MOL_OP_OUT:
+                if (outs) outs->push_back({in.imm, s.ia[pc]});
+                break;
+            default: break;
+        }
+        (void)keep_terms;
+    }
+}
+
+// Reverse sweep.  `seed(k)` is the adjoint expression of output k.
+template <class SeedFn>
+void emit_reverse(Emitter& e, const SSA& s, const Leaves& L, const std::string& pre, SeedFn seed) {
+    const int n = (int)s.ins.size();
+    for (int pc = 0; pc < n; ++pc)
+        if (s.ins[pc].op != MOL_OP_OUT) e << "    T " << pre << a(pc) << " = T(0);\n";
+    for (int pc = n - 1; pc >= 0; --pc) {
+        const mol_instr& in = s.ins[pc];
+        const std::string G = pre + a(pc);
+        const std::string V = pre + v(pc);
+        const std::string A = s.ia[pc] >= 0 ? pre + v(s.ia[pc]) : "";
+        const std::string B = s.ib[pc] >= 0 ? pre + v(s.ib[pc]) : "";
+        const std::string GA = s.ia[pc] >= 0 ? pre + a(s.ia[pc]) : "";
+        const std::string GB = s.ib[pc] >= 0 ? pre + a(s.ib[pc]) : "";
+        const std::string GC = s.ic[pc] >= 0 ? pre + a(s.ic[pc]) : "";
+        switch (in.op) {
+            case MOL_OP_OUT: e << "    " << GA << " += " << seed(in.imm) << ";\n"; break;
+            case MOL_OP_PARAM: e << "    lp[" << in.imm << "] += " << G << ";\n"; break;
+            case MOL_OP_FIELD: e << L.field_adj(in.imm, G); break;
+            case MOL_OP_AUX: e << L.aux_adj(in.imm, G); break;
+            case MOL_OP_TERM: e << L.term_adj(in.imm, G); break;
+            case MOL_OP_UPWIND:
+                e << "    " << GA << " += " << G << " * " << pre << "tv" << pc << ";\n";
+                e << "    if (" << A << " < T(0)) {\n" << L.term_adj(in.b, G + " * " + A) << "    } else {\n"
+                  << L.term_adj(in.c, G + " * " + A) << "    }\n";
+                break;
+            case MOL_OP_ADD: e << "    " << GA << " += " << G << "; " << GB << " += " << G << ";\n"; break;
+            case MOL_OP_SUB: e << "    " << GA << " += " << G << "; " << GB << " -= " << G << ";\n"; break;
+            case MOL_OP_MUL:
+                e << "    " << GA << " += " << G << " * " << B << "; " << GB << " += " << G << " * " << A << ";\n";
+                break;
+            case MOL_OP_DIV:
+                e << "    " << GA << " += " << G << " / " << B << "; " << GB << " -= " << G << " * " << V << " / " << B
+                  << ";\n";
+                break;
+            case MOL_OP_NEG: e << "    " << GA << " -= " << G << ";\n"; break;
+            case MOL_OP_POWI:
+                if (in.imm == 0) break;
+                e << "    " << GA << " += " << G << " * T(" << in.imm << ") * powi(" << A << ", " << (in.imm - 1)
+                  << ");\n";
+                break;
+            case MOL_OP_POW:
+                e << "    " << GA << " += " << G << " * " << B << " * pow(" << A << ", " << B << " - T(1));\n";
+                e << "    " << GB << " += " << G << " * " << V << " * log(" << A << ");\n";
+                break;
+            case MOL_OP_FN: e << "    " << GA << " += " << G << " * " << fn_deriv(in.imm, A, V) << ";\n"; break;
+            case MOL_OP_IFELSE:
+                e << "    if (" << A << " != T(0)) " << GB << " += " << G << "; else " << GC << " += " << G << ";\n";
+                break;
+            default: break;
+        }
+    }
+}
+
+bool zero_w(const mol_problem_desc* d, long long off) { return d->weights[off] == 0.0; }
+
+// Leaves of the cell program.
+struct CellLeaves : Leaves {
+    std::string field(int f) const override { return "u[(long long)" + std::to_string(f) + " * P.ncell + c]"; }
+    std::string aux(int k) const override { return "P.aux[P.aux_off[" + std::to_string(k) + "] + c]"; }
+    std::string coord(int dd) const override {
+        return "P.coords[" + std::to_string(dd) + "][I[" + std::to_string(dd) + "] - 1]";
+    }
+    std::string term(int k) const override { return "gt" + std::to_string(k) + "<T>(P, u, c, I, t, p)"; }
+    std::string field_adj(int f, const std::string& g) const override {
+        return "    atomicAdd(lam_u + (long long)" + std::to_string(f) + " * P.ncell + c, " + g + ");\n";
+    }
+    std::string aux_adj(int k, const std::string& g) const override {
+        return "    if (lam_aux) atomicAdd(lam_aux + P.aux_off[" + std::to_string(k) + "] + c, " + g + ");\n";
+    }
+    std::string term_adj(int k, const std::string& g) const override {
+        return "    gt" + std::to_string(k) + "_vjp<T>(P, u, c, I, t, p, " + g + ", lam_u, lp, lam_aux);\n";
+    }
+};
+
+// Leaves of a nonlinear-Laplacian face program: fields are the interpolated
+// values uf<f>, aux arrays the face values fa<k>.
+struct FaceLeaves : Leaves {
+    std::string tag;
+    explicit FaceLeaves(std::string t) : tag(std::move(t)) {}
+    std::string field(int f) const override { return tag + "uf" + std::to_string(f); }
+    std::string aux(int k) const override { return tag + "fa" + std::to_string(k); }
+    std::string coord(int) const override { return "T(0)"; }
+    std::string term(int) const override { return "T(0)"; }
+    std::string field_adj(int f, const std::string& g) const override {
+        return "    " + tag + "guf" + std::to_string(f) + " += " + g + ";\n";
+    }
+    std::string aux_adj(int k, const std::string& g) const override {
+        return "    " + tag + "gfa" + std::to_string(k) + " += " + g + ";\n";
+    }
+    std::string term_adj(int, const std::string&) const override { return ""; }
+};
+
+void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
+    const mol_term& tm = d->terms[k];
+    const mol_op1d& o = d->ops[tm.op];
+    const std::string K = std::to_string(k), F = std::to_string(tm.field), D = std::to_string(tm.dim);
+    std::vector<int> nz;
+    for (int m = 0; m < o.L; ++m)
+        if (!zero_w(d, o.w_int + m)) nz.push_back(m);
+    auto fast_cond = "fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + D + ", I[" + D + "])";
+    e << "template <class T>\n__device__ __forceinline__ T gt" << K
+      << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) {\n"
+      << "    if (" << fast_cond << ") {\n"
+      << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int;\n"
+      << "        const T* __restrict__ b = u + (long long)" << F << " * P.ncell + c;\n"
+      << "        const long long s = gstride(P, " << D << ");\n";
+    if (nz.empty()) {
+        e << "        return T(0);\n";
+    } else {
+        for (size_t q = 0; q < nz.size(); ++q) {
+            const int m = nz[q];
+            const std::string tap = "b[(long long)(" + std::to_string(o.omin + m) + ") * s]";
+            if (q == 0) e << "        T acc = w[" << m << "] * " << tap << ";\n";
+            else e << "        acc = fma(w[" << m << "], " << tap << ", acc);\n";
+        }
+        e << "        return acc;\n";
+    }
+    e << "    }\n    return apply_op(P, P.ops[" << tm.op << "], u, " << F << ", " << D << ", I, t, p);\n}\n";
+    // vjp
+    e << "template <class T>\n__device__ __forceinline__ void gt" << K
+      << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
+         "T g, T* lam_u, T* lp, T* lam_aux) {\n"
+      << "    if (" << fast_cond << ") {\n"
+      << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int;\n"
+      << "        T* b = lam_u + (long long)" << F << " * P.ncell + c;\n"
+      << "        const long long s = gstride(P, " << D << ");\n";
+    for (int m : nz)
+        e << "        atomicAdd(b + (long long)(" << (o.omin + m) << ") * s, g * w[" << m << "]);\n";
+    e << "        return;\n    }\n    scatter_op(P, P.ops[" << tm.op << "], lam_u, " << F << ", " << D << ", I, I[" << D
+      << "], P.n[" << D << "], g, t, p);\n}\n";
+}
+
+void emit_mixed(Emitter& e, const mol_problem_desc* d, int k) {
+    const mol_term& tm = d->terms[k];
+    const mol_op1d& o1 = d->ops[tm.op];
+    const mol_op1d& o2 = d->ops[tm.op2];
+    const std::string K = std::to_string(k), F = std::to_string(tm.field);
+    const std::string D1 = std::to_string(tm.dim), D2 = std::to_string(tm.dim2);
+    std::vector<std::pair<int, int>> nz;
+    for (int x = 0; x < o1.L; ++x)
+        for (int y = 0; y < o2.L; ++y)
+            if (!zero_w(d, o1.w_int + x) && !zero_w(d, o2.w_int + y)) nz.push_back({x, y});
+    const std::string cond = "fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + D1 + ", I[" + D1 +
+                             "]) && fast_line(P, P.ops[" + std::to_string(tm.op2) + "], " + F + ", " + D2 + ", I[" +
+                             D2 + "])";
+    // the product weights sit in the pool at term.reserved0 (filled by the library), row-major [L1][L2]
+    auto body = [&](bool vjp) {
+        e << "    if (" << cond << ") {\n"
+          << "        const T* __restrict__ ww = P.w + P.terms[" << k << "].reserved0;\n"
+          << "        const long long s1 = gstride(P, " << D1 << "), s2 = gstride(P, " << D2 << ");\n";
+        if (!vjp) e << "        const T* __restrict__ b = u + (long long)" << F << " * P.ncell + c;\n";
+        else e << "        T* b = lam_u + (long long)" << F << " * P.ncell + c;\n";
+        for (size_t q = 0; q < nz.size(); ++q) {
+            const int x = nz[q].first, y = nz[q].second;
+            const std::string W = "ww[" + std::to_string(x * o2.L + y) + "]";
+            const std::string off = "(long long)(" + std::to_string(o1.omin + x) + ") * s1 + (long long)(" +
+                                    std::to_string(o2.omin + y) + ") * s2";
+            if (vjp) e << "        atomicAdd(b + " << off << ", g * " << W << ");\n";
+            else if (q == 0) e << "        T acc = " << W << " * b[" << off << "];\n";
+            else e << "        acc = fma(" << W << ", b[" << off << "], acc);\n";
+        }
+        if (vjp) e << "        return;\n    }\n";
+        else e << "        return " << (nz.empty() ? "T(0)" : "acc") << ";\n    }\n";
+    };
+    e << "template <class T>\n__device__ __forceinline__ T gt" << K
+      << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) {\n";
+    body(false);
+    e << "    return apply_mixed(P, P.terms[" << k << "], u, I, t, p);\n}\n";
+    e << "template <class T>\n__device__ __forceinline__ void gt" << K
+      << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
+         "T g, T* lam_u, T* lp, T* lam_aux) {\n";
+    body(true);
+    e << "    scatter_mixed(P, P.terms[" << k << "], lam_u, I, g, t, p);\n}\n";
+}
+
+void emit_weno(Emitter& e, const mol_problem_desc* d, int k) {
+    const mol_term& tm = d->terms[k];
+    const std::string K = std::to_string(k), F = std::to_string(tm.field), D = std::to_string(tm.dim);
+    const std::string cond = "fast_weno(P, " + F + ", " + D + ", I[" + D + "])";
+    e << "template <class T>\n__device__ __forceinline__ T gt" << K
+      << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) {\n"
+      << "    if (" << cond << ") {\n"
+      << "        const T* __restrict__ b = u + (long long)" << F << " * P.ncell + c;\n"
+      << "        const long long s = gstride(P, " << D << ");\n"
+      << "        return weno5_point<T>(b[-2 * s], b[-s], b[0], b[s], b[2 * s], T(P.terms[" << K << "].eps), T(P.terms["
+      << K << "].dx));\n    }\n"
+      << "    return apply_weno(P, P.terms[" << K << "], u, I, t, p);\n}\n";
+    e << "template <class T>\n__device__ __forceinline__ void gt" << K
+      << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
+         "T g, T* lam_u, T* lp, T* lam_aux) {\n"
+      << "    if (" << cond << ") {\n"
+      << "        const T* __restrict__ b = u + (long long)" << F << " * P.ncell + c;\n"
+      << "        T* lb = lam_u + (long long)" << F << " * P.ncell + c;\n"
+      << "        const long long s = gstride(P, " << D << ");\n"
+      << "        T gr[5];\n"
+      << "        weno5_grad<T>(b[-2 * s], b[-s], b[0], b[s], b[2 * s], T(P.terms[" << K << "].eps), T(P.terms[" << K
+      << "].dx), gr);\n"
+      << "#pragma unroll\n        for (int m = 0; m < 5; ++m) atomicAdd(lb + (long long)(m - 2) * s, g * gr[m]);\n"
+      << "        return;\n    }\n"
+      << "    scatter_weno(P, P.terms[" << K << "], u, lam_u, I, g, t, p);\n}\n";
+}
+
+// Nonlinear Laplacian.  The face value a(x~, u~) * (D_inner u) at half point Ih
+// is emitted twice: with compile-time offsets for interior cells and with
+// runtime tap tables for the rest.
+void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
+    const mol_term& tm = d->terms[k];
+    const mol_op1d& oo = d->ops[tm.op];
+    const mol_op1d& oi = d->ops[tm.op2];
+    const mol_op1d& op = d->ops[tm.op3];
+    const std::string K = std::to_string(k), F = std::to_string(tm.field), D = std::to_string(tm.dim);
+    SSA fs;
+    bool has_prog = tm.prog >= 0;
+    std::vector<int> used_fields, used_aux;
+    if (has_prog) {
+        fs = to_ssa(d, tm.prog);
+        for (auto& in : fs.ins) {
+            if (in.op == MOL_OP_FIELD && std::find(used_fields.begin(), used_fields.end(), in.imm) == used_fields.end())
+                used_fields.push_back(in.imm);
+            if (in.op == MOL_OP_AUX && std::find(used_aux.begin(), used_aux.end(), in.imm) == used_aux.end())
+                used_aux.push_back(in.imm);
+        }
+    }
+    std::vector<int> nzo;
+    for (int m = 0; m < oo.L; ++m)
+        if (!zero_w(d, oo.w_int + m)) nzo.push_back(m);
+    std::vector<int> nzi, nzp;
+    for (int m = 0; m < oi.L; ++m)
+        if (!zero_w(d, oi.w_int + m)) nzi.push_back(m);
+    for (int m = 0; m < op.L; ++m)
+        if (!zero_w(d, op.w_int + m)) nzp.push_back(m);
+    const std::string opi = std::to_string(tm.op2), opp = std::to_string(tm.op3), opo = std::to_string(tm.op);
+
+    // face program (forward), given uf*/fa* variables named with `tag`, result in `tag`a
+    auto face_forward = [&](const std::string& tag) {
+        if (!has_prog) {
+            e << "    const T " << tag << "a = T(1);\n";
+            return;
+        }
+        FaceLeaves L(tag);
+        std::vector<std::pair<int, int>> outs;
+        emit_forward(e, d, fs, L, tag, &outs, false);
+        e << "    const T " << tag << "a = " << (outs.empty() ? "T(1)" : tag + v(outs[0].second)) << ";\n";
+    };
+
+    // generic face (runtime taps)
+    e << "template <class T>\n__device__ __noinline__ T gface" << K
+      << "(const DevProb<T>& P, const T* __restrict__ u, const int* I, int Ih, T t, const T* __restrict__ p) {\n"
+      << "    const T du = apply_op_at(P, P.ops[" << opi << "], u, " << F << ", " << D << ", I, Ih, P.n[" << D
+      << "], t, p);\n";
+    for (int f : used_fields)
+        e << "    const T uf" << f << " = apply_op_at(P, P.ops[" << opp << "], u, " << f << ", " << D << ", I, Ih, P.n["
+          << D << "], t, p);\n";
+    for (int j : used_aux)
+        e << "    const T fa" << j << " = P.aux[P.aux_off[P.terms[" << K << "].aux0 + " << j << "] + face_index(P, " << D
+          << ", Ih, I)];\n";
+    face_forward("");
+    e << "    return a * du;\n}\n";
+
+    // generic face adjoint
+    e << "template <class T>\n__device__ __noinline__ void gface" << K
+      << "_vjp(const DevProb<T>& P, const T* __restrict__ u, const int* I, int Ih, T t, const T* __restrict__ p, T g, "
+         "T* lam_u, T* lp, T* lam_aux) {\n"
+      << "    const T du = apply_op_at(P, P.ops[" << opi << "], u, " << F << ", " << D << ", I, Ih, P.n[" << D
+      << "], t, p);\n";
+    for (int f : used_fields)
+        e << "    const T uf" << f << " = apply_op_at(P, P.ops[" << opp << "], u, " << f << ", " << D << ", I, Ih, P.n["
+          << D << "], t, p);\n    T guf" << f << " = T(0);\n";
+    for (int j : used_aux)
+        e << "    const long long fi" << j << " = P.aux_off[P.terms[" << K << "].aux0 + " << j << "] + face_index(P, "
+          << D << ", Ih, I);\n    const T fa" << j << " = P.aux[fi" << j << "];\n    T gfa" << j << " = T(0);\n";
+    face_forward("");
+    e << "    scatter_op(P, P.ops[" << opi << "], lam_u, " << F << ", " << D << ", I, Ih, P.n[" << D << "], g * a, t, p);\n";
+    if (has_prog) {
+        FaceLeaves L("");
+        emit_reverse(e, fs, L, "", [&](int) { return std::string("g * du"); });
+        for (int f : used_fields)
+            e << "    scatter_op(P, P.ops[" << opp << "], lam_u, " << f << ", " << D << ", I, Ih, P.n[" << D
+              << "], guf" << f << ", t, p);\n";
+        for (int j : used_aux) e << "    if (lam_aux) atomicAdd(lam_aux + fi" << j << ", gfa" << j << ");\n";
+    }
+    e << "}\n";
+
+    // fast path helpers: relative face offsets r = omin_outer + m - 1 (outer stencil sits at II - 1)
+    auto fast_face = [&](int m, bool vjp) {
+        const int r = oo.omin + m - 1;
+        const std::string tag = "f" + std::to_string(m) + "_";
+        e << "    {\n";
+        // inner derivative
+        for (size_t q = 0; q < nzi.size(); ++q) {
+            const int t_ = nzi[q];
+            const std::string tap = "bF[(long long)(" + std::to_string(r + oi.omin + t_) + ") * s]";
+            if (q == 0) e << "    T " << tag << "du = wi[" << t_ << "] * " << tap << ";\n";
+            else e << "    " << tag << "du = fma(wi[" << t_ << "], " << tap << ", " << tag << "du);\n";
+        }
+        if (nzi.empty()) e << "    T " << tag << "du = T(0);\n";
+        for (int f : used_fields) {
+            e << "    const T* __restrict__ bf" << f << " = u + (long long)" << f << " * P.ncell + c;\n";
+            for (size_t q = 0; q < nzp.size(); ++q) {
+                const int t_ = nzp[q];
+                const std::string tap = "bf" + std::to_string(f) + "[(long long)(" + std::to_string(r + op.omin + t_) +
+                                        ") * s]";
+                if (q == 0) e << "    T " << tag << "uf" << f << " = wp[" << t_ << "] * " << tap << ";\n";
+                else e << "    " << tag << "uf" << f << " = fma(wp[" << t_ << "], " << tap << ", " << tag << "uf" << f
+                       << ");\n";
+            }
+            if (nzp.empty()) e << "    T " << tag << "uf" << f << " = T(0);\n";
+            if (vjp) e << "    T " << tag << "guf" << f << " = T(0);\n";
+        }
+        for (int j : used_aux) {
+            e << "    const long long " << tag << "fi" << j << " = P.aux_off[P.terms[" << K << "].aux0 + " << j
+              << "] + face_index(P, " << D << ", I[" << D << "] + (" << r << "), I);\n";
+            e << "    const T " << tag << "fa" << j << " = P.aux[" << tag << "fi" << j << "];\n";
+            if (vjp) e << "    T " << tag << "gfa" << j << " = T(0);\n";
+        }
+        face_forward(tag);
+        if (!vjp) {
+            e << "    const T " << tag << "F = " << tag << "a * " << tag << "du;\n";
+            e << "    acc = started ? fma(wo[" << m << "], " << tag << "F, acc) : wo[" << m << "] * " << tag << "F;\n"
+              << "    started = true;\n";
+        } else {
+            e << "    const T " << tag << "g = g * wo[" << m << "];\n";
+            e << "    { const T gd = " << tag << "g * " << tag << "a;\n";
+            for (int t_ : nzi)
+                e << "      atomicAdd(lF + (long long)(" << (r + oi.omin + t_) << ") * s, gd * wi[" << t_ << "]);\n";
+            e << "    }\n";
+            if (has_prog) {
+                FaceLeaves L(tag);
+                const std::string seed = tag + "g * " + tag + "du";
+                emit_reverse(e, fs, L, tag, [&](int) { return seed; });
+                for (int f : used_fields)
+                    for (int t_ : nzp)
+                        e << "    atomicAdd(lam_u + (long long)" << f << " * P.ncell + c + (long long)("
+                          << (r + op.omin + t_) << ") * s, " << tag << "guf" << f << " * wp[" << t_ << "]);\n";
+                for (int j : used_aux)
+                    e << "    if (lam_aux) atomicAdd(lam_aux + " << tag << "fi" << j << ", " << tag << "gfa" << j
+                      << ");\n";
+            }
+        }
+        e << "    }\n";
+    };
+    const std::string cond = "fast_nonlinlap(P, P.ops[" + opo + "], P.ops[" + opi + "], P.ops[" + opp + "], " + F +
+                             ", " + D + ", I[" + D + "])";
+    for (int vjp = 0; vjp < 2; ++vjp) {
+        if (!vjp)
+            e << "template <class T>\n__device__ __forceinline__ T gt" << K
+              << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ "
+                 "p) {\n";
+        else
+            e << "template <class T>\n__device__ __forceinline__ void gt" << K
+              << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* "
+                 "__restrict__ p, T g, T* lam_u, T* lp, T* lam_aux) {\n";
+        e << "    if (" << cond << ") {\n"
+          << "    const T* __restrict__ wo = P.w + P.ops[" << opo << "].w_int;\n"
+          << "    const T* __restrict__ wi = P.w + P.ops[" << opi << "].w_int;\n"
+          << "    const T* __restrict__ wp = P.w + P.ops[" << opp << "].w_int;\n"
+          << "    const T* __restrict__ bF = u + (long long)" << F << " * P.ncell + c;\n"
+          << "    const long long s = gstride(P, " << D << ");\n";
+        if (!vjp) e << "    T acc = T(0);\n    bool started = false;\n";
+        else e << "    T* lF = lam_u + (long long)" << F << " * P.ncell + c;\n";
+        for (int m : nzo) fast_face(m, vjp);
+        if (!vjp) e << "    return acc;\n    }\n";
+        else e << "    return;\n    }\n";
+        // generic path: runtime outer taps
+        e << "    const bool per = (P.permask[" << F << "] >> " << D << ") & 1;\n"
+          << "    const TapSel so = select_taps(P.ops[" << opo << "], I[" << D << "] - 1, P.n[" << D << "] - 1, per);\n";
+        if (!vjp) e << "    T acc = T(0);\n    bool started = false;\n";
+        e << "    for (int q = 0; q < so.cnt; ++q) {\n"
+          << "        const T w_ = P.w[so.woff + q];\n        if (w_ == T(0)) continue;\n";
+        if (!vjp)
+            e << "        const T F_ = gface" << K << "<T>(P, u, I, so.first + q, t, p);\n"
+              << "        acc = started ? fma(w_, F_, acc) : w_ * F_;\n        started = true;\n    }\n    return acc;\n";
+        else
+            e << "        gface" << K << "_vjp<T>(P, u, I, so.first + q, t, p, g * w_, lam_u, lp, lam_aux);\n    }\n";
+        e << "}\n";
+    }
+}
+
+}  // namespace
+
+std::string generate_source(const mol_problem_desc* d, std::string& why) {
+    Emitter e;
+    e << "// generated by libmolgpu for one problem structure\n"
+      << "#include \"mol_kernels.cuh\"\n"
+      << "namespace mol {\n";
+    for (int k = 0; k < d->nterms; ++k) {
+        switch (d->terms[k].kind) {
+            case MOL_TERM_LINEAR: emit_linear(e, d, k); break;
+            case MOL_TERM_MIXED: emit_mixed(e, d, k); break;
+            case MOL_TERM_WENO: emit_weno(e, d, k); break;
+            case MOL_TERM_NONLINLAP: emit_nonlinlap(e, d, k); break;
+            default: why = "unknown term"; return "";
+        }
+    }
+    SSA cs = to_ssa(d, d->cell_prog);
+    if (!cs.ok) {
+        why = "program reads an undefined register";
+        return "";
+    }
+    CellLeaves L;
+    // one out-of-line copy of the cell per precision, shared by every kernel template
+    e << "template <class T>\n__device__ __noinline__ void gen_cell(const DevProb<T>& P, const T* __restrict__ u, "
+         "long long c, const int* I, T t, const T* __restrict__ p, T* out) {\n";
+    std::vector<std::pair<int, int>> outs;
+    emit_forward(e, d, cs, L, "", &outs, false);
+    for (auto& pr : outs) e << "    out[" << pr.first << "] = " << v(pr.second) << ";\n";
+    e << "}\n";
+    e << "template <class T>\n__device__ __noinline__ void gen_cell_vjp(const DevProb<T>& P, const T* __restrict__ u, "
+         "long long c, const int* I, T t, const T* __restrict__ p, const T* seed, T* lam_u, T* lp, T* lam_aux) {\n";
+    emit_forward(e, d, cs, L, "", nullptr, true);
+    emit_reverse(e, cs, L, "", [&](int k) { return "seed[" + std::to_string(k) + "]"; });
+    e << "}\n";
+    e << "struct GenCell {\n"
+         "template <class T>\nstatic __device__ __forceinline__ void cell(const DevProb<T>& P, const T* __restrict__ u, "
+         "long long c, const int* I, T t, const T* __restrict__ p, T* out) { gen_cell<T>(P, u, c, I, t, p, out); }\n"
+         "template <class T>\nstatic __device__ __forceinline__ void cell_vjp(const DevProb<T>& P, const T* __restrict__ "
+         "u, long long c, const int* I, T t, const T* __restrict__ p, const T* seed, T* lam_u, T* lp, T* lam_aux) "
+         "{ gen_cell_vjp<T>(P, u, c, I, t, p, seed, lam_u, lp, lam_aux); }\n};\n}  // namespace mol\n";
+    return e.o.str();
+}
+
+// ---------------------------------------------------------------------------
+// NVRTC (loaded at run time) and the runtime library API
+// ---------------------------------------------------------------------------
+
+namespace {
+
+typedef int nvrtcResult_t;
+typedef struct _nvrtcProgram* nvrtcProgram_t;
+struct Nvrtc {
+    bool ok = false;
+    std::string err;
+    nvrtcResult_t (*create)(nvrtcProgram_t*, const char*, const char*, int, const char* const*, const char* const*);
+    nvrtcResult_t (*compile)(nvrtcProgram_t, int, const char* const*);
+    nvrtcResult_t (*logsize)(nvrtcProgram_t, size_t*);
+    nvrtcResult_t (*log)(nvrtcProgram_t, char*);
+    nvrtcResult_t (*cubinsize)(nvrtcProgram_t, size_t*);
+    nvrtcResult_t (*cubin)(nvrtcProgram_t, char*);
+    nvrtcResult_t (*destroy)(nvrtcProgram_t*);
+    nvrtcResult_t (*addname)(nvrtcProgram_t, const char*);
+    nvrtcResult_t (*lowered)(nvrtcProgram_t, const char*, const char**);
+};
+
+Nvrtc& nvrtc() {
+    static Nvrtc N;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char* names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13",
+                               "/usr/local/cuda/lib64/libnvrtc.so"};
+        void* h = nullptr;
+        for (const char* n : names)
+            if ((h = dlopen(n, RTLD_NOW | RTLD_LOCAL))) break;
+        if (!h) {
+            N.err = "libnvrtc not found";
+            return;
+        }
+        auto sym = [&](const char* s) { return dlsym(h, s); };
+        N.create = (decltype(N.create))sym("nvrtcCreateProgram");
+        N.compile = (decltype(N.compile))sym("nvrtcCompileProgram");
+        N.logsize = (decltype(N.logsize))sym("nvrtcGetProgramLogSize");
+        N.log = (decltype(N.log))sym("nvrtcGetProgramLog");
+        N.cubinsize = (decltype(N.cubinsize))sym("nvrtcGetCUBINSize");
+        N.cubin = (decltype(N.cubin))sym("nvrtcGetCUBIN");
+        N.destroy = (decltype(N.destroy))sym("nvrtcDestroyProgram");
+        N.addname = (decltype(N.addname))sym("nvrtcAddNameExpression");
+        N.lowered = (decltype(N.lowered))sym("nvrtcGetLoweredName");
+        N.ok = N.create && N.compile && N.logsize && N.log && N.cubinsize && N.cubin && N.destroy && N.addname &&
+               N.lowered;
+        if (!N.ok) N.err = "libnvrtc lacks required symbols";
+    });
+    return N;
+}
+
+struct CacheEntry {
+    cudaLibrary_t lib = nullptr;
+    std::vector<cudaKernel_t> kernels;
+};
+std::mutex g_cache_mu;
+std::map<std::string, CacheEntry> g_cache;
+
+}  // namespace
+
+// Compiled modules are kept on disk (MOL_CACHE_DIR, else $HOME/.cache/molgpu) keyed by a
+// hash of the generated source, the compile options and the kernel list.
+std::string disk_cache_path(const std::string& src, int nparams) {
+    const char* dir = getenv("MOL_CACHE_DIR");
+    std::string base;
+    if (dir && dir[0]) base = dir;
+    else if (getenv("HOME")) base = std::string(getenv("HOME")) + "/.cache/molgpu";
+    else return "";
+    if (getenv("MOL_NO_DISK_CACHE")) return "";
+    uint64_t h = 1469598103934665603ull;  // FNV-1a
+    auto mix = [&](const std::string& x) {
+        for (unsigned char ch : x) {
+            h ^= ch;
+            h *= 1099511628211ull;
+        }
+    };
+    mix(src);
+    mix("sm_103a|c++17|lineinfo|fmad|v2|" + std::to_string(nparams));
+    for (int i = 0; i < (int)(sizeof(kEmbedTexts) / sizeof(kEmbedTexts[0])); ++i) mix(kEmbedTexts[i]);
+    char name[64];
+    std::snprintf(name, sizeof name, "/%016llx.molmod", (unsigned long long)h);
+    return base + name;
+}
+
+bool disk_cache_load(const std::string& path, size_t nnames, std::vector<char>* cubin,
+                     std::vector<std::string>* lowered) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    bool ok = true;
+    uint64_t n = 0, sz = 0;
+    ok = std::fread(&n, 8, 1, f) == 1 && n == nnames;
+    lowered->clear();
+    for (uint64_t i = 0; ok && i < n; ++i) {
+        uint64_t l = 0;
+        ok = std::fread(&l, 8, 1, f) == 1 && l < 4096;
+        std::string s(l, '\0');
+        if (ok && l) ok = std::fread(&s[0], 1, l, f) == l;
+        lowered->push_back(s);
+    }
+    if (ok) ok = std::fread(&sz, 8, 1, f) == 1 && sz > 0 && sz < (1ull << 30);
+    if (ok) {
+        cubin->resize(sz);
+        ok = std::fread(cubin->data(), 1, sz, f) == sz;
+    }
+    std::fclose(f);
+    return ok;
+}
+
+void disk_cache_store(const std::string& path, const std::vector<char>& cubin, const std::vector<std::string>& lowered) {
+    const std::string dir = path.substr(0, path.rfind('/'));
+    std::string cmd_dir;
+    // create the directory chain (no shell)
+    for (size_t pos = 1; pos != std::string::npos && pos <= dir.size(); pos = dir.find('/', pos + 1)) {
+        const std::string sub = dir.substr(0, pos == std::string::npos ? dir.size() : pos);
+        mkdir(sub.c_str(), 0755);
+        if (pos == std::string::npos) break;
+    }
+    mkdir(dir.c_str(), 0755);
+    const std::string tmp = path + ".tmp" + std::to_string((long long)getpid());
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return;
+    uint64_t n = lowered.size();
+    bool ok = std::fwrite(&n, 8, 1, f) == 1;
+    for (auto& s : lowered) {
+        uint64_t l = s.size();
+        ok = ok && std::fwrite(&l, 8, 1, f) == 1 && (l == 0 || std::fwrite(s.data(), 1, l, f) == l);
+    }
+    uint64_t sz = cubin.size();
+    ok = ok && std::fwrite(&sz, 8, 1, f) == 1 && std::fwrite(cubin.data(), 1, sz, f) == sz;
+    std::fclose(f);
+    if (ok) std::rename(tmp.c_str(), path.c_str());
+    else std::remove(tmp.c_str());
+}
+
+std::vector<std::string> jit_kernel_names(int nparams, int group) {
+    const std::string NP = std::to_string(nparams > 0 ? nparams : 0);
+    std::vector<std::string> n;
+    switch (group) {
+        case JIT_FWD64:
+            n = {"&mol::k_rhs_t<double, mol::GenCell>", "&mol::k_ssprk_t<double, mol::GenCell, 1>",
+                 "&mol::k_ssprk_t<double, mol::GenCell, 2>", "&mol::k_ssprk_t<double, mol::GenCell, 3>",
+                 "&mol::k_tsit_stage_t<double, mol::GenCell>"};
+            break;
+        case JIT_FWD32:
+            n = {"&mol::k_rhs_t<float, mol::GenCell>", "&mol::k_ssprk_t<float, mol::GenCell, 1>",
+                 "&mol::k_ssprk_t<float, mol::GenCell, 2>", "&mol::k_ssprk_t<float, mol::GenCell, 3>"};
+            break;
+        case JIT_BATCH:
+            n = {"&mol::k_batch_ssprk_t<double, mol::GenCell>", "&mol::k_batch_ssprk_t<float, mol::GenCell>"};
+            break;
+        case JIT_VJP:
+            n = {"&mol::k_vjp_t<double, mol::GenCell, " + NP + ">"};
+            break;
+    }
+    return n;
+}
+
+int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<char>* cubin,
+                  std::vector<std::string>* lowered, std::string& err) {
+    const std::vector<std::string> names = jit_kernel_names(nparams, group);
+    Nvrtc& N = nvrtc();
+    if (!N.ok) {
+        err = "nvrtc: " + N.err;
+        return MOL_ERR_UNSUPPORTED;
+    }
+    nvrtcProgram_t prog;
+    const int nh = (int)(sizeof(kEmbedNames) / sizeof(kEmbedNames[0]));
+    if (N.create(&prog, src.c_str(), "mol_generated.cu", nh, kEmbedTexts, kEmbedNames) != 0) {
+        err = "nvrtcCreateProgram failed";
+        return MOL_ERR_CUDA;
+    }
+    for (auto& n : names) N.addname(prog, n.c_str());
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
+                          "-default-device", "-DMOL_JIT=1"};
+    const int rc = N.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    if (rc != 0) {
+        size_t ls = 0;
+        N.logsize(prog, &ls);
+        std::string log(ls, '\0');
+        if (ls) N.log(prog, &log[0]);
+        N.destroy(&prog);
+        err = "nvrtc compile failed: " + log.substr(0, 6000);
+        return MOL_ERR_UNSUPPORTED;
+    }
+    size_t cs = 0;
+    N.cubinsize(prog, &cs);
+    if (cubin) {
+        cubin->resize(cs);
+        N.cubin(prog, cubin->data());
+    }
+    if (lowered) {
+        lowered->clear();
+        for (auto& n : names) {
+            const char* l = nullptr;
+            N.lowered(prog, n.c_str(), &l);
+            lowered->push_back(l ? l : "");
+        }
+    }
+    N.destroy(&prog);
+    return MOL_OK;
+}
+
+int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k, std::string& err) {
+    const std::vector<std::string> names = jit_kernel_names(nparams, group);
+    const std::string key = src + "\n//group " + std::to_string(group);
+    std::vector<cudaKernel_t> got;
+    {
+        std::lock_guard<std::mutex> g(g_cache_mu);
+        auto it = g_cache.find(key);
+        if (it != g_cache.end()) got = it->second.kernels;
+    }
+    if (got.empty()) {
+        std::vector<char> cubin;
+        std::vector<std::string> lowered;
+        const std::string cache_path = disk_cache_path(key, nparams);
+        if (!(cache_path.size() && disk_cache_load(cache_path, names.size(), &cubin, &lowered))) {
+            int st = nvrtc_compile(src, nparams, group, &cubin, &lowered, err);
+            if (st) return st;
+            if (cache_path.size()) disk_cache_store(cache_path, cubin, lowered);
+        }
+        cudaLibrary_t lib;
+        cudaError_t ce = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+        if (ce != cudaSuccess) {
+            err = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(ce);
+            cudaGetLastError();
+            return MOL_ERR_CUDA;
+        }
+        for (size_t i = 0; i < names.size(); ++i) {
+            cudaKernel_t kk;
+            ce = cudaLibraryGetKernel(&kk, lib, lowered[i].c_str());
+            if (ce != cudaSuccess) {
+                err = "cudaLibraryGetKernel(" + names[i] + "): " + cudaGetErrorString(ce);
+                cudaGetLastError();
+                return MOL_ERR_CUDA;
+            }
+            got.push_back(kk);
+        }
+        std::lock_guard<std::mutex> g(g_cache_mu);
+        g_cache[key] = CacheEntry{lib, got};
+    }
+    switch (group) {
+        case JIT_FWD64:
+            k->rhs64 = got[0];
+            k->ssp64[0] = got[1];
+            k->ssp64[1] = got[2];
+            k->ssp64[2] = got[3];
+            k->tsit64 = got[4];
+            break;
+        case JIT_FWD32:
+            k->rhs32 = got[0];
+            k->ssp32[0] = got[1];
+            k->ssp32[1] = got[2];
+            k->ssp32[2] = got[3];
+            break;
+        case JIT_BATCH:
+            k->batch64 = got[0];
+            k->batch32 = got[1];
+            break;
+        case JIT_VJP:
+            k->vjp64 = got[0];
+            break;
+    }
+    k->loaded |= 1u << group;
+    return MOL_OK;
+}
+
+int jit_compile(const mol_problem_desc* d, JitKernels* out, std::string& err, std::string* src_out) {
+    std::string why;
+    std::string src = generate_source(d, why);
+    if (src.empty()) {
+        err = "codegen: " + why;
+        return MOL_ERR_UNSUPPORTED;
+    }
+    if (src_out) *src_out = src;
+    JitKernels k;
+    k.src = src;
+    k.nparams = d->nparams;
+    int st = jit_load_group(src, d->nparams, JIT_FWD64, &k, err);
+    if (st) return st;
+    k.ok = true;
+    *out = k;
+    return MOL_OK;
+}
+
+int jit_ensure(JitKernels* k, int group, std::string& err) {
+    if (!k->ok) return MOL_ERR_UNSUPPORTED;
+    if (k->loaded & (1u << group)) return MOL_OK;
+    return jit_load_group(k->src, k->nparams, group, k, err);
+}
+
+}  // namespace mol

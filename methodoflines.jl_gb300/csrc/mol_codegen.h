@@ -1,0 +1,44 @@
+// Generated right-hand side (see mol_codegen.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "molgpu.h"
+
+namespace mol {
+
+enum { JIT_FWD64 = 0, JIT_FWD32 = 1, JIT_BATCH = 2, JIT_VJP = 3 };
+
+// Kernels of a generated module; groups other than the FP64 forward kernels are
+// compiled on first use.
+struct JitKernels {
+    bool ok = false;
+    unsigned loaded = 0;
+    std::string src;
+    int nparams = 0;
+    cudaKernel_t rhs64 = nullptr, ssp64[3] = {nullptr, nullptr, nullptr}, batch64 = nullptr, tsit64 = nullptr;
+    cudaKernel_t rhs32 = nullptr, ssp32[3] = {nullptr, nullptr, nullptr}, batch32 = nullptr, tsit32 = nullptr;
+    cudaKernel_t vjp64 = nullptr;
+};
+
+std::string generate_source(const mol_problem_desc* d, std::string& why);
+std::vector<std::string> jit_kernel_names(int nparams, int group);
+// Generates, compiles (NVRTC, sm_103a) and loads the module of a problem structure;
+// modules are cached per generated source for the life of the process.
+int jit_compile(const mol_problem_desc* d, JitKernels* out, std::string& err, std::string* src_out);
+// NVRTC compile of generated source (no device needed); cubin and lowered kernel names optional.
+int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<char>* cubin,
+                  std::vector<std::string>* lowered, std::string& err);
+// Compiles and loads a kernel group of an already generated module on first use.
+int jit_ensure(JitKernels* k, int group, std::string& err);
+
+template <class... A>
+cudaError_t launch_k(cudaKernel_t k, int grid, int block, cudaStream_t s, A... args) {
+    void* pa[] = {(void*)&args...};
+    return cudaLaunchKernel((const void*)k, dim3(grid), dim3(block), pa, 0, s);
+}
+
+}  // namespace mol

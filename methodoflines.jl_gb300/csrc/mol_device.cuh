@@ -11,12 +11,27 @@
 // reciprocals in WENO, Markstein division by 3).
 #pragma once
 
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
 #include <stdint.h>
+#endif
 
 #include "molgpu.h"
 
 namespace mol {
+
+// Device-resident integrator state; kernels read t/dt from here so a captured
+// CUDA graph can be replayed step after step.
+struct SolverState {
+    double t, dt, t1, abstol, reltol;
+    double qold, EEst, dtmin;
+    double dta[8][8];   // dt * a_ij of the Tsit5 tableau (row = stage index)
+    double dtb[8];      // dt * btilde_j
+    double sums[4];
+    long long naccept, nreject, nf, iter, maxiters;
+    int done, status, accepted, pad;
+    unsigned int blocks_done, pad2;
+};
 
 template <class T>
 struct DevBC {
@@ -177,22 +192,75 @@ __device__ __forceinline__ TapSel select_taps(const mol_op1d& op, int i, int len
     return s;
 }
 
-// sum_k w_k u[tap_k] along dimension d (centered_difference.jl:5-30, upwind_difference.jl:1-28).
+// sum_k w_k u[tap_k] along dimension d at position `pos` of a line of `len` points
+// (centered_difference.jl:5-30, upwind_difference.jl:1-28, half_offset_centred_difference.jl:9-37).
 template <class T>
-__device__ T apply_op(const DevProb<T>& P, const mol_op1d& op, const T* u, int f, int d, const int* I,
-                      T t, const T* p) {
+__device__ T apply_op_at(const DevProb<T>& P, const mol_op1d& op, const T* u, int f, int d, const int* I, int pos,
+                         int len, T t, const T* p) {
     const bool per = (P.permask[f] >> d) & 1;
-    const TapSel s = select_taps(op, I[d], P.n[d], per);
+    const TapSel s = select_taps(op, pos, len, per);
     int J[3] = {I[0], I[1], I[2]};
     T acc = T(0);
     for (int k = 0; k < s.cnt; ++k) {
         int tp = s.first + k;
-        if (s.wrap) tp = wrap_periodic(tp, P.n[d]);
+        if (per) tp = wrap_periodic(tp, P.n[d]);
         J[d] = tp;
         const T v = load_pt(P, u, f, J[0], J[1], J[2], t, p);
         acc = k == 0 ? P.w[s.woff] * v : fma(P.w[s.woff + k], v, acc);
     }
     return acc;
+}
+
+template <class T>
+__device__ __forceinline__ T apply_op(const DevProb<T>& P, const mol_op1d& op, const T* u, int f, int d, const int* I,
+                                      T t, const T* p) {
+    return apply_op_at(P, op, u, f, d, I, I[d], P.n[d], t, p);
+}
+
+// Stride of dimension d in the interior (unknown) layout.
+template <class T>
+__device__ __forceinline__ long long gstride(const DevProb<T>& P, int d) {
+    return d == 0 ? 1ll : (d == 1 ? (long long)P.ni[0] : (long long)P.ni[0] * P.ni[1]);
+}
+
+// True when operator `o` at position i of dimension d uses its interior weights and
+// every tap is an unknown of the same line without wrapping: the generated code
+// then reads the taps at compile-time offsets.
+template <class T>
+__device__ __forceinline__ bool fast_line(const DevProb<T>& P, const mol_op1d& o, int f, int d, int i) {
+    const int first = i + o.omin, last = first + o.L - 1;
+    if ((P.permask[f] >> d) & 1) return first > P.lo[d] && last <= P.n[d];
+    return i > o.nlo && i <= P.n[d] - o.nhi && first > P.lo[d] && last <= P.n[d] - P.up[d];
+}
+
+template <class T>
+__device__ __forceinline__ bool fast_weno(const DevProb<T>& P, int f, int d, int i) {
+    return ((P.permask[f] >> d) & 1) && i - 2 > P.lo[d] && i + 2 <= P.n[d];
+}
+
+// Nonlinear Laplacian at i: the outer half-offset stencil (position i-1 on n-1 points) uses
+// interior weights and every face's inner derivative and interpolation do too.
+template <class T>
+__device__ __forceinline__ bool fast_nonlinlap(const DevProb<T>& P, const mol_op1d& oo, const mol_op1d& oi,
+                                               const mol_op1d& op, int f, int d, int i) {
+    const bool per = (P.permask[f] >> d) & 1;
+    const int pos = i - 1;
+    if (!per && !(pos > oo.nlo && pos <= (P.n[d] - 1) - oo.nhi)) return false;
+    for (int m = 0; m < oo.L; ++m) {
+        const int Ih = pos + oo.omin + m;
+        if (!fast_line(P, oi, f, d, Ih) || !fast_line(P, op, f, d, Ih)) return false;
+    }
+    return true;
+}
+
+// Face arrays have npts[d] + 1 entries along d (half point Ih + 1/2 at index Ih) and the
+// full grid extents elsewhere.
+template <class T>
+__device__ __forceinline__ long long face_index(const DevProb<T>& P, int d, int Ih, const int* I) {
+    Ih = Ih < 0 ? 0 : (Ih > P.n[d] ? P.n[d] : Ih);
+    const long long e0 = P.n[0] + (d == 0), e1 = P.n[1] + (d == 1);
+    const long long j0 = d == 0 ? Ih : I[0] - 1, j1 = d == 1 ? Ih : I[1] - 1, j2 = d == 2 ? Ih : I[2] - 1;
+    return j0 + e0 * (j1 + e1 * j2);
 }
 
 // Mixed derivative: tensor product of two first-derivative centered stencils
@@ -268,7 +336,8 @@ __device__ T apply_weno(const DevProb<T>& P, const mol_term& tm, const T* u, con
         J[d] = wrap_periodic(I[d] - 2 + k, n);
         v[k] = load_pt(P, u, f, J[0], J[1], J[2], t, p);
     }
-    return weno5_point<T>(v[0], v[1], v[2], v[3], v[4], T(tm.eps), T(1.0 / tm.dx));
+    // the device copy of a WENO term stores 1/dx in `dx`
+    return weno5_point<T>(v[0], v[1], v[2], v[3], v[4], T(tm.eps), T(tm.dx));
 }
 
 template <class T>
@@ -323,16 +392,7 @@ __device__ __noinline__ T nonlinlap_face(const DevProb<T>& P, const mol_term& tm
     const bool per = (P.permask[f] >> d) & 1;
     int J[3] = {I[0], I[1], I[2]};
     // inner derivative at the half point
-    const mol_op1d oin = P.ops[tm.op2];
-    const TapSel si = select_taps(oin, Ih, n, per);
-    T du = T(0);
-    for (int k = 0; k < si.cnt; ++k) {
-        int tp = si.first + k;
-        if (per) tp = wrap_periodic(tp, n);
-        J[d] = tp;
-        const T v = load_pt(P, u, f, J[0], J[1], J[2], t, p);
-        du = k == 0 ? P.w[si.woff] * v : fma(P.w[si.woff + k], v, du);
-    }
+    const T du = apply_op_at(P, P.ops[tm.op2], u, f, d, I, Ih, n, t, p);
     if (tm.prog < 0) return du;
     // face program: a(x~, u~, p)
     const mol_op1d oip = P.ops[tm.op3];
@@ -361,11 +421,7 @@ __device__ __noinline__ T nonlinlap_face(const DevProb<T>& P, const mol_term& tm
             }
             case MOL_OP_AUX: {
                 // face array: extent n[d]+1 along d (index Ih), full-grid extents elsewhere
-                const int ax = tm.aux0 + in.imm;
-                Ih = Ih < 0 ? 0 : (Ih > P.n[d] ? P.n[d] : Ih);
-                long long e0 = P.n[0] + (d == 0), e1 = P.n[1] + (d == 1);
-                long long j0 = d == 0 ? Ih : I[0] - 1, j1 = d == 1 ? Ih : I[1] - 1, j2 = d == 2 ? Ih : I[2] - 1;
-                R = P.aux[P.aux_off[ax] + j0 + e0 * (j1 + e1 * j2)];
+                R = P.aux[P.aux_off[tm.aux0 + in.imm] + face_index(P, d, Ih, I)];
                 break;
             }
             case MOL_OP_ADD: R = r[in.a] + r[in.b]; break;
@@ -467,16 +523,5 @@ __device__ __noinline__ void eval_cell(const DevProb<T>& P, const T* u, long lon
         }
     }
 }
-
-// Correctly rounded x/3 with one multiply and two FMAs (Markstein's theorem:
-// with c = RN(1/3) and q0 within an ulp of x/3, q0 + (x - 3 q0) c rounds to
-// RN(x/3)); replaces the FP64 division in SSPRK33's last stage.
-__device__ __forceinline__ double div3(double x) {
-    const double c = 0.33333333333333331483;  // RN(1/3)
-    const double q0 = x * c;
-    const double r = fma(-q0, 3.0, x);
-    return fma(r, c, q0);
-}
-__device__ __forceinline__ float div3(float x) { return x / 3.0f; }
 
 }  // namespace mol

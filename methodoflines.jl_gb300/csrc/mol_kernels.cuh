@@ -1,0 +1,301 @@
+// Kernel templates of the hot path.  `G` supplies the per-cell right-hand side
+// (`G::cell`) and its vector-Jacobian product (`G::cell_vjp`): either the
+// register-machine interpreter (always built) or the straight-line code that
+// the library generates for a plan and compiles with NVRTC.
+#pragma once
+
+#include "mol_device.cuh"
+#include "mol_vjp.cuh"
+
+namespace mol {
+
+constexpr int kThreads = 256;
+
+// Correctly rounded x/3 with one multiply and two FMAs (Markstein's theorem:
+// with c = RN(1/3) and q0 within an ulp of x/3, q0 + (x - 3 q0) c rounds to
+// RN(x/3)); replaces the FP64 division of SSPRK33's last stage.
+__device__ __forceinline__ double div3m(double x) {
+    const double c = 0.33333333333333331483;  // RN(1/3)
+    const double q0 = x * c;
+    const double r = fma(-q0, 3.0, x);
+    return fma(r, c, q0);
+}
+__device__ __forceinline__ float div3m(float x) { return x / 3.0f; }
+
+struct InterpCell {
+    template <class T>
+    static __device__ __forceinline__ void cell(const DevProb<T>& P, const T* __restrict__ u, long long c,
+                                                const int* I, T t, const T* __restrict__ p, T* out) {
+        eval_cell(P, u, c, I, t, p, out);
+    }
+};
+
+template <class T, class G>
+__global__ void __launch_bounds__(kThreads) k_rhs_t(DevProb<T> P, const T* __restrict__ u, T* __restrict__ du,
+                                                    const T* __restrict__ p, double t) {
+    T out[MOL_MAX_FIELDS];
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        G::cell(P, u, c, I, T(t), p, out);
+        for (int f = 0; f < P.nfields; ++f) du[(long long)f * P.ncell + c] = out[f];
+    }
+}
+
+// SSPRK33 stage epilogue with OrdinaryDiffEq's evaluation order:
+//   1: u1 = u0 + dt k     2: u2 = (3 u0 + u1 + dt k)/4     3: u = (u0 + 2 u2 + 2 dt k)/3
+template <class T, int STAGE>
+__device__ __forceinline__ T ssprk_combine(T u0, T uin, T k, T dt, T dt2) {
+    if (STAGE == 1) return u0 + dt * k;
+    if (STAGE == 2) return ((T(3) * u0 + uin) + dt * k) * T(0.25);
+    return div3m((u0 + T(2) * uin) + dt2 * k);
+}
+
+__device__ __forceinline__ void last_block_advance(SolverState* S, double t_new) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned v = atomicAdd(&S->blocks_done, 1u);
+        if (v == gridDim.x - 1) {
+            S->t = t_new;
+            S->blocks_done = 0;
+            __threadfence();
+        }
+    }
+}
+
+template <class T, class G, int STAGE>
+__global__ void __launch_bounds__(kThreads) k_ssprk_t(DevProb<T> P, const T* __restrict__ uin, const T* u0, T* uout,
+                                                      const T* __restrict__ p, SolverState* S, double dt) {
+    const double t0 = S->t;
+    const double ts = STAGE == 1 ? t0 : (STAGE == 2 ? t0 + dt : t0 + dt / 2);
+    T out[MOL_MAX_FIELDS];
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        G::cell(P, uin, c, I, T(ts), p, out);
+        for (int f = 0; f < P.nfields; ++f) {
+            const long long g = (long long)f * P.ncell + c;
+            uout[g] = ssprk_combine<T, STAGE>(u0[g], uin[g], out[f], T(dt), T(2 * dt));
+        }
+    }
+    if (STAGE == 3) last_block_advance(S, t0 + dt);
+}
+
+// Vector-Jacobian product of the RHS: lam_u += scale * (df/du)^T lam, lam_p and lam_aux likewise.
+// Parameter adjoints are reduced per block before one atomic per block and parameter.
+template <class T, class G, int NP>
+__global__ void __launch_bounds__(kThreads) k_vjp_t(DevProb<T> P, const T* __restrict__ lam, T scale,
+                                                    const T* __restrict__ u, const T* __restrict__ p, double t,
+                                                    T* lam_u, T* lam_p, T* lam_aux) {
+    T lp[NP > 0 ? NP : 1];
+#pragma unroll
+    for (int k = 0; k < (NP > 0 ? NP : 1); ++k) lp[k] = T(0);
+    T seed[MOL_MAX_FIELDS];
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        for (int f = 0; f < P.nfields; ++f) seed[f] = scale * lam[(long long)f * P.ncell + c];
+        G::cell_vjp(P, u, c, I, T(t), p, seed, lam_u, lp, lam_aux);
+    }
+    if (NP > 0 && lam_p) {
+        __shared__ T red[kThreads / 32];
+        for (int k = 0; k < NP; ++k) {
+            T v = lp[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                T s = T(0);
+                for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
+                atomicAdd(lam_p + k, s);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// One persistent launch for a whole ensemble: each CTA takes the next instance
+// (largest first, dynamic via an atomic ticket) and integrates it for `nsteps`
+// SSPRK33 steps, synchronising only its own threads between stages.
+template <class T, class G>
+__global__ void __launch_bounds__(kThreads) k_batch_ssprk_t(const DevProb<T>* __restrict__ probs,
+                                                            const long long* __restrict__ off,
+                                                            const int* __restrict__ order, int ninst, T* U, T* U1,
+                                                            T* U2, const T* const* __restrict__ params,
+                                                            const double* __restrict__ dts, double t0,
+                                                            long long nsteps, unsigned* ticket) {
+    __shared__ int slot;
+    T out[MOL_MAX_FIELDS];
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) slot = (int)atomicAdd(ticket, 1u);
+        __syncthreads();
+        if (slot >= ninst) return;
+        const int i = order[slot];
+        const DevProb<T>& P = probs[i];
+        T* u = U + off[i];
+        T* u1 = U1 + off[i];
+        T* u2 = U2 + off[i];
+        const T* p = params[i];
+        const double dt = dts[i];
+        const long long nc = P.ncell;
+        double t = t0;
+        for (long long s = 0; s < nsteps; ++s) {
+            for (long long c = threadIdx.x; c < nc; c += blockDim.x) {
+                int I[3];
+                cell_index(P, c, I);
+                G::cell(P, u, c, I, T(t), p, out);
+                for (int f = 0; f < P.nfields; ++f) {
+                    const long long g = (long long)f * nc + c;
+                    u1[g] = ssprk_combine<T, 1>(u[g], u[g], out[f], T(dt), T(2 * dt));
+                }
+            }
+            __syncthreads();
+            for (long long c = threadIdx.x; c < nc; c += blockDim.x) {
+                int I[3];
+                cell_index(P, c, I);
+                G::cell(P, u1, c, I, T(t + dt), p, out);
+                for (int f = 0; f < P.nfields; ++f) {
+                    const long long g = (long long)f * nc + c;
+                    u2[g] = ssprk_combine<T, 2>(u[g], u1[g], out[f], T(dt), T(2 * dt));
+                }
+            }
+            __syncthreads();
+            for (long long c = threadIdx.x; c < nc; c += blockDim.x) {
+                int I[3];
+                cell_index(P, c, I);
+                G::cell(P, u2, c, I, T(t + dt / 2), p, out);
+                for (int f = 0; f < P.nfields; ++f) {
+                    const long long g = (long long)f * nc + c;
+                    u[g] = ssprk_combine<T, 3>(u[g], u2[g], out[f], T(dt), T(2 * dt));
+                }
+            }
+            __syncthreads();
+            t = t + dt;
+        }
+    }
+}
+
+
+// Tsitouras (2011) nodes c_i of the 5(4) pair OrdinaryDiffEq's Tsit5 implements.
+__device__ __forceinline__ double tsit_c(int i) {
+    switch (i) {
+        case 2: return 0.161;
+        case 3: return 0.327;
+        case 4: return 0.9;
+        case 5: return 0.9800255409045097;
+        default: return 1.0;
+    }
+}
+
+// Stage i (2..7): k_i = f(y_i, t + c_i dt); the epilogue writes y_{i+1} = u + sum_j (dt a_{i+1,j}) k_j.
+// Stage 7 accumulates the scaled error sum_j (dt btilde_j) k_j; the last block to finish
+// reduces it deterministically and runs the PI step-size controller.
+template <class T, class G>
+__global__ void __launch_bounds__(kThreads) k_tsit_stage_t(DevProb<T> P, int stage, const T* __restrict__ y,
+                                                           T* ynext, const T* __restrict__ u, T* const* k,
+                                                           const T* __restrict__ p, SolverState* S,
+                                                           double* partials) {
+    if (S->done) return;
+    const double t = S->t + tsit_c(stage) * S->dt;
+    T out[MOL_MAX_FIELDS];
+    double errsq = 0.0;
+    const double abstol = S->abstol, reltol = S->reltol;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        G::cell(P, y, c, I, T(t), p, out);
+        for (int f = 0; f < P.nfields; ++f) {
+            const long long g = (long long)f * P.ncell + c;
+            k[stage - 1][g] = out[f];
+            if (stage < 7) {
+                T acc = u[g];
+                for (int j = 1; j <= stage; ++j) {
+                    const T kj = j == stage ? out[f] : k[j - 1][g];
+                    acc = fma(T(S->dta[stage + 1][j]), kj, acc);
+                }
+                ynext[g] = acc;
+            } else {
+                T e = T(0);
+                for (int j = 1; j <= 7; ++j) {
+                    const T kj = j == 7 ? out[f] : k[j - 1][g];
+                    e = fma(T(S->dtb[j]), kj, e);
+                }
+                const double sc = abstol + fmax(fabs((double)u[g]), fabs((double)y[g])) * reltol;
+                const double r = (double)e / sc;
+                errsq = fma(r, r, errsq);
+            }
+        }
+    }
+    if (stage < 7) return;
+    __shared__ double red[kThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = errsq;
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) s += red[w];
+        partials[blockIdx.x] = s;
+        __threadfence();
+        const unsigned v = atomicAdd(&S->blocks_done, 1u);
+        last = (v == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double s = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[b];
+    S->blocks_done = 0;
+    const double N = (double)P.ncell * P.nfields;
+    const double EEst = sqrt(s / N);
+    S->EEst = EEst;
+    S->nf += 6;
+    S->iter += 1;
+    if (!isfinite(EEst)) {
+        S->status = MOL_ERR_NONFINITE;
+        S->done = 1;
+        S->accepted = 0;
+        return;
+    }
+    // PI controller (beta1 = 7/50, beta2 = 2/25, qmin = 1/5, qmax = 10, gamma = 9/10)
+    const double beta1 = 0.14, beta2 = 0.08, qmin = 0.2, qmax = 10.0, gamma = 0.9, qoldinit = 1e-4;
+    const double q11 = pow(EEst, beta1);
+    const double dt = S->dt;
+    double dtnew;
+    if (EEst <= 1.0) {
+        double q = q11 / pow(S->qold, beta2);
+        q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gamma));
+        S->t = S->t + dt;
+        S->qold = fmax(EEst, qoldinit);
+        dtnew = dt / q;
+        S->naccept += 1;
+        S->accepted = 1;
+        if (S->t >= S->t1) S->done = 1;
+    } else {
+        const double q = fmin(1.0 / qmin, q11 / gamma);
+        dtnew = dt / q;
+        S->nreject += 1;
+        S->accepted = 0;
+    }
+    if (!S->done) {
+        if (S->t + dtnew > S->t1) dtnew = S->t1 - S->t;
+        if (!(dtnew > S->dtmin) && S->t < S->t1) {
+            S->status = MOL_ERR_DTMIN;
+            S->done = 1;
+        }
+        if (S->iter >= S->maxiters) {
+            S->status = MOL_ERR_MAXITERS;
+            S->done = 1;
+        }
+    }
+    S->dt = dtnew;
+    __threadfence();
+}
+
+}  // namespace mol

@@ -8,11 +8,14 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <string>
 #include <vector>
 
 #include "mol_device.cuh"
+#include "mol_kernels.cuh"
 #include "mol_plan.h"
 
 namespace mol {
@@ -80,182 +83,9 @@ static int ensure_slot(mol_plan* plan, int slot) {
     return MOL_OK;
 }
 
-constexpr int kThreads = 256;
-
 // ----------------------------------------------------------------------------
-// kernels
+// kernels that do not evaluate the right-hand side (the others are in mol_kernels.cuh)
 // ----------------------------------------------------------------------------
-
-template <class T>
-__global__ void __launch_bounds__(kThreads) k_rhs(DevProb<T> P, const T* __restrict__ u, T* __restrict__ du,
-                                                  const T* __restrict__ p, double t) {
-    T out[MOL_MAX_FIELDS];
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
-         c += (long long)gridDim.x * blockDim.x) {
-        int I[3];
-        cell_index(P, c, I);
-        eval_cell(P, u, c, I, T(t), p, out);
-        for (int f = 0; f < P.nfields; ++f) du[(long long)f * P.ncell + c] = out[f];
-    }
-}
-
-// One SSPRK33 stage with OrdinaryDiffEq's evaluation order fused as the epilogue:
-//   stage 1: u1 = u0 + dt*f(u0, t)
-//   stage 2: u2 = (3*u0 + u1 + dt*f(u1, t+dt)) / 4
-//   stage 3: u  = (u0 + 2*u2 + 2*dt*f(u2, t+dt/2)) / 3,  then t += dt
-template <class T, int STAGE>
-__global__ void __launch_bounds__(kThreads) k_ssprk(DevProb<T> P, const T* __restrict__ uin, const T* u0,
-                                                    T* uout, const T* __restrict__ p, SolverState* S, double dt) {
-    const double t0 = S->t;
-    const double ts = STAGE == 1 ? t0 : (STAGE == 2 ? t0 + dt : t0 + dt / 2);
-    const T dtT = T(dt);
-    const T dt2 = T(2 * dt);
-    T out[MOL_MAX_FIELDS];
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
-         c += (long long)gridDim.x * blockDim.x) {
-        int I[3];
-        cell_index(P, c, I);
-        eval_cell(P, uin, c, I, T(ts), p, out);
-        for (int f = 0; f < P.nfields; ++f) {
-            const long long g = (long long)f * P.ncell + c;
-            const T k = out[f];
-            T r;
-            if (STAGE == 1) {
-                r = u0[g] + dtT * k;
-            } else if (STAGE == 2) {
-                const T s = T(3) * u0[g] + uin[g];
-                r = (s + dtT * k) * T(0.25);
-            } else {
-                const T s = u0[g] + T(2) * uin[g];
-                r = div3(s + dt2 * k);
-            }
-            uout[g] = r;
-        }
-    }
-    if (STAGE == 3) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            const unsigned v = atomicAdd(&S->blocks_done, 1u);
-            if (v == gridDim.x - 1) {
-                S->t = t0 + dt;
-                S->blocks_done = 0;
-                __threadfence();
-            }
-        }
-    }
-}
-
-// Tsitouras (2011) 5(4) pair, the tableau OrdinaryDiffEq's Tsit5 implements.
-__constant__ double c_tsit_c[8] = {0.0, 0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0};
-
-// Stage i (2..7): k_i = f(y_i, t + c_i dt); epilogue writes y_{i+1} = u + sum_j (dt a_{i+1,j}) k_j.
-// Stage 7 instead accumulates the scaled error sum_j (dt btilde_j) k_j and the last
-// block runs the PI controller.
-template <class T>
-__global__ void __launch_bounds__(kThreads) k_tsit_stage(DevProb<T> P, int stage, const T* __restrict__ y,
-                                                         T* ynext, const T* __restrict__ u, T* const* k,
-                                                         const T* __restrict__ p, SolverState* S,
-                                                         double* partials) {
-    if (S->done) return;
-    const double t = S->t + c_tsit_c[stage] * S->dt;
-    T out[MOL_MAX_FIELDS];
-    double errsq = 0.0;
-    const double abstol = S->abstol, reltol = S->reltol;
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
-         c += (long long)gridDim.x * blockDim.x) {
-        int I[3];
-        cell_index(P, c, I);
-        eval_cell(P, y, c, I, T(t), p, out);
-        for (int f = 0; f < P.nfields; ++f) {
-            const long long g = (long long)f * P.ncell + c;
-            k[stage - 1][g] = out[f];
-            if (stage < 7) {
-                T acc = u[g];
-                for (int j = 1; j <= stage; ++j) {
-                    const T kj = j == stage ? out[f] : k[j - 1][g];
-                    acc = fma(T(S->dta[stage + 1][j]), kj, acc);
-                }
-                ynext[g] = acc;
-            } else {
-                T e = T(0);
-                for (int j = 1; j <= 7; ++j) {
-                    const T kj = j == 7 ? out[f] : k[j - 1][g];
-                    e = fma(T(S->dtb[j]), kj, e);
-                }
-                const double un = (double)y[g];
-                const double uo = (double)u[g];
-                const double sc = abstol + fmax(fabs(uo), fabs(un)) * reltol;
-                const double r = (double)e / sc;
-                errsq = fma(r, r, errsq);
-            }
-        }
-    }
-    if (stage < 7) return;
-    // deterministic block reduction of the error sum
-    __shared__ double red[kThreads / 32];
-    for (int o = 16; o > 0; o >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = errsq;
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) s += red[w];
-        partials[blockIdx.x] = s;
-        __threadfence();
-        const unsigned v = atomicAdd(&S->blocks_done, 1u);
-        last = (v == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!last || threadIdx.x != 0) return;
-    __threadfence();
-    double s = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[b];
-    S->blocks_done = 0;
-    const double N = (double)P.ncell * P.nfields;
-    const double EEst = sqrt(s / N);
-    S->EEst = EEst;
-    S->nf += 6;
-    S->iter += 1;
-    if (!isfinite(EEst)) {
-        S->status = MOL_ERR_NONFINITE;
-        S->done = 1;
-        S->accepted = 0;
-        return;
-    }
-    // PI controller (beta1 = 7/50, beta2 = 2/25, qmin = 1/5, qmax = 10, gamma = 9/10)
-    const double beta1 = 0.14, beta2 = 0.08, qmin = 0.2, qmax = 10.0, gamma = 0.9, qoldinit = 1e-4;
-    const double q11 = pow(EEst, beta1);
-    double dt = S->dt, dtnew;
-    if (EEst <= 1.0) {
-        double q = q11 / pow(S->qold, beta2);
-        q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gamma));
-        S->t = S->t + dt;
-        S->qold = fmax(EEst, qoldinit);
-        dtnew = dt / q;
-        S->naccept += 1;
-        S->accepted = 1;
-        if (S->t >= S->t1) S->done = 1;
-    } else {
-        const double q = fmin(1.0 / qmin, q11 / gamma);
-        dtnew = dt / q;
-        S->nreject += 1;
-        S->accepted = 0;
-    }
-    if (!S->done) {
-        if (S->t + dtnew > S->t1) dtnew = S->t1 - S->t;
-        if (!(dtnew > S->dtmin) && S->t < S->t1) {
-            S->status = MOL_ERR_DTMIN;
-            S->done = 1;
-        }
-        if (S->iter >= S->maxiters) {
-            S->status = MOL_ERR_MAXITERS;
-            S->done = 1;
-        }
-    }
-    S->dt = dtnew;
-    __threadfence();
-}
 
 // Row updates of the controller's dt-scaled tableau; one thread.
 __device__ void tsit_scale(SolverState* S) {
@@ -393,7 +223,15 @@ __global__ void k_set_time(SolverState* S, double t) {
 
 template <class T>
 int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t) {
-    k_rhs<T><<<plan->nblocks, kThreads, 0, plan->stream>>>(prob<T>(plan), u, du, p, t);
+    const bool is64 = std::is_same<T, double>::value;
+    if (plan->use_jit) {
+        int st = jit_ensure(&plan->jit, is64 ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
+        if (st) return set_err(plan, st, plan->jit_err);
+        ++g_launches;
+        return cuda_check(plan, launch_k(is64 ? plan->jit.rhs64 : plan->jit.rhs32, plan->nblocks, kThreads,
+                                         plan->stream, prob<T>(plan), u, du, p, t), "rhs launch");
+    }
+    k_rhs_t<T, InterpCell><<<plan->nblocks, kThreads, 0, plan->stream>>>(prob<T>(plan), u, du, p, t);
     ++g_launches;
     return cuda_check(plan, cudaGetLastError(), "k_rhs launch");
 }
@@ -403,10 +241,23 @@ template int launch_rhs<float>(mol_plan*, float*, const float*, const float*, do
 template <class T>
 int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt) {
     const DevProb<T>& P = prob<T>(plan);
-    k_ssprk<T, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt);
-    k_ssprk<T, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt);
-    k_ssprk<T, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, u, p, plan->d_state, dt);
     g_launches += 3;
+    if (plan->use_jit) {
+        const bool is64 = std::is_same<T, double>::value;
+        int st = jit_ensure(&plan->jit, is64 ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
+        if (st) return set_err(plan, st, plan->jit_err);
+        cudaKernel_t* k = is64 ? plan->jit.ssp64 : plan->jit.ssp32;
+        const T* cu = u;
+        const T* cu1 = u1;
+        const T* cu2 = u2;
+        cudaError_t e = launch_k(k[0], plan->nblocks, kThreads, plan->stream, P, cu, cu, u1, p, plan->d_state, dt);
+        if (e == cudaSuccess) e = launch_k(k[1], plan->nblocks, kThreads, plan->stream, P, cu1, cu, u2, p, plan->d_state, dt);
+        if (e == cudaSuccess) e = launch_k(k[2], plan->nblocks, kThreads, plan->stream, P, cu2, cu, u, p, plan->d_state, dt);
+        return cuda_check(plan, e, "ssprk launch");
+    }
+    k_ssprk_t<T, InterpCell, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt);
+    k_ssprk_t<T, InterpCell, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt);
+    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, u, p, plan->d_state, dt);
     return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
 }
 template int launch_ssprk_step<double>(mol_plan*, double*, double*, double*, const double*, double);
@@ -677,6 +528,13 @@ const char* mol_status_string(int s) {
 
 int64_t mol_launch_count(void) { return g_launches.load(); }
 
+int mol_plan_uses_codegen(const mol_plan* plan) { return plan && plan->use_jit ? 1 : 0; }
+
+const char* mol_plan_codegen_source(const mol_plan* plan) {
+    if (!plan) return "";
+    return plan->use_jit ? plan->jit_src.c_str() : plan->jit_err.c_str();
+}
+
 const char* mol_last_error(const mol_plan* plan) { return plan ? plan->err.c_str() : "null plan"; }
 
 int64_t mol_plan_n_unknowns(const mol_plan* plan) { return plan ? plan->nunk : -1; }
@@ -701,6 +559,44 @@ int mol_plan_destroy(mol_plan* plan) {
     if (plan->own_stream && plan->stream) cudaStreamDestroy(plan->stream);
     delete plan;
     return MOL_OK;
+}
+
+int mol_generate_code(const mol_problem_desc* desc, char* buf, int64_t bufsize, int64_t* needed) {
+    mol_plan tmp;
+    int st = validate_desc(&tmp, desc);
+    if (st) return st;
+    std::string why;
+    const std::string src = generate_source(desc, why);
+    if (src.empty()) return MOL_ERR_UNSUPPORTED;
+    if (needed) *needed = (int64_t)src.size() + 1;
+    if (buf && bufsize > 0) {
+        const size_t n = std::min<size_t>((size_t)bufsize - 1, src.size());
+        std::memcpy(buf, src.data(), n);
+        buf[n] = 0;
+    }
+    return MOL_OK;
+}
+
+int mol_codegen_compile_check(const mol_problem_desc* desc, char* log, int64_t logsize) {
+    mol_plan tmp;
+    int st = validate_desc(&tmp, desc);
+    std::string err = tmp.err;
+    if (!st) {
+        std::string why;
+        const std::string src = generate_source(desc, why);
+        if (src.empty()) {
+            st = MOL_ERR_UNSUPPORTED;
+            err = why;
+        } else {
+            for (int grp = 0; grp < 4 && !st; ++grp) st = nvrtc_compile(src, desc->nparams, grp, nullptr, nullptr, err);
+        }
+    }
+    if (log && logsize > 0) {
+        const size_t n = std::min<size_t>((size_t)logsize - 1, err.size());
+        std::memcpy(log, err.data(), n);
+        log[n] = 0;
+    }
+    return st;
 }
 
 int mol_plan_create(const mol_problem_desc* d, mol_plan** out) {
@@ -734,10 +630,33 @@ int mol_plan_create(const mol_problem_desc* d, mol_plan** out) {
         *out = plan;
         return code;
     };
+    // Derived copies the kernels use: product weights of every mixed derivative appended
+    // to the pool (term.reserved0 = their offset, row-major [L1][L2]) and 1/dx in WENO terms.
+    std::vector<double> weights(d->weights, d->weights + d->nweights);
+    std::vector<mol_term> terms(d->terms, d->terms + d->nterms);
+    for (int k = 0; k < d->nterms; ++k) {
+        mol_term& tm = terms[k];
+        if (tm.kind == MOL_TERM_MIXED) {
+            const mol_op1d& o1 = d->ops[tm.op];
+            const mol_op1d& o2 = d->ops[tm.op2];
+            tm.reserved0 = (int32_t)weights.size();
+            for (int x = 0; x < o1.L; ++x)
+                for (int y = 0; y < o2.L; ++y) weights.push_back(d->weights[o1.w_int + x] * d->weights[o2.w_int + y]);
+        }
+    }
+    mol_problem_desc dd = *d;
+    dd.weights = weights.data();
+    dd.nweights = (int64_t)weights.size();
+    dd.terms = terms.data();
+    std::vector<mol_term> dev_terms = terms;
+    for (auto& tm : dev_terms)
+        if (tm.kind == MOL_TERM_WENO) tm.dx = 1.0 / tm.dx;
+    d = &dd;
     if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->stream, cudaStreamNonBlocking), "stream"))) return fail(st);
     plan->own_stream = true;
     if ((st = copy_struct(plan, (void**)&plan->d_ops, d->ops, sizeof(mol_op1d) * d->nops))) return fail(st);
-    if ((st = copy_struct(plan, (void**)&plan->d_terms, d->terms, sizeof(mol_term) * d->nterms))) return fail(st);
+    if ((st = copy_struct(plan, (void**)&plan->d_terms, dev_terms.data(), sizeof(mol_term) * d->nterms)))
+        return fail(st);
     if ((st = copy_struct(plan, (void**)&plan->d_code, d->code, sizeof(mol_instr) * d->ninstr))) return fail(st);
     if ((st = copy_struct(plan, (void**)&plan->d_progs, d->prog_ranges, sizeof(int) * 2 * d->nprogs))) return fail(st);
     if ((st = copy_struct(plan, (void**)&plan->d_aux_off, plan->aux_off_host.data(), sizeof(long long) * (d->naux + 1))))
@@ -751,6 +670,16 @@ int mol_plan_create(const mol_problem_desc* d, mol_plan** out) {
     long long want = (ncell + kThreads - 1) / kThreads;
     plan->nblocks = (int)std::max<long long>(1, std::min<long long>(want, (long long)sms * 8));
     if ((st = plan_alloc(plan, (void**)&plan->d_partials, sizeof(double) * 3 * plan->nblocks))) return fail(st);
+    // the generated right-hand side; MOL_DISABLE_CODEGEN=1 keeps the interpreter (used to cross-check)
+    const char* off_env = getenv("MOL_DISABLE_CODEGEN");
+    if (!(off_env && off_env[0] == '1')) {
+        st = jit_compile(d, &plan->jit, plan->jit_err, &plan->jit_src);
+        plan->use_jit = (st == MOL_OK) && plan->jit.ok;
+        if (!plan->use_jit) {
+            const char* req = getenv("MOL_REQUIRE_CODEGEN");
+            if (req && req[0] == '1') return fail(set_err(plan, st ? st : MOL_ERR_UNSUPPORTED, plan->jit_err));
+        }
+    }
     *out = plan;
     return MOL_OK;
 }
@@ -846,6 +775,10 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
         return st;
     const T* pp = params_ptr<T>(plan, p, &st);
     if (st) return st;
+    if (plan->use_jit) {  // modules are loaded before any stream capture begins
+        st = jit_ensure(&plan->jit, std::is_same<T, double>::value ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
+        if (st) return set_err(plan, st, plan->jit_err);
+    }
     k_set_time<<<1, 1, 0, plan->stream>>>(plan->d_state, t0);
     ++g_launches;
     T* u1 = ws[1];
@@ -858,7 +791,9 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     const void*& gp = is64 ? plan->g_ssp64_p : plan->g_ssp32_p;
     const void*& gpp = is64 ? plan->g_ssp64_pp : plan->g_ssp32_pp;
     int64_t done = 0;
-    if (nsteps >= chunk) {
+    // the legacy default stream cannot be captured: launch directly there
+    const bool can_capture = plan->stream != nullptr && plan->stream != cudaStreamLegacy;
+    if (nsteps >= chunk && can_capture) {
         // the state buffer, parameter pointer and dt are baked into the captured graph
         if (gx && (gdt != dt || gp != (const void*)ud || gpp != (const void*)pp)) {
             cudaGraphExecDestroy(gx);
@@ -983,30 +918,43 @@ int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, doubl
         for (int s = 2; s <= 7; ++s) {
             const double* yin = (s % 2 == 0) ? yb0 : yb1;
             double* yout = (s % 2 == 0) ? yb1 : yb0;
-            k_tsit_stage<double><<<nb, kThreads, 0, plan->stream>>>(plan->P64, s, yin, yout, ud, d_k, pp,
-                                                                    plan->d_state, plan->d_partials);
+            if (plan->use_jit)
+                launch_k(plan->jit.tsit64, nb, kThreads, plan->stream, plan->P64, s, yin, yout, (const double*)ud,
+                         (double* const*)d_k, pp, plan->d_state, plan->d_partials);
+            else
+                k_tsit_stage_t<double, InterpCell><<<nb, kThreads, 0, plan->stream>>>(
+                    plan->P64, s, yin, yout, ud, d_k, pp, plan->d_state, plan->d_partials);
         }
         k_tsit_commit<double><<<nb, kThreads, 0, plan->stream>>>(plan->P64, ud, k1, k7, yb1, yb0, plan->d_state, 0);
     };
     const int M = 32;
     cudaGraph_t graph;
     cudaGraphExec_t gx = nullptr;
-    if ((st = cuda_check(plan, cudaStreamBeginCapture(plan->stream, cudaStreamCaptureModeThreadLocal), "capture")))
-        return st;
-    for (int i = 0; i < M; ++i) attempt();
-    if ((st = cuda_check(plan, cudaStreamEndCapture(plan->stream, &graph), "end capture"))) return st;
-    st = cuda_check(plan, cudaGraphInstantiate(&gx, graph, 0), "instantiate");
-    cudaGraphDestroy(graph);
-    if (st) return st;
+    const bool can_capture = plan->stream != nullptr && plan->stream != cudaStreamLegacy;
+    if (can_capture) {
+        if ((st = cuda_check(plan, cudaStreamBeginCapture(plan->stream, cudaStreamCaptureModeThreadLocal),
+                             "capture")))
+            return st;
+        for (int i = 0; i < M; ++i) attempt();
+        if ((st = cuda_check(plan, cudaStreamEndCapture(plan->stream, &graph), "end capture"))) return st;
+        st = cuda_check(plan, cudaGraphInstantiate(&gx, graph, 0), "instantiate");
+        cudaGraphDestroy(graph);
+        if (st) return st;
+    }
     SolverState hs;
     for (;;) {
-        if ((st = cuda_check(plan, cudaGraphLaunch(gx, plan->stream), "graph launch"))) break;
+        if (can_capture) {
+            if ((st = cuda_check(plan, cudaGraphLaunch(gx, plan->stream), "graph launch"))) break;
+        } else {
+            for (int i = 0; i < M; ++i) attempt();
+            if ((st = cuda_check(plan, cudaGetLastError(), "tsit5 launch"))) break;
+        }
         g_launches += 7 * M;
         cudaMemcpyAsync(&hs, plan->d_state, sizeof(SolverState), cudaMemcpyDeviceToHost, plan->stream);
         if ((st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "tsit5 sync"))) break;
         if (hs.done) break;
     }
-    cudaGraphExecDestroy(gx);
+    if (gx) cudaGraphExecDestroy(gx);
     if (st) return st;
     if (stats) {
         stats->naccept = hs.naccept;

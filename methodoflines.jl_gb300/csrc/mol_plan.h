@@ -7,25 +7,13 @@
 #include <string>
 #include <vector>
 
+#include "mol_codegen.h"
 #include "mol_device.cuh"
 #include "molgpu.h"
 
 namespace mol {
 
 extern std::atomic<long long> g_launches;
-
-// Device-resident integrator state; kernels read t/dt from here so a captured
-// CUDA graph can be replayed step after step.
-struct SolverState {
-    double t, dt, t1, abstol, reltol;
-    double qold, EEst, dtmin;
-    double dta[8][8];   // dt * a_ij of the Tsit5 tableau (row = stage index)
-    double dtb[8];      // dt * btilde_j
-    double sums[4];     // norms of the initial-step heuristic
-    long long naccept, nreject, nf, iter, maxiters;
-    int done, status, accepted, pad;
-    unsigned int blocks_done, pad2;
-};
 
 struct PlanArrays {
     // per-precision copies of everything the kernels read
@@ -81,6 +69,10 @@ struct mol_plan {
     const void* g_ssp64_pp = nullptr;
     const void* g_ssp32_pp = nullptr;
     int g_chunk = 16;
+    // generated right-hand side (NVRTC); the interpreter serves when it is off
+    mol::JitKernels jit;
+    bool use_jit = false;
+    std::string jit_src, jit_err;
 };
 
 namespace mol {

@@ -89,10 +89,14 @@ _PROTOS = {
     "mol_status_string": (C.c_char_p, [C.c_int]),
     "mol_plan_create": (C.c_int, [C.POINTER(mol_problem_desc), C.POINTER(C.c_void_p)]),
     "mol_plan_destroy": (C.c_int, [C.c_void_p]),
+    "mol_generate_code": (C.c_int, [C.POINTER(mol_problem_desc), C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "mol_codegen_compile_check": (C.c_int, [C.POINTER(mol_problem_desc), C.c_char_p, C.c_int64]),
     "mol_last_error": (C.c_char_p, [C.c_void_p]),
     "mol_plan_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mol_plan_n_unknowns": (C.c_int64, [C.c_void_p]),
     "mol_launch_count": (C.c_int64, []),
+    "mol_plan_uses_codegen": (C.c_int, [C.c_void_p]),
+    "mol_plan_codegen_source": (C.c_char_p, [C.c_void_p]),
     "mol_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
     "mol_rhs_f32state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
     "mol_step_ssprk33": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64]),

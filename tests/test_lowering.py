@@ -173,3 +173,20 @@ def test_register_allocation_reuses_registers():
     pb.out(tree, 0)
     code = pb.finish()
     assert max(max(r[1], r[2], r[3]) for r in code) < 8
+
+
+@pytest.mark.parametrize("name,kw", [("brusselator", dict(N=8)), ("adr3d", dict(N=6, nz_pts=8))])
+def test_generated_code_compiles_for_sm103a(name, kw):
+    """generate_code + NVRTC compile of every kernel group, without a device."""
+    from molgpu import Descriptor
+    sys_, disc, _ = getattr(problems, name)(**kw)
+    D = Descriptor(lower(sys_.to_spec(disc)))
+    need = C.c_int64()
+    assert L.lib().mol_generate_code(C.byref(D.desc), None, 0, C.byref(need)) == 0
+    buf = C.create_string_buffer(need.value)
+    assert L.lib().mol_generate_code(C.byref(D.desc), buf, need.value, C.byref(need)) == 0
+    src = buf.value.decode()
+    assert "gen_cell" in src and "fast_line" in src
+    log = C.create_string_buffer(1 << 16)
+    st = L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16)
+    assert st == 0, log.value.decode()
