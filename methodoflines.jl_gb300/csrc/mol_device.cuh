@@ -297,33 +297,42 @@ __device__ T apply_mixed(const DevProb<T>& P, const mol_term& tm, const T* u, co
 }
 
 // Jiang-Shu WENO5 node derivative (WENO.jl:6-57), periodic taps i-2..i+2.
-// Algebraically identical to the reference; the six nonlinear weights share
-// one reciprocal of each (eps + beta)^2 and one reciprocal of each weight sum,
-// which replaces 12 FP64 divisions by 5.
+// Algebraically identical to the reference.  In FP64 the six nonlinear weights
+// gamma_k / (eps + beta_k)^2 are brought to the common denominator
+// prod_j (eps + beta_j)^2, so (hp - hm) costs one division instead of the twelve
+// the reference spells out; eps >= 1e-6 keeps every product far from underflow.
+// FP32 keeps the reciprocal form (the products would underflow in float).
 template <class T>
 __device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps, T inv_dx) {
     const T c13_12 = T(13) / T(12);
     const T a1 = u0 - T(2) * up1 + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
     const T a2 = um1 - T(2) * u0 + up1, b2 = um1 - up1;
     const T a3 = um2 - T(2) * um1 + u0, b3 = um2 - T(4) * um1 + T(3) * u0;
-    const T beta1 = fma(c13_12 * a1, a1, T(0.25) * (b1 * b1));
-    const T beta2 = fma(c13_12 * a2, a2, T(0.25) * (b2 * b2));
-    const T beta3 = fma(c13_12 * a3, a3, T(0.25) * (b3 * b3));
-    const T e1 = eps + beta1, e2 = eps + beta2, e3 = eps + beta3;
+    const T e1 = eps + fma(c13_12 * a1, a1, T(0.25) * (b1 * b1));
+    const T e2 = eps + fma(c13_12 * a2, a2, T(0.25) * (b2 * b2));
+    const T e3 = eps + fma(c13_12 * a3, a3, T(0.25) * (b3 * b3));
+    // candidate reconstructions, scaled by 6 (the common 1/6 is folded into inv_dx below)
+    const T hm1 = T(11) * u0 - T(7) * up1 + T(2) * up2;
+    const T hm2 = T(5) * u0 - up1 + T(2) * um1;
+    const T hm3 = T(2) * u0 + T(5) * um1 - um2;
+    const T hp1 = T(2) * u0 + T(5) * up1 - up2;
+    const T hp2 = T(5) * u0 + T(2) * up1 - um1;
+    const T hp3 = T(11) * u0 - T(7) * um1 + T(2) * um2;
+    if (sizeof(T) == 8) {
+        const T s1 = e1 * e1, s2 = e2 * e2, s3 = e3 * e3;
+        const T P1 = s2 * s3, P2 = s1 * s3, P3 = s1 * s2;   // P_k = prod_{j != k} (eps + beta_j)^2
+        const T wm1 = T(0.1) * P1, wm2 = T(0.6) * P2, wm3 = T(0.3) * P3;
+        const T wp1 = T(0.3) * P1, wp2 = T(0.6) * P2, wp3 = T(0.1) * P3;
+        const T Np = fma(wp1, hp1, fma(wp2, hp2, wp3 * hp3)), Dp = wp1 + wp2 + wp3;
+        const T Nm = fma(wm1, hm1, fma(wm2, hm2, wm3 * hm3)), Dm = wm1 + wm2 + wm3;
+        return fma(Np, Dm, -Nm * Dp) / (Dp * Dm) * (inv_dx * T(1.0 / 6.0));
+    }
     const T q1 = T(1) / (e1 * e1), q2 = T(1) / (e2 * e2), q3 = T(1) / (e3 * e3);
-    // minus side: gamma = (1/10, 3/5, 3/10); plus side: gamma = (3/10, 3/5, 1/10)
     const T wm1 = T(0.1) * q1, wm2 = T(0.6) * q2, wm3 = T(0.3) * q3;
     const T wp1 = T(0.3) * q1, wp2 = T(0.6) * q2, wp3 = T(0.1) * q3;
-    const T sixth = T(1) / T(6);
-    const T hm1 = (T(11) * u0 - T(7) * up1 + T(2) * up2) * sixth;
-    const T hm2 = (T(5) * u0 - up1 + T(2) * um1) * sixth;
-    const T hm3 = (T(2) * u0 + T(5) * um1 - um2) * sixth;
-    const T hp1 = (T(2) * u0 + T(5) * up1 - up2) * sixth;
-    const T hp2 = (T(5) * u0 + T(2) * up1 - um1) * sixth;
-    const T hp3 = (T(11) * u0 - T(7) * um1 + T(2) * um2) * sixth;
     const T hp = fma(wp1, hp1, fma(wp2, hp2, wp3 * hp3)) / (wp1 + wp2 + wp3);
     const T hm = fma(wm1, hm1, fma(wm2, hm2, wm3 * hm3)) / (wm1 + wm2 + wm3);
-    return (hp - hm) * inv_dx;
+    return (hp - hm) * (inv_dx * T(1.0 / 6.0));
 }
 
 template <class T>

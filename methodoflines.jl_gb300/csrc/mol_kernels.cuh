@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(kThreads) k_tsit_stage_t(DevProb<T> P, int sta
     __shared__ bool last;
     if (threadIdx.x == 0) {
         double s = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) s += red[w];
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
         partials[blockIdx.x] = s;
         __threadfence();
         const unsigned v = atomicAdd(&S->blocks_done, 1u);

@@ -55,6 +55,24 @@ int plan_alloc(mol_plan* plan, void** ptr, size_t bytes) {
 
 int plan_grid(const mol_plan* plan) { return plan->nblocks; }
 
+// Grid of a grid-stride kernel: a multiple of the SM count when the problem fills
+// the machine, otherwise one block per kThreads cells.
+int grid_for(long long ncell, int sms, int blocks_per_sm) {
+    const long long full = (long long)sms * blocks_per_sm;
+    const long long want = (ncell + kThreads - 1) / kThreads;
+    return (int)std::max<long long>(1, std::min<long long>(want, full));
+}
+
+// Threads per block: kThreads, or fewer for problems smaller than one full wave so
+// that every SM gets the same number of cells (a multiple of 32, at least 64).
+int threads_for(long long ncell, int sms, int blocks_per_sm) {
+    const long long slots = (long long)sms * blocks_per_sm;
+    if (ncell >= slots * kThreads) return kThreads;
+    long long t = (ncell + slots - 1) / slots;
+    t = (t + 31) / 32 * 32;
+    return (int)std::max<long long>(64, std::min<long long>(kThreads, t));
+}
+
 template <class T>
 int ensure_ws(mol_plan* plan, int count) {
     T** ws = workspace<T>(plan);
@@ -176,7 +194,7 @@ __global__ void k_init_norms(long long n, const T* u0, const T* f0, const T* f1,
     __syncthreads();
     if (threadIdx.x == 0) {
         double a = 0, b = 0, c = 0;
-        for (int w = 0; w < kThreads / 32; ++w) { a += red[0][w]; b += red[1][w]; c += red[2][w]; }
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) { a += red[0][w]; b += red[1][w]; c += red[2][w]; }
         partials[3 * blockIdx.x + 0] = a;
         partials[3 * blockIdx.x + 1] = b;
         partials[3 * blockIdx.x + 2] = c;
@@ -228,7 +246,7 @@ int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t) {
         int st = jit_ensure(&plan->jit, is64 ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
         if (st) return set_err(plan, st, plan->jit_err);
         ++g_launches;
-        return cuda_check(plan, launch_k(is64 ? plan->jit.rhs64 : plan->jit.rhs32, plan->nblocks, kThreads,
+        return cuda_check(plan, launch_k(is64 ? plan->jit.rhs64 : plan->jit.rhs32, plan->nblocks, plan->nthreads,
                                          plan->stream, prob<T>(plan), u, du, p, t), "rhs launch");
     }
     k_rhs_t<T, InterpCell><<<plan->nblocks, kThreads, 0, plan->stream>>>(prob<T>(plan), u, du, p, t);
@@ -250,9 +268,9 @@ int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt)
         const T* cu = u;
         const T* cu1 = u1;
         const T* cu2 = u2;
-        cudaError_t e = launch_k(k[0], plan->nblocks, kThreads, plan->stream, P, cu, cu, u1, p, plan->d_state, dt);
-        if (e == cudaSuccess) e = launch_k(k[1], plan->nblocks, kThreads, plan->stream, P, cu1, cu, u2, p, plan->d_state, dt);
-        if (e == cudaSuccess) e = launch_k(k[2], plan->nblocks, kThreads, plan->stream, P, cu2, cu, u, p, plan->d_state, dt);
+        cudaError_t e = launch_k(k[0], plan->nblocks, plan->nthreads, plan->stream, P, cu, cu, u1, p, plan->d_state, dt);
+        if (e == cudaSuccess) e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, P, cu1, cu, u2, p, plan->d_state, dt);
+        if (e == cudaSuccess) e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, P, cu2, cu, u, p, plan->d_state, dt);
         return cuda_check(plan, e, "ssprk launch");
     }
     k_ssprk_t<T, InterpCell, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt);
@@ -599,7 +617,13 @@ int mol_codegen_compile_check(const mol_problem_desc* desc, char* log, int64_t l
     return st;
 }
 
-int mol_plan_create(const mol_problem_desc* d, mol_plan** out) {
+int mol_plan_create(const mol_problem_desc* d, mol_plan** out) { return mol::plan_create_impl(d, out, false); }
+
+}  // extern "C"
+
+// `member` plans belong to an ensemble: no stream, no solver workspace, no code
+// generation of their own (the ensemble compiles one module for all members).
+int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member) {
     if (!out) return MOL_ERR_INVALID;
     *out = nullptr;
     mol_plan* plan = new mol_plan();
@@ -652,8 +676,11 @@ int mol_plan_create(const mol_problem_desc* d, mol_plan** out) {
     for (auto& tm : dev_terms)
         if (tm.kind == MOL_TERM_WENO) tm.dx = 1.0 / tm.dx;
     d = &dd;
-    if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->stream, cudaStreamNonBlocking), "stream"))) return fail(st);
-    plan->own_stream = true;
+    if (!member) {
+        if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->stream, cudaStreamNonBlocking), "stream")))
+            return fail(st);
+        plan->own_stream = true;
+    }
     if ((st = copy_struct(plan, (void**)&plan->d_ops, d->ops, sizeof(mol_op1d) * d->nops))) return fail(st);
     if ((st = copy_struct(plan, (void**)&plan->d_terms, dev_terms.data(), sizeof(mol_term) * d->nterms)))
         return fail(st);
@@ -663,18 +690,36 @@ int mol_plan_create(const mol_problem_desc* d, mol_plan** out) {
         return fail(st);
     if ((st = build_prec<double>(plan, d, plan->a64, plan->P64))) return fail(st);
     if ((st = build_prec<float>(plan, d, plan->a32, plan->P32))) return fail(st);
+    if (member) {
+        *out = plan;
+        return MOL_OK;
+    }
     if ((st = plan_alloc(plan, (void**)&plan->d_state, sizeof(SolverState)))) return fail(st);
     cudaMemset(plan->d_state, 0, sizeof(SolverState));
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->dev);
-    long long want = (ncell + kThreads - 1) / kThreads;
-    plan->nblocks = (int)std::max<long long>(1, std::min<long long>(want, (long long)sms * 8));
-    if ((st = plan_alloc(plan, (void**)&plan->d_partials, sizeof(double) * 3 * plan->nblocks))) return fail(st);
+    plan->sms = sms;
+    // provisional grid (refined once the kernels' register use is known)
+    plan->nblocks = grid_for(ncell, sms, 2);
+    if ((st = plan_alloc(plan, (void**)&plan->d_partials, sizeof(double) * 3 * (size_t)sms * 8))) return fail(st);
     // the generated right-hand side; MOL_DISABLE_CODEGEN=1 keeps the interpreter (used to cross-check)
     const char* off_env = getenv("MOL_DISABLE_CODEGEN");
     if (!(off_env && off_env[0] == '1')) {
         st = jit_compile(d, &plan->jit, plan->jit_err, &plan->jit_src);
         plan->use_jit = (st == MOL_OK) && plan->jit.ok;
+        if (plan->use_jit) {
+            // Grid = SMs x resident CTAs: every SM gets the same share of the grid-stride loop.
+            cudaFuncAttributes fa;
+            if (cudaFuncGetAttributes(&fa, (const void*)plan->jit.ssp64[0]) == cudaSuccess && fa.numRegs > 0) {
+                const int bps = std::max(1, std::min(8, 65536 / (fa.numRegs * kThreads)));
+                plan->nthreads = threads_for(ncell, sms, bps);
+                const long long slots = (long long)sms * bps;
+                plan->nblocks = (int)std::max<long long>(
+                    1, std::min<long long>(slots, (ncell + plan->nthreads - 1) / plan->nthreads));
+            } else {
+                cudaGetLastError();
+            }
+        }
         if (!plan->use_jit) {
             const char* req = getenv("MOL_REQUIRE_CODEGEN");
             if (req && req[0] == '1') return fail(set_err(plan, st ? st : MOL_ERR_UNSUPPORTED, plan->jit_err));
@@ -683,8 +728,6 @@ int mol_plan_create(const mol_problem_desc* d, mol_plan** out) {
     *out = plan;
     return MOL_OK;
 }
-
-}  // extern "C"
 
 // ----------------------------------------------------------------------------
 // host/device staging
@@ -919,7 +962,7 @@ int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, doubl
             const double* yin = (s % 2 == 0) ? yb0 : yb1;
             double* yout = (s % 2 == 0) ? yb1 : yb0;
             if (plan->use_jit)
-                launch_k(plan->jit.tsit64, nb, kThreads, plan->stream, plan->P64, s, yin, yout, (const double*)ud,
+                launch_k(plan->jit.tsit64, nb, plan->nthreads, plan->stream, plan->P64, s, yin, yout, (const double*)ud,
                          (double* const*)d_k, pp, plan->d_state, plan->d_partials);
             else
                 k_tsit_stage_t<double, InterpCell><<<nb, kThreads, 0, plan->stream>>>(

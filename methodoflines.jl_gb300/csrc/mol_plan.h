@@ -56,6 +56,8 @@ struct mol_plan {
     mol::SolverState* d_state = nullptr;
     double* d_partials = nullptr;
     int nblocks = 0;
+    int sms = 152;
+    int nthreads = 256;
     // adjoint workspaces
     double* adj[16] = {nullptr};
     double* d_snap = nullptr;
@@ -82,6 +84,9 @@ int cuda_check(mol_plan* plan, cudaError_t e, const char* what);
 bool is_device_ptr(const void* p);
 int plan_alloc(mol_plan* plan, void** ptr, size_t bytes);
 int plan_grid(const mol_plan* plan);
+int grid_for(long long ncell, int sms, int blocks_per_sm);
+int threads_for(long long ncell, int sms, int blocks_per_sm);
+int plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member);
 
 template <class T>
 DevProb<T>& prob(mol_plan* plan);

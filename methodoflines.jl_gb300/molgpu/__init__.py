@@ -5,14 +5,14 @@ of MethodOfLines.jl's discretisation front end; every numerical evaluation runs
 in ``libmolgpu.so`` on the GPU.
 """
 from . import _lib
-from .api import (MOLFiniteDifference, ODEFunction, ODEProblem, Plan, Solution, SSPRK33, Tsit5, UpwindScheme,
+from .api import (Batch, MOLFiniteDifference, ODEFunction, ODEProblem, Plan, Solution, SSPRK33, Tsit5, UpwindScheme,
                   WENOScheme, discretize, solve)
 from .lowering import Descriptor, Lowered, lower
 from .symbolic import (Differential, Eq, Equation, Field, Interval, IV, Param, PDESystem, abs_, atan, cos, cosh,
                        exp, ifelse, log, register, sin, sinh, sqrt, tan, tanh)
 
 __all__ = [
-    "MOLFiniteDifference", "ODEFunction", "ODEProblem", "Plan", "Solution", "SSPRK33", "Tsit5", "UpwindScheme",
+    "Batch", "MOLFiniteDifference", "ODEFunction", "ODEProblem", "Plan", "Solution", "SSPRK33", "Tsit5", "UpwindScheme",
     "WENOScheme", "discretize", "solve", "Descriptor", "Lowered", "lower", "Differential", "Eq", "Equation",
     "Field", "Interval", "IV", "Param", "PDESystem", "abs_", "atan", "cos", "cosh", "exp", "ifelse", "log",
     "register", "sin", "sinh", "sqrt", "tan", "tanh",

@@ -129,6 +129,14 @@ class Plan:
                                         float(dt0), int(maxiters), C.byref(stats)), self._h)
         return {"naccept": stats.naccept, "nreject": stats.nreject, "nf": stats.nf, "t": stats.t, "dt": stats.dt}
 
+    @property
+    def uses_codegen(self) -> bool:
+        return bool(L.lib().mol_plan_uses_codegen(self._h))
+
+    @property
+    def generated_source(self) -> str:
+        return (L.lib().mol_plan_codegen_source(self._h) or b"").decode()
+
     def vjp(self, lam, u, p=None, t: float = 0.0, lam_u=None, lam_p=None, lam_aux=None):
         L.check(L.lib().mol_rhs_vjp(self._h, _ptr(lam)[0], _ptr(u)[0], _ptr(p)[0], float(t), _ptr(lam_u)[0],
                                     _ptr(lam_p)[0], _ptr(lam_aux)[0]), self._h)
@@ -146,6 +154,61 @@ class Plan:
     @property
     def aux_sizes(self):
         return [a.size for a in self.lowered.aux]
+
+
+class Batch:
+    """An ensemble of instances of one PDE structure (uneven grids, own parameters) run by
+    one persistent, graph-captured launch (``mol_batch_*``)."""
+
+    def __init__(self, lowereds):
+        self.lowereds = list(lowereds)
+        self.descs = [Descriptor(lw) for lw in self.lowereds]
+        n = len(self.descs)
+        arr = (C.POINTER(L.mol_problem_desc) * n)(*[C.pointer(d.desc) for d in self.descs])
+        h = C.c_void_p()
+        st = L.lib().mol_batch_create(arr, n, C.byref(h))
+        self._h = h
+        if st != 0:
+            msg = (L.lib().mol_batch_last_error(h) or b"").decode() if h.value else ""
+            if h.value:
+                L.lib().mol_batch_destroy(h)
+            self._h = None
+            raise L.MolError(st, msg)
+        off = (C.c_int64 * (n + 1))()
+        L.check(L.lib().mol_batch_offsets(h, off), batch=h)
+        self.offsets = np.array(off[:], dtype=np.int64)
+        self.n = n
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().mol_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int):
+        L.check(L.lib().mol_batch_set_stream(self._h, C.c_void_p(stream_handle)), batch=self._h)
+
+    def pack(self, parts):
+        return np.concatenate([np.asarray(p, dtype=np.float64) for p in parts])
+
+    def step_ssprk33(self, u, dts, nsteps: int, t0: float = 0.0):
+        pu, f32 = _ptr(u)
+        d = np.ascontiguousarray(dts, dtype=np.float64)
+        fn = L.lib().mol_batch_step_ssprk33_f32state if f32 else L.lib().mol_batch_step_ssprk33
+        L.check(fn(self._h, pu, C.c_void_p(d.ctypes.data), float(t0), int(nsteps)), batch=self._h)
+        return u
+
+    def tune(self, threads: int = 0, ctas_per_sm: int = 0):
+        L.check(L.lib().mol_batch_tune(self._h, int(threads), int(ctas_per_sm), 0), batch=self._h)
 
 
 class ODEFunction:

@@ -1,0 +1,66 @@
+"""Batched ensemble: one persistent launch for many uneven instances, against per-instance plans."""
+import numpy as np
+import pytest
+
+from molgpu import Batch, Plan, lower, problems
+from oracle.integrators import ssprk33
+from oracle.mol_oracle import OracleProblem
+
+pytestmark = pytest.mark.gpu
+
+
+def _members(specs):
+    lws, dts = [], []
+    for n, k, seed in specs:
+        sys_, disc, _ = problems.nonlinear_diffusion(n, k, seed)
+        lw = lower(sys_.to_spec(disc))
+        lws.append(lw)
+        dx = 1.0 / (n - 1)
+        dts.append(0.125 * dx * dx / float(np.max(lw.u0)) ** 2)
+    return lws, np.array(dts)
+
+
+SPECS = [(9, 1.3, 1000), (33, 0.2, 1001), (5, 1.9, 1002), (17, 0.7, 1003), (40, 1.1, 1004), (12, 0.0, 1005),
+         (64, 1.6, 1006)]
+
+
+def test_batch_matches_individual_plans(gpu_lib):
+    lws, dts = _members(SPECS)
+    batch = Batch(lws)
+    assert batch.offsets[-1] == sum(lw.n_unknowns for lw in lws)
+    u = batch.pack([lw.u0 for lw in lws])
+    batch.step_ssprk33(u, dts, 25, t0=0.0)
+    for i, lw in enumerate(lws):
+        ref = lw.u0.copy()
+        Plan(lw).step_ssprk33(ref, dts[i], 25, t0=0.0)
+        got = u[batch.offsets[i]:batch.offsets[i + 1]]
+        assert np.allclose(got, ref, rtol=1e-13, atol=1e-15), i
+
+
+def test_batch_against_oracle(gpu_lib):
+    lws, dts = _members(SPECS[:3])
+    batch = Batch(lws)
+    u = batch.pack([lw.u0 for lw in lws])
+    batch.step_ssprk33(u, dts, 10, t0=0.0)
+    for i, (n, k, seed) in enumerate(SPECS[:3]):
+        sys_, disc, _ = problems.nonlinear_diffusion(n, k, seed)
+        orc = OracleProblem(sys_.to_spec(disc))
+        ref, _ = ssprk33(lambda v, t: orc.rhs(v, t), lws[i].u0, 0.0, dts[i], 10)
+        got = u[batch.offsets[i]:batch.offsets[i + 1]]
+        assert np.linalg.norm(got - ref) <= 1e-10 * np.linalg.norm(ref)
+
+
+def test_batch_f32state_and_tuning(gpu_lib):
+    lws, dts = _members(SPECS)
+    batch = Batch(lws)
+    u64 = batch.pack([lw.u0 for lw in lws])
+    u32 = u64.astype(np.float32)
+    batch.tune(128, 2)
+    batch.step_ssprk33(u64, dts, 15)
+    batch.step_ssprk33(u32, dts, 15)
+    err = np.linalg.norm(u32.astype(np.float64) - u64) / np.linalg.norm(u64)
+    assert err < 1e-5
+    batch.tune()  # back to autotuning
+    again = batch.pack([lw.u0 for lw in lws])
+    batch.step_ssprk33(again, dts, 15)
+    assert np.allclose(again, u64, rtol=1e-13, atol=1e-15)

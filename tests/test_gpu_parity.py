@@ -159,3 +159,28 @@ def test_device_pointers_match_host(gpu_lib):
     h = lw.u0.copy()
     plan.step_ssprk33(h, ex["dt"], 33, t0=0.0)
     assert np.array_equal(u.cpu().numpy(), h)
+
+
+@pytest.mark.parametrize("name,kw", [("brusselator", dict(N=64)), ("burgers", dict(npts=1025)),
+                                     ("nonlinear_diffusion", dict(n=33, k=0.7, seed=1004)),
+                                     ("adr3d", dict(N=16, nz_pts=18))])
+def test_generated_rhs_matches_interpreter(gpu_lib, name, kw, monkeypatch):
+    """The generated straight-line RHS and the register-machine interpreter agree."""
+    from molgpu import _lib as L
+    sys_, disc, ex = getattr(problems, name)(**kw)
+    lw = lower(sys_.to_spec(disc))
+    gen = Plan(lw)
+    assert L.lib().mol_plan_uses_codegen(gen.handle) == 1, L.lib().mol_plan_codegen_source(gen.handle)
+    monkeypatch.setenv("MOL_DISABLE_CODEGEN", "1")
+    interp = Plan(lw)
+    assert L.lib().mol_plan_uses_codegen(interp.handle) == 0
+    u = lw.u0 * 1.01
+    a, b = np.zeros_like(u), np.zeros_like(u)
+    gen.rhs(a, u, None, 0.9)
+    interp.rhs(b, u, None, 0.9)
+    assert _rel(a, b) < 1e-13
+    dt = ex.get("dt", ex.get("dt_ssprk", 1e-6))
+    x, y = lw.u0.copy(), lw.u0.copy()
+    gen.step_ssprk33(x, dt, 20)
+    interp.step_ssprk33(y, dt, 20)
+    assert _rel(x, y) < 1e-12
