@@ -1,0 +1,535 @@
+"""Benchmark of the method-of-lines hot path on GB300.
+
+Headline workload: the 2-D periodic Brusselator at 1024 x 1024 (2 fields, 2,097,152
+unknowns), Float64, one fixed SSPRK33 step per bench step (the fixed-step run of the
+Brusselator configuration).  Metric: Mcell-updates/s, a cell-update being one unknown
+advanced by one full step.  Inputs are synthetic (the reference's own initial
+condition and forcing), resident in HBM when timing starts; the 48 MB of state fit in
+L2, so L2 is flushed (a 256 MB write) between timed steps, outside the timed events.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--full]
+
+`--impl reference` times the CPU restatement of the reference's discretisation
+(numpy, the oracle) on the same workload; the reference itself is Julia and cannot
+run on this machine.  `--full` adds the long runs of every configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "methodoflines.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Mcell-updates/s + %HBM roofline; batched & adjoint vs plain, 1 GPU, 1e-10 rel"
+UNIT = "Mcell-updates/s"
+HEADLINE_N = 1024
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# FP64 pipe peak measured on this machine's GB300 with an 8-chain DFMA probe (TFLOP/s).
+FP64_PEAK_TFLOPS = 1.2558
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return rank, world
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed work runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.out = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.out = open(os.path.join("/tmp", f"molgpu_clocks_{os.getpid()}.csv"), "w+")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        res = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            return res
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.seek(0)
+        rows = [r.split(",") for r in self.out.read().strip().splitlines() if r.strip()]
+        self.out.close()
+        try:
+            os.remove(self.out.name)
+        except OSError:
+            pass
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        res.update(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows))
+        return res
+
+
+def brusselator_plan(N):
+    from molgpu import Plan, lower, problems
+    sys_, disc, ex = problems.brusselator(N=N)
+    lw = lower(sys_.to_spec(disc))
+    return Plan(lw), lw, ex
+
+
+# ---------------------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------------------
+
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+    from molgpu import _lib as L
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    hbm_peak, peak_kind = _peaks()
+    plan, lw, ex = brusselator_plan(HEADLINE_N)
+    plan.set_stream(stream.cuda_stream)
+    n = lw.n_unknowns
+    dt = ex["dt_ssprk"]
+    p = torch.tensor(lw.param_values, device=dev)
+    u = torch.tensor(lw.u0, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    t = 0.0
+    for _ in range(args.warmup):
+        plan.step_ssprk33(u, dt, 1, t0=t, p=p)
+        t += dt
+    torch.cuda.synchronize()
+    sampler = ClockSampler(dev.index)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.lib().mol_launch_count()
+    evs = []
+    wall0 = time.perf_counter()
+    reps = max(1, args.steps)
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.step_ssprk33(u, dt, 1, t0=t, p=p)
+        e1.record(stream)
+        evs.append((e0, e1))
+        t += dt
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = L.lib().mol_launch_count() - launches0
+    # keep the GPU busy a little longer so the clock sampler sees the kernels under load
+    tl = time.perf_counter()
+    while time.perf_counter() - tl < 1.0:
+        for _ in range(50):
+            plan.step_ssprk33(u, dt, 1, t0=t, p=p)
+        torch.cuda.synchronize()
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms_total = sum(step_ms)
+    if world > 1:
+        tt = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(tt.item())
+    ms_per_step = ms_total / reps
+    value = world * n * reps / (ms_total * 1e-3) / 1e6
+    # roofline of the dominant kernel: the SSPRK33 stage kernel, 3 launches per step,
+    # 64 algorithmic bytes per unknown and step (16 + 24 + 24), FP64 state
+    bytes_per_step = 64.0 * n
+    achieved = bytes_per_step / (ms_per_step * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("brusselator_1024_ssprk33_step_bytes")
+        except Exception:
+            traffic = None
+    fp64_per_unknown = None
+    if os.path.exists(prof):
+        try:
+            fp64_per_unknown = json.load(open(prof)).get("brusselator_1024_fp64_flops_per_unknown_step")
+        except Exception:
+            pass
+    # e2e: the public C-ABI call with pinned host buffers (H2D + step + D2H each step)
+    host = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    host.copy_(torch.from_numpy(lw.u0))
+    hnp = host.numpy()
+    pnp = lw.param_values.copy()
+    for _ in range(2):
+        plan.step_ssprk33(hnp, dt, 1, t0=0.0, p=pnp)
+    e2e_reps = max(3, min(reps, 50))
+    te = time.perf_counter()
+    for k in range(e2e_reps):
+        plan.step_ssprk33(hnp, dt, 1, t0=k * dt, p=pnp)
+    te = time.perf_counter() - te
+    e2e_value = world * n * e2e_reps / te / 1e6
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": reps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: the reference Brusselator test's initial condition and forcing "
+                "(test/Brusselator/brusselator_eq.jl), 1024x1024 periodic grid",
+        "config": {"workload": "brusselator2d_1024x1024_periodic_ssprk33_step", "unknowns": n,
+                   "fields": 2, "grid": [1024, 1024], "dt": dt, "integrator": "SSPRK33 (fixed step)",
+                   "l2": "flushed between timed steps (256 MB write, outside the timed events)",
+                   "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "codegen": bool(plan.uses_codegen)},
+        "gpu_launches": int(launches),
+        "wall_s_timed_loop": wall,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "kernel": "k_ssprk_t (generated cell, 3 stage launches per step)",
+                     "algorithmic_bytes_per_unknown_step": 64,
+                     "note": "FP64-pipe bound on GB300 (FP64 = 1/64 of FP32); see fp64"},
+        "fp64": {"peak_tflops": FP64_PEAK_TFLOPS,
+                 "flops_per_unknown_step": fp64_per_unknown,
+                 "achieved_tflops": (fp64_per_unknown * n / (ms_per_step * 1e-3) / 1e12) if fp64_per_unknown else None,
+                 "frac": (fp64_per_unknown * n / (ms_per_step * 1e-3) / 1e12 / FP64_PEAK_TFLOPS)
+                 if fp64_per_unknown else None},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
+                "path": "mol_step_ssprk33 with pinned host buffers, one step per call"},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(lw, ex, samples=1)
+    if rank == 0 and not args.headline_only:
+        out["workloads"] = workloads(args, dev, stream)
+    return out
+
+
+def cpu_baseline(lw, ex, samples=1):
+    """The oracle (numpy restatement of the reference discretisation) on the host, one full
+    SSPRK33 step of the same 1024x1024 system per sample."""
+    import numpy as np
+    from molgpu import problems
+    from oracle.integrators import ssprk33
+    from oracle.mol_oracle import OracleProblem
+    sys_, disc, _ = problems.brusselator(N=HEADLINE_N)
+    orc = OracleProblem(sys_.to_spec(disc))
+    u0 = orc.initial_condition()
+    t0 = time.perf_counter()
+    ssprk33(lambda v, t: orc.rhs(v, t), u0, 0.0, ex["dt_ssprk"], samples)
+    el = time.perf_counter() - t0
+    return {"value": orc.n_unknowns * samples / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{samples} full SSPRK33 step(s) of the 1024x1024 Brusselator (2,097,152 unknowns), "
+                      "numpy oracle, single thread"}
+
+
+# ---------------------------------------------------------------------------------------
+# secondary workloads (every configuration; short runs unless --full)
+# ---------------------------------------------------------------------------------------
+
+def _time(fn, stream, reps, warm=True):
+    import torch
+    if warm:
+        fn()  # first call may compile a kernel group (NVRTC) and capture graphs
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def workloads(args, dev, stream):
+    import numpy as np
+    import torch
+    from molgpu import Batch, Plan, lower, problems
+    hbm_peak, _ = _peaks()
+    res = {}
+    full = args.full
+
+    # config 1: heat, Tsit5 1e-10 to t=0.1
+    sys_, disc, _ = problems.heat1d(101)
+    lw = lower(sys_.to_spec(disc))
+    plan = Plan(lw)
+    plan.set_stream(stream.cuda_stream)
+    u = lw.u0.copy()
+    t0 = time.perf_counter()
+    st = plan.solve_tsit5(u, 0.0, 0.1, 1e-10, 1e-10)
+    el = time.perf_counter() - t0
+    lam = -(4 / 0.01 ** 2) * math.sin(math.pi * 0.01 / 2) ** 2
+    res["heat1d_n101_tsit5"] = {"wall_s": el, "naccept": st["naccept"], "nreject": st["nreject"],
+                                "max_err_vs_semidiscrete_exact": float(np.max(np.abs(u - math.exp(lam * 0.1) * lw.u0)))}
+    plan.close()
+
+    # config 2: Brusselator RHS at 256^2 and 1024^2, SSPRK33 step, Tsit5 (short horizon unless --full)
+    for N in (256, 1024):
+        plan, lw, ex = brusselator_plan(N)
+        plan.set_stream(stream.cuda_stream)
+        n = lw.n_unknowns
+        ud = torch.tensor(lw.u0, device=dev)
+        du = torch.zeros_like(ud)
+        ms = _time(lambda: plan.rhs(du, ud, None, 0.5), stream, 20)
+        ms_step = _time(lambda: plan.step_ssprk33(ud, ex["dt_ssprk"], 16), stream, 3) / 16
+        u32 = torch.tensor(lw.u0, device=dev, dtype=torch.float32)
+        du32 = torch.zeros_like(u32)
+        ms32 = _time(lambda: plan.rhs(du32, u32, None, 0.5), stream, 20)
+        res[f"brusselator_{N}"] = {"unknowns": n, "rhs_ms": ms, "rhs_Mcell_s": n / ms / 1e3,
+                                   "rhs_hbm_frac": 16 * n / (ms * 1e-3) / 1e9 / hbm_peak,
+                                   "ssprk33_step_ms": ms_step, "ssprk33_Mcell_s": n / ms_step / 1e3,
+                                   "f32state_rhs_ms": ms32, "f32state_rhs_hbm_frac": 8 * n / (ms32 * 1e-3) / 1e9 / hbm_peak}
+        if N == 256:
+            # explicit Tsit5 on this stiff system is step-size limited by diffusion (dt ~ 6.6e-7):
+            # t = 11.5 needs ~1.7e7 steps, so the timed run covers a short horizon
+            uh = lw.u0.copy()
+            t_end = 0.02 if full else 0.002
+            t0 = time.perf_counter()
+            st = plan.solve_tsit5(uh, 0.0, t_end, 1e-8, 1e-8)
+            res[f"brusselator_{N}"]["tsit5"] = {"t_end": t_end, "wall_s": time.perf_counter() - t0,
+                                                "naccept": st["naccept"], "nreject": st["nreject"]}
+        plan.close()
+
+    # config 3: Burgers WENO5, SSPRK33 (20000 steps with --full) and the discrete adjoint
+    sys_, disc, ex = problems.burgers()
+    lw = lower(sys_.to_spec(disc))
+    plan = Plan(lw)
+    plan.set_stream(stream.cuda_stream)
+    n = lw.n_unknowns
+    nsteps = 20000 if full else 2000
+    ud = torch.tensor(lw.u0, device=dev)
+    plan.step_ssprk33(ud, ex["dt"], 32)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fwd_ms = _time(lambda: plan.step_ssprk33(ud, ex["dt"], nsteps), stream, 1, warm=False)
+    tgt = torch.tensor(ex["target"], device=dev)
+    g = torch.zeros(n, dtype=torch.float64, device=dev)
+    gp = torch.zeros(1, dtype=torch.float64, device=dev)
+    u0d = torch.tensor(lw.u0, device=dev)
+    plan.adjoint_ssprk33(u0d, ex["dt"], 2, tgt, nsnap=2, dLdu0=g, dLdp=gp)   # warm: compiles the VJP
+    torch.cuda.synchronize()
+    ta = time.perf_counter()
+    loss, nfw = plan.adjoint_ssprk33(u0d, ex["dt"], nsteps, tgt, nsnap=64, dLdu0=g, dLdp=gp)
+    torch.cuda.synchronize()
+    adj_s = time.perf_counter() - ta
+    ta = time.perf_counter()
+    plan.adjoint_ssprk33(u0d, ex["dt"], nsteps, tgt, nsnap=0, dLdu0=g, dLdp=gp)
+    torch.cuda.synchronize()
+    adj_all_s = time.perf_counter() - ta
+    res["burgers_65536_weno5"] = {"unknowns": n, "steps": nsteps, "ssprk33_ms_per_step": fwd_ms / nsteps,
+                                  "ssprk33_Mcell_s": n * nsteps / fwd_ms / 1e3,
+                                  "adjoint_64_snapshots_s": adj_s, "adjoint_vs_forward": adj_s / (fwd_ms * 1e-3),
+                                  "adjoint_forward_steps_recomputed": nfw,
+                                  "adjoint_all_steps_stored_s": adj_all_s,
+                                  "adjoint_all_stored_vs_forward": adj_all_s / (fwd_ms * 1e-3),
+                                  "loss": loss, "dLdnu": float(gp.item())}
+    plan.close()
+
+    # config 5: 3-D ADR at 256^3 (RHS, SSPRK33; adjoint dL/dK over a short horizon unless --full)
+    t0 = time.perf_counter()
+    sys_, disc, ex = problems.adr3d(N=256 if full or args.adr256 else 128, nz_pts=258 if full or args.adr256 else 130)
+    lw = lower(sys_.to_spec(disc))
+    setup = time.perf_counter() - t0
+    plan = Plan(lw)
+    plan.set_stream(stream.cuda_stream)
+    n = lw.n_unknowns
+    ud = torch.tensor(lw.u0, device=dev)
+    du = torch.zeros_like(ud)
+    ms = _time(lambda: plan.rhs(du, ud, None, 0.1), stream, 5)
+    ms_step = _time(lambda: plan.step_ssprk33(ud, ex["dt"], 16), stream, 1) / 16
+    u32 = torch.tensor(lw.u0, device=dev, dtype=torch.float32)
+    du32 = torch.zeros_like(u32)
+    ms32 = _time(lambda: plan.rhs(du32, u32, None, 0.1), stream, 5)
+    adj_steps = 500 if full else 20
+    tgt = torch.tensor(np.random.default_rng(12).standard_normal(n) * 1e-3, device=dev)
+    u0d = torch.tensor(lw.u0, device=dev)
+    gaux = torch.zeros(sum(a.size for a in lw.aux), dtype=torch.float64, device=dev)
+    fwd = _time(lambda: plan.step_ssprk33(u0d.clone(), ex["dt"], adj_steps), stream, 1)
+    plan.adjoint_ssprk33(u0d, ex["dt"], 2, tgt, nsnap=2, dLdaux=gaux)   # warm: compiles the VJP
+    torch.cuda.synchronize()
+    ta = time.perf_counter()
+    plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=64, dLdaux=gaux)
+    torch.cuda.synchronize()
+    adj_s = time.perf_counter() - ta
+    side = round(n ** (1 / 3))
+    res[f"adr3d_{side}^3"] = {"unknowns": n, "setup_s": setup, "rhs_ms": ms, "rhs_Mcell_s": n / ms / 1e3,
+                              "rhs_hbm_frac": (16 + 24) * n / (ms * 1e-3) / 1e9 / hbm_peak,
+                              "ssprk33_ms_per_step": ms_step, "ssprk33_Mcell_s": n / ms_step / 1e3,
+                              "f32state_rhs_ms": ms32,
+                              "f32state_rhs_hbm_frac": (8 + 12) * n / (ms32 * 1e-3) / 1e9 / hbm_peak,
+                              "adjoint_steps": adj_steps, "adjoint_dLdK_s": adj_s,
+                              "adjoint_vs_forward": adj_s / (fwd * 1e-3)}
+    plan.close()
+
+    # config 4: batched ensemble of uneven nonlinear-diffusion problems vs sequential plain solves
+    res["batched_nonlinear_diffusion"] = batched(args, dev, stream)
+    return res
+
+
+def batched(args, dev, stream):
+    import numpy as np
+    import torch
+    from molgpu import Batch, Plan, lower, problems
+    count = 4096 if (args.full or args.batch4096) else 512
+    members = problems.ensemble_members(4096)[:count]
+    t0 = time.perf_counter()
+    lws, dts = [], []
+    for (n, k, seed) in members:
+        sys_, disc, _ = problems.nonlinear_diffusion(n, k, seed)
+        lw = lower(sys_.to_spec(disc))
+        lws.append(lw)
+        dx = 1.0 / (n - 1)
+        dts.append(0.125 * dx * dx / float(np.max(lw.u0)) ** 2)
+    dts = np.array(dts)
+    batch = Batch(lws)
+    batch.set_stream(stream.cuda_stream)
+    setup = time.perf_counter() - t0
+    total = int(batch.offsets[-1])
+    steps = 1000 if args.full else 10
+    u = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev)
+    batch.step_ssprk33(u, dts, 2)          # autotune + warm
+    torch.cuda.synchronize()
+    ms = _time(lambda: batch.step_ssprk33(u, dts, steps), stream, 1, warm=False)
+    u32 = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev, dtype=torch.float32)
+    u64 = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev)
+    batch.step_ssprk33(u64, dts, steps)
+    batch.step_ssprk33(u32, dts, 2)
+    ms32 = _time(lambda: batch.step_ssprk33(u32, dts, steps), stream, 1, warm=False)
+    # the f32-state error is measured on a fresh run of the same steps
+    a = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev)
+    b = a.float()
+    batch.step_ssprk33(a, dts, steps)
+    batch.step_ssprk33(b, dts, steps)
+    torch.cuda.synchronize()
+    f32err = float(torch.linalg.norm(b.double() - a) / torch.linalg.norm(a))
+    # sequential plain solves (one plan per instance, same steps) on a stratified sample
+    idx = list(range(0, count, max(1, count // 64)))
+    seq_ms = 0.0
+    for i in idx:
+        p = Plan(lws[i])
+        p.set_stream(stream.cuda_stream)
+        ui = torch.tensor(lws[i].u0, device=dev)
+        p.step_ssprk33(ui, dts[i], 2)
+        seq_ms += _time(lambda: p.step_ssprk33(ui, dts[i], steps), stream, 1, warm=False)
+        p.close()
+    seq_ms *= count / len(idx)
+    batch.close()
+    return {"instances": count, "unknowns": total, "steps": steps, "setup_s": setup,
+            "batched_ms": ms, "batched_Mcell_s": total * steps / ms / 1e3,
+            "f32state_batched_ms": ms32, "f32state_rel_err_vs_f64": f32err,
+            "sequential_plain_ms_estimated": seq_ms,
+            "sequential_sample": f"{len(idx)} of {count} instances, scaled by {count / len(idx):.1f}",
+            "batched_vs_sequential": seq_ms / ms}
+
+
+# ---------------------------------------------------------------------------------------
+# reference arm: the reference's discretisation on the host (numpy oracle)
+# ---------------------------------------------------------------------------------------
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import numpy as np
+    from molgpu import problems
+    from oracle.integrators import ssprk33
+    from oracle.mol_oracle import OracleProblem
+    sys_, disc, ex = problems.brusselator(N=HEADLINE_N)
+    orc = OracleProblem(sys_.to_spec(disc))
+    u = orc.initial_condition()
+    dt = ex["dt_ssprk"]
+    w = max(0, min(args.warmup, 1))
+    for _ in range(w):
+        u, _ = ssprk33(lambda v, t: orc.rhs(v, t), u, 0.0, dt, 1)
+    reps = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    t = 0.0
+    for _ in range(reps):
+        u, t = ssprk33(lambda v, tt: orc.rhs(v, tt), u, t, dt, 1)
+    el = time.perf_counter() - t0
+    value = orc.n_unknowns * reps / el / 1e6
+    sample = (f"{reps} full SSPRK33 step(s) of the 1024x1024 Brusselator (2,097,152 unknowns) per run; "
+              "numpy restatement of the reference discretisation (the reference is Julia and is not "
+              "runnable here)")
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": reps, "warmup": w,
+            "ms_per_step": el / reps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "brusselator2d_1024x1024_periodic_ssprk33_step"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--full", action="store_true", help="long runs of every configuration")
+    ap.add_argument("--adr256", action="store_true", help="3-D ADR at 256^3 in the secondary workloads")
+    ap.add_argument("--batch4096", action="store_true", help="all 4096 ensemble members")
+    ap.add_argument("--headline-only", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world = _dist()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
