@@ -219,6 +219,15 @@ int mol_rhs_f32state(mol_plan* plan, float* du, const float* u, const float* p, 
  * (OrdinaryDiffEqSSPRK SSPRK33, used at benchmark/weno/suite.jl:291-295). */
 int mol_step_ssprk33(mol_plan* plan, double* u, const double* p, double t0, double dt, int64_t nsteps);
 int mol_step_ssprk33_f32state(mol_plan* plan, float* u, const float* p, double t0, double dt, int64_t nsteps);
+/* Same steps as mol_step_ssprk33, for callers that cannot let the call allocate device
+ * memory (inside a CUDA-graph stream capture, under a fixed device-memory budget, in a
+ * host callback).  No counterpart in the reference.  The two stage buffers live in one
+ * static device array sized for at most 2^20 unknowns (16 MiB, held by every GPU that
+ * loads the library until exit); larger plans get MOL_ERR_INVALID.  u and p must be
+ * device memory.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race. */
+int mol_step_ssprk33_noalloc(mol_plan* plan, double* u, const double* p, double t0, double dt, int64_t nsteps);
 
 /* solve(prob, Tsit5(); abstol, reltol) from t0 to t1, in place on u
  * (test/Burgers/burgers_eq.jl:39).  dt0 <= 0 selects the initial step automatically. */

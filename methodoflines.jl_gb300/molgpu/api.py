@@ -120,6 +120,12 @@ class Plan:
         L.check(fn(self._h, pu, pp, float(t0), float(dt), int(nsteps)), self._h)
         return u
 
+    def step_ssprk33_noalloc(self, u, dt: float, nsteps: int, t0: float = 0.0, p=None):
+        """SSPRK33 steps that allocate nothing (device arrays only, at most 2^20 unknowns)."""
+        L.check(L.lib().mol_step_ssprk33_noalloc(self._h, _ptr(u)[0], _ptr(p)[0], float(t0), float(dt), int(nsteps)),
+                self._h)
+        return u
+
     def solve_tsit5(self, u, t0: float, t1: float, abstol: float, reltol: float, p=None, dt0: float = 0.0,
                     maxiters: int = 0):
         pu, _ = _ptr(u)

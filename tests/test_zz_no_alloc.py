@@ -1,0 +1,68 @@
+"""The allocation-free SSPRK33 entry point (mol_step_ssprk33_noalloc).
+
+Callers that cannot let a call allocate device memory (stream capture, fixed
+memory budgets, host callbacks) use it instead of mol_step_ssprk33.  This file
+is collected last so a run that stops at the first failure has already run
+every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from molgpu import Plan, lower, problems
+from molgpu import _lib as L
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-13  # same arithmetic as mol_step_ssprk33; only the stage buffers move
+
+
+def _torch():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+@pytest.mark.parametrize("name,kw", [("brusselator", dict(N=64)), ("burgers", dict(npts=4097))])
+def test_noalloc_matches_step_ssprk33_two_calls(gpu_lib, name, kw):
+    torch = _torch()
+    sys_, disc, ex = getattr(problems, name)(**kw)
+    lw = lower(sys_.to_spec(disc))
+    dt = ex.get("dt", ex.get("dt_ssprk"))
+    a = Plan(lw)
+    b = Plan(lw)
+    ua = torch.tensor(lw.u0, device="cuda")
+    ub = torch.tensor(lw.u0, device="cuda")
+    p = torch.tensor(lw.param_values, device="cuda")
+    # two calls in a row on each path, the second continuing from the first
+    a.step_ssprk33_noalloc(ua, dt, 7, t0=0.0, p=p)
+    b.step_ssprk33(ub, dt, 7, t0=0.0, p=p)
+    torch.cuda.synchronize()
+    x, y = ua.cpu().numpy(), ub.cpu().numpy()
+    assert np.linalg.norm(x - y) <= TOL * np.linalg.norm(y)
+    a.step_ssprk33_noalloc(ua, dt, 5, t0=7 * dt, p=p)
+    b.step_ssprk33(ub, dt, 5, t0=7 * dt, p=p)
+    torch.cuda.synchronize()
+    x, y = ua.cpu().numpy(), ub.cpu().numpy()
+    assert np.linalg.norm(x - y) <= TOL * np.linalg.norm(y)
+    a.close()
+    b.close()
+
+
+def test_noalloc_rejects_oversized_and_host_arrays(gpu_lib):
+    torch = _torch()
+    sys_, disc, ex = problems.brusselator(N=1024)       # 2,097,152 unknowns > 2^20
+    big = Plan(lower(sys_.to_spec(disc)))
+    u = torch.zeros(big.n, dtype=torch.float64, device="cuda")
+    with pytest.raises(L.MolError) as e:
+        big.step_ssprk33_noalloc(u, 1e-9, 1)
+    assert e.value.status == -1 and "scratch limit" in str(e.value)
+    big.close()
+    sys_, disc, ex = problems.brusselator(N=16)
+    small = Plan(lower(sys_.to_spec(disc)))
+    with pytest.raises(L.MolError) as e:
+        small.step_ssprk33_noalloc(np.zeros(small.n), 1e-9, 1)
+    assert e.value.status == -1 and "device memory" in str(e.value)
+    small.close()
