@@ -205,6 +205,9 @@ int64_t mol_launch_count(void);
  * register-machine interpreter; the source text (or the reason it is off). */
 int mol_plan_uses_codegen(const mol_plan* plan);
 const char* mol_plan_codegen_source(const mol_plan* plan);
+/* Registers per thread of the generated stage kernel (0 for the interpreter), threads per
+ * CTA and CTAs of the plan's grid-stride launches. */
+int mol_plan_launch_config(const mol_plan* plan, int32_t* regs, int32_t* threads, int32_t* blocks);
 
 /* ------------------------------------------------------------------------ */
 /* Hot path                                                                  */
@@ -266,9 +269,15 @@ int mol_batch_offsets(const mol_batch* batch, int64_t* offsets);
 /* One persistent launch advances every instance nsteps SSPRK33 steps with its own dt. */
 int mol_batch_step_ssprk33(mol_batch* batch, double* u_packed, const double* dts, double t0, int64_t nsteps);
 int mol_batch_step_ssprk33_f32state(mol_batch* batch, float* u_packed, const double* dts, double t0, int64_t nsteps);
-/* Tuning: threads per CTA, CTAs per SM, and the largest instance (cells) kept in
- * shared memory; 0 keeps the autotuned value. */
-int mol_batch_tune(mol_batch* batch, int32_t threads, int32_t ctas_per_sm, int64_t smem_cells);
+/* Tuning: threads per CTA, CTAs per SM and the schedule: tile_cells > 0 splits every
+ * stage of every instance into tiles of that many cells (units handed out across the
+ * GPU, stages ordered per instance by counters), tile_cells < 0 runs one CTA per
+ * instance.  0 leaves a setting as it is; all three 0 autotune again on the next run. */
+int mol_batch_tune(mol_batch* batch, int32_t threads, int32_t ctas_per_sm, int64_t tile_cells);
+/* Waits for the batch's stream and reports a run that was abandoned because a stage
+ * dependency wait ran out of its poll budget (MOL_ERR_CUDA; the flag is then cleared).
+ * Steps on host arrays call it themselves. */
+int mol_batch_check(mol_batch* batch);
 
 #ifdef __cplusplus
 }

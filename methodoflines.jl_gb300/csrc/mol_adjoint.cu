@@ -116,11 +116,10 @@ struct Adj {
 
     void stage(int which, const double* uin, const double* u0, double* uout, double t) {
         if (err) return;
-        set_time(t);
         const DevProb<double>& P = plan->P64;
         const double* cu = uin;
         cudaError_t e = launch_k(plan->jit.ssp64[which - 1], plan->nblocks, plan->nthreads, plan->stream, P, cu, u0, uout,
-                                 p, plan->d_state, dt);
+                                 p, plan->d_state, dt, t);
         ++g_launches;
         ck(e, "stage launch");
     }

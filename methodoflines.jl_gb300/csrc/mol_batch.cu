@@ -1,12 +1,16 @@
 // Batched ensemble: many instances of one PDE structure with uneven grids.
 //
 // Every instance is lowered on the host exactly like a single problem; the
-// ensemble then runs one persistent kernel in which each CTA takes the next
-// instance (largest first, handed out by an atomic ticket) and integrates it
-// for all requested SSPRK33 steps, synchronising only its own threads between
-// stages.  There is no grid-wide barrier and no inter-CTA wait.  The launch
-// (ticket reset + kernel) is captured once in a CUDA graph and replayed.
-// Threads per CTA and CTAs per SM are autotuned on the ensemble itself.
+// ensemble then runs one persistent kernel, captured once in a CUDA graph with
+// the resets of its work counters and replayed.  Two schedules:
+//  - tiles (default): the work unit is one tile of one SSPRK33 stage of one
+//    instance; a 64-bit ticket hands units out round by round (largest instances
+//    first) and a per-instance counter of finished tiles orders the stages of an
+//    instance across CTAs, so one large member spreads over the whole GPU;
+//  - instances: each CTA takes the next whole instance and integrates it for all
+//    steps, synchronising only its own threads between stages.
+// Schedule, threads per CTA, CTAs per SM and tile size are autotuned on the
+// ensemble itself.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,18 +42,24 @@ struct mol_batch {
     int* d_order = nullptr;
     double* d_dt = nullptr;
     unsigned* d_ticket = nullptr;
+    // tiled schedule: [ticket u64][status i32 + pad][done u64 x n] in one allocation
+    unsigned long long* d_sync = nullptr;
+    long long* d_tile_pre = nullptr;
+    int tile_cells_uploaded = 0;
     const double** d_par64 = nullptr;
     const float** d_par32 = nullptr;
     double* s64[3] = {nullptr, nullptr, nullptr};  // state (staging), u1, u2
     float* s32[3] = {nullptr, nullptr, nullptr};
     int threads = 256, ctas_per_sm = 2, sms = 152;
+    int tile_cells = 2048;   // > 0 tiled schedule, 0 one CTA per instance
     bool tuned = false;
     std::vector<void*> allocs;
     cudaGraphExec_t graph = nullptr;
     const void* g_key[4] = {nullptr, nullptr, nullptr, nullptr};
     long long g_steps = -1;
     double g_t0 = 0.0;
-    int g_cfg[2] = {0, 0};
+    int g_cfg[3] = {0, 0, 0};
+    std::vector<int> order;       // slot -> instance (largest first)
 };
 
 namespace {
@@ -73,30 +83,61 @@ int balloc(mol_batch* b, void** p, size_t bytes) {
     return MOL_OK;
 }
 
+// Tile prefix sums of the instances in slot order for a tile size.
+int upload_tiles(mol_batch* b, int tile_cells) {
+    if (b->tile_cells_uploaded == tile_cells) return MOL_OK;
+    std::vector<long long> pre(b->n + 1, 0);
+    for (int s = 0; s < b->n; ++s) {
+        const long long nc = b->plans[b->order[s]]->ncell;
+        pre[s + 1] = pre[s] + (nc + tile_cells - 1) / tile_cells;
+    }
+    int st = bcheck(b, cudaMemcpyAsync(b->d_tile_pre, pre.data(), sizeof(long long) * (b->n + 1),
+                                       cudaMemcpyHostToDevice, b->stream), "tile table");
+    if (!st) st = bcheck(b, cudaStreamSynchronize(b->stream), "tile table");
+    if (!st) b->tile_cells_uploaded = tile_cells;
+    return st;
+}
+
 template <class T>
-int run(mol_batch* b, T* U, const double* dts_host, double t0, long long nsteps, int threads, int ctas) {
+int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, int tile_cells) {
     const bool is64 = std::is_same<T, double>::value;
-    T* const* S = nullptr;
-    (void)S;
     T* U1 = is64 ? (T*)b->s64[1] : (T*)b->s32[1];
     T* U2 = is64 ? (T*)b->s64[2] : (T*)b->s32[2];
     const DevProb<T>* probs = is64 ? (const DevProb<T>*)b->d_p64 : (const DevProb<T>*)b->d_p32;
     const T* const* params = is64 ? (const T* const*)b->d_par64 : (const T* const*)b->d_par32;
-    cudaKernel_t k = is64 ? b->jit.batch64 : b->jit.batch32;
+    const bool tiled = tile_cells > 0;
+    cudaKernel_t k = tiled ? (is64 ? b->jit.tiles64 : b->jit.tiles32) : (is64 ? b->jit.batch64 : b->jit.batch32);
     int st;
-    if (dts_host)
-        if ((st = bcheck(b, cudaMemcpyAsync(b->d_dt, dts_host, sizeof(double) * b->n,
-                                            is_device_ptr(dts_host) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                                            b->stream), "dt")))
-            return st;
+    if (tiled && (st = upload_tiles(b, tile_cells))) return st;
     const int grid = b->sms * ctas;
     const long long* off = b->d_off;
     const int* order = b->d_order;
     const int ninst = b->n;
     unsigned* ticket = b->d_ticket;
-    // one replayable graph: ticket reset + persistent kernel
+    BatchSync sync;
+    sync.ticket = b->d_sync;
+    sync.status = (int*)(b->d_sync + 1);
+    sync.done = b->d_sync + 2;
+    const size_t sync_bytes = sizeof(unsigned long long) * (2 + (size_t)b->n);
+    auto enqueue = [&]() -> cudaError_t {
+        if (tiled) {
+            // the status word survives replays so a failed run stays visible to mol_batch_check
+            cudaError_t e = cudaMemsetAsync(b->d_sync, 0, sizeof(unsigned long long), b->stream);
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(b->d_sync + 2, 0, sync_bytes - 2 * sizeof(unsigned long long), b->stream);
+            if (e != cudaSuccess) return e;
+            return launch_k(k, grid, threads, b->stream, probs, off, order, (const long long*)b->d_tile_pre, ninst,
+                            tile_cells, U, U1, U2, params, (const double*)b->d_dt, t0, nsteps, sync);
+        }
+        cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned), b->stream);
+        if (e != cudaSuccess) return e;
+        return launch_k(k, grid, threads, b->stream, probs, off, order, ninst, U, U1, U2, params,
+                        (const double*)b->d_dt, t0, nsteps, ticket);
+    };
+    // one replayable graph: counter resets + persistent kernel
     const bool key_ok = b->graph && b->g_key[0] == (const void*)U && b->g_key[1] == (const void*)k &&
-                        b->g_steps == nsteps && b->g_t0 == t0 && b->g_cfg[0] == threads && b->g_cfg[1] == ctas;
+                        b->g_steps == nsteps && b->g_t0 == t0 && b->g_cfg[0] == threads && b->g_cfg[1] == ctas &&
+                        b->g_cfg[2] == tile_cells;
     const bool can_capture = b->stream != nullptr && b->stream != cudaStreamLegacy;
     if (!key_ok && can_capture) {
         if (b->graph) {
@@ -105,10 +146,10 @@ int run(mol_batch* b, T* U, const double* dts_host, double t0, long long nsteps,
         }
         cudaGraph_t g;
         if ((st = bcheck(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture"))) return st;
-        cudaMemsetAsync(ticket, 0, sizeof(unsigned), b->stream);
-        launch_k(k, grid, threads, b->stream, probs, off, order, ninst, U, U1, U2, params, (const double*)b->d_dt, t0,
-                 nsteps, ticket);
-        if ((st = bcheck(b, cudaStreamEndCapture(b->stream, &g), "end capture"))) return st;
+        cudaError_t ee = enqueue();
+        cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+        if ((st = bcheck(b, ee, "batch capture"))) return st;
+        if ((st = bcheck(b, ec, "end capture"))) return st;
         st = bcheck(b, cudaGraphInstantiate(&b->graph, g, 0), "instantiate");
         cudaGraphDestroy(g);
         if (st) return st;
@@ -118,29 +159,43 @@ int run(mol_batch* b, T* U, const double* dts_host, double t0, long long nsteps,
         b->g_t0 = t0;
         b->g_cfg[0] = threads;
         b->g_cfg[1] = ctas;
+        b->g_cfg[2] = tile_cells;
     }
     ++g_launches;
     if (can_capture) return bcheck(b, cudaGraphLaunch(b->graph, b->stream), "batch graph launch");
-    cudaMemsetAsync(ticket, 0, sizeof(unsigned), b->stream);
-    return bcheck(b, launch_k(k, grid, threads, b->stream, probs, off, order, ninst, U, U1, U2, params,
-                              (const double*)b->d_dt, t0, nsteps, ticket), "batch launch");
+    return bcheck(b, enqueue(), "batch launch");
+}
+
+// CTAs of `k` that fit on one SM at `threads` per CTA (0 if the query fails).
+int resident_ctas(cudaKernel_t k, int threads) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k, threads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nb;
 }
 
 template <class T>
 int tune(mol_batch* b, T* U, long long probe_steps) {
-    // Candidates within the register budget of the kernel (launch bound 256 threads).
-    cudaFuncAttributes fa;
-    int regs = 128;
-    if (cudaFuncGetAttributes(&fa, (const void*)(std::is_same<T, double>::value ? b->jit.batch64 : b->jit.batch32)) ==
-            cudaSuccess && fa.numRegs > 0)
-        regs = fa.numRegs;
-    else
-        cudaGetLastError();
-    std::vector<std::pair<int, int>> cand;
-    for (int th : {128, 256})
-        for (int c : {1, 2, 3, 4, 6, 8})
-            if ((long long)th * c * regs <= 65536 && th * c <= 2048) cand.push_back({th, c});
-    if (cand.empty()) cand.push_back({128, 1});
+    const bool is64 = std::is_same<T, double>::value;
+    struct Cand {
+        int threads, ctas, tile;
+    };
+    std::vector<Cand> cand;
+    for (int tiled = 0; tiled < 2; ++tiled) {
+        cudaKernel_t k = tiled ? (is64 ? b->jit.tiles64 : b->jit.tiles32) : (is64 ? b->jit.batch64 : b->jit.batch32);
+        for (int th : {128, 256}) {
+            const int maxc = resident_ctas(k, th);
+            for (int c : {1, 2, 3, 4, 6, 8}) {
+                if (c > maxc) continue;
+                if (!tiled) cand.push_back({th, c, 0});
+                else
+                    for (int per : {4, 16}) cand.push_back({th, c, th * per});
+            }
+        }
+    }
+    if (cand.empty()) cand.push_back({128, 1, 0});
     // time on a scratch copy of the state so tuning leaves the caller's data alone
     T* scratch = nullptr;
     if (cudaMalloc(&scratch, sizeof(T) * b->total) != cudaSuccess) {
@@ -151,11 +206,11 @@ int tune(mol_batch* b, T* U, long long probe_steps) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    std::pair<int, int> pick = cand[0];
+    Cand pick = cand[0];
     for (auto& c : cand) {
         cudaMemcpyAsync(scratch, U, sizeof(T) * b->total, cudaMemcpyDeviceToDevice, b->stream);
         cudaEventRecord(e0, b->stream);
-        int st = run<T>(b, scratch, nullptr, 0.0, probe_steps, c.first, c.second);
+        int st = run<T>(b, scratch, 0.0, probe_steps, c.threads, c.ctas, c.tile);
         cudaEventRecord(e1, b->stream);
         cudaEventSynchronize(e1);
         if (st) break;
@@ -173,8 +228,9 @@ int tune(mol_batch* b, T* U, long long probe_steps) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
-    b->threads = pick.first;
-    b->ctas_per_sm = pick.second;
+    b->threads = pick.threads;
+    b->ctas_per_sm = pick.ctas;
+    b->tile_cells = pick.tile;
     b->tuned = true;
     return MOL_OK;
 }
@@ -197,11 +253,11 @@ int step_impl(mol_batch* b, T* u, const double* dts, double t0, int64_t nsteps) 
                                         b->stream), "dt")))
         return st;
     if (!b->tuned && nsteps > 0) tune<T>(b, U, std::min<int64_t>(nsteps, 2));
-    if ((st = run<T>(b, U, nullptr, t0, nsteps, b->threads, b->ctas_per_sm))) return st;
+    if ((st = run<T>(b, U, t0, nsteps, b->threads, b->ctas_per_sm, b->tile_cells))) return st;
     if (host) {
         if ((st = bcheck(b, cudaMemcpyAsync(u, U, sizeof(T) * b->total, cudaMemcpyDeviceToHost, b->stream), "D2H")))
             return st;
-        return bcheck(b, cudaStreamSynchronize(b->stream), "sync");
+        return mol_batch_check(b);
     }
     return bcheck(b, cudaGetLastError(), "batch");
 }
@@ -249,6 +305,7 @@ int mol_batch_create(const mol_problem_desc* const* descs, int32_t n, mol_batch*
     std::string err;
     b->jit.src = b->src;
     b->jit.nparams = descs[0]->nparams;
+    b->jit.min_blocks = 2;
     b->jit.ok = true;
     if ((st = jit_ensure(&b->jit, JIT_BATCH, err))) return berr(b, st, err);
     if ((st = bcheck(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream"))) return st;
@@ -268,6 +325,10 @@ int mol_batch_create(const mol_problem_desc* const* descs, int32_t n, mol_batch*
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int c) { return b->plans[a]->ncell > b->plans[c]->ncell; });
+    b->order = order;
+    if ((st = balloc(b, (void**)&b->d_sync, sizeof(unsigned long long) * (2 + (size_t)n)))) return st;
+    if ((st = balloc(b, (void**)&b->d_tile_pre, sizeof(long long) * (n + 1)))) return st;
+    cudaMemset(b->d_sync, 0, sizeof(unsigned long long) * (2 + (size_t)n));
     if ((st = balloc(b, (void**)&b->d_p64, sizeof(DevProb<double>) * n))) return st;
     if ((st = balloc(b, (void**)&b->d_p32, sizeof(DevProb<float>) * n))) return st;
     if ((st = balloc(b, (void**)&b->d_off, sizeof(long long) * (n + 1)))) return st;
@@ -324,9 +385,27 @@ int mol_batch_step_ssprk33_f32state(mol_batch* b, float* u, const double* dts, d
     return step_impl<float>(b, u, dts, t0, nsteps);
 }
 
-int mol_batch_tune(mol_batch* b, int32_t threads, int32_t ctas_per_sm, int64_t smem_cells) {
+int mol_batch_check(mol_batch* b) {
     if (!b) return MOL_ERR_INVALID;
-    (void)smem_cells;
+    int st = bcheck(b, cudaStreamSynchronize(b->stream), "batch sync");
+    if (st) return st;
+    int status = 0;
+    if ((st = bcheck(b, cudaMemcpy(&status, (int*)(b->d_sync + 1), sizeof(int), cudaMemcpyDeviceToHost), "status")))
+        return st;
+    if (status) {
+        cudaMemset((int*)(b->d_sync + 1), 0, sizeof(int));
+        return berr(b, MOL_ERR_CUDA, "batch: a stage dependency wait ran out of its poll budget; the run was abandoned");
+    }
+    return MOL_OK;
+}
+
+int mol_batch_tune(mol_batch* b, int32_t threads, int32_t ctas_per_sm, int64_t tile_cells) {
+    if (!b) return MOL_ERR_INVALID;
+    if (tile_cells != 0) {
+        if (tile_cells > (1ll << 30)) return berr(b, MOL_ERR_INVALID, "tile_cells too large");
+        b->tile_cells = tile_cells < 0 ? 0 : (int)tile_cells;
+        b->tuned = true;
+    }
     if (threads > 0) {
         if (threads % 32 || threads > 256) return berr(b, MOL_ERR_INVALID, "threads must be a multiple of 32, <= 256");
         b->threads = threads;
@@ -336,7 +415,7 @@ int mol_batch_tune(mol_batch* b, int32_t threads, int32_t ctas_per_sm, int64_t s
         b->ctas_per_sm = ctas_per_sm;
         b->tuned = true;
     }
-    if (threads == 0 && ctas_per_sm == 0) b->tuned = false;  // autotune again on the next run
+    if (threads == 0 && ctas_per_sm == 0 && tile_cells == 0) b->tuned = false;  // autotune again on the next run
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;

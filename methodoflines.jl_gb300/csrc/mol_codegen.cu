@@ -248,6 +248,12 @@ void emit_reverse(Emitter& e, const SSA& s, const Leaves& L, const std::string& 
 
 bool zero_w(const mol_problem_desc* d, long long off) { return d->weights[off] == 0.0; }
 
+// Warp-shuffle aggregation of contiguous-axis VJP scatters (MOL_JIT_WARP_SCATTER=0 turns it off).
+bool warp_scatter() {
+    const char* w = getenv("MOL_JIT_WARP_SCATTER");
+    return !(w && w[0] == '0');
+}
+
 // Leaves of the cell program.
 struct CellLeaves : Leaves {
     std::string field(int f) const override { return "u[(long long)" + std::to_string(f) + " * P.ncell + c]"; }
@@ -256,14 +262,35 @@ struct CellLeaves : Leaves {
         return "P.coords[" + std::to_string(dd) + "][I[" + std::to_string(dd) + "] - 1]";
     }
     std::string term(int k) const override { return "gt" + std::to_string(k) + "<T>(P, u, c, I, t, p)"; }
+    // inside the cell VJP the own-cell share of field f collects in own<f>
+    const mol_problem_desc* d = nullptr;
     std::string field_adj(int f, const std::string& g) const override {
-        return "    atomicAdd(lam_u + (long long)" + std::to_string(f) + " * P.ncell + c, " + g + ");\n";
+        return "    own" + std::to_string(f) + " += " + g + ";\n";
     }
     std::string aux_adj(int k, const std::string& g) const override {
         return "    if (lam_aux) atomicAdd(lam_aux + P.aux_off[" + std::to_string(k) + "] + c, " + g + ");\n";
     }
     std::string term_adj(int k, const std::string& g) const override {
-        return "    gt" + std::to_string(k) + "_vjp<T>(P, u, c, I, t, p, " + g + ", lam_u, lp, lam_aux);\n";
+        return "    gt" + std::to_string(k) + "_vjp<T>(P, u, c, I, t, p, " + g + ", lam_u, lp, lam_aux, own" +
+               std::to_string(d->terms[k].field) + ");\n";
+    }
+};
+
+// Leaves of the cell program inside the cell VJP: WENO terms named in `split` use
+// their split forward/backward pair, which share the partials in fwK/gwK.
+struct VjpCellLeaves : CellLeaves {
+    std::vector<int> split;
+    bool is_split(int k) const { return std::find(split.begin(), split.end(), k) != split.end(); }
+    std::string term(int k) const override {
+        if (!is_split(k)) return CellLeaves::term(k);
+        const std::string K = std::to_string(k);
+        return "gt" + K + "_fg<T>(P, u, c, I, t, p, fw" + K + ", gw" + K + ")";
+    }
+    std::string term_adj(int k, const std::string& g) const override {
+        if (!is_split(k)) return CellLeaves::term_adj(k, g);
+        const std::string K = std::to_string(k);
+        return "    gt" + K + "_bg<T>(P, u, c, I, t, p, " + g + ", fw" + K + ", gw" + K + ", lam_u, lp, lam_aux, own" +
+               std::to_string(d->terms[k].field) + ");\n";
     }
 };
 
@@ -314,13 +341,20 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
     // vjp
     e << "template <class T>\n__device__ __forceinline__ void gt" << K
       << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
-         "T g, T* lam_u, T* lp, T* lam_aux) {\n"
+         "T g, T* lam_u, T* lp, T* lam_aux, T& own) {\n"
       << "    if (" << fast_cond << ") {\n"
       << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int;\n"
       << "        T* b = lam_u + (long long)" << F << " * P.ncell + c;\n"
       << "        const long long s = gstride(P, " << D << ");\n";
-    for (int m : nz)
-        e << "        atomicAdd(b + (long long)(" << (o.omin + m) << ") * s, g * w[" << m << "]);\n";
+    if (!nz.empty()) {
+        e << "        const T vv[" << o.L << "] = {";
+        for (int m = 0; m < o.L; ++m) {
+            const bool z = std::find(nz.begin(), nz.end(), m) == nz.end();
+            e << (m ? ", " : "") << (z ? std::string("T(0)") : "g * w[" + std::to_string(m) + "]");
+        }
+        e << "};\n        scatter_taps<T, " << o.L << ", " << o.omin << ", " << (warp_scatter() ? "true" : "false")
+          << ">(b, c, s, vv, own);\n";
+    }
     e << "        return;\n    }\n    scatter_op(P, P.ops[" << tm.op << "], lam_u, " << F << ", " << D << ", I, I[" << D
       << "], P.n[" << D << "], g, t, p);\n}\n";
 }
@@ -363,36 +397,56 @@ void emit_mixed(Emitter& e, const mol_problem_desc* d, int k) {
     e << "    return apply_mixed(P, P.terms[" << k << "], u, I, t, p);\n}\n";
     e << "template <class T>\n__device__ __forceinline__ void gt" << K
       << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
-         "T g, T* lam_u, T* lp, T* lam_aux) {\n";
+         "T g, T* lam_u, T* lp, T* lam_aux, T& own) {\n";
     body(true);
     e << "    scatter_mixed(P, P.terms[" << k << "], lam_u, I, g, t, p);\n}\n";
 }
 
+// WENO5 term.  Only the tap loads (and, in the VJP, the scatters) differ between
+// interior cells and cells near an edge; the FP64 arithmetic is emitted once after
+// the branch so a warp that straddles the edge runs it converged.
 void emit_weno(Emitter& e, const mol_problem_desc* d, int k) {
     const mol_term& tm = d->terms[k];
     const std::string K = std::to_string(k), F = std::to_string(tm.field), D = std::to_string(tm.dim);
     const std::string cond = "fast_weno(P, " + F + ", " + D + ", I[" + D + "])";
-    e << "template <class T>\n__device__ __forceinline__ T gt" << K
-      << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) {\n"
-      << "    if (" << cond << ") {\n"
-      << "        const T* __restrict__ b = u + (long long)" << F << " * P.ncell + c;\n"
-      << "        const long long s = gstride(P, " << D << ");\n"
-      << "        return weno5_point<T>(b[-2 * s], b[-s], b[0], b[s], b[2 * s], T(P.terms[" << K << "].eps), T(P.terms["
-      << K << "].dx));\n    }\n"
-      << "    return apply_weno(P, P.terms[" << K << "], u, I, t, p);\n}\n";
-    e << "template <class T>\n__device__ __forceinline__ void gt" << K
-      << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
-         "T g, T* lam_u, T* lp, T* lam_aux) {\n"
-      << "    if (" << cond << ") {\n"
-      << "        const T* __restrict__ b = u + (long long)" << F << " * P.ncell + c;\n"
-      << "        T* lb = lam_u + (long long)" << F << " * P.ncell + c;\n"
-      << "        const long long s = gstride(P, " << D << ");\n"
-      << "        T gr[5];\n"
-      << "        weno5_grad<T>(b[-2 * s], b[-s], b[0], b[s], b[2 * s], T(P.terms[" << K << "].eps), T(P.terms[" << K
-      << "].dx), gr);\n"
-      << "#pragma unroll\n        for (int m = 0; m < 5; ++m) atomicAdd(lb + (long long)(m - 2) * s, g * gr[m]);\n"
-      << "        return;\n    }\n"
-      << "    scatter_weno(P, P.terms[" << K << "], u, lam_u, I, g, t, p);\n}\n";
+    const char* W = warp_scatter() ? "true" : "false";
+    const std::string sig = "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, "
+                            "const T* __restrict__ p";
+    const std::string load =
+        "    T v[5];\n"
+        "    if (" + cond + ") {\n"
+        "        const T* __restrict__ b = u + (long long)" + F + " * P.ncell + c;\n"
+        "        const long long s = gstride(P, " + D + ");\n"
+        "        v[0] = b[-2 * s]; v[1] = b[-s]; v[2] = b[0]; v[3] = b[s]; v[4] = b[2 * s];\n"
+        "    } else {\n"
+        "        weno_taps(P, P.terms[" + K + "], u, I, t, p, v);\n"
+        "    }\n";
+    const std::string args = "v[0], v[1], v[2], v[3], v[4], T(P.terms[" + K + "].eps), T(P.terms[" + K + "].dx)";
+    // scatter of vv[5] (already multiplied by the adjoint seed) on the path `fastexpr` picks
+    auto scatter = [&](const std::string& fastexpr) {
+        return "    if (" + fastexpr + ") {\n"
+               "        T* lb = lam_u + (long long)" + F + " * P.ncell + c;\n"
+               "        scatter_taps<T, 5, -2, " + W + ">(lb, c, gstride(P, " + D + "), vv, own);\n"
+               "    } else {\n"
+               "        scatter_weno_taps(P, P.terms[" + K + "], lam_u, I, vv, t, p);\n"
+               "    }\n";
+    };
+    e << "template <class T>\n__device__ __forceinline__ T gt" << K << sig << ") {\n"
+      << load << "    return weno5_point<T>(" << args << ");\n}\n";
+    e << "template <class T>\n__device__ __forceinline__ void gt" << K << "_vjp" << sig
+      << ", T g, T* lam_u, T* lp, T* lam_aux, T& own) {\n"
+      << load << "    T gr[5];\n    weno5_grad<T>(" << args << ", gr);\n"
+      << "    const T vv[5] = {g * gr[0], g * gr[1], g * gr[2], g * gr[3], g * gr[4]};\n"
+      << scatter(cond) << "}\n";
+    // split form for the cell VJP: the forward keeps the five partials in registers,
+    // the backward only scatters them (one reciprocal per cell instead of two)
+    e << "template <class T>\n__device__ __forceinline__ T gt" << K << "_fg" << sig << ", bool& fast, T* gr) {\n"
+      << "    fast = " << cond << ";\n"
+      << load << "    return weno5_valgrad<T>(" << args << ", gr);\n}\n";
+    e << "template <class T>\n__device__ __forceinline__ void gt" << K << "_bg" << sig
+      << ", T g, bool fast, const T* gr, T* lam_u, T* lp, T* lam_aux, T& own) {\n"
+      << "    const T vv[5] = {g * gr[0], g * gr[1], g * gr[2], g * gr[3], g * gr[4]};\n"
+      << scatter("fast") << "}\n";
 }
 
 // Nonlinear Laplacian.  The face value a(x~, u~) * (D_inner u) at half point Ih
@@ -544,7 +598,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
         else
             e << "template <class T>\n__device__ __forceinline__ void gt" << K
               << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* "
-                 "__restrict__ p, T g, T* lam_u, T* lp, T* lam_aux) {\n";
+                 "__restrict__ p, T g, T* lam_u, T* lp, T* lam_aux, T& own) {\n";
         e << "    if (" << cond << ") {\n"
           << "    const T* __restrict__ wo = P.w + P.ops[" << opo << "].w_int;\n"
           << "    const T* __restrict__ wi = P.w + P.ops[" << opi << "].w_int;\n"
@@ -573,6 +627,299 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
 
 }  // namespace
 
+// ----------------------------------------------------------------------------
+// The cell function: uniform hoisting and linear-stencil fusion.
+//
+// Values that depend only on constants, parameters and time are computed once per
+// thread (gen_uniform) instead of once per cell.  A linear combination of LINEAR /
+// MIXED terms of one field with uniform coefficients (e.g. alpha*(Dxx u + Dyy u)) is
+// evaluated, where every member term is on its interior fast path, as ONE stencil over
+// the union of the taps with pre-combined weights (shared centre tap, coefficient
+// folded in); elsewhere the original statements run.  On GB300 this removes FP64
+// operations, the binding resource.
+// ----------------------------------------------------------------------------
+
+struct LinInfo {
+    bool ok = false;
+    int field = -1;
+    std::map<int, std::string> coef;  // term -> coefficient expression (uniform)
+    std::vector<int> members;         // non-uniform pcs of the tree (terms included)
+};
+
+static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s, const std::string& cell_attr) {
+    const int n = (int)s.ins.size();
+    std::vector<char> uni(n, 0);
+    std::vector<int> uses(n, 0);
+    for (int pc = 0; pc < n; ++pc) {
+        const mol_instr& in = s.ins[pc];
+        for (int x : {s.ia[pc], s.ib[pc], s.ic[pc]})
+            if (x >= 0) uses[x]++;
+        switch (in.op) {
+            case MOL_OP_CONST: case MOL_OP_PARAM: case MOL_OP_TIME: uni[pc] = 1; break;
+            case MOL_OP_ADD: case MOL_OP_SUB: case MOL_OP_MUL: case MOL_OP_DIV: case MOL_OP_POW: case MOL_OP_CMP:
+                uni[pc] = uni[s.ia[pc]] && uni[s.ib[pc]];
+                break;
+            case MOL_OP_NEG: case MOL_OP_POWI: case MOL_OP_FN: uni[pc] = uni[s.ia[pc]]; break;
+            case MOL_OP_IFELSE: uni[pc] = uni[s.ia[pc]] && uni[s.ib[pc]] && uni[s.ic[pc]]; break;
+            default: uni[pc] = 0;
+        }
+    }
+    auto name = [&](int pc) { return uni[pc] ? "U.u" + std::to_string(pc) : v(pc); };
+    // linear analysis
+    std::vector<LinInfo> lin(n);
+    for (int pc = 0; pc < n; ++pc) {
+        const mol_instr& in = s.ins[pc];
+        LinInfo L;
+        if (in.op == MOL_OP_TERM) {
+            const mol_term& tm = d->terms[in.imm];
+            if (tm.kind == MOL_TERM_LINEAR || tm.kind == MOL_TERM_MIXED) {
+                L.ok = true;
+                L.field = tm.field;
+                L.coef[in.imm] = "T(1)";
+                L.members = {pc};
+            }
+        } else if ((in.op == MOL_OP_ADD || in.op == MOL_OP_SUB) && !uni[pc]) {
+            const LinInfo& A = lin[s.ia[pc]];
+            const LinInfo& B = lin[s.ib[pc]];
+            if (A.ok && B.ok && A.field == B.field && uses[s.ia[pc]] == 1 && uses[s.ib[pc]] == 1) {
+                L = A;
+                for (auto& kv : B.coef) {
+                    const std::string c = in.op == MOL_OP_SUB ? "(-" + kv.second + ")" : kv.second;
+                    L.coef[kv.first] = L.coef.count(kv.first) ? "(" + L.coef[kv.first] + " + " + c + ")" : c;
+                }
+                L.members.insert(L.members.end(), B.members.begin(), B.members.end());
+                L.members.push_back(pc);
+            }
+        } else if (in.op == MOL_OP_MUL && !uni[pc]) {
+            const int a = s.ia[pc], b = s.ib[pc];
+            const int li = lin[a].ok ? a : (lin[b].ok ? b : -1);
+            const int ui = li == a ? b : a;
+            if (li >= 0 && uni[ui] && uses[li] == 1) {
+                L = lin[li];
+                for (auto& kv : L.coef) kv.second = "(" + kv.second + " * " + name(ui) + ")";
+                L.members.push_back(pc);
+            }
+        } else if (in.op == MOL_OP_NEG && !uni[pc]) {
+            if (lin[s.ia[pc]].ok && uses[s.ia[pc]] == 1) {
+                L = lin[s.ia[pc]];
+                for (auto& kv : L.coef) kv.second = "(-" + kv.second + ")";
+                L.members.push_back(pc);
+            }
+        }
+        lin[pc] = L;
+    }
+    // roots: linear nodes whose single user is not linear in them, with >= 2 terms or a scaling
+    std::vector<int> user(n, -1);
+    for (int pc = 0; pc < n; ++pc)
+        for (int x : {s.ia[pc], s.ib[pc], s.ic[pc]})
+            if (x >= 0) user[x] = pc;
+    std::vector<char> root(n, 0), absorbed(n, 0);
+    // Off by default: on GB300 the fused stencil's extra live weights cost more occupancy than
+    // the FP64 operations it saves (measured); MOL_JIT_FUSE=1 turns it on.
+    const char* fz = getenv("MOL_JIT_FUSE");
+    const bool fuse = fz && fz[0] == '1';
+    for (int pc = n - 1; pc >= 0 && fuse; --pc) {
+        if (!lin[pc].ok || absorbed[pc]) continue;
+        if (s.ins[pc].op == MOL_OP_TERM) continue;  // a lone term gains nothing
+        const int u = user[pc];
+        const bool extends = u >= 0 && lin[u].ok && std::find(lin[u].members.begin(), lin[u].members.end(), pc) !=
+                                                       lin[u].members.end();
+        if (extends) continue;
+        root[pc] = 1;
+        for (int m : lin[pc].members)
+            if (m != pc) absorbed[m] = 1;
+    }
+    // tap unions of the roots
+    struct Tap {
+        int o[3];
+        std::vector<std::pair<int, std::string>> parts;  // (term k, weight expression)
+    };
+    std::map<int, std::vector<Tap>> taps;
+    for (int pc = 0; pc < n; ++pc) {
+        if (!root[pc]) continue;
+        std::vector<Tap>& T = taps[pc];
+        auto add = [&](int o0, int o1, int o2, int k, const std::string& w) {
+            for (auto& t : T)
+                if (t.o[0] == o0 && t.o[1] == o1 && t.o[2] == o2) {
+                    t.parts.push_back({k, w});
+                    return;
+                }
+            Tap t;
+            t.o[0] = o0;
+            t.o[1] = o1;
+            t.o[2] = o2;
+            t.parts.push_back({k, w});
+            T.push_back(t);
+        };
+        for (auto& kv : lin[pc].coef) {
+            const mol_term& tm = d->terms[kv.first];
+            if (tm.kind == MOL_TERM_LINEAR) {
+                const mol_op1d& o = d->ops[tm.op];
+                for (int m = 0; m < o.L; ++m) {
+                    if (zero_w(d, o.w_int + m)) continue;
+                    int off[3] = {0, 0, 0};
+                    off[tm.dim] = o.omin + m;
+                    add(off[0], off[1], off[2], kv.first,
+                        "P.w[P.ops[" + std::to_string(tm.op) + "].w_int + " + std::to_string(m) + "]");
+                }
+            } else {
+                const mol_op1d& o1 = d->ops[tm.op];
+                const mol_op1d& o2 = d->ops[tm.op2];
+                for (int x = 0; x < o1.L; ++x)
+                    for (int y = 0; y < o2.L; ++y) {
+                        if (zero_w(d, o1.w_int + x) || zero_w(d, o2.w_int + y)) continue;
+                        int off[3] = {0, 0, 0};
+                        off[tm.dim] += o1.omin + x;
+                        off[tm.dim2] += o2.omin + y;
+                        add(off[0], off[1], off[2], kv.first,
+                            "P.w[P.terms[" + std::to_string(kv.first) + "].reserved0 + " +
+                                std::to_string(x * o2.L + y) + "]");
+                    }
+            }
+        }
+    }
+    // uniform struct and its initialiser
+    e << "template <class T>\nstruct GenUniform {\n    T _pad;\n";
+    for (int pc = 0; pc < n; ++pc)
+        if (uni[pc]) e << "    T u" << pc << ";\n";
+    for (auto& kv : taps)
+        for (size_t i = 0; i < kv.second.size(); ++i) e << "    T fw" << kv.first << "_" << i << ";\n";
+    e << "};\n";
+    e << "template <class T>\n__device__ __forceinline__ void gen_uniform(const DevProb<T>& P, T t, const T* __restrict__ "
+         "p, GenUniform<T>& U) {\n    U._pad = T(0);\n";
+    for (int pc = 0; pc < n; ++pc) {
+        if (!uni[pc]) continue;
+        const mol_instr& in = s.ins[pc];
+        const std::string A = s.ia[pc] >= 0 ? name(s.ia[pc]) : "", B = s.ib[pc] >= 0 ? name(s.ib[pc]) : "",
+                          C = s.ic[pc] >= 0 ? name(s.ic[pc]) : "";
+        std::string rhs;
+        switch (in.op) {
+            case MOL_OP_CONST: {
+                rhs = lit(d->consts[in.imm]);
+                if (rhs.empty()) rhs = "P.consts[" + std::to_string(in.imm) + "]";
+                break;
+            }
+            case MOL_OP_PARAM: rhs = "p[" + std::to_string(in.imm) + "]"; break;
+            case MOL_OP_TIME: rhs = "t"; break;
+            case MOL_OP_ADD: rhs = A + " + " + B; break;
+            case MOL_OP_SUB: rhs = A + " - " + B; break;
+            case MOL_OP_MUL: rhs = A + " * " + B; break;
+            case MOL_OP_DIV: rhs = A + " / " + B; break;
+            case MOL_OP_NEG: rhs = "-" + A; break;
+            case MOL_OP_POWI:
+                rhs = in.imm == 2 ? A + " * " + A : (in.imm == 3 ? A + " * " + A + " * " + A
+                                                                  : "powi(" + A + ", " + std::to_string(in.imm) + ")");
+                break;
+            case MOL_OP_POW: rhs = "pow(" + A + ", " + B + ")"; break;
+            case MOL_OP_FN: rhs = fn_expr(in.imm, A); break;
+            case MOL_OP_CMP: {
+                static const char* ops[] = {"<=", "<", ">=", ">", "=="};
+                rhs = "(" + A + " " + ops[in.imm] + " " + B + ") ? T(1) : T(0)";
+                break;
+            }
+            case MOL_OP_IFELSE: rhs = "(" + A + " != T(0)) ? " + B + " : " + C; break;
+            default: rhs = "T(0)";
+        }
+        e << "    U.u" << pc << " = " << rhs << ";\n";
+    }
+    for (auto& kv : taps) {
+        const int r = kv.first;
+        for (size_t i = 0; i < kv.second.size(); ++i) {
+            std::string ex;
+            for (auto& part : kv.second[i].parts) {
+                const std::string term = lin[r].coef.at(part.first) + " * " + part.second;
+                ex = ex.empty() ? term : ex + " + " + term;
+            }
+            e << "    U.fw" << r << "_" << i << " = " << ex << ";\n";
+        }
+    }
+    e << "}\n";
+    // the cell
+    CellLeaves CL;
+    e << "template <class T>\n__device__ " << cell_attr
+      << " void gen_cell(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, "
+         "const T* __restrict__ p, const GenUniform<T>& U, T* out) {\n";
+    auto stmt = [&](int pc) -> std::string {
+        const mol_instr& in = s.ins[pc];
+        const std::string V = v(pc);
+        const std::string A = s.ia[pc] >= 0 ? name(s.ia[pc]) : "", B = s.ib[pc] >= 0 ? name(s.ib[pc]) : "",
+                          C = s.ic[pc] >= 0 ? name(s.ic[pc]) : "";
+        switch (in.op) {
+            case MOL_OP_FIELD: return "const T " + V + " = " + CL.field(in.imm) + ";";
+            case MOL_OP_AUX: return "const T " + V + " = " + CL.aux(in.imm) + ";";
+            case MOL_OP_COORD: return "const T " + V + " = " + CL.coord(in.imm) + ";";
+            case MOL_OP_TERM: return "const T " + V + " = " + CL.term(in.imm) + ";";
+            case MOL_OP_UPWIND:
+                return "const T tv" + std::to_string(pc) + " = (" + A + " < T(0)) ? " + CL.term(in.b) + " : " +
+                       CL.term(in.c) + ";\n    const T " + V + " = " + A + " * tv" + std::to_string(pc) + ";";
+            case MOL_OP_ADD: return "const T " + V + " = " + A + " + " + B + ";";
+            case MOL_OP_SUB: return "const T " + V + " = " + A + " - " + B + ";";
+            case MOL_OP_MUL: return "const T " + V + " = " + A + " * " + B + ";";
+            case MOL_OP_DIV: return "const T " + V + " = " + A + " / " + B + ";";
+            case MOL_OP_NEG: return "const T " + V + " = -" + A + ";";
+            case MOL_OP_POWI:
+                if (in.imm == 2) return "const T " + V + " = " + A + " * " + A + ";";
+                if (in.imm == 3) return "const T " + V + " = " + A + " * " + A + " * " + A + ";";
+                return "const T " + V + " = powi(" + A + ", " + std::to_string(in.imm) + ");";
+            case MOL_OP_POW: return "const T " + V + " = pow(" + A + ", " + B + ");";
+            case MOL_OP_FN: return "const T " + V + " = " + fn_expr(in.imm, A) + ";";
+            case MOL_OP_CMP: {
+                static const char* ops[] = {"<=", "<", ">=", ">", "=="};
+                return "const T " + V + " = (" + A + " " + ops[in.imm] + " " + B + ") ? T(1) : T(0);";
+            }
+            case MOL_OP_IFELSE: return "const T " + V + " = (" + A + " != T(0)) ? " + B + " : " + C + ";";
+            default: return "";
+        }
+    };
+    for (int pc = 0; pc < n; ++pc) {
+        const mol_instr& in = s.ins[pc];
+        if (in.op == MOL_OP_OUT) {
+            e << "    out[" << in.imm << "] = " << name(s.ia[pc]) << ";\n";
+            continue;
+        }
+        if (uni[pc] || absorbed[pc]) continue;
+        if (!root[pc]) {
+            e << "    " << stmt(pc) << "\n";
+            continue;
+        }
+        // fused root
+        std::string cond;
+        for (auto& kv : lin[pc].coef) {
+            const mol_term& tm = d->terms[kv.first];
+            const std::string F = std::to_string(tm.field);
+            std::string c1 = "fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + std::to_string(tm.dim) +
+                             ", I[" + std::to_string(tm.dim) + "])";
+            if (tm.kind == MOL_TERM_MIXED)
+                c1 += " && fast_line(P, P.ops[" + std::to_string(tm.op2) + "], " + F + ", " + std::to_string(tm.dim2) +
+                      ", I[" + std::to_string(tm.dim2) + "])";
+            cond = cond.empty() ? c1 : cond + " && " + c1;
+        }
+        e << "    T " << v(pc) << ";\n    if (" << cond << ") {\n"
+          << "        const T* __restrict__ b = u + (long long)" << lin[pc].field << " * P.ncell + c;\n"
+          << "        const long long s1 = gstride(P, 1), s2 = gstride(P, 2);\n";
+        const std::vector<Tap>& T = taps[pc];
+        for (size_t i = 0; i < T.size(); ++i) {
+            const std::string off = "(long long)(" + std::to_string(T[i].o[0]) + ") + (long long)(" +
+                                    std::to_string(T[i].o[1]) + ") * s1 + (long long)(" + std::to_string(T[i].o[2]) +
+                                    ") * s2";
+            if (i == 0) e << "        T acc = U.fw" << pc << "_" << i << " * b[" << off << "];\n";
+            else e << "        acc = fma(U.fw" << pc << "_" << i << ", b[" << off << "], acc);\n";
+        }
+        if (T.empty()) e << "        T acc = T(0);\n";
+        e << "        " << v(pc) << " = acc;\n    } else {\n";
+        std::vector<int> mem = lin[pc].members;
+        std::sort(mem.begin(), mem.end());
+        for (int m : mem)
+            if (m != pc) e << "        " << stmt(m) << "\n";
+        std::string st = stmt(pc);
+        // turn "const T vX = expr;" into "vX = expr;"
+        const std::string head = "const T " + v(pc) + " = ";
+        if (st.compare(0, head.size(), head) == 0) st = v(pc) + " = " + st.substr(head.size());
+        e << "        " << st << "\n    }\n";
+    }
+    e << "}\n";
+}
+
 std::string generate_source(const mol_problem_desc* d, std::string& why) {
     Emitter e;
     e << "// generated by libmolgpu for one problem structure\n"
@@ -594,20 +941,43 @@ std::string generate_source(const mol_problem_desc* d, std::string& why) {
     }
     CellLeaves L;
     // one out-of-line copy of the cell per precision, shared by every kernel template
-    e << "template <class T>\n__device__ __noinline__ void gen_cell(const DevProb<T>& P, const T* __restrict__ u, "
-         "long long c, const int* I, T t, const T* __restrict__ p, T* out) {\n";
-    std::vector<std::pair<int, int>> outs;
-    emit_forward(e, d, cs, L, "", &outs, false);
-    for (auto& pr : outs) e << "    out[" << pr.first << "] = " << v(pr.second) << ";\n";
-    e << "}\n";
-    e << "template <class T>\n__device__ __noinline__ void gen_cell_vjp(const DevProb<T>& P, const T* __restrict__ u, "
+    // (inlined into every kernel; MOL_JIT_INLINE_CELL=0 keeps one out-of-line copy instead)
+    const char* inl = getenv("MOL_JIT_INLINE_CELL");
+    const std::string cell_attr = (inl && inl[0] == '0') ? "__noinline__" : "__forceinline__";
+    emit_cell_fused(e, d, cs, cell_attr);
+    e << "template <class T>\n__device__ __forceinline__ void gen_cell_vjp(const DevProb<T>& P, const T* __restrict__ u, "
          "long long c, const int* I, T t, const T* __restrict__ p, const T* seed, T* lam_u, T* lp, T* lam_aux) {\n";
-    emit_forward(e, d, cs, L, "", nullptr, true);
-    emit_reverse(e, cs, L, "", [&](int k) { return "seed[" + std::to_string(k) + "]"; });
+    VjpCellLeaves VL;
+    VL.d = d;
+    for (int f = 0; f < d->nfields; ++f) e << "    T own" << f << " = T(0);\n";
+    {
+        // WENO terms read by exactly one TERM instruction (and by no upwind select)
+        std::vector<int> refs(d->nterms, 0);
+        for (auto& in : cs.ins) {
+            if (in.op == MOL_OP_TERM && in.imm >= 0 && in.imm < d->nterms) refs[in.imm] += 1;
+            if (in.op == MOL_OP_UPWIND) {
+                if (in.b < d->nterms) refs[in.b] += 2;
+                if (in.c < d->nterms) refs[in.c] += 2;
+            }
+        }
+        for (int k = 0; k < d->nterms; ++k)
+            if (d->terms[k].kind == MOL_TERM_WENO && refs[k] == 1) {
+                VL.split.push_back(k);
+                e << "    bool fw" << k << " = false;\n    T gw" << k << "[5];\n";
+            }
+    }
+    emit_forward(e, d, cs, VL, "", nullptr, true);
+    emit_reverse(e, cs, VL, "", [&](int k) { return "seed[" + std::to_string(k) + "]"; });
+    for (int f = 0; f < d->nfields; ++f)
+        e << "    atomicAdd(lam_u + (long long)" << f << " * P.ncell + c, own" << f << ");\n";
     e << "}\n";
     e << "struct GenCell {\n"
+         "template <class T> using Uniform = GenUniform<T>;\n"
+         "template <class T>\nstatic __device__ __forceinline__ void uniform(const DevProb<T>& P, T t, const T* "
+         "__restrict__ p, GenUniform<T>& U) { gen_uniform<T>(P, t, p, U); }\n"
          "template <class T>\nstatic __device__ __forceinline__ void cell(const DevProb<T>& P, const T* __restrict__ u, "
-         "long long c, const int* I, T t, const T* __restrict__ p, T* out) { gen_cell<T>(P, u, c, I, t, p, out); }\n"
+         "long long c, const int* I, T t, const T* __restrict__ p, const GenUniform<T>& U, T* out) { "
+         "gen_cell<T>(P, u, c, I, t, p, U, out); }\n"
          "template <class T>\nstatic __device__ __forceinline__ void cell_vjp(const DevProb<T>& P, const T* __restrict__ "
          "u, long long c, const int* I, T t, const T* __restrict__ p, const T* seed, T* lam_u, T* lp, T* lam_aux) "
          "{ gen_cell_vjp<T>(P, u, c, I, t, p, seed, lam_u, lp, lam_aux); }\n};\n}  // namespace mol\n";
@@ -675,9 +1045,25 @@ std::map<std::string, CacheEntry> g_cache;
 
 }  // namespace
 
+// NVRTC options.  MOL_JIT_MIN_BLOCKS sets the CTAs per SM the register allocator must allow
+// for the right-hand-side kernels; MOL_JIT_MAXRREG caps registers per thread.
+constexpr int kDefaultMinBlocks = 2;
+std::vector<std::string> jit_options(int min_blocks) {
+    std::vector<std::string> o = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
+                                  "-default-device", "-DMOL_JIT=1"};
+    const char* r = getenv("MOL_JIT_MAXRREG");
+    if (r && atoi(r) > 0) o.push_back(std::string("--maxrregcount=") + std::to_string(atoi(r)));
+    const char* mb = getenv("MOL_JIT_MIN_BLOCKS");
+    const int minb = (mb && atoi(mb) > 0) ? atoi(mb) : (min_blocks > 0 ? min_blocks : kDefaultMinBlocks);
+    o.push_back("-DMOL_MIN_BLOCKS=" + std::to_string(minb));
+    // MOL_JIT_VERBOSE=1: ptxas resource report (registers, stack, spills) on stderr
+    if (getenv("MOL_JIT_VERBOSE")) o.push_back("--ptxas-options=-v");
+    return o;
+}
+
 // Compiled modules are kept on disk (MOL_CACHE_DIR, else $HOME/.cache/molgpu) keyed by a
 // hash of the generated source, the compile options and the kernel list.
-std::string disk_cache_path(const std::string& src, int nparams) {
+std::string disk_cache_path(const std::string& src, int nparams, int min_blocks) {
     const char* dir = getenv("MOL_CACHE_DIR");
     std::string base;
     if (dir && dir[0]) base = dir;
@@ -692,7 +1078,8 @@ std::string disk_cache_path(const std::string& src, int nparams) {
         }
     };
     mix(src);
-    mix("sm_103a|c++17|lineinfo|fmad|v2|" + std::to_string(nparams));
+    for (auto& o : jit_options(min_blocks)) mix(o);
+    mix("v4|" + std::to_string(nparams));
     for (int i = 0; i < (int)(sizeof(kEmbedTexts) / sizeof(kEmbedTexts[0])); ++i) mix(kEmbedTexts[i]);
     char name[64];
     std::snprintf(name, sizeof name, "/%016llx.molmod", (unsigned long long)h);
@@ -763,7 +1150,8 @@ std::vector<std::string> jit_kernel_names(int nparams, int group) {
                  "&mol::k_ssprk_t<float, mol::GenCell, 2>", "&mol::k_ssprk_t<float, mol::GenCell, 3>"};
             break;
         case JIT_BATCH:
-            n = {"&mol::k_batch_ssprk_t<double, mol::GenCell>", "&mol::k_batch_ssprk_t<float, mol::GenCell>"};
+            n = {"&mol::k_batch_ssprk_t<double, mol::GenCell>", "&mol::k_batch_ssprk_t<float, mol::GenCell>",
+                 "&mol::k_batch_tiles_t<double, mol::GenCell>", "&mol::k_batch_tiles_t<float, mol::GenCell>"};
             break;
         case JIT_VJP:
             n = {"&mol::k_vjp_t<double, mol::GenCell, " + NP + ">"};
@@ -773,7 +1161,7 @@ std::vector<std::string> jit_kernel_names(int nparams, int group) {
 }
 
 int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<char>* cubin,
-                  std::vector<std::string>* lowered, std::string& err) {
+                  std::vector<std::string>* lowered, std::string& err, int min_blocks) {
     const std::vector<std::string> names = jit_kernel_names(nparams, group);
     Nvrtc& N = nvrtc();
     if (!N.ok) {
@@ -787,9 +1175,10 @@ int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<ch
         return MOL_ERR_CUDA;
     }
     for (auto& n : names) N.addname(prog, n.c_str());
-    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
-                          "-default-device", "-DMOL_JIT=1"};
-    const int rc = N.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    std::vector<std::string> ostr = jit_options(min_blocks);
+    std::vector<const char*> opts;
+    for (auto& o : ostr) opts.push_back(o.c_str());
+    const int rc = N.compile(prog, (int)opts.size(), opts.data());
     if (rc != 0) {
         size_t ls = 0;
         N.logsize(prog, &ls);
@@ -798,6 +1187,13 @@ int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<ch
         N.destroy(&prog);
         err = "nvrtc compile failed: " + log.substr(0, 6000);
         return MOL_ERR_UNSUPPORTED;
+    }
+    if (getenv("MOL_JIT_VERBOSE")) {
+        size_t ls = 0;
+        N.logsize(prog, &ls);
+        std::string log(ls, '\0');
+        if (ls) N.log(prog, &log[0]);
+        fprintf(stderr, "[molgpu jit group %d]\n%s\n", group, log.c_str());
     }
     size_t cs = 0;
     N.cubinsize(prog, &cs);
@@ -819,7 +1215,7 @@ int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<ch
 
 int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k, std::string& err) {
     const std::vector<std::string> names = jit_kernel_names(nparams, group);
-    const std::string key = src + "\n//group " + std::to_string(group);
+    const std::string key = src + "\n//group " + std::to_string(group) + " minblocks " + std::to_string(k->min_blocks);
     std::vector<cudaKernel_t> got;
     {
         std::lock_guard<std::mutex> g(g_cache_mu);
@@ -829,9 +1225,9 @@ int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k
     if (got.empty()) {
         std::vector<char> cubin;
         std::vector<std::string> lowered;
-        const std::string cache_path = disk_cache_path(key, nparams);
+        const std::string cache_path = disk_cache_path(key, nparams, k->min_blocks);
         if (!(cache_path.size() && disk_cache_load(cache_path, names.size(), &cubin, &lowered))) {
-            int st = nvrtc_compile(src, nparams, group, &cubin, &lowered, err);
+            int st = nvrtc_compile(src, nparams, group, &cubin, &lowered, err, k->min_blocks);
             if (st) return st;
             if (cache_path.size()) disk_cache_store(cache_path, cubin, lowered);
         }
@@ -872,6 +1268,8 @@ int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k
         case JIT_BATCH:
             k->batch64 = got[0];
             k->batch32 = got[1];
+            k->tiles64 = got[2];
+            k->tiles32 = got[3];
             break;
         case JIT_VJP:
             k->vjp64 = got[0];
@@ -881,7 +1279,7 @@ int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k
     return MOL_OK;
 }
 
-int jit_compile(const mol_problem_desc* d, JitKernels* out, std::string& err, std::string* src_out) {
+int jit_compile(const mol_problem_desc* d, JitKernels* out, std::string& err, std::string* src_out, int min_blocks) {
     std::string why;
     std::string src = generate_source(d, why);
     if (src.empty()) {
@@ -892,6 +1290,7 @@ int jit_compile(const mol_problem_desc* d, JitKernels* out, std::string& err, st
     JitKernels k;
     k.src = src;
     k.nparams = d->nparams;
+    k.min_blocks = min_blocks;
     int st = jit_load_group(src, d->nparams, JIT_FWD64, &k, err);
     if (st) return st;
     k.ok = true;

@@ -19,19 +19,21 @@ struct JitKernels {
     unsigned loaded = 0;
     std::string src;
     int nparams = 0;
+    int min_blocks = 2;
     cudaKernel_t rhs64 = nullptr, ssp64[3] = {nullptr, nullptr, nullptr}, batch64 = nullptr, tsit64 = nullptr;
     cudaKernel_t rhs32 = nullptr, ssp32[3] = {nullptr, nullptr, nullptr}, batch32 = nullptr, tsit32 = nullptr;
     cudaKernel_t vjp64 = nullptr;
+    cudaKernel_t tiles64 = nullptr, tiles32 = nullptr;
 };
 
 std::string generate_source(const mol_problem_desc* d, std::string& why);
 std::vector<std::string> jit_kernel_names(int nparams, int group);
 // Generates, compiles (NVRTC, sm_103a) and loads the module of a problem structure;
 // modules are cached per generated source for the life of the process.
-int jit_compile(const mol_problem_desc* d, JitKernels* out, std::string& err, std::string* src_out);
+int jit_compile(const mol_problem_desc* d, JitKernels* out, std::string& err, std::string* src_out, int min_blocks);
 // NVRTC compile of generated source (no device needed); cubin and lowered kernel names optional.
 int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<char>* cubin,
-                  std::vector<std::string>* lowered, std::string& err);
+                  std::vector<std::string>* lowered, std::string& err, int min_blocks = 2);
 // Compiles and loads a kernel group of an already generated module on first use.
 int jit_ensure(JitKernels* k, int group, std::string& err);
 

@@ -335,16 +335,25 @@ __device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps
     return (hp - hm) * (inv_dx * T(1.0 / 6.0));
 }
 
+// The five WENO taps of a cell through the generic path (periodic wrap, observed
+// boundary rows).  Kept inline so the generated code can load its taps on either
+// path and then run the FP64 arithmetic once, with the warp converged.
 template <class T>
-__device__ T apply_weno(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, T t, const T* p) {
+__device__ __forceinline__ void weno_taps(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, T t,
+                                          const T* p, T v[5]) {
     const int f = tm.field, d = tm.dim, n = P.n[d];
     int J[3] = {I[0], I[1], I[2]};
-    T v[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
         J[d] = wrap_periodic(I[d] - 2 + k, n);
         v[k] = load_pt(P, u, f, J[0], J[1], J[2], t, p);
     }
+}
+
+template <class T>
+__device__ T apply_weno(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, T t, const T* p) {
+    T v[5];
+    weno_taps(P, tm, u, I, t, p, v);
     // the device copy of a WENO term stores 1/dx in `dx`
     return weno5_point<T>(v[0], v[1], v[2], v[3], v[4], T(tm.eps), T(tm.dx));
 }

@@ -11,6 +11,12 @@ namespace mol {
 
 constexpr int kThreads = 256;
 
+// Minimum resident CTAs per SM requested from the register allocator for the kernels that
+// evaluate the right-hand side (set for generated modules, MOL_JIT_MIN_BLOCKS).
+#ifndef MOL_MIN_BLOCKS
+#define MOL_MIN_BLOCKS 1
+#endif
+
 // Correctly rounded x/3 with one multiply and two FMAs (Markstein's theorem:
 // with c = RN(1/3) and q0 within an ulp of x/3, q0 + (x - 3 q0) c rounds to
 // RN(x/3)); replaces the FP64 division of SSPRK33's last stage.
@@ -24,21 +30,28 @@ __device__ __forceinline__ float div3m(float x) { return x / 3.0f; }
 
 struct InterpCell {
     template <class T>
+    struct Uniform {};
+    template <class T>
+    static __device__ __forceinline__ void uniform(const DevProb<T>&, T, const T*, Uniform<T>&) {}
+    template <class T>
     static __device__ __forceinline__ void cell(const DevProb<T>& P, const T* __restrict__ u, long long c,
-                                                const int* I, T t, const T* __restrict__ p, T* out) {
+                                                const int* I, T t, const T* __restrict__ p, const Uniform<T>&,
+                                                T* out) {
         eval_cell(P, u, c, I, t, p, out);
     }
 };
 
 template <class T, class G>
-__global__ void __launch_bounds__(kThreads) k_rhs_t(DevProb<T> P, const T* __restrict__ u, T* __restrict__ du,
+__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_rhs_t(const __grid_constant__ DevProb<T> P, const T* __restrict__ u, T* __restrict__ du,
                                                     const T* __restrict__ p, double t) {
     T out[MOL_MAX_FIELDS];
+    typename G::template Uniform<T> U;
+    G::uniform(P, T(t), p, U);
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
          c += (long long)gridDim.x * blockDim.x) {
         int I[3];
         cell_index(P, c, I);
-        G::cell(P, u, c, I, T(t), p, out);
+        G::cell(P, u, c, I, T(t), p, U, out);
         for (int f = 0; f < P.nfields; ++f) du[(long long)f * P.ncell + c] = out[f];
     }
 }
@@ -65,29 +78,35 @@ __device__ __forceinline__ void last_block_advance(SolverState* S, double t_new)
     }
 }
 
+// `tfix` (when not NaN) is the step's start time, used instead of S->t and leaving S alone:
+// the adjoint recomputes single stages at known times without touching the solver state.
 template <class T, class G, int STAGE>
-__global__ void __launch_bounds__(kThreads) k_ssprk_t(DevProb<T> P, const T* __restrict__ uin, const T* u0, T* uout,
-                                                      const T* __restrict__ p, SolverState* S, double dt) {
-    const double t0 = S->t;
+__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_ssprk_t(const __grid_constant__ DevProb<T> P, const T* __restrict__ uin, const T* u0, T* uout,
+                                                      const T* __restrict__ p, SolverState* S, double dt,
+                                                      double tfix) {
+    const bool from_state = !(tfix == tfix);
+    const double t0 = from_state ? S->t : tfix;
     const double ts = STAGE == 1 ? t0 : (STAGE == 2 ? t0 + dt : t0 + dt / 2);
     T out[MOL_MAX_FIELDS];
+    typename G::template Uniform<T> U;
+    G::uniform(P, T(ts), p, U);
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
          c += (long long)gridDim.x * blockDim.x) {
         int I[3];
         cell_index(P, c, I);
-        G::cell(P, uin, c, I, T(ts), p, out);
+        G::cell(P, uin, c, I, T(ts), p, U, out);
         for (int f = 0; f < P.nfields; ++f) {
             const long long g = (long long)f * P.ncell + c;
             uout[g] = ssprk_combine<T, STAGE>(u0[g], uin[g], out[f], T(dt), T(2 * dt));
         }
     }
-    if (STAGE == 3) last_block_advance(S, t0 + dt);
+    if (STAGE == 3 && from_state) last_block_advance(S, t0 + dt);
 }
 
 // Vector-Jacobian product of the RHS: lam_u += scale * (df/du)^T lam, lam_p and lam_aux likewise.
 // Parameter adjoints are reduced per block before one atomic per block and parameter.
 template <class T, class G, int NP>
-__global__ void __launch_bounds__(kThreads) k_vjp_t(DevProb<T> P, const T* __restrict__ lam, T scale,
+__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_vjp_t(const __grid_constant__ DevProb<T> P, const T* __restrict__ lam, T scale,
                                                     const T* __restrict__ u, const T* __restrict__ p, double t,
                                                     T* lam_u, T* lam_p, T* lam_aux) {
     T lp[NP > 0 ? NP : 1];
@@ -130,6 +149,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_ssprk_t(const DevProb<T>* __
                                                             long long nsteps, unsigned* ticket) {
     __shared__ int slot;
     T out[MOL_MAX_FIELDS];
+    typename G::template Uniform<T> UN;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) slot = (int)atomicAdd(ticket, 1u);
@@ -145,30 +165,33 @@ __global__ void __launch_bounds__(kThreads) k_batch_ssprk_t(const DevProb<T>* __
         const long long nc = P.ncell;
         double t = t0;
         for (long long s = 0; s < nsteps; ++s) {
+            G::uniform(P, T(t), p, UN);
             for (long long c = threadIdx.x; c < nc; c += blockDim.x) {
                 int I[3];
                 cell_index(P, c, I);
-                G::cell(P, u, c, I, T(t), p, out);
+                G::cell(P, u, c, I, T(t), p, UN, out);
                 for (int f = 0; f < P.nfields; ++f) {
                     const long long g = (long long)f * nc + c;
                     u1[g] = ssprk_combine<T, 1>(u[g], u[g], out[f], T(dt), T(2 * dt));
                 }
             }
             __syncthreads();
+            G::uniform(P, T(t + dt), p, UN);
             for (long long c = threadIdx.x; c < nc; c += blockDim.x) {
                 int I[3];
                 cell_index(P, c, I);
-                G::cell(P, u1, c, I, T(t + dt), p, out);
+                G::cell(P, u1, c, I, T(t + dt), p, UN, out);
                 for (int f = 0; f < P.nfields; ++f) {
                     const long long g = (long long)f * nc + c;
                     u2[g] = ssprk_combine<T, 2>(u[g], u1[g], out[f], T(dt), T(2 * dt));
                 }
             }
             __syncthreads();
+            G::uniform(P, T(t + dt / 2), p, UN);
             for (long long c = threadIdx.x; c < nc; c += blockDim.x) {
                 int I[3];
                 cell_index(P, c, I);
-                G::cell(P, u2, c, I, T(t + dt / 2), p, out);
+                G::cell(P, u2, c, I, T(t + dt / 2), p, UN, out);
                 for (int f = 0; f < P.nfields; ++f) {
                     const long long g = (long long)f * nc + c;
                     u[g] = ssprk_combine<T, 3>(u[g], u2[g], out[f], T(dt), T(2 * dt));
@@ -180,6 +203,140 @@ __global__ void __launch_bounds__(kThreads) k_batch_ssprk_t(const DevProb<T>* __
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Tiled ensemble kernel.  The unit of work is one tile (tile_cells consecutive
+// cells) of one stage of one instance, so a large instance spreads over many
+// CTAs while small ones still take a single tile.  Work items are handed out by
+// one 64-bit ticket in round-major order (round r = 3 * step + stage; within a
+// round, instances largest first, then their tiles).  Before a tile of round r
+// runs, every tile of rounds < r of the same instance must be done: a
+// per-instance counter of finished tiles (release-add after the tile, acquire
+// poll before it) carries that dependency.  A CTA only ever waits for items
+// with smaller tickets, which were handed to CTAs that are already running, so
+// the lowest unfinished ticket can always proceed.  Each wait is bounded: past
+// MOL_BATCH_SPIN_LIMIT polls it sets the shared status word and every CTA
+// leaves at its next poll or ticket.
+
+#define MOL_BATCH_SPIN_LIMIT (1ll << 25)
+
+struct BatchSync {
+    unsigned long long* ticket;   // next work item
+    unsigned long long* done;     // [instance] tiles finished, all rounds so far
+    int* status;                  // 0 ok, 1 a wait ran out of budget
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+template <class T, class G>
+__global__ void __launch_bounds__(kThreads) k_batch_tiles_t(const DevProb<T>* __restrict__ probs,
+                                                            const long long* __restrict__ off,
+                                                            const int* __restrict__ order,
+                                                            const long long* __restrict__ tile_pre, int ninst,
+                                                            int tile_cells, T* U, T* U1, T* U2,
+                                                            const T* const* __restrict__ params,
+                                                            const double* __restrict__ dts, double t0,
+                                                            long long nsteps, BatchSync sync) {
+    __shared__ long long s_item;
+    __shared__ int s_ok;
+    const long long ntiles = tile_pre[ninst];
+    const long long nitems = 3 * nsteps * ntiles;
+    T out[MOL_MAX_FIELDS];
+    typename G::template Uniform<T> UN;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_item = *(volatile int*)sync.status ? nitems : (long long)atomicAdd(sync.ticket, 1ull);
+        __syncthreads();
+        const long long item = s_item;
+        if (item >= nitems) return;
+        const long long r = item / ntiles;
+        const long long g = item - r * ntiles;
+        int lo = 0, hi = ninst;  // tile_pre[lo] <= g < tile_pre[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (tile_pre[mid] <= g) lo = mid;
+            else hi = mid;
+        }
+        const int i = order[lo];
+        const long long tiles_i = tile_pre[lo + 1] - tile_pre[lo];
+        const long long j = g - tile_pre[lo];
+        if (threadIdx.x == 0) {
+            const unsigned long long need = (unsigned long long)(r * tiles_i);
+            int ok = 1;
+            long long polls = 0;
+            while (ld_acquire_u64(sync.done + i) < need) {
+                if (*(volatile int*)sync.status != 0) {
+                    ok = 0;
+                    break;
+                }
+                if (++polls > MOL_BATCH_SPIN_LIMIT) {
+                    atomicExch(sync.status, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        const DevProb<T>& P = probs[i];
+        T* u = U + off[i];
+        T* u1 = U1 + off[i];
+        T* u2 = U2 + off[i];
+        const T* p = params[i];
+        const double dt = dts[i];
+        const long long nc = P.ncell;
+        const int stage = (int)(r % 3);
+        const double t = t0 + (double)(r / 3) * dt;
+        const long long c_end = min(nc, (j + 1) * (long long)tile_cells);
+        if (stage == 0) {
+            G::uniform(P, T(t), p, UN);
+            for (long long c = j * tile_cells + threadIdx.x; c < c_end; c += blockDim.x) {
+                int I[3];
+                cell_index(P, c, I);
+                G::cell(P, u, c, I, T(t), p, UN, out);
+                for (int f = 0; f < P.nfields; ++f) {
+                    const long long q = (long long)f * nc + c;
+                    u1[q] = ssprk_combine<T, 1>(u[q], u[q], out[f], T(dt), T(2 * dt));
+                }
+            }
+        } else if (stage == 1) {
+            G::uniform(P, T(t + dt), p, UN);
+            for (long long c = j * tile_cells + threadIdx.x; c < c_end; c += blockDim.x) {
+                int I[3];
+                cell_index(P, c, I);
+                G::cell(P, u1, c, I, T(t + dt), p, UN, out);
+                for (int f = 0; f < P.nfields; ++f) {
+                    const long long q = (long long)f * nc + c;
+                    u2[q] = ssprk_combine<T, 2>(u[q], u1[q], out[f], T(dt), T(2 * dt));
+                }
+            }
+        } else {
+            G::uniform(P, T(t + dt / 2), p, UN);
+            for (long long c = j * tile_cells + threadIdx.x; c < c_end; c += blockDim.x) {
+                int I[3];
+                cell_index(P, c, I);
+                G::cell(P, u2, c, I, T(t + dt / 2), p, UN, out);
+                for (int f = 0; f < P.nfields; ++f) {
+                    const long long q = (long long)f * nc + c;
+                    u[q] = ssprk_combine<T, 3>(u[q], u2[q], out[f], T(dt), T(2 * dt));
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) red_release_add_u64(sync.done + i, 1ull);
+    }
+}
 
 // Tsitouras (2011) nodes c_i of the 5(4) pair OrdinaryDiffEq's Tsit5 implements.
 __device__ __forceinline__ double tsit_c(int i) {
@@ -196,7 +353,7 @@ __device__ __forceinline__ double tsit_c(int i) {
 // Stage 7 accumulates the scaled error sum_j (dt btilde_j) k_j; the last block to finish
 // reduces it deterministically and runs the PI step-size controller.
 template <class T, class G>
-__global__ void __launch_bounds__(kThreads) k_tsit_stage_t(DevProb<T> P, int stage, const T* __restrict__ y,
+__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_tsit_stage_t(const __grid_constant__ DevProb<T> P, int stage, const T* __restrict__ y,
                                                            T* ynext, const T* __restrict__ u, T* const* k,
                                                            const T* __restrict__ p, SolverState* S,
                                                            double* partials) {
@@ -205,11 +362,13 @@ __global__ void __launch_bounds__(kThreads) k_tsit_stage_t(DevProb<T> P, int sta
     T out[MOL_MAX_FIELDS];
     double errsq = 0.0;
     const double abstol = S->abstol, reltol = S->reltol;
+    typename G::template Uniform<T> U;
+    G::uniform(P, T(t), p, U);
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
          c += (long long)gridDim.x * blockDim.x) {
         int I[3];
         cell_index(P, c, I);
-        G::cell(P, y, c, I, T(t), p, out);
+        G::cell(P, y, c, I, T(t), p, U, out);
         for (int f = 0; f < P.nfields; ++f) {
             const long long g = (long long)f * P.ncell + c;
             k[stage - 1][g] = out[f];

@@ -127,7 +127,7 @@ __device__ void tsit_scale(SolverState* S) {
 // After the controller: commit an accepted step (u <- y7, k1 <- k7), rescale the
 // tableau for the new dt and form y2 = u + dt a21 k1 for the next attempt.
 template <class T>
-__global__ void __launch_bounds__(kThreads) k_tsit_commit(DevProb<T> P, T* u, T* k1, const T* k7, const T* y7,
+__global__ void __launch_bounds__(kThreads) k_tsit_commit(const __grid_constant__ DevProb<T> P, T* u, T* k1, const T* k7, const T* y7,
                                                           T* y2, SolverState* S, int first) {
     const bool acc = !first && S->accepted;
     const bool done = S->done;
@@ -268,14 +268,18 @@ int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt)
         const T* cu = u;
         const T* cu1 = u1;
         const T* cu2 = u2;
-        cudaError_t e = launch_k(k[0], plan->nblocks, plan->nthreads, plan->stream, P, cu, cu, u1, p, plan->d_state, dt);
-        if (e == cudaSuccess) e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, P, cu1, cu, u2, p, plan->d_state, dt);
-        if (e == cudaSuccess) e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, P, cu2, cu, u, p, plan->d_state, dt);
+        const double nan = std::nan("");
+        cudaError_t e = launch_k(k[0], plan->nblocks, plan->nthreads, plan->stream, P, cu, cu, u1, p, plan->d_state, dt, nan);
+        if (e == cudaSuccess)
+            e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, P, cu1, cu, u2, p, plan->d_state, dt, nan);
+        if (e == cudaSuccess)
+            e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, P, cu2, cu, u, p, plan->d_state, dt, nan);
         return cuda_check(plan, e, "ssprk launch");
     }
-    k_ssprk_t<T, InterpCell, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt);
-    k_ssprk_t<T, InterpCell, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt);
-    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, u, p, plan->d_state, dt);
+    const double nan = std::nan("");
+    k_ssprk_t<T, InterpCell, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt, nan);
+    k_ssprk_t<T, InterpCell, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt, nan);
+    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, u, p, plan->d_state, dt, nan);
     return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
 }
 template int launch_ssprk_step<double>(mol_plan*, double*, double*, double*, const double*, double);
@@ -548,6 +552,21 @@ int64_t mol_launch_count(void) { return g_launches.load(); }
 
 int mol_plan_uses_codegen(const mol_plan* plan) { return plan && plan->use_jit ? 1 : 0; }
 
+int mol_plan_launch_config(const mol_plan* plan, int32_t* regs, int32_t* threads, int32_t* blocks) {
+    if (!plan) return MOL_ERR_INVALID;
+    int r = 0;
+    cudaFuncAttributes fa;
+    if (plan->use_jit && plan->jit.ssp64[0] &&
+        cudaFuncGetAttributes(&fa, (const void*)plan->jit.ssp64[0]) == cudaSuccess)
+        r = fa.numRegs;
+    else
+        cudaGetLastError();
+    if (regs) *regs = r;
+    if (threads) *threads = plan->use_jit ? plan->nthreads : kThreads;
+    if (blocks) *blocks = plan->nblocks;
+    return MOL_OK;
+}
+
 const char* mol_plan_codegen_source(const mol_plan* plan) {
     if (!plan) return "";
     return plan->use_jit ? plan->jit_src.c_str() : plan->jit_err.c_str();
@@ -705,7 +724,10 @@ int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member
     // the generated right-hand side; MOL_DISABLE_CODEGEN=1 keeps the interpreter (used to cross-check)
     const char* off_env = getenv("MOL_DISABLE_CODEGEN");
     if (!(off_env && off_env[0] == '1')) {
-        st = jit_compile(d, &plan->jit, plan->jit_err, &plan->jit_src);
+        // Resident CTAs per SM the register allocator must allow: 3 for large problems (hides
+        // more load latency), 2 below a million unknowns (measured on GB300).
+        const int minb = plan->nunk >= (1ll << 20) ? 3 : 2;
+        st = jit_compile(d, &plan->jit, plan->jit_err, &plan->jit_src, minb);
         plan->use_jit = (st == MOL_OK) && plan->jit.ok;
         if (plan->use_jit) {
             // Grid = SMs x resident CTAs: every SM gets the same share of the grid-stride loop.

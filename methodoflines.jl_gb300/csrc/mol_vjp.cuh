@@ -106,9 +106,50 @@ __device__ __noinline__ void scatter_mixed(const DevProb<T>& P, const mol_term& 
     }
 }
 
-// d/du_k of weno5_point (reverse mode through the same formula).
+// Transpose of one interior stencil line: adds v[m] to the adjoint at offset
+// (OMIN + m) * s from this cell, `base` pointing at this cell's adjoint.  The share at
+// offset 0 goes to `own`, which the caller adds to its cell once for all terms.  Along
+// the contiguous axis (s == 1), when the 32 lanes of the warp are converged on 32
+// consecutive cells, the shares that land inside the warp are summed with shuffles into
+// the receiving lane's `own`; only shares leaving the warp (|offset| lanes per tap at
+// each edge) are atomics.  Everything else is one atomic per nonzero share.
+template <class T, int L, int OMIN, bool WARP>
+__device__ __forceinline__ void scatter_taps(T* base, long long c, long long s, const T (&v)[L], T& own) {
+    if (WARP && s == 1 && __activemask() == 0xffffffffu) {
+        const int lane = threadIdx.x & 31;
+        const long long c0 = __shfl_sync(0xffffffffu, c, 0);
+        if (__all_sync(0xffffffffu, c == c0 + lane)) {
+#pragma unroll
+            for (int m = 0; m < L; ++m) {
+                const int off = OMIN + m;
+                if (off == 0) {
+                    own += v[m];
+                    continue;
+                }
+                const int src = lane - off;
+                const T x = __shfl_sync(0xffffffffu, v[m], src & 31);
+                if (src >= 0 && src < 32) own += x;
+                const int dst = lane + off;
+                if (dst < 0 || dst >= 32) atomicAdd(base + off, v[m]);
+            }
+            return;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < L; ++m) {
+        const int off = OMIN + m;
+        if (off == 0) own += v[m];
+        else atomicAdd(base + (long long)off * s, v[m]);
+    }
+}
+
+// d/du_k of weno5_point: reverse mode through the same formula.  In FP64 the sweep runs
+// through the one-division common-denominator form (one reciprocal of Dp*Dm serves the
+// whole gradient); FP32 keeps the reciprocal form.
+// Returns the point value as well (rounded differently from weno5_point: a reciprocal
+// times the numerator instead of a quotient), for VJPs that need both.
 template <class T>
-__device__ __forceinline__ void weno5_grad(T um2, T um1, T u0, T up1, T up2, T eps, T inv_dx, T gr[5]) {
+__device__ __forceinline__ T weno5_valgrad(T um2, T um1, T u0, T up1, T up2, T eps, T inv_dx, T gr[5]) {
     const T c13_12 = T(13) / T(12);
     const T a1 = u0 - T(2) * up1 + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
     const T a2 = um1 - T(2) * u0 + up1, b2 = um1 - up1;
@@ -116,66 +157,99 @@ __device__ __forceinline__ void weno5_grad(T um2, T um1, T u0, T up1, T up2, T e
     const T e1 = eps + fma(c13_12 * a1, a1, T(0.25) * (b1 * b1));
     const T e2 = eps + fma(c13_12 * a2, a2, T(0.25) * (b2 * b2));
     const T e3 = eps + fma(c13_12 * a3, a3, T(0.25) * (b3 * b3));
-    const T q1 = T(1) / (e1 * e1), q2 = T(1) / (e2 * e2), q3 = T(1) / (e3 * e3);
-    const T wm1 = T(0.1) * q1, wm2 = T(0.6) * q2, wm3 = T(0.3) * q3;
-    const T wp1 = T(0.3) * q1, wp2 = T(0.6) * q2, wp3 = T(0.1) * q3;
-    const T sixth = T(1) / T(6);
-    const T hm1 = (T(11) * u0 - T(7) * up1 + T(2) * up2) * sixth;
-    const T hm2 = (T(5) * u0 - up1 + T(2) * um1) * sixth;
-    const T hm3 = (T(2) * u0 + T(5) * um1 - um2) * sixth;
-    const T hp1 = (T(2) * u0 + T(5) * up1 - up2) * sixth;
-    const T hp2 = (T(5) * u0 + T(2) * up1 - um1) * sixth;
-    const T hp3 = (T(11) * u0 - T(7) * um1 + T(2) * um2) * sixth;
-    const T Dp = wp1 + wp2 + wp3, Dm = wm1 + wm2 + wm3;
-    const T hp = (wp1 * hp1 + wp2 * hp2 + wp3 * hp3) / Dp;
-    const T hm = (wm1 * hm1 + wm2 * hm2 + wm3 * hm3) / Dm;
-    // reverse
-    const T gSp = inv_dx / Dp, gDp = -inv_dx * hp / Dp;
-    const T gSm = -inv_dx / Dm, gDm = inv_dx * hm / Dm;
-    const T gwp1 = gSp * hp1 + gDp, gwp2 = gSp * hp2 + gDp, gwp3 = gSp * hp3 + gDp;
-    const T gwm1 = gSm * hm1 + gDm, gwm2 = gSm * hm2 + gDm, gwm3 = gSm * hm3 + gDm;
-    const T ghp1 = gSp * wp1, ghp2 = gSp * wp2, ghp3 = gSp * wp3;
-    const T ghm1 = gSm * wm1, ghm2 = gSm * wm2, ghm3 = gSm * wm3;
-    const T gq1 = T(0.1) * gwm1 + T(0.3) * gwp1;
-    const T gq2 = T(0.6) * (gwm2 + gwp2);
-    const T gq3 = T(0.3) * gwm3 + T(0.1) * gwp3;
-    const T ge1 = -T(2) * q1 / e1 * gq1, ge2 = -T(2) * q2 / e2 * gq2, ge3 = -T(2) * q3 / e3 * gq3;
+    // candidate reconstructions scaled by 6 (1/6 folded into c below)
+    const T hm1 = T(11) * u0 - T(7) * up1 + T(2) * up2;
+    const T hm2 = T(5) * u0 - up1 + T(2) * um1;
+    const T hm3 = T(2) * u0 + T(5) * um1 - um2;
+    const T hp1 = T(2) * u0 + T(5) * up1 - up2;
+    const T hp2 = T(5) * u0 + T(2) * up1 - um1;
+    const T hp3 = T(11) * u0 - T(7) * um1 + T(2) * um2;
+    const T c = inv_dx * T(1.0 / 6.0);
+    T gwp1, gwp2, gwp3, gwm1, gwm2, gwm3, ghp1, ghp2, ghp3, ghm1, ghm2, ghm3, ge1, ge2, ge3, val;
+    if (sizeof(T) == 8) {
+        const T s1 = e1 * e1, s2 = e2 * e2, s3 = e3 * e3;
+        const T P1 = s2 * s3, P2 = s1 * s3, P3 = s1 * s2;
+        const T wm1 = T(0.1) * P1, wm2 = T(0.6) * P2, wm3 = T(0.3) * P3;
+        const T wp1 = T(0.3) * P1, wp2 = T(0.6) * P2, wp3 = T(0.1) * P3;
+        const T Np = fma(wp1, hp1, fma(wp2, hp2, wp3 * hp3)), Dp = wp1 + wp2 + wp3;
+        const T Nm = fma(wm1, hm1, fma(wm2, hm2, wm3 * hm3)), Dm = wm1 + wm2 + wm3;
+        const T B = Dp * Dm;
+        const T iB = T(1) / B;
+        const T R = fma(Np, Dm, -Nm * Dp) * iB;
+        val = c * R;
+        // T = c * R, R = A / B, A = Np Dm - Nm Dp, B = Dp Dm
+        const T gA = c * iB, gB = -c * R * iB;
+        const T gNp = gA * Dm, gNm = -gA * Dp;
+        const T gDp = -gA * Nm + gB * Dm, gDm = gA * Np + gB * Dp;
+        gwp1 = fma(gNp, hp1, gDp); gwp2 = fma(gNp, hp2, gDp); gwp3 = fma(gNp, hp3, gDp);
+        gwm1 = fma(gNm, hm1, gDm); gwm2 = fma(gNm, hm2, gDm); gwm3 = fma(gNm, hm3, gDm);
+        ghp1 = gNp * wp1; ghp2 = gNp * wp2; ghp3 = gNp * wp3;
+        ghm1 = gNm * wm1; ghm2 = gNm * wm2; ghm3 = gNm * wm3;
+        const T gP1 = T(0.3) * gwp1 + T(0.1) * gwm1;
+        const T gP2 = T(0.6) * (gwp2 + gwm2);
+        const T gP3 = T(0.1) * gwp3 + T(0.3) * gwm3;
+        const T gs1 = gP2 * s3 + gP3 * s2, gs2 = gP1 * s3 + gP3 * s1, gs3 = gP1 * s2 + gP2 * s1;
+        ge1 = T(2) * e1 * gs1; ge2 = T(2) * e2 * gs2; ge3 = T(2) * e3 * gs3;
+    } else {
+        const T q1 = T(1) / (e1 * e1), q2 = T(1) / (e2 * e2), q3 = T(1) / (e3 * e3);
+        const T wm1 = T(0.1) * q1, wm2 = T(0.6) * q2, wm3 = T(0.3) * q3;
+        const T wp1 = T(0.3) * q1, wp2 = T(0.6) * q2, wp3 = T(0.1) * q3;
+        const T Dp = wp1 + wp2 + wp3, Dm = wm1 + wm2 + wm3;
+        const T hp = (wp1 * hp1 + wp2 * hp2 + wp3 * hp3) / Dp;
+        const T hm = (wm1 * hm1 + wm2 * hm2 + wm3 * hm3) / Dm;
+        val = (hp - hm) * c;
+        const T gSp = c / Dp, gDp = -c * hp / Dp;
+        const T gSm = -c / Dm, gDm = c * hm / Dm;
+        gwp1 = gSp * hp1 + gDp; gwp2 = gSp * hp2 + gDp; gwp3 = gSp * hp3 + gDp;
+        gwm1 = gSm * hm1 + gDm; gwm2 = gSm * hm2 + gDm; gwm3 = gSm * hm3 + gDm;
+        ghp1 = gSp * wp1; ghp2 = gSp * wp2; ghp3 = gSp * wp3;
+        ghm1 = gSm * wm1; ghm2 = gSm * wm2; ghm3 = gSm * wm3;
+        const T gq1 = T(0.1) * gwm1 + T(0.3) * gwp1;
+        const T gq2 = T(0.6) * (gwm2 + gwp2);
+        const T gq3 = T(0.3) * gwm3 + T(0.1) * gwp3;
+        ge1 = -T(2) * q1 / e1 * gq1; ge2 = -T(2) * q2 / e2 * gq2; ge3 = -T(2) * q3 / e3 * gq3;
+    }
     const T ga1 = ge1 * T(2) * c13_12 * a1, gb1 = ge1 * T(0.5) * b1;
     const T ga2 = ge2 * T(2) * c13_12 * a2, gb2 = ge2 * T(0.5) * b2;
     const T ga3 = ge3 * T(2) * c13_12 * a3, gb3 = ge3 * T(0.5) * b3;
-    // linear maps to (um2, um1, u0, up1, up2)
-    T g_um2 = ga3 + gb3 - ghm3 * sixth + T(2) * ghp3 * sixth;
-    T g_um1 = ga2 + gb2 - T(2) * ga3 - T(4) * gb3 + T(2) * ghm2 * sixth + T(5) * ghm3 * sixth - ghp2 * sixth -
-              T(7) * ghp3 * sixth;
-    T g_u0 = ga1 + T(3) * gb1 - T(2) * ga2 + ga3 + T(3) * gb3 +
-             (T(11) * ghm1 + T(5) * ghm2 + T(2) * ghm3 + T(2) * ghp1 + T(5) * ghp2 + T(11) * ghp3) * sixth;
-    T g_up1 = -T(2) * ga1 - T(4) * gb1 + ga2 - gb2 + (-T(7) * ghm1 - ghm2 + T(5) * ghp1 + T(2) * ghp2) * sixth;
-    T g_up2 = ga1 + gb1 + (T(2) * ghm1 - ghp1) * sixth;
-    gr[0] = g_um2;
-    gr[1] = g_um1;
-    gr[2] = g_u0;
-    gr[3] = g_up1;
-    gr[4] = g_up2;
+    // linear maps to (um2, um1, u0, up1, up2); the h's are unscaled here
+    gr[0] = ga3 + gb3 - ghm3 + T(2) * ghp3;
+    gr[1] = ga2 + gb2 - T(2) * ga3 - T(4) * gb3 + T(2) * ghm2 + T(5) * ghm3 - ghp2 - T(7) * ghp3;
+    gr[2] = ga1 + T(3) * gb1 - T(2) * ga2 + ga3 + T(3) * gb3 + T(11) * ghm1 + T(5) * ghm2 + T(2) * ghm3 +
+            T(2) * ghp1 + T(5) * ghp2 + T(11) * ghp3;
+    gr[3] = -T(2) * ga1 - T(4) * gb1 + ga2 - gb2 - T(7) * ghm1 - ghm2 + T(5) * ghp1 + T(2) * ghp2;
+    gr[4] = ga1 + gb1 + T(2) * ghm1 - ghp1;
+    return val;
+}
+
+template <class T>
+__device__ __forceinline__ void weno5_grad(T um2, T um1, T u0, T up1, T up2, T eps, T inv_dx, T gr[5]) {
+    (void)weno5_valgrad<T>(um2, um1, u0, up1, up2, eps, inv_dx, gr);
+}
+
+// Transpose of weno_taps: gv[k] goes to tap k through the generic path.
+template <class T>
+__device__ __forceinline__ void scatter_weno_taps(const DevProb<T>& P, const mol_term& tm, T* lam, const int* I,
+                                                  const T* gv, T t, const T* p) {
+    const int f = tm.field, d = tm.dim, n = P.n[d];
+    int J[3] = {I[0], I[1], I[2]};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        J[d] = wrap_periodic(I[d] - 2 + k, n);
+        scatter_pt(P, lam, f, J[0], J[1], J[2], gv[k], t, p);
+    }
 }
 
 template <class T>
 __device__ __noinline__ void scatter_weno(const DevProb<T>& P, const mol_term& tm, const T* u, T* lam, const int* I, T g,
                                           T t, const T* p) {
-    const int f = tm.field, d = tm.dim, n = P.n[d];
-    int J[3] = {I[0], I[1], I[2]};
     T v[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-        J[d] = wrap_periodic(I[d] - 2 + k, n);
-        v[k] = load_pt(P, u, f, J[0], J[1], J[2], t, p);
-    }
+    weno_taps(P, tm, u, I, t, p, v);
     T gr[5];
     weno5_grad<T>(v[0], v[1], v[2], v[3], v[4], T(tm.eps), T(tm.dx), gr);
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-        J[d] = wrap_periodic(I[d] - 2 + k, n);
-        scatter_pt(P, lam, f, J[0], J[1], J[2], g * gr[k], t, p);
-    }
+    for (int k = 0; k < 5; ++k) gr[k] *= g;
+    scatter_weno_taps(P, tm, lam, I, gr, t, p);
 }
 
 }  // namespace mol

@@ -97,6 +97,8 @@ _PROTOS = {
     "mol_launch_count": (C.c_int64, []),
     "mol_plan_uses_codegen": (C.c_int, [C.c_void_p]),
     "mol_plan_codegen_source": (C.c_char_p, [C.c_void_p]),
+    "mol_plan_launch_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int32)]),
     "mol_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
     "mol_rhs_f32state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
     "mol_step_ssprk33": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64]),
@@ -118,6 +120,7 @@ _PROTOS = {
     "mol_batch_step_ssprk33": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int64]),
     "mol_batch_step_ssprk33_f32state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int64]),
     "mol_batch_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64]),
+    "mol_batch_check": (C.c_int, [C.c_void_p]),
 }
 
 EXPORTED = sorted(_PROTOS)

@@ -140,6 +140,12 @@ class Plan:
         return bool(L.lib().mol_plan_uses_codegen(self._h))
 
     @property
+    def launch_config(self) -> dict:
+        r, t, b = C.c_int32(), C.c_int32(), C.c_int32()
+        L.check(L.lib().mol_plan_launch_config(self._h, C.byref(r), C.byref(t), C.byref(b)), self._h)
+        return {"registers": r.value, "threads": t.value, "blocks": b.value}
+
+    @property
     def generated_source(self) -> str:
         return (L.lib().mol_plan_codegen_source(self._h) or b"").decode()
 
@@ -213,8 +219,13 @@ class Batch:
         L.check(fn(self._h, pu, C.c_void_p(d.ctypes.data), float(t0), int(nsteps)), batch=self._h)
         return u
 
-    def tune(self, threads: int = 0, ctas_per_sm: int = 0):
-        L.check(L.lib().mol_batch_tune(self._h, int(threads), int(ctas_per_sm), 0), batch=self._h)
+    def tune(self, threads: int = 0, ctas_per_sm: int = 0, tile_cells: int = 0):
+        """tile_cells > 0: tiled schedule with that tile; < 0: one CTA per instance; all 0: autotune."""
+        L.check(L.lib().mol_batch_tune(self._h, int(threads), int(ctas_per_sm), int(tile_cells)), batch=self._h)
+
+    def check(self):
+        """Waits for the stream; raises if a run was abandoned after a dependency wait ran out."""
+        L.check(L.lib().mol_batch_check(self._h), batch=self._h)
 
 
 class ODEFunction:

@@ -64,3 +64,44 @@ def test_batch_f32state_and_tuning(gpu_lib):
     again = batch.pack([lw.u0 for lw in lws])
     batch.step_ssprk33(again, dts, 15)
     assert np.allclose(again, u64, rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("tile_cells", [-1, 32, 128, 4096])
+def test_batch_schedules_agree(gpu_lib, tile_cells):
+    """Tiled schedule (instances split over many CTAs, stages ordered by counters) and the
+    one-CTA-per-instance schedule give the per-instance plans' trajectories; tiles of 32
+    cells split every member here, 4096 leaves each member in one tile."""
+    lws, dts = _members(SPECS)
+    batch = Batch(lws)
+    batch.tune(128, 4, tile_cells)
+    u = batch.pack([lw.u0 for lw in lws])
+    batch.step_ssprk33(u, dts, 20, t0=0.0)
+    batch.check()
+    for i, lw in enumerate(lws):
+        ref = lw.u0.copy()
+        Plan(lw).step_ssprk33(ref, dts[i], 20, t0=0.0)
+        got = u[batch.offsets[i]:batch.offsets[i + 1]]
+        assert np.allclose(got, ref, rtol=1e-13, atol=1e-15), (tile_cells, i)
+
+
+def test_batch_tiled_device_arrays_repeat(gpu_lib):
+    """Graph replays of the tiled schedule on device arrays reset their counters: two
+    runs of 7 steps (the second a replay of the first's graph; the members are
+    autonomous, so t0 does not matter) equal one plan run of 14."""
+    torch = pytest.importorskip("torch")
+    lws, dts = _members(SPECS)
+    batch = Batch(lws)
+    batch.tune(256, 2, 64)
+    st = torch.cuda.Stream()
+    batch.set_stream(st.cuda_stream)
+    u = torch.tensor(batch.pack([lw.u0 for lw in lws]), device="cuda")
+    with torch.cuda.stream(st):
+        batch.step_ssprk33(u, dts, 7)
+        batch.step_ssprk33(u, dts, 7)
+    batch.check()
+    got_all = u.cpu().numpy()
+    for i, lw in enumerate(lws):
+        ref = lw.u0.copy()
+        Plan(lw).step_ssprk33(ref, dts[i], 14, t0=0.0)
+        got = got_all[batch.offsets[i]:batch.offsets[i + 1]]
+        assert np.allclose(got, ref, rtol=1e-13, atol=1e-15), i
