@@ -12,12 +12,22 @@
 //   lam_u = 1/3 lam + 3/4 l2 + l1 + dt J(u)^T l1
 // with the same scaled products accumulated into dL/dp and dL/daux.  The
 // vector-Jacobian products are the generated reverse sweep of f (mol_codegen.cu).
+// With the three products kept in accumulators
+//   C = 2dt/3 J(u2)^T lam,  A1 = dt/4 J(u1)^T l2,  A0 = dt J(u)^T l1
+// the combinations become l2 = 2/3 lam + C, l1 = 1/6 lam + 1/4 C + A1 and
+// lam_u = lam + C + A1 + A0.  Each VJP launch reads its seed as such a combination
+// (k_vjp_t's VjpSeed), and the first launch of the next reverse step folds the
+// previous step's accumulators into lam and clears them, so a reverse step is two
+// stage recomputations and three VJP launches with no separate combination pass.
+// C alternates between two buffers so the launch accumulating the new C never
+// shares a buffer with the one it folds.
 // States between checkpoints are recomputed; checkpoint positions follow the
 // binomial (revolve) schedule of Griewank & Walther for `nsnap` slots.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "mol_kernels.cuh"
@@ -56,11 +66,6 @@ __global__ void k_misfit(long long n, const double* u, const double* target, dou
     }
 }
 
-__global__ void k_set_t(SolverState* S, double t) {
-    S->t = t;
-    S->blocks_done = 0;
-}
-
 struct Adj {
     mol_plan* plan;
     long long n;
@@ -72,7 +77,8 @@ struct Adj {
     int64_t N;
     // buffers
     std::vector<double*> slots;
-    double *work, *u1, *u2, *lam, *l2, *l1, *tmp;
+    double *work, *u1, *u2, *lam, *cbuf[2], *a1, *a0, *tmp;
+    int cur = 0;                 // cbuf[cur] holds C of the latest reverse step
     double* lam_p;
     double* lam_aux;
     bool have_lam = false;
@@ -80,6 +86,14 @@ struct Adj {
     double* uT_dev = nullptr;
     long long fwd_steps = 0;
     int err = MOL_OK;
+    // Launches are recorded into CUDA graphs of about kGraphLaunches kernels and replayed
+    // once each: a reverse step is five short launches, and on small grids the gaps
+    // between stream launches would otherwise cost as much as the kernels.
+    static constexpr int kGraphLaunches = 240;
+    bool graphs = false;
+    bool capturing = false;
+    int pending = 0;
+    std::vector<cudaGraphExec_t> execs;
 
     int ck(cudaError_t e, const char* w) {
         if (err) return err;
@@ -87,47 +101,94 @@ struct Adj {
         return err;
     }
 
-    void set_time(double t) {
-        k_set_t<<<1, 1, 0, plan->stream>>>(plan->d_state, t);
-        ++g_launches;
-    }
-
-    // state at step `from` in src -> state at step `from + k` in dst
-    void advance(const double* src, double* dst, int64_t from, int64_t k) {
-        if (err) return;
-        if (dst != src) ck(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, plan->stream), "copy");
-        set_time(t0 + from * dt);
-        for (int64_t s = 0; s < k && !err; ++s) {
-            int st = launch_ssprk_step<double>(plan, dst, u1, u2, p, dt);
-            if (st) err = st;
+    void cap_begin() {
+        if (!graphs || capturing || err) return;
+        cudaError_t e = cudaStreamBeginCapture(plan->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            graphs = false;
+            return;
         }
-        fwd_steps += k;
+        capturing = true;
+        pending = 0;
     }
 
-    void vjp(const double* seed, double scale, const double* u, double t, double* out) {
-        if (err) return;
-        const DevProb<double>& P = plan->P64;
-        const double* cseed = seed;
-        cudaError_t e = launch_k(plan->jit.vjp64, plan->nblocks, plan->nthreads, plan->stream, P, cseed, scale, u, p, t,
-                                 out, lam_p, lam_aux);
-        ++g_launches;
-        ck(e, "vjp launch");
+    void cap_end() {
+        if (!capturing) return;
+        capturing = false;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(plan->stream, &g);
+        if (e != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            ck(e != cudaSuccess ? e : cudaErrorStreamCaptureInvalidated, "adjoint capture");
+            return;
+        }
+        cudaGraphExec_t x = nullptr;
+        e = cudaGraphInstantiate(&x, g, 0);
+        cudaGraphDestroy(g);
+        if (ck(e, "adjoint graph instantiate")) return;
+        execs.push_back(x);
+        ck(cudaGraphLaunch(x, plan->stream), "adjoint graph launch");
     }
+
+    void counted() {
+        if (capturing && ++pending >= kGraphLaunches) cap_end();
+    }
+
+    void release_graphs() {
+        for (cudaGraphExec_t x : execs) cudaGraphExecDestroy(x);
+        execs.clear();
+    }
+
+    double time_of(int64_t m) const { return t0 + (double)m * dt; }
 
     void stage(int which, const double* uin, const double* u0, double* uout, double t) {
         if (err) return;
         const DevProb<double>& P = plan->P64;
         const double* cu = uin;
+        cap_begin();
         cudaError_t e = launch_k(plan->jit.ssp64[which - 1], plan->nblocks, plan->nthreads, plan->stream, P, cu, u0, uout,
                                  p, plan->d_state, dt, t);
         ++g_launches;
         ck(e, "stage launch");
+        counted();
+    }
+
+    // state at step `from` in src -> state at step `from + k` in dst; the first step
+    // writes dst directly, later ones update it in place.  Stage times are t0 + m dt.
+    void advance(const double* src, double* dst, int64_t from, int64_t k) {
+        if (err) return;
+        if (k == 0) {
+            if (dst != src)
+                ck(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, plan->stream), "copy");
+            return;
+        }
+        const double* in = src;
+        for (int64_t s = 0; s < k && !err; ++s) {
+            const double tm = time_of(from + s);
+            stage(1, in, in, u1, tm);
+            stage(2, u1, in, u2, tm);
+            stage(3, u2, in, dst, tm);
+            in = dst;
+        }
+        fwd_steps += k;
+    }
+
+    void vjp(const VjpSeed<double>& in, double scale, const double* u, double t, double* out) {
+        if (err) return;
+        const DevProb<double>& P = plan->P64;
+        cap_begin();
+        cudaError_t e = launch_k(plan->jit.vjp64, plan->nblocks, plan->nthreads, plan->stream, P, in, scale, u, p, t,
+                                 out, lam_p, lam_aux);
+        ++g_launches;
+        ck(e, "vjp launch");
+        counted();
     }
 
     // Reverse step m, the state u_m being in `um`.
     void reverse_step(const double* um, int64_t m) {
         if (err) return;
-        const double tm = t0 + m * dt;
+        const double tm = time_of(m);
         stage(1, um, um, u1, tm);
         stage(2, u1, um, u2, tm);
         fwd_steps += 1;
@@ -138,6 +199,7 @@ struct Adj {
             if (loss_kind == MOL_LOSS_MISFIT) {
                 k_misfit<<<nb, kThreads, 0, plan->stream>>>(n, tmp, target, lam, plan->d_partials);
                 ++g_launches;
+                cap_end();  // the loss is read on the host here
                 std::vector<double> hp(nb);
                 ck(cudaMemcpyAsync(hp.data(), plan->d_partials, sizeof(double) * nb, cudaMemcpyDeviceToHost,
                                    plan->stream), "loss");
@@ -150,16 +212,37 @@ struct Adj {
             }
             have_lam = true;
         }
-        // l2 = 2/3 lam + (2dt/3) J(u2)^T lam
-        k_lincomb3<<<nb, kThreads, 0, plan->stream>>>(n, l2, 2.0 / 3.0, lam, 0.0, nullptr, 0.0, nullptr);
-        vjp(lam, 2.0 * dt / 3.0, u2, tm + dt / 2, l2);
-        // l1 = 1/4 l2 + (dt/4) J(u1)^T l2
-        k_lincomb3<<<nb, kThreads, 0, plan->stream>>>(n, l1, 0.25, l2, 0.0, nullptr, 0.0, nullptr);
-        vjp(l2, dt / 4.0, u1, tm + dt, l1);
-        // lam = 1/3 lam + 3/4 l2 + l1 + dt J(u)^T l1
-        k_lincomb3<<<nb, kThreads, 0, plan->stream>>>(n, lam, 1.0 / 3.0, lam, 0.75, l2, 1.0, l1);
-        vjp(l1, dt, um, tm, lam);
-        g_launches += 3;
+        double* Cold = cbuf[cur];
+        double* Cnew = cbuf[cur ^ 1];
+        cur ^= 1;
+        // lam <- lam + C + A1 + A0 of the step before (all zero before the first), then
+        // Cnew = 2dt/3 J(u2)^T lam
+        VjpSeed<double> s2 = {};
+        s2.x[0] = lam; s2.x[1] = Cold; s2.x[2] = a1; s2.x[3] = a0;
+        s2.a[0] = s2.a[1] = s2.a[2] = s2.a[3] = 1.0;
+        s2.upd = lam;
+        s2.zero[0] = Cold; s2.zero[1] = a1; s2.zero[2] = a0;
+        vjp(s2, 2.0 * dt / 3.0, u2, tm + dt / 2, Cnew);
+        // A1 = dt/4 J(u1)^T l2,  l2 = 2/3 lam + C
+        VjpSeed<double> s1 = {};
+        s1.x[0] = lam; s1.x[1] = Cnew;
+        s1.a[0] = 2.0 / 3.0; s1.a[1] = 1.0;
+        vjp(s1, dt / 4.0, u1, tm + dt, a1);
+        // A0 = dt J(u)^T l1,  l1 = 1/6 lam + 1/4 C + A1
+        VjpSeed<double> s0 = {};
+        s0.x[0] = lam; s0.x[1] = Cnew; s0.x[2] = a1;
+        s0.a[0] = 1.0 / 6.0; s0.a[1] = 0.25; s0.a[2] = 1.0;
+        vjp(s0, dt, um, tm, a0);
+    }
+
+    // dL/du_0 = lam + C + A1 + A0 of the last reverse step, into lam.
+    void finish() {
+        cap_end();
+        if (err) return;
+        k_lincomb3<<<nb, kThreads, 0, plan->stream>>>(n, lam, 1.0, lam, 1.0, cbuf[cur], 1.0, a1);
+        k_lincomb3<<<nb, kThreads, 0, plan->stream>>>(n, lam, 1.0, lam, 1.0, a0, 0.0, nullptr);
+        g_launches += 2;
+        ck(cudaGetLastError(), "adjoint combine");
     }
 
     static double beta(int s, int t) {  // C(s + t, t), saturating
@@ -293,7 +376,10 @@ int mol_rhs_vjp(mol_plan* plan, const double* lambda, const double* u, const dou
     double* op = prep(lam_p, A[3], std::max(plan->nparams, 1));
     double* oa = lam_aux ? prep(lam_aux, A[4], std::max<long long>(plan->aux_total, 1)) : nullptr;
     const DevProb<double>& P = plan->P64;
-    cudaError_t e = launch_k(plan->jit.vjp64, plan->nblocks, plan->nthreads, plan->stream, P, dl, 1.0, du, pp, t, ou,
+    VjpSeed<double> in = {};
+    in.x[0] = dl;
+    in.a[0] = 1.0;
+    cudaError_t e = launch_k(plan->jit.vjp64, plan->nblocks, plan->nthreads, plan->stream, P, in, 1.0, du, pp, t, ou,
                              lam_p ? op : (double*)nullptr, oa);
     ++g_launches;
     if ((st = cuda_check(plan, e, "vjp"))) return st;
@@ -342,6 +428,10 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
     A.t0 = t0;
     A.loss_kind = loss_kind;
     A.N = nsteps;
+    {
+        const char* g = getenv("MOL_ADJOINT_GRAPHS");
+        A.graphs = plan->stream != nullptr && plan->stream != cudaStreamLegacy && !(g && g[0] == '0');
+    }
     for (int64_t i = 0; i < slots; ++i) {
         double* q = get(n);
         if (!q) {
@@ -354,14 +444,17 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
     A.u1 = get(n);
     A.u2 = get(n);
     A.lam = get(n);
-    A.l2 = get(n);
-    A.l1 = get(n);
+    A.cbuf[0] = get(n);
+    A.cbuf[1] = get(n);
+    A.a1 = get(n);
+    A.a0 = get(n);
     A.tmp = get(n);
     A.target = get(n);
     A.lam_p = get(std::max(plan->nparams, 1));
     A.lam_aux = get((size_t)std::max<long long>(plan->aux_total, 1));
     double* pbuf = get(std::max(plan->nparams, 1));
-    if (!A.work || !A.u1 || !A.u2 || !A.lam || !A.l2 || !A.l1 || !A.tmp || !A.target || !A.lam_p || !A.lam_aux || !pbuf) {
+    if (!A.work || !A.u1 || !A.u2 || !A.lam || !A.cbuf[0] || !A.cbuf[1] || !A.a1 || !A.a0 || !A.tmp || !A.target ||
+        !A.lam_p || !A.lam_aux || !pbuf) {
         release();
         return set_err(plan, MOL_ERR_OOM, "adjoint buffers do not fit in device memory");
     }
@@ -387,6 +480,7 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
     }
     k_zero<<<64, 256, 0, plan->stream>>>(std::max(plan->nparams, 1), A.lam_p);
     k_zero<<<1024, 256, 0, plan->stream>>>(std::max<long long>(plan->aux_total, 1), A.lam_aux);
+    for (double* q : {A.cbuf[0], A.cbuf[1], A.a1, A.a0}) k_zero<<<1024, 256, 0, plan->stream>>>(n, q);
     if (nsteps == 0) {
         // L depends on u0 directly
         if (loss_kind == MOL_LOSS_MISFIT) {
@@ -403,7 +497,9 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
     } else {
         std::vector<double*> free(A.slots.begin() + 1, A.slots.end());
         A.rev(0, nsteps, A.slots[0], free);
+        A.finish();
     }
+    A.cap_end();
     st = A.err;
     if (!st && uT) st = dev_out(plan, uT, A.uT_dev, n);
     if (!st && dLdu0) st = dev_out(plan, dLdu0, A.lam, n);
@@ -413,6 +509,7 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
     if (loss) *loss = A.loss;
     if (nforward_steps) *nforward_steps = A.fwd_steps;
     release();
+    A.release_graphs();
     return st;
 }
 

@@ -248,6 +248,19 @@ void emit_reverse(Emitter& e, const SSA& s, const Leaves& L, const std::string& 
 
 bool zero_w(const mol_problem_desc* d, long long off) { return d->weights[off] == 0.0; }
 
+// Largest tap count of an operator over its interior and boundary tables.
+int max_taps(const mol_op1d& o) { return std::max(1, std::max(o.L, std::max(o.bLlo, o.bLhi))); }
+
+// "true" when a boundary row of field f along dimension dim has program coefficients.
+const char* dyn_bc(const mol_problem_desc* d, int f, int dim) {
+    if (f < 0 || f >= d->nfields || dim < 0 || dim >= d->ndim) return "true";
+    for (int side = 0; side < 2; ++side) {
+        const mol_bc& b = d->bc[f][dim][side];
+        if (b.kind == MOL_BC_ROBIN && b.prog >= 0) return "true";
+    }
+    return "false";
+}
+
 // Warp-shuffle aggregation of contiguous-axis VJP scatters (MOL_JIT_WARP_SCATTER=0 turns it off).
 bool warp_scatter() {
     const char* w = getenv("MOL_JIT_WARP_SCATTER");
@@ -337,7 +350,9 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
         }
         e << "        return acc;\n";
     }
-    e << "    }\n    return apply_op(P, P.ops[" << tm.op << "], u, " << F << ", " << D << ", I, t, p);\n}\n";
+    const std::string DY = dyn_bc(d, tm.field, tm.dim);
+    e << "    }\n    return apply_op_line<T, " << D << ", " << max_taps(o) << ", " << DY << ">(P, P.ops[" << tm.op
+      << "], u, " << F << ", I, c, I[" << D << "], P.n[" << D << "], t, p);\n}\n";
     // vjp
     e << "template <class T>\n__device__ __forceinline__ void gt" << K
       << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
@@ -355,8 +370,8 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
         e << "};\n        scatter_taps<T, " << o.L << ", " << o.omin << ", " << (warp_scatter() ? "true" : "false")
           << ">(b, c, s, vv, own);\n";
     }
-    e << "        return;\n    }\n    scatter_op(P, P.ops[" << tm.op << "], lam_u, " << F << ", " << D << ", I, I[" << D
-      << "], P.n[" << D << "], g, t, p);\n}\n";
+    e << "        return;\n    }\n    scatter_op_line<T, " << D << ", " << max_taps(o) << ", " << DY << ">(P, P.ops["
+      << tm.op << "], lam_u, " << F << ", I, c, I[" << D << "], P.n[" << D << "], g, t, p);\n}\n";
 }
 
 void emit_mixed(Emitter& e, const mol_problem_desc* d, int k) {
@@ -410,6 +425,7 @@ void emit_weno(Emitter& e, const mol_problem_desc* d, int k) {
     const std::string K = std::to_string(k), F = std::to_string(tm.field), D = std::to_string(tm.dim);
     const std::string cond = "fast_weno(P, " + F + ", " + D + ", I[" + D + "])";
     const char* W = warp_scatter() ? "true" : "false";
+    const std::string DY = dyn_bc(d, tm.field, tm.dim);
     const std::string sig = "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, "
                             "const T* __restrict__ p";
     const std::string load =
@@ -419,7 +435,7 @@ void emit_weno(Emitter& e, const mol_problem_desc* d, int k) {
         "        const long long s = gstride(P, " + D + ");\n"
         "        v[0] = b[-2 * s]; v[1] = b[-s]; v[2] = b[0]; v[3] = b[s]; v[4] = b[2 * s];\n"
         "    } else {\n"
-        "        weno_taps(P, P.terms[" + K + "], u, I, t, p, v);\n"
+        "        weno_taps_line<T, " + D + ", " + DY + ">(P, " + F + ", u, I, c, t, p, v);\n"
         "    }\n";
     const std::string args = "v[0], v[1], v[2], v[3], v[4], T(P.terms[" + K + "].eps), T(P.terms[" + K + "].dx)";
     // scatter of vv[5] (already multiplied by the adjoint seed) on the path `fastexpr` picks
@@ -428,7 +444,7 @@ void emit_weno(Emitter& e, const mol_problem_desc* d, int k) {
                "        T* lb = lam_u + (long long)" + F + " * P.ncell + c;\n"
                "        scatter_taps<T, 5, -2, " + W + ">(lb, c, gstride(P, " + D + "), vv, own);\n"
                "    } else {\n"
-               "        scatter_weno_taps(P, P.terms[" + K + "], lam_u, I, vv, t, p);\n"
+               "        scatter_weno_taps_line<T, " + D + ", " + DY + ">(P, " + F + ", lam_u, I, c, vv, t, p);\n"
                "    }\n";
     };
     e << "template <class T>\n__device__ __forceinline__ T gt" << K << sig << ") {\n"
@@ -493,13 +509,16 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
     };
 
     // generic face (runtime taps)
-    e << "template <class T>\n__device__ __noinline__ T gface" << K
-      << "(const DevProb<T>& P, const T* __restrict__ u, const int* I, int Ih, T t, const T* __restrict__ p) {\n"
-      << "    const T du = apply_op_at(P, P.ops[" << opi << "], u, " << F << ", " << D << ", I, Ih, P.n[" << D
-      << "], t, p);\n";
+    const std::string NTI = std::to_string(max_taps(oi)), NTP = std::to_string(max_taps(op)),
+                      NTO = std::to_string(max_taps(oo));
+    e << "template <class T>\n__device__ __forceinline__ T gface" << K
+      << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, int Ih, T t, const T* __restrict__ "
+         "p) {\n"
+      << "    const T du = apply_op_line<T, " << D << ", " << NTI << ", " << dyn_bc(d, tm.field, tm.dim) << ">(P, P.ops["
+      << opi << "], u, " << F << ", I, c, Ih, P.n[" << D << "], t, p);\n";
     for (int f : used_fields)
-        e << "    const T uf" << f << " = apply_op_at(P, P.ops[" << opp << "], u, " << f << ", " << D << ", I, Ih, P.n["
-          << D << "], t, p);\n";
+        e << "    const T uf" << f << " = apply_op_line<T, " << D << ", " << NTP << ", " << dyn_bc(d, f, tm.dim)
+          << ">(P, P.ops[" << opp << "], u, " << f << ", I, c, Ih, P.n[" << D << "], t, p);\n";
     for (int j : used_aux)
         e << "    const T fa" << j << " = P.aux[P.aux_off[P.terms[" << K << "].aux0 + " << j << "] + face_index(P, " << D
           << ", Ih, I)];\n";
@@ -507,25 +526,27 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
     e << "    return a * du;\n}\n";
 
     // generic face adjoint
-    e << "template <class T>\n__device__ __noinline__ void gface" << K
-      << "_vjp(const DevProb<T>& P, const T* __restrict__ u, const int* I, int Ih, T t, const T* __restrict__ p, T g, "
-         "T* lam_u, T* lp, T* lam_aux) {\n"
-      << "    const T du = apply_op_at(P, P.ops[" << opi << "], u, " << F << ", " << D << ", I, Ih, P.n[" << D
-      << "], t, p);\n";
+    e << "template <class T>\n__device__ __forceinline__ void gface" << K
+      << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, int Ih, T t, const T* "
+         "__restrict__ p, T g, T* lam_u, T* lp, T* lam_aux) {\n"
+      << "    const T du = apply_op_line<T, " << D << ", " << NTI << ", " << dyn_bc(d, tm.field, tm.dim) << ">(P, P.ops["
+      << opi << "], u, " << F << ", I, c, Ih, P.n[" << D << "], t, p);\n";
     for (int f : used_fields)
-        e << "    const T uf" << f << " = apply_op_at(P, P.ops[" << opp << "], u, " << f << ", " << D << ", I, Ih, P.n["
-          << D << "], t, p);\n    T guf" << f << " = T(0);\n";
+        e << "    const T uf" << f << " = apply_op_line<T, " << D << ", " << NTP << ", " << dyn_bc(d, f, tm.dim)
+          << ">(P, P.ops[" << opp << "], u, " << f << ", I, c, Ih, P.n[" << D << "], t, p);\n    T guf" << f
+          << " = T(0);\n";
     for (int j : used_aux)
         e << "    const long long fi" << j << " = P.aux_off[P.terms[" << K << "].aux0 + " << j << "] + face_index(P, "
           << D << ", Ih, I);\n    const T fa" << j << " = P.aux[fi" << j << "];\n    T gfa" << j << " = T(0);\n";
     face_forward("");
-    e << "    scatter_op(P, P.ops[" << opi << "], lam_u, " << F << ", " << D << ", I, Ih, P.n[" << D << "], g * a, t, p);\n";
+    e << "    scatter_op_line<T, " << D << ", " << NTI << ", " << dyn_bc(d, tm.field, tm.dim) << ">(P, P.ops[" << opi
+      << "], lam_u, " << F << ", I, c, Ih, P.n[" << D << "], g * a, t, p);\n";
     if (has_prog) {
         FaceLeaves L("");
         emit_reverse(e, fs, L, "", [&](int) { return std::string("g * du"); });
         for (int f : used_fields)
-            e << "    scatter_op(P, P.ops[" << opp << "], lam_u, " << f << ", " << D << ", I, Ih, P.n[" << D
-              << "], guf" << f << ", t, p);\n";
+            e << "    scatter_op_line<T, " << D << ", " << NTP << ", " << dyn_bc(d, f, tm.dim) << ">(P, P.ops[" << opp
+              << "], lam_u, " << f << ", I, c, Ih, P.n[" << D << "], guf" << f << ", t, p);\n";
         for (int j : used_aux) e << "    if (lam_aux) atomicAdd(lam_aux + fi" << j << ", gfa" << j << ");\n";
     }
     e << "}\n";
@@ -614,13 +635,14 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
         e << "    const bool per = (P.permask[" << F << "] >> " << D << ") & 1;\n"
           << "    const TapSel so = select_taps(P.ops[" << opo << "], I[" << D << "] - 1, P.n[" << D << "] - 1, per);\n";
         if (!vjp) e << "    T acc = T(0);\n    bool started = false;\n";
-        e << "    for (int q = 0; q < so.cnt; ++q) {\n"
+        e << "#pragma unroll\n    for (int q = 0; q < " << NTO << "; ++q) {\n"
+          << "        if (q >= so.cnt) break;\n"
           << "        const T w_ = P.w[so.woff + q];\n        if (w_ == T(0)) continue;\n";
         if (!vjp)
-            e << "        const T F_ = gface" << K << "<T>(P, u, I, so.first + q, t, p);\n"
+            e << "        const T F_ = gface" << K << "<T>(P, u, c, I, so.first + q, t, p);\n"
               << "        acc = started ? fma(w_, F_, acc) : w_ * F_;\n        started = true;\n    }\n    return acc;\n";
         else
-            e << "        gface" << K << "_vjp<T>(P, u, I, so.first + q, t, p, g * w_, lam_u, lp, lam_aux);\n    }\n";
+            e << "        gface" << K << "_vjp<T>(P, u, c, I, so.first + q, t, p, g * w_, lam_u, lp, lam_aux);\n    }\n";
         e << "}\n";
     }
 }
@@ -972,6 +994,7 @@ std::string generate_source(const mol_problem_desc* d, std::string& why) {
         e << "    atomicAdd(lam_u + (long long)" << f << " * P.ncell + c, own" << f << ");\n";
     e << "}\n";
     e << "struct GenCell {\n"
+      << "static constexpr int kFields = " << d->nfields << ";\n"
          "template <class T> using Uniform = GenUniform<T>;\n"
          "template <class T>\nstatic __device__ __forceinline__ void uniform(const DevProb<T>& P, T t, const T* "
          "__restrict__ p, GenUniform<T>& U) { gen_uniform<T>(P, t, p, U); }\n"

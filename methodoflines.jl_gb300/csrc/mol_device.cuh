@@ -33,10 +33,14 @@ struct SolverState {
     unsigned int blocks_done, pad2;
 };
 
+// One boundary row.  For rows with constant coefficients (prog < 0) the host also
+// stores inv = 1 / (a + b w_kb) (Robin/Neumann: the boundary value is
+// (g - b sum_{k != kb} w_k u_k) * inv) and c0 = g / a (Dirichlet, b == 0).
 template <class T>
 struct DevBC {
     int kind, prog, op, pad;
     T a, b, g;
+    T inv, c0;
 };
 
 // Everything a kernel needs to evaluate f(du, u, p, t) of one problem instance.
@@ -143,13 +147,14 @@ __device__ __noinline__ T bc_value(const DevProb<T>& P, const T* u, int f, int* 
     if ((side == 0 && I[dout] != 1) || (side == 1 && I[dout] != P.n[dout])) return T(0);
     const DevBC<T> B = P.bc[(f * 3 + dout) * 2 + side];
     if (B.kind != MOL_BC_ROBIN) return T(0);
+    const bool dyn = B.prog >= 0;
     T a = B.a, b = B.b, g = B.g;
-    if (B.prog >= 0) {
+    if (dyn) {
         a = run_bc_prog(P, B.prog, 0, I, t, p);
         b = run_bc_prog(P, B.prog, 1, I, t, p);
         g = run_bc_prog(P, B.prog, 2, I, t, p);
     }
-    if (b == T(0)) return g / a;
+    if (b == T(0)) return dyn ? g / a : B.c0;
     const mol_op1d op = P.ops[B.op];
     const int n = P.n[dout];
     const T* w = side == 0 ? P.w + op.w_lo : P.w + op.w_hi;  // centered table at the last point
@@ -166,7 +171,7 @@ __device__ __noinline__ T bc_value(const DevProb<T>& P, const T* u, int f, int* 
         acc = started ? acc + term : term;
         started = true;
     }
-    return (g - b * acc) / (a + b * w[kb]);
+    return dyn ? (g - b * acc) / (a + b * w[kb]) : (g - b * acc) * B.inv;
 }
 
 struct TapSel {
@@ -221,6 +226,92 @@ __device__ __forceinline__ T apply_op(const DevProb<T>& P, const mol_op1d& op, c
 template <class T>
 __device__ __forceinline__ long long gstride(const DevProb<T>& P, int d) {
     return d == 0 ? 1ll : (d == 1 ? (long long)P.ni[0] : (long long)P.ni[0] * P.ni[1]);
+}
+
+// ---------------------------------------------------------------------------
+// Line helpers for 1-D terms along a compile-time dimension D.  The cell being
+// evaluated is an unknown, so only the coordinate along D can leave the interior,
+// and an interior tap sits at a fixed flat offset from the cell's own index c.
+// Loops over taps are unrolled to the operator's largest tap count NT (known when
+// the code is generated), so a cell near an edge issues its loads together
+// instead of walking them one call at a time.
+
+// Boundary value of field f at the end `side` of the line through the cell: the
+// observed boundary row solved for the boundary point (same arithmetic as bc_value).
+// Out of line (edge cells only; inlined into every tap it multiplies compile time
+// several-fold) and with scalar arguments, so callers keep their index arrays in
+// registers.  DYN: some boundary row of this field along D has coefficients given by
+// a program (time or coordinate dependent); only then is bc_value reachable.
+template <class T, int D, bool DYN>
+__device__ __noinline__ T bc_line_value(const DevProb<T>& P, const T* __restrict__ u, int f, int i0, int i1, int i2,
+                                        long long c, int side, T t, const T* __restrict__ p) {
+    const int iD = D == 0 ? i0 : (D == 1 ? i1 : i2);
+    const DevBC<T>& B = P.bc[(f * 3 + D) * 2 + side];
+    if (B.kind != MOL_BC_ROBIN) return T(0);
+    if (DYN && B.prog >= 0) {
+        int J[3] = {i0, i1, i2};
+        J[D] = side == 0 ? 1 : P.n[D];
+        return bc_value(P, u, f, J, D, side, t, p);
+    }
+    if (B.b == T(0)) return B.c0;
+    const mol_op1d& op = P.ops[B.op];
+    const int n = P.n[D];
+    const T* __restrict__ w = side == 0 ? P.w + op.w_lo : P.w + op.w_hi;
+    const int first = side == 0 ? 1 : n - op.bLhi + 1;
+    const int cnt = side == 0 ? op.bLlo : op.bLhi;
+    const int kb = side == 0 ? 0 : cnt - 1;
+    const long long s = gstride(P, D);
+    const T* __restrict__ uf = u + (long long)f * P.ncell + c;
+    T acc = T(0);
+    bool started = false;
+#pragma unroll 4
+    for (int k = 0; k < cnt; ++k) {
+        if (k == kb) continue;
+        const int q = first + k;
+        const T v = (q > P.lo[D] && q <= n - P.up[D]) ? uf[(long long)(q - iD) * s] : T(0);
+        const T term = w[k] * v;
+        acc = started ? acc + term : term;
+        started = true;
+    }
+    return (B.g - B.b * acc) * B.inv;
+}
+
+// Field f at full-grid position q of the line through the cell (load_pt restricted to D).
+template <class T, int D, bool DYN>
+__device__ __forceinline__ T line_pt(const DevProb<T>& P, const T* __restrict__ u, int f, const int* I, long long c,
+                                     int q, T t, const T* __restrict__ p) {
+    const int n = P.n[D];
+    if ((P.permask[f] >> D) & 1) q = wrap_periodic(q, n);
+    if (q > P.lo[D] && q <= n - P.up[D])
+        return u[(long long)f * P.ncell + c + (long long)(q - I[D]) * gstride(P, D)];
+    if (q <= P.lo[D]) return q == 1 ? bc_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 0, t, p) : T(0);
+    return q == n ? bc_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 1, t, p) : T(0);
+}
+
+// apply_op_at restricted to D: sum_k w_k u[tap_k] at position `pos` of a line of `len` points.
+template <class T, int D, int NT, bool DYN>
+__device__ __forceinline__ T apply_op_line(const DevProb<T>& P, const mol_op1d& op, const T* __restrict__ u, int f,
+                                           const int* I, long long c, int pos, int len, T t,
+                                           const T* __restrict__ p) {
+    const bool per = (P.permask[f] >> D) & 1;
+    const TapSel s = select_taps(op, pos, len, per);
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        if (k < s.cnt) {
+            const T v = line_pt<T, D, DYN>(P, u, f, I, c, s.first + k, t, p);
+            acc = k == 0 ? P.w[s.woff] * v : fma(P.w[s.woff + k], v, acc);
+        }
+    }
+    return acc;
+}
+
+// The five WENO taps of the cell along D (weno_taps restricted to D).
+template <class T, int D, bool DYN>
+__device__ __forceinline__ void weno_taps_line(const DevProb<T>& P, int f, const T* __restrict__ u, const int* I,
+                                               long long c, T t, const T* __restrict__ p, T v[5]) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) v[k] = line_pt<T, D, DYN>(P, u, f, I, c, wrap_periodic(I[D] - 2 + k, P.n[D]), t, p);
 }
 
 // True when operator `o` at position i of dimension d uses its interior weights and

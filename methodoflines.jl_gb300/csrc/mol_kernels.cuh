@@ -29,6 +29,7 @@ __device__ __forceinline__ double div3m(double x) {
 __device__ __forceinline__ float div3m(float x) { return x / 3.0f; }
 
 struct InterpCell {
+    static constexpr int kFields = 0;  // field count known only at run time
     template <class T>
     struct Uniform {};
     template <class T>
@@ -41,6 +42,13 @@ struct InterpCell {
     }
 };
 
+// Fields per cell: a compile-time constant for generated cells (so per-field loops unroll
+// and the per-cell output arrays stay in registers), the descriptor's count otherwise.
+template <class G, class T>
+__device__ __forceinline__ int nfields_of(const DevProb<T>& P) {
+    return G::kFields > 0 ? G::kFields : P.nfields;
+}
+
 template <class T, class G>
 __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_rhs_t(const __grid_constant__ DevProb<T> P, const T* __restrict__ u, T* __restrict__ du,
                                                     const T* __restrict__ p, double t) {
@@ -52,7 +60,8 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_rhs_t(const __grid
         int I[3];
         cell_index(P, c, I);
         G::cell(P, u, c, I, T(t), p, U, out);
-        for (int f = 0; f < P.nfields; ++f) du[(long long)f * P.ncell + c] = out[f];
+        #pragma unroll
+        for (int f = 0; f < nfields_of<G>(P); ++f) du[(long long)f * P.ncell + c] = out[f];
     }
 }
 
@@ -95,7 +104,8 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_ssprk_t(const __gr
         int I[3];
         cell_index(P, c, I);
         G::cell(P, uin, c, I, T(ts), p, U, out);
-        for (int f = 0; f < P.nfields; ++f) {
+        #pragma unroll
+        for (int f = 0; f < nfields_of<G>(P); ++f) {
             const long long g = (long long)f * P.ncell + c;
             uout[g] = ssprk_combine<T, STAGE>(u0[g], uin[g], out[f], T(dt), T(2 * dt));
         }
@@ -105,10 +115,24 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_ssprk_t(const __gr
 
 // Vector-Jacobian product of the RHS: lam_u += scale * (df/du)^T lam, lam_p and lam_aux likewise.
 // Parameter adjoints are reduced per block before one atomic per block and parameter.
+// The adjoint seed of a VJP launch, read cell by cell: v = sum_k a[k] x[k] (null x[k]
+// skipped), seed = scale * v.  When `upd` is set, v is also written there, and the
+// `zero` arrays are cleared, all at the cell being processed (so one of the x[k] may be
+// updated in place).  This folds the linear combinations of the reverse RK sweep into
+// the VJP launches that read them.
+template <class T>
+struct VjpSeed {
+    const T* x[4];
+    T a[4];
+    T* upd;
+    T* zero[3];
+};
+
 template <class T, class G, int NP>
-__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_vjp_t(const __grid_constant__ DevProb<T> P, const T* __restrict__ lam, T scale,
-                                                    const T* __restrict__ u, const T* __restrict__ p, double t,
-                                                    T* lam_u, T* lam_p, T* lam_aux) {
+__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_vjp_t(const __grid_constant__ DevProb<T> P,
+                                                                    const VjpSeed<T> in, T scale,
+                                                                    const T* __restrict__ u, const T* __restrict__ p,
+                                                                    double t, T* lam_u, T* lam_p, T* lam_aux) {
     T lp[NP > 0 ? NP : 1];
 #pragma unroll
     for (int k = 0; k < (NP > 0 ? NP : 1); ++k) lp[k] = T(0);
@@ -117,7 +141,19 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_vjp_t(const __grid
          c += (long long)gridDim.x * blockDim.x) {
         int I[3];
         cell_index(P, c, I);
-        for (int f = 0; f < P.nfields; ++f) seed[f] = scale * lam[(long long)f * P.ncell + c];
+        #pragma unroll
+        for (int f = 0; f < nfields_of<G>(P); ++f) {
+            const long long q = (long long)f * P.ncell + c;
+            T v = in.a[0] * in.x[0][q];
+#pragma unroll
+            for (int k = 1; k < 4; ++k)
+                if (in.x[k]) v += in.a[k] * in.x[k][q];
+            if (in.upd) in.upd[q] = v;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (in.zero[k]) in.zero[k][q] = T(0);
+            seed[f] = scale * v;
+        }
         G::cell_vjp(P, u, c, I, T(t), p, seed, lam_u, lp, lam_aux);
     }
     if (NP > 0 && lam_p) {
@@ -141,7 +177,7 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_vjp_t(const __grid
 // (largest first, dynamic via an atomic ticket) and integrates it for `nsteps`
 // SSPRK33 steps, synchronising only its own threads between stages.
 template <class T, class G>
-__global__ void __launch_bounds__(kThreads) k_batch_ssprk_t(const DevProb<T>* __restrict__ probs,
+__global__ void __launch_bounds__(kThreads, 1) k_batch_ssprk_t(const DevProb<T>* __restrict__ probs,
                                                             const long long* __restrict__ off,
                                                             const int* __restrict__ order, int ninst, T* U, T* U1,
                                                             T* U2, const T* const* __restrict__ params,
@@ -170,7 +206,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_ssprk_t(const DevProb<T>* __
                 int I[3];
                 cell_index(P, c, I);
                 G::cell(P, u, c, I, T(t), p, UN, out);
-                for (int f = 0; f < P.nfields; ++f) {
+                #pragma unroll
+                for (int f = 0; f < nfields_of<G>(P); ++f) {
                     const long long g = (long long)f * nc + c;
                     u1[g] = ssprk_combine<T, 1>(u[g], u[g], out[f], T(dt), T(2 * dt));
                 }
@@ -181,7 +218,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_ssprk_t(const DevProb<T>* __
                 int I[3];
                 cell_index(P, c, I);
                 G::cell(P, u1, c, I, T(t + dt), p, UN, out);
-                for (int f = 0; f < P.nfields; ++f) {
+                #pragma unroll
+                for (int f = 0; f < nfields_of<G>(P); ++f) {
                     const long long g = (long long)f * nc + c;
                     u2[g] = ssprk_combine<T, 2>(u[g], u1[g], out[f], T(dt), T(2 * dt));
                 }
@@ -192,7 +230,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_ssprk_t(const DevProb<T>* __
                 int I[3];
                 cell_index(P, c, I);
                 G::cell(P, u2, c, I, T(t + dt / 2), p, UN, out);
-                for (int f = 0; f < P.nfields; ++f) {
+                #pragma unroll
+                for (int f = 0; f < nfields_of<G>(P); ++f) {
                     const long long g = (long long)f * nc + c;
                     u[g] = ssprk_combine<T, 3>(u[g], u2[g], out[f], T(dt), T(2 * dt));
                 }
@@ -237,7 +276,7 @@ __device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsig
 }
 
 template <class T, class G>
-__global__ void __launch_bounds__(kThreads) k_batch_tiles_t(const DevProb<T>* __restrict__ probs,
+__global__ void __launch_bounds__(kThreads, 1) k_batch_tiles_t(const DevProb<T>* __restrict__ probs,
                                                             const long long* __restrict__ off,
                                                             const int* __restrict__ order,
                                                             const long long* __restrict__ tile_pre, int ninst,
@@ -305,7 +344,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_tiles_t(const DevProb<T>* __
                 int I[3];
                 cell_index(P, c, I);
                 G::cell(P, u, c, I, T(t), p, UN, out);
-                for (int f = 0; f < P.nfields; ++f) {
+                #pragma unroll
+                for (int f = 0; f < nfields_of<G>(P); ++f) {
                     const long long q = (long long)f * nc + c;
                     u1[q] = ssprk_combine<T, 1>(u[q], u[q], out[f], T(dt), T(2 * dt));
                 }
@@ -316,7 +356,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_tiles_t(const DevProb<T>* __
                 int I[3];
                 cell_index(P, c, I);
                 G::cell(P, u1, c, I, T(t + dt), p, UN, out);
-                for (int f = 0; f < P.nfields; ++f) {
+                #pragma unroll
+                for (int f = 0; f < nfields_of<G>(P); ++f) {
                     const long long q = (long long)f * nc + c;
                     u2[q] = ssprk_combine<T, 2>(u[q], u1[q], out[f], T(dt), T(2 * dt));
                 }
@@ -327,7 +368,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_tiles_t(const DevProb<T>* __
                 int I[3];
                 cell_index(P, c, I);
                 G::cell(P, u2, c, I, T(t + dt / 2), p, UN, out);
-                for (int f = 0; f < P.nfields; ++f) {
+                #pragma unroll
+                for (int f = 0; f < nfields_of<G>(P); ++f) {
                     const long long q = (long long)f * nc + c;
                     u[q] = ssprk_combine<T, 3>(u[q], u2[q], out[f], T(dt), T(2 * dt));
                 }
@@ -369,7 +411,8 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_tsit_stage_t(const
         int I[3];
         cell_index(P, c, I);
         G::cell(P, y, c, I, T(t), p, U, out);
-        for (int f = 0; f < P.nfields; ++f) {
+        #pragma unroll
+        for (int f = 0; f < nfields_of<G>(P); ++f) {
             const long long g = (long long)f * P.ncell + c;
             k[stage - 1][g] = out[f];
             if (stage < 7) {

@@ -479,6 +479,18 @@ static int build_prec(mol_plan* plan, const mol_problem_desc* d, PlanArrays& A, 
                     b.a = (T)src.a;
                     b.b = (T)src.b;
                     b.g = (T)src.g;
+                    // constant rows: the reciprocal of the solved-for coefficient, and the
+                    // Dirichlet value, once on the host (the device multiplies)
+                    if (src.kind == MOL_BC_ROBIN && src.prog < 0) {
+                        if (b.b == (T)0) {
+                            b.c0 = b.g / b.a;
+                        } else if (src.op >= 0 && src.op < d->nops) {
+                            const mol_op1d& o = d->ops[src.op];
+                            const long long wkb = s == 0 ? o.w_lo : o.w_hi + (o.bLhi - 1);
+                            const T den = std::fma(b.b, (T)d->weights[wkb], b.a);
+                            b.inv = (T)1 / den;
+                        }
+                    }
                 }
                 bc[(f * 3 + q) * 2 + s] = b;
             }

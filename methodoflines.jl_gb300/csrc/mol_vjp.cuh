@@ -30,7 +30,7 @@ __device__ __noinline__ void bc_scatter(const DevProb<T>& P, T* lam, int f, cons
     const int first = side == 0 ? 1 : n - op.bLhi + 1;
     const int cnt = side == 0 ? op.bLlo : op.bLhi;
     const int kb = side == 0 ? 0 : cnt - 1;
-    const T s = -b * g / (a + b * w[kb]);
+    const T s = B.prog >= 0 ? -b * g / (a + b * w[kb]) : -b * g * B.inv;
     int J[3] = {I[0], I[1], I[2]};
     for (int k = 0; k < cnt; ++k) {
         if (k == kb) continue;
@@ -104,6 +104,73 @@ __device__ __noinline__ void scatter_mixed(const DevProb<T>& P, const mol_term& 
             scatter_pt(P, lam, f, J[0], J[1], J[2], g * (wa * wb), t, p);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Transposes of the line helpers of mol_device.cuh (compile-time dimension D).
+
+template <class T, int D, bool DYN>
+__device__ __noinline__ void scatter_bc_line(const DevProb<T>& P, T* lam, int f, int i0, int i1, int i2, long long c,
+                                             int side, T g, T t, const T* __restrict__ p) {
+    const int iD = D == 0 ? i0 : (D == 1 ? i1 : i2);
+    const DevBC<T>& B = P.bc[(f * 3 + D) * 2 + side];
+    if (B.kind != MOL_BC_ROBIN) return;
+    if (DYN && B.prog >= 0) {
+        int J[3] = {i0, i1, i2};
+        J[D] = side == 0 ? 1 : P.n[D];
+        bc_scatter(P, lam, f, J, D, side, g, t, p);
+        return;
+    }
+    if (B.b == T(0)) return;
+    const mol_op1d& op = P.ops[B.op];
+    const int n = P.n[D];
+    const T* __restrict__ w = side == 0 ? P.w + op.w_lo : P.w + op.w_hi;
+    const int first = side == 0 ? 1 : n - op.bLhi + 1;
+    const int cnt = side == 0 ? op.bLlo : op.bLhi;
+    const int kb = side == 0 ? 0 : cnt - 1;
+    const T sg = -B.b * g * B.inv;
+    const long long s = gstride(P, D);
+    T* lf = lam + (long long)f * P.ncell + c;
+#pragma unroll 4
+    for (int k = 0; k < cnt; ++k) {
+        if (k == kb) continue;
+        const int q = first + k;
+        if (q > P.lo[D] && q <= n - P.up[D]) atomicAdd(lf + (long long)(q - iD) * s, sg * w[k]);
+    }
+}
+
+template <class T, int D, bool DYN>
+__device__ __forceinline__ void scatter_line_pt(const DevProb<T>& P, T* lam, int f, const int* I, long long c, int q,
+                                                T g, T t, const T* __restrict__ p) {
+    const int n = P.n[D];
+    if ((P.permask[f] >> D) & 1) q = wrap_periodic(q, n);
+    if (q > P.lo[D] && q <= n - P.up[D]) {
+        atomicAdd(lam + (long long)f * P.ncell + c + (long long)(q - I[D]) * gstride(P, D), g);
+        return;
+    }
+    if (q <= P.lo[D]) {
+        if (q == 1) scatter_bc_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 0, g, t, p);
+    } else if (q == n) {
+        scatter_bc_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 1, g, t, p);
+    }
+}
+
+template <class T, int D, int NT, bool DYN>
+__device__ __forceinline__ void scatter_op_line(const DevProb<T>& P, const mol_op1d& op, T* lam, int f, const int* I,
+                                                long long c, int pos, int len, T g, T t, const T* __restrict__ p) {
+    const bool per = (P.permask[f] >> D) & 1;
+    const TapSel s = select_taps(op, pos, len, per);
+#pragma unroll
+    for (int k = 0; k < NT; ++k)
+        if (k < s.cnt) scatter_line_pt<T, D, DYN>(P, lam, f, I, c, s.first + k, g * P.w[s.woff + k], t, p);
+}
+
+template <class T, int D, bool DYN>
+__device__ __forceinline__ void scatter_weno_taps_line(const DevProb<T>& P, int f, T* lam, const int* I, long long c,
+                                                       const T* gv, T t, const T* __restrict__ p) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        scatter_line_pt<T, D, DYN>(P, lam, f, I, c, wrap_periodic(I[D] - 2 + k, P.n[D]), gv[k], t, p);
 }
 
 // Transpose of one interior stencil line: adds v[m] to the adjoint at offset
