@@ -325,6 +325,17 @@ struct FaceLeaves : Leaves {
     std::string term_adj(int, const std::string&) const override { return ""; }
 };
 
+// True when field f is periodic along dimension dim (interior weights everywhere).
+bool periodic_dim(const mol_problem_desc* d, int f, int dim) {
+    return f >= 0 && f < d->nfields && dim >= 0 && dim < d->ndim && d->bc[f][dim][0].kind == MOL_BC_PERIODIC;
+}
+
+// Largest |offset| of an operator's interior taps.
+int reach_of(const mol_op1d& o) { return std::max(std::abs(o.omin), std::abs(o.omin + o.L - 1)); }
+
+// Linear stencil term.  Along a periodic dimension every cell uses the interior weights
+// with wrapped offsets (one uniform branch, no edge path); otherwise interior cells use
+// compile-time offsets and cells near an edge the line helpers.
 void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
     const mol_term& tm = d->terms[k];
     const mol_op1d& o = d->ops[tm.op];
@@ -332,10 +343,18 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
     std::vector<int> nz;
     for (int m = 0; m < o.L; ++m)
         if (!zero_w(d, o.w_int + m)) nz.push_back(m);
-    auto fast_cond = "fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + D + ", I[" + D + "])";
+    const bool per = periodic_dim(d, tm.field, tm.dim);
+    const std::string cond = per ? "wrap_line_ok(P, " + F + ", " + D + ", " + std::to_string(reach_of(o)) + ")"
+                                 : "warp_all(fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + D +
+                                       ", I[" + D + "]))";
+    auto off = [&](int m) {
+        const int of = o.omin + m;
+        return per ? "(long long)wrap_off(I[" + D + "], " + std::to_string(of) + ", P.n[" + D + "]) * s"
+                   : "(long long)(" + std::to_string(of) + ") * s";
+    };
     e << "template <class T>\n__device__ __forceinline__ T gt" << K
       << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) {\n"
-      << "    if (" << fast_cond << ") {\n"
+      << "    if (" << cond << ") {\n"
       << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int;\n"
       << "        const T* __restrict__ b = u + (long long)" << F << " * P.ncell + c;\n"
       << "        const long long s = gstride(P, " << D << ");\n";
@@ -344,7 +363,7 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
     } else {
         for (size_t q = 0; q < nz.size(); ++q) {
             const int m = nz[q];
-            const std::string tap = "b[(long long)(" + std::to_string(o.omin + m) + ") * s]";
+            const std::string tap = "b[" + off(m) + "]";
             if (q == 0) e << "        T acc = w[" << m << "] * " << tap << ";\n";
             else e << "        acc = fma(w[" << m << "], " << tap << ", acc);\n";
         }
@@ -357,7 +376,7 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
     e << "template <class T>\n__device__ __forceinline__ void gt" << K
       << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
          "T g, T* lam_u, T* lp, T* lam_aux, T& own) {\n"
-      << "    if (" << fast_cond << ") {\n"
+      << "    if (" << cond << ") {\n"
       << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int;\n"
       << "        T* b = lam_u + (long long)" << F << " * P.ncell + c;\n"
       << "        const long long s = gstride(P, " << D << ");\n";
@@ -367,8 +386,12 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
             const bool z = std::find(nz.begin(), nz.end(), m) == nz.end();
             e << (m ? ", " : "") << (z ? std::string("T(0)") : "g * w[" + std::to_string(m) + "]");
         }
-        e << "};\n        scatter_taps<T, " << o.L << ", " << o.omin << ", " << (warp_scatter() ? "true" : "false")
-          << ">(b, c, s, vv, own);\n";
+        const char* W = warp_scatter() ? "true" : "false";
+        if (per)
+            e << "};\n        scatter_taps_wrap<T, " << o.L << ", " << o.omin << ", " << W << ">(b, c, I[" << D
+              << "], P.n[" << D << "], s, vv, own);\n";
+        else
+            e << "};\n        scatter_taps<T, " << o.L << ", " << o.omin << ", " << W << ">(b, c, s, vv, own);\n";
     }
     e << "        return;\n    }\n    scatter_op_line<T, " << D << ", " << max_taps(o) << ", " << DY << ">(P, P.ops["
       << tm.op << "], lam_u, " << F << ", I, c, I[" << D << "], P.n[" << D << "], g, t, p);\n}\n";
@@ -384,9 +407,13 @@ void emit_mixed(Emitter& e, const mol_problem_desc* d, int k) {
     for (int x = 0; x < o1.L; ++x)
         for (int y = 0; y < o2.L; ++y)
             if (!zero_w(d, o1.w_int + x) && !zero_w(d, o2.w_int + y)) nz.push_back({x, y});
-    const std::string cond = "fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + D1 + ", I[" + D1 +
-                             "]) && fast_line(P, P.ops[" + std::to_string(tm.op2) + "], " + F + ", " + D2 + ", I[" +
-                             D2 + "])";
+    // both dimensions periodic: wrapped offsets everywhere (uniform branch)
+    const bool per = periodic_dim(d, tm.field, tm.dim) && periodic_dim(d, tm.field, tm.dim2);
+    const std::string cond =
+        per ? "wrap_line_ok(P, " + F + ", " + D1 + ", " + std::to_string(reach_of(o1)) + ") && wrap_line_ok(P, " + F +
+                  ", " + D2 + ", " + std::to_string(reach_of(o2)) + ")"
+            : "warp_all(fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + D1 + ", I[" + D1 +
+                  "]) && fast_line(P, P.ops[" + std::to_string(tm.op2) + "], " + F + ", " + D2 + ", I[" + D2 + "]))";
     // the product weights sit in the pool at term.reserved0 (filled by the library), row-major [L1][L2]
     auto body = [&](bool vjp) {
         e << "    if (" << cond << ") {\n"
@@ -397,8 +424,11 @@ void emit_mixed(Emitter& e, const mol_problem_desc* d, int k) {
         for (size_t q = 0; q < nz.size(); ++q) {
             const int x = nz[q].first, y = nz[q].second;
             const std::string W = "ww[" + std::to_string(x * o2.L + y) + "]";
-            const std::string off = "(long long)(" + std::to_string(o1.omin + x) + ") * s1 + (long long)(" +
-                                    std::to_string(o2.omin + y) + ") * s2";
+            const std::string a1 = std::to_string(o1.omin + x), a2 = std::to_string(o2.omin + y);
+            const std::string off =
+                per ? "(long long)wrap_off(I[" + D1 + "], " + a1 + ", P.n[" + D1 + "]) * s1 + (long long)wrap_off(I[" + D2 +
+                          "], " + a2 + ", P.n[" + D2 + "]) * s2"
+                    : "(long long)(" + a1 + ") * s1 + (long long)(" + a2 + ") * s2";
             if (vjp) e << "        atomicAdd(b + " << off << ", g * " << W << ");\n";
             else if (q == 0) e << "        T acc = " << W << " * b[" << off << "];\n";
             else e << "        acc = fma(" << W << ", b[" << off << "], acc);\n";
@@ -423,7 +453,7 @@ void emit_mixed(Emitter& e, const mol_problem_desc* d, int k) {
 void emit_weno(Emitter& e, const mol_problem_desc* d, int k) {
     const mol_term& tm = d->terms[k];
     const std::string K = std::to_string(k), F = std::to_string(tm.field), D = std::to_string(tm.dim);
-    const std::string cond = "fast_weno(P, " + F + ", " + D + ", I[" + D + "])";
+    const std::string cond = "warp_all(fast_weno(P, " + F + ", " + D + ", I[" + D + "]))";
     const char* W = warp_scatter() ? "true" : "false";
     const std::string DY = dyn_bc(d, tm.field, tm.dim);
     const std::string sig = "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, "
@@ -551,6 +581,21 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
     }
     e << "}\n";
 
+    // Along a periodic dimension (this field and every interpolated one) all cells use the
+    // interior weights with wrapped tap offsets; face indices stay unwrapped as on the
+    // edge path.
+    bool per = periodic_dim(d, tm.field, tm.dim);
+    for (int f : used_fields) per = per && periodic_dim(d, f, tm.dim);
+    int reach = 0;
+    for (int m : nzo) {
+        const int r = oo.omin + m - 1;
+        for (int t_ : nzi) reach = std::max(reach, std::abs(r + oi.omin + t_));
+        for (int t_ : nzp) reach = std::max(reach, std::abs(r + op.omin + t_));
+    }
+    auto toff = [&](int x) {
+        return per ? "(long long)wrap_off(I[" + D + "], " + std::to_string(x) + ", P.n[" + D + "]) * s"
+                   : "(long long)(" + std::to_string(x) + ") * s";
+    };
     // fast path helpers: relative face offsets r = omin_outer + m - 1 (outer stencil sits at II - 1)
     auto fast_face = [&](int m, bool vjp) {
         const int r = oo.omin + m - 1;
@@ -559,7 +604,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
         // inner derivative
         for (size_t q = 0; q < nzi.size(); ++q) {
             const int t_ = nzi[q];
-            const std::string tap = "bF[(long long)(" + std::to_string(r + oi.omin + t_) + ") * s]";
+            const std::string tap = "bF[" + toff(r + oi.omin + t_) + "]";
             if (q == 0) e << "    T " << tag << "du = wi[" << t_ << "] * " << tap << ";\n";
             else e << "    " << tag << "du = fma(wi[" << t_ << "], " << tap << ", " << tag << "du);\n";
         }
@@ -568,8 +613,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
             e << "    const T* __restrict__ bf" << f << " = u + (long long)" << f << " * P.ncell + c;\n";
             for (size_t q = 0; q < nzp.size(); ++q) {
                 const int t_ = nzp[q];
-                const std::string tap = "bf" + std::to_string(f) + "[(long long)(" + std::to_string(r + op.omin + t_) +
-                                        ") * s]";
+                const std::string tap = "bf" + std::to_string(f) + "[" + toff(r + op.omin + t_) + "]";
                 if (q == 0) e << "    T " << tag << "uf" << f << " = wp[" << t_ << "] * " << tap << ";\n";
                 else e << "    " << tag << "uf" << f << " = fma(wp[" << t_ << "], " << tap << ", " << tag << "uf" << f
                        << ");\n";
@@ -592,7 +636,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
             e << "    const T " << tag << "g = g * wo[" << m << "];\n";
             e << "    { const T gd = " << tag << "g * " << tag << "a;\n";
             for (int t_ : nzi)
-                e << "      atomicAdd(lF + (long long)(" << (r + oi.omin + t_) << ") * s, gd * wi[" << t_ << "]);\n";
+                e << "      atomicAdd(lF + " << toff(r + oi.omin + t_) << ", gd * wi[" << t_ << "]);\n";
             e << "    }\n";
             if (has_prog) {
                 FaceLeaves L(tag);
@@ -600,8 +644,8 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
                 emit_reverse(e, fs, L, tag, [&](int) { return seed; });
                 for (int f : used_fields)
                     for (int t_ : nzp)
-                        e << "    atomicAdd(lam_u + (long long)" << f << " * P.ncell + c + (long long)("
-                          << (r + op.omin + t_) << ") * s, " << tag << "guf" << f << " * wp[" << t_ << "]);\n";
+                        e << "    atomicAdd(lam_u + (long long)" << f << " * P.ncell + c + " << toff(r + op.omin + t_)
+                          << ", " << tag << "guf" << f << " * wp[" << t_ << "]);\n";
                 for (int j : used_aux)
                     e << "    if (lam_aux) atomicAdd(lam_aux + " << tag << "fi" << j << ", " << tag << "gfa" << j
                       << ");\n";
@@ -609,8 +653,13 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
         }
         e << "    }\n";
     };
-    const std::string cond = "fast_nonlinlap(P, P.ops[" + opo + "], P.ops[" + opi + "], P.ops[" + opp + "], " + F +
-                             ", " + D + ", I[" + D + "])";
+    std::string cond = "warp_all(fast_nonlinlap(P, P.ops[" + opo + "], P.ops[" + opi + "], P.ops[" + opp + "], " + F +
+                       ", " + D + ", I[" + D + "]))";
+    if (per) {
+        cond = "wrap_line_ok(P, " + F + ", " + D + ", " + std::to_string(reach) + ")";
+        for (int f : used_fields)
+            if (f != tm.field) cond += " && wrap_line_ok(P, " + std::to_string(f) + ", " + D + ", " + std::to_string(reach) + ")";
+    }
     for (int vjp = 0; vjp < 2; ++vjp) {
         if (!vjp)
             e << "template <class T>\n__device__ __forceinline__ T gt" << K

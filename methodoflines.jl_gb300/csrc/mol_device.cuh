@@ -71,6 +71,27 @@ __device__ __forceinline__ int wrap_periodic(int i, int l) {
     return i <= 1 ? i + (l - 1) : (i > l ? i - (l - 1) : i);
 }
 
+// True when `p` holds on every lane converged here.  The generated terms branch on it:
+// FP64 instructions cost the same however few lanes are active, so a warp that straddles
+// an edge runs the edge path for all its lanes (it also gives interior cells their exact
+// result) instead of both paths one after the other.
+__device__ __forceinline__ bool warp_all(bool p) { return __all_sync(__activemask(), p); }
+
+// Offset, along a periodic line of n points, of the tap at i + off after the same single
+// wrap (the unknowns being points 2..n).  Valid while |off| <= n - 2.
+__device__ __forceinline__ int wrap_off(int i, int off, int n) {
+    const int q = i + off;
+    return q <= 1 ? off + (n - 1) : (q > n ? off - (n - 1) : off);
+}
+
+// True when dimension d of field f is periodic with unknowns 2..n and at least `reach`
+// points beyond every tap offset, so every cell can use interior weights with wrapped
+// offsets (the same for the whole grid: a uniform branch).
+template <class T>
+__device__ __forceinline__ bool wrap_line_ok(const DevProb<T>& P, int f, int d, int reach) {
+    return ((P.permask[f] >> d) & 1) && P.lo[d] == 1 && P.up[d] == 0 && P.n[d] - 2 >= reach;
+}
+
 template <class T>
 __device__ __forceinline__ long long flat_interior(const DevProb<T>& P, int i0, int i1, int i2) {
     return (long long)(i0 - 1 - P.lo[0]) +

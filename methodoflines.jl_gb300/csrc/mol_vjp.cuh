@@ -210,6 +210,26 @@ __device__ __forceinline__ void scatter_taps(T* base, long long c, long long s, 
     }
 }
 
+// scatter_taps on a periodic line: taps past either end wrap (wrap_off).  Warps with no
+// wrapping lane take the shuffle path of scatter_taps.
+template <class T, int L, int OMIN, bool WARP>
+__device__ __forceinline__ void scatter_taps_wrap(T* base, long long c, int i, int n, long long s, const T (&v)[L],
+                                                  T& own) {
+    const bool wraps = i + OMIN <= 1 || i + OMIN + L - 1 > n;
+    if (WARP && s == 1 && __activemask() == 0xffffffffu) {
+        if (!__any_sync(0xffffffffu, wraps)) {
+            scatter_taps<T, L, OMIN, true>(base, c, s, v, own);
+            return;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < L; ++m) {
+        const int off = OMIN + m;
+        if (off == 0) own += v[m];
+        else atomicAdd(base + (long long)wrap_off(i, off, n) * s, v[m]);
+    }
+}
+
 // d/du_k of weno5_point: reverse mode through the same formula.  In FP64 the sweep runs
 // through the one-division common-denominator form (one reciprocal of Dp*Dm serves the
 // whole gradient); FP32 keeps the reciprocal form.

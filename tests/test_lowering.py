@@ -186,7 +186,10 @@ def test_generated_code_compiles_for_sm103a(name, kw):
     buf = C.create_string_buffer(need.value)
     assert L.lib().mol_generate_code(C.byref(D.desc), buf, need.value, C.byref(need)) == 0
     src = buf.value.decode()
-    assert "gen_cell" in src and "fast_line" in src
+    assert "gen_cell" in src
+    # periodic dimensions use wrapped interior offsets, the others the interior fast path
+    assert "wrap_line_ok" in src
+    assert ("fast_nonlinlap" in src) == (name == "adr3d")  # z of the 3-D problem is Dirichlet
     log = C.create_string_buffer(1 << 16)
     st = L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16)
     assert st == 0, log.value.decode()
