@@ -10,8 +10,8 @@ L2, so L2 is flushed (a 256 MB write) between timed steps, outside the timed eve
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--full]
 
 `--impl reference` times the CPU restatement of the reference's discretisation
-(numpy, the oracle) on the same workload; the reference itself is Julia and cannot
-run on this machine.  `--full` adds the long runs of every configuration.
+(C/OpenMP, oracle/c, on every host core) on the same workload; the reference itself
+is Julia and cannot run on this machine.  `--full` adds the long runs of every configuration.
 """
 from __future__ import annotations
 
@@ -249,25 +249,32 @@ def run_ours(args, rank, world):
 
 
 def cpu_baseline(lw, ex, samples=1):
-    """The oracle (numpy restatement of the reference discretisation) on the host, one full
-    SSPRK33 step of the same 1024x1024 system per sample."""
-    import numpy as np
-    from molgpu import problems
-    from oracle.integrators import ssprk33
-    from oracle.mol_oracle import OracleProblem
-    sys_, disc, _ = problems.brusselator(N=HEADLINE_N)
-    orc = OracleProblem(sys_.to_spec(disc))
-    u0 = orc.initial_condition()
+    """The C/OpenMP restatement of the reference discretisation and SSPRK33 (oracle/c) on the
+    host cores: SSPRK33 steps of the same 1024x1024 system, in chunks of 10 steps until at
+    least 10 s have passed, on every core, then 10 steps on one core."""
+    from oracle.c_port import Brusselator, max_threads
+    b = Brusselator(lw)
+    dt = ex["dt_ssprk"]
+    u = b.ssprk33(lw.u0, 0.0, dt, 1)      # warm (pages, threads)
+    steps, el = 0, 0.0
+    while el < 10.0 and steps < 4000:
+        t0 = time.perf_counter()
+        u = b.ssprk33(u, steps * dt, dt, 10)
+        el += time.perf_counter() - t0
+        steps += 10
+    cores = max_threads()
     t0 = time.perf_counter()
-    ssprk33(lambda v, t: orc.rhs(v, t), u0, 0.0, ex["dt_ssprk"], samples)
-    el = time.perf_counter() - t0
-    return {"value": orc.n_unknowns * samples / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{samples} full SSPRK33 step(s) of the 1024x1024 Brusselator (2,097,152 unknowns), "
-                      "numpy oracle, single thread"}
+    b.ssprk33(lw.u0, 0.0, dt, 10, 1)
+    one = lw.n_unknowns * 10 / (time.perf_counter() - t0) / 1e6
+    return {"value": lw.n_unknowns * steps / el / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} SSPRK33 steps of the 1024x1024 Brusselator (2,097,152 unknowns) in "
+                      f"{el:.1f} s, C/OpenMP restatement of the reference discretisation on {cores} "
+                      f"threads; one thread: {one:.1f} Mcell-updates/s"}
 
 
 # ---------------------------------------------------------------------------------------
-# secondary workloads (every configuration; short runs unless --full)
+# secondary workloads (every configuration at its size; the ensemble runs 1000 steps and
+# Tsit5 a longer horizon with --full)
 # ---------------------------------------------------------------------------------------
 
 def _time(fn, stream, reps, warm=True):
@@ -334,13 +341,13 @@ def workloads(args, dev, stream):
                                                 "naccept": st["naccept"], "nreject": st["nreject"]}
         plan.close()
 
-    # config 3: Burgers WENO5, SSPRK33 (20000 steps with --full) and the discrete adjoint
+    # config 3: Burgers WENO5, SSPRK33 for 20000 steps and the discrete adjoint
     sys_, disc, ex = problems.burgers()
     lw = lower(sys_.to_spec(disc))
     plan = Plan(lw)
     plan.set_stream(stream.cuda_stream)
     n = lw.n_unknowns
-    nsteps = 20000 if full else 2000
+    nsteps = 20000
     ud = torch.tensor(lw.u0, device=dev)
     plan.step_ssprk33(ud, ex["dt"], 32)
     torch.cuda.synchronize()
@@ -369,9 +376,9 @@ def workloads(args, dev, stream):
                                   "loss": loss, "dLdnu": float(gp.item())}
     plan.close()
 
-    # config 5: 3-D ADR at 256^3 (RHS, SSPRK33; adjoint dL/dK over a short horizon unless --full)
+    # config 5: 3-D ADR at 256^3 (RHS, SSPRK33, adjoint dL/dK over 500 steps)
     t0 = time.perf_counter()
-    sys_, disc, ex = problems.adr3d(N=256 if full or args.adr256 else 128, nz_pts=258 if full or args.adr256 else 130)
+    sys_, disc, ex = problems.adr3d(N=256, nz_pts=258)
     lw = lower(sys_.to_spec(disc))
     setup = time.perf_counter() - t0
     plan = Plan(lw)
@@ -384,7 +391,7 @@ def workloads(args, dev, stream):
     u32 = torch.tensor(lw.u0, device=dev, dtype=torch.float32)
     du32 = torch.zeros_like(u32)
     ms32 = _time(lambda: plan.rhs(du32, u32, None, 0.1), stream, 5)
-    adj_steps = 500 if full else 20
+    adj_steps = 500
     tgt = torch.tensor(np.random.default_rng(12).standard_normal(n) * 1e-3, device=dev)
     u0d = torch.tensor(lw.u0, device=dev)
     gaux = torch.zeros(sum(a.size for a in lw.aux), dtype=torch.float64, device=dev)
@@ -392,17 +399,25 @@ def workloads(args, dev, stream):
     plan.adjoint_ssprk33(u0d, ex["dt"], 2, tgt, nsnap=2, dLdaux=gaux)   # warm: compiles the VJP
     torch.cuda.synchronize()
     ta = time.perf_counter()
-    plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=64, dLdaux=gaux)
+    _, nfw64 = plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=64, dLdaux=gaux)
     torch.cuda.synchronize()
     adj_s = time.perf_counter() - ta
+    ta = time.perf_counter()
+    _, nfw0 = plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=0, dLdaux=gaux)
+    torch.cuda.synchronize()
+    adj_all_s = time.perf_counter() - ta
     side = round(n ** (1 / 3))
     res[f"adr3d_{side}^3"] = {"unknowns": n, "setup_s": setup, "rhs_ms": ms, "rhs_Mcell_s": n / ms / 1e3,
                               "rhs_hbm_frac": (16 + 24) * n / (ms * 1e-3) / 1e9 / hbm_peak,
                               "ssprk33_ms_per_step": ms_step, "ssprk33_Mcell_s": n / ms_step / 1e3,
                               "f32state_rhs_ms": ms32,
                               "f32state_rhs_hbm_frac": (8 + 12) * n / (ms32 * 1e-3) / 1e9 / hbm_peak,
-                              "adjoint_steps": adj_steps, "adjoint_dLdK_s": adj_s,
-                              "adjoint_vs_forward": adj_s / (fwd * 1e-3)}
+                              "adjoint_steps": adj_steps, "adjoint_dLdK_64_snapshots_s": adj_s,
+                              "adjoint_64_snapshots_vs_forward": adj_s / (fwd * 1e-3),
+                              "adjoint_64_snapshots_forward_steps": nfw64,
+                              "adjoint_dLdK_states_kept_s": adj_all_s,
+                              "adjoint_states_kept_vs_forward": adj_all_s / (fwd * 1e-3),
+                              "adjoint_states_kept_forward_steps": nfw0}
     plan.close()
 
     # config 4: batched ensemble of uneven nonlinear-diffusion problems vs sequential plain solves
@@ -414,7 +429,7 @@ def batched(args, dev, stream):
     import numpy as np
     import torch
     from molgpu import Batch, Plan, lower, problems
-    count = 4096 if (args.full or args.batch4096) else 512
+    count = 4096
     members = problems.ensemble_members(4096)[:count]
     t0 = time.perf_counter()
     lws, dts = [], []
@@ -429,7 +444,7 @@ def batched(args, dev, stream):
     batch.set_stream(stream.cuda_stream)
     setup = time.perf_counter() - t0
     total = int(batch.offsets[-1])
-    steps = 1000 if args.full else 10
+    steps = 1000 if args.full else 20
     u = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev)
     batch.step_ssprk33(u, dts, 2)          # autotune + warm
     torch.cuda.synchronize()
@@ -467,39 +482,114 @@ def batched(args, dev, stream):
 
 
 # ---------------------------------------------------------------------------------------
-# reference arm: the reference's discretisation on the host (numpy oracle)
+# reference arm: the reference's discretisation on the host (C/OpenMP restatement)
 # ---------------------------------------------------------------------------------------
 
 def run_reference(args, rank, world):
+    """The reference's CPU path for the headline workload: the reference itself is Julia and
+    cannot run on this machine, so its discretisation and SSPRK33 are timed through the
+    C/OpenMP restatement (oracle/c) on every host core, K steps after W warm-up steps."""
     if rank != 0:
         return None
-    import numpy as np
-    from molgpu import problems
-    from oracle.integrators import ssprk33
-    from oracle.mol_oracle import OracleProblem
+    from molgpu import lower, problems
+    from oracle.c_port import Brusselator, max_threads
     sys_, disc, ex = problems.brusselator(N=HEADLINE_N)
-    orc = OracleProblem(sys_.to_spec(disc))
-    u = orc.initial_condition()
+    lw = lower(sys_.to_spec(disc))
+    b = Brusselator(lw)
     dt = ex["dt_ssprk"]
-    w = max(0, min(args.warmup, 1))
-    for _ in range(w):
-        u, _ = ssprk33(lambda v, t: orc.rhs(v, t), u, 0.0, dt, 1)
-    reps = max(1, min(args.steps, 20))
+    w = max(0, args.warmup)
+    u = b.ssprk33(lw.u0, 0.0, dt, w) if w else lw.u0.copy()
+    reps = max(1, args.steps)
     t0 = time.perf_counter()
-    t = 0.0
-    for _ in range(reps):
-        u, t = ssprk33(lambda v, tt: orc.rhs(v, tt), u, t, dt, 1)
+    b.ssprk33(u, w * dt, dt, reps)
     el = time.perf_counter() - t0
-    value = orc.n_unknowns * reps / el / 1e6
-    sample = (f"{reps} full SSPRK33 step(s) of the 1024x1024 Brusselator (2,097,152 unknowns) per run; "
-              "numpy restatement of the reference discretisation (the reference is Julia and is not "
-              "runnable here)")
+    value = lw.n_unknowns * reps / el / 1e6
+    cores = max_threads()
+    sample = (f"{reps} SSPRK33 steps of the 1024x1024 Brusselator (2,097,152 unknowns) after {w} warm-up "
+              f"steps; C/OpenMP restatement of the reference discretisation on {cores} threads (the "
+              "reference is Julia and is not runnable here)")
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": reps, "warmup": w,
             "ms_per_step": el / reps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": "brusselator2d_1024x1024_periodic_ssprk33_step"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ---------------------------------------------------------------------------------------
+# small single-path cases, the commands the ncu summaries under profiles/ were taken with
+
+def run_case(name, args):
+    import numpy as np
+    import torch
+    from molgpu import Batch, Plan, lower, problems
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    out = {"case": name}
+    if name == "burgers_adjoint":
+        # Burgers WENO5 (65,536 unknowns): 30-step adjoint, every state and stage kept
+        sys_, disc, ex = problems.burgers()
+        lw = lower(sys_.to_spec(disc))
+        plan = Plan(lw)
+        plan.set_stream(stream.cuda_stream)
+        u0 = torch.tensor(lw.u0, device=dev)
+        tgt = torch.tensor(ex["target"], device=dev)
+        g = torch.zeros_like(u0)
+        gp = torch.zeros(1, dtype=torch.float64, device=dev)
+        for _ in range(2):
+            loss, nfw = plan.adjoint_ssprk33(u0, ex["dt"], 30, tgt, nsnap=0, dLdu0=g, dLdp=gp)
+        torch.cuda.synchronize()
+        out.update(loss=loss, dLdnu=float(gp.item()))
+        plan.close()
+    elif name == "ensemble":
+        # the first 512 ensemble members, 5 steps of the tiled persistent kernel
+        lws, dts = [], []
+        for (n, k, seed) in problems.ensemble_members(4096)[:512]:
+            sys_, disc, _ = problems.nonlinear_diffusion(n, k, seed)
+            lw = lower(sys_.to_spec(disc))
+            lws.append(lw)
+            dts.append(0.125 / (n - 1) ** 2 / float(np.max(lw.u0)) ** 2)
+        batch = Batch(lws)
+        batch.set_stream(stream.cuda_stream)
+        batch.tune(128, 4, 512)
+        u = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev)
+        for _ in range(3):
+            batch.step_ssprk33(u, np.array(dts), 5)
+        batch.check()
+        out.update(unknowns=int(batch.offsets[-1]), norm=float(torch.linalg.norm(u)))
+        batch.close()
+    elif name in ("brusselator_rhs_generated", "brusselator_rhs_interpreted"):
+        # one RHS of the 1024^2 Brusselator through the generated cell or the interpreter
+        if name.endswith("interpreted"):
+            os.environ["MOL_DISABLE_CODEGEN"] = "1"
+        sys_, disc, _ = problems.brusselator(N=1024)
+        lw = lower(sys_.to_spec(disc))
+        plan = Plan(lw)
+        plan.set_stream(stream.cuda_stream)
+        u = torch.tensor(lw.u0, device=dev)
+        du = torch.zeros_like(u)
+        for _ in range(5):
+            plan.rhs(du, u, None, 0.5)
+        torch.cuda.synchronize()
+        out.update(codegen=plan.uses_codegen, norm=float(torch.linalg.norm(du)))
+        plan.close()
+    elif name == "adr3d_rhs":
+        # one RHS of the 3-D ADR problem at 128^3
+        sys_, disc, _ = problems.adr3d(N=128, nz_pts=130)
+        lw = lower(sys_.to_spec(disc))
+        plan = Plan(lw)
+        plan.set_stream(stream.cuda_stream)
+        u = torch.tensor(lw.u0, device=dev)
+        du = torch.zeros_like(u)
+        for _ in range(5):
+            plan.rhs(du, u, None, 0.1)
+        torch.cuda.synchronize()
+        out.update(norm=float(torch.linalg.norm(du)))
+        plan.close()
+    else:
+        raise SystemExit(f"unknown case {name}")
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -509,11 +599,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--full", action="store_true", help="long runs of every configuration")
-    ap.add_argument("--adr256", action="store_true", help="3-D ADR at 256^3 in the secondary workloads")
-    ap.add_argument("--batch4096", action="store_true", help="all 4096 ensemble members")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default=None,
+                    choices=["burgers_adjoint", "ensemble", "brusselator_rhs_generated",
+                             "brusselator_rhs_interpreted", "adr3d_rhs"],
+                    help="run one small single-path case (for profiling) and exit")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case, args)
+        return
     rank, world = _dist()
     if args.impl == "reference":
         out = run_reference(args, rank, world)

@@ -185,7 +185,7 @@ struct Adj {
         counted();
     }
 
-    // Reverse step m, the state u_m being in `um`.
+    // Reverse step m, the state u_m being in `um`: its stage values are recomputed.
     void reverse_step(const double* um, int64_t m) {
         if (err) return;
         const double tm = time_of(m);
@@ -195,9 +195,18 @@ struct Adj {
         if (!have_lam) {
             // last step: u_N and dL/du_N
             stage(3, u2, um, tmp, tm);
-            if (uT_dev) ck(cudaMemcpyAsync(uT_dev, tmp, sizeof(double) * n, cudaMemcpyDeviceToDevice, plan->stream), "uT");
+            start_lambda(tmp);
+        }
+        reverse_vjps(um, u1, u2, tm);
+    }
+
+    // u_N is in uN: the loss, and dL/du_N into lam.
+    void start_lambda(const double* uN) {
+        if (err) return;
+        {
+            if (uT_dev) ck(cudaMemcpyAsync(uT_dev, uN, sizeof(double) * n, cudaMemcpyDeviceToDevice, plan->stream), "uT");
             if (loss_kind == MOL_LOSS_MISFIT) {
-                k_misfit<<<nb, kThreads, 0, plan->stream>>>(n, tmp, target, lam, plan->d_partials);
+                k_misfit<<<nb, kThreads, 0, plan->stream>>>(n, uN, target, lam, plan->d_partials);
                 ++g_launches;
                 cap_end();  // the loss is read on the host here
                 std::vector<double> hp(nb);
@@ -212,6 +221,11 @@ struct Adj {
             }
             have_lam = true;
         }
+    }
+
+    // The three VJP launches of reverse step m given u_m and its stage values u1, u2.
+    void reverse_vjps(const double* um, const double* su1, const double* su2, double tm) {
+        if (err) return;
         double* Cold = cbuf[cur];
         double* Cnew = cbuf[cur ^ 1];
         cur ^= 1;
@@ -222,17 +236,33 @@ struct Adj {
         s2.a[0] = s2.a[1] = s2.a[2] = s2.a[3] = 1.0;
         s2.upd = lam;
         s2.zero[0] = Cold; s2.zero[1] = a1; s2.zero[2] = a0;
-        vjp(s2, 2.0 * dt / 3.0, u2, tm + dt / 2, Cnew);
+        vjp(s2, 2.0 * dt / 3.0, su2, tm + dt / 2, Cnew);
         // A1 = dt/4 J(u1)^T l2,  l2 = 2/3 lam + C
         VjpSeed<double> s1 = {};
         s1.x[0] = lam; s1.x[1] = Cnew;
         s1.a[0] = 2.0 / 3.0; s1.a[1] = 1.0;
-        vjp(s1, dt / 4.0, u1, tm + dt, a1);
+        vjp(s1, dt / 4.0, su1, tm + dt, a1);
         // A0 = dt J(u)^T l1,  l1 = 1/6 lam + 1/4 C + A1
         VjpSeed<double> s0 = {};
         s0.x[0] = lam; s0.x[1] = Cnew; s0.x[2] = a1;
         s0.a[0] = 1.0 / 6.0; s0.a[1] = 0.25; s0.a[2] = 1.0;
         vjp(s0, dt, um, tm, a0);
+    }
+
+    // Everything kept: states S[0..N] and the stage values U1[m], U2[m] of every step, so
+    // the reverse sweep is the three VJP launches per step and nothing is recomputed
+    // (the GB300's HBM holds tens of thousands of states of a mid-size grid).
+    void stored_sweep(double* const* S, double* const* U1, double* const* U2) {
+        for (int64_t m = 0; m < N && !err; ++m) {
+            const double tm = time_of(m);
+            stage(1, S[m], S[m], U1[m], tm);
+            stage(2, U1[m], S[m], U2[m], tm);
+            stage(3, U2[m], S[m], S[m + 1], tm);
+        }
+        fwd_steps += N;
+        cap_end();
+        start_lambda(S[N]);
+        for (int64_t m = N - 1; m >= 0 && !err; --m) reverse_vjps(S[m], U1[m], U2[m], time_of(m));
     }
 
     // dL/du_0 = lam + C + A1 + A0 of the last reverse step, into lam.
@@ -412,11 +442,15 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
         cudaStreamSynchronize(plan->stream);
         for (void* q : mine) cudaFree(q);
     };
-    // checkpoint slots: nsnap <= 0 stores every step that fits in half of the free memory
+    // checkpoint slots.  nsnap <= 0: keep every state and both stage values of every step
+    // when they fit in half of the free memory (no recomputation at all), else as many
+    // states as fit (binomial schedule over them).
     int64_t slots = nsnap;
+    bool keep_stages = false;
     if (slots <= 0) {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
+        keep_stages = nsteps > 0 && (3.0 * nsteps + 1.0) * 8.0 * n <= 0.5 * fr;
         slots = (int64_t)std::max<double>(2.0, std::min<double>((double)nsteps + 1, 0.5 * fr / (8.0 * n)));
     }
     slots = std::max<int64_t>(1, std::min<int64_t>(slots, nsteps + 1));
@@ -432,7 +466,20 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
         const char* g = getenv("MOL_ADJOINT_GRAPHS");
         A.graphs = plan->stream != nullptr && plan->stream != cudaStreamLegacy && !(g && g[0] == '0');
     }
-    for (int64_t i = 0; i < slots; ++i) {
+    std::vector<double*> S1, S2;
+    if (keep_stages) {
+        double* all = get((size_t)(3 * nsteps + 1) * (size_t)n);
+        if (!all) {
+            keep_stages = false;
+        } else {
+            for (int64_t i = 0; i <= nsteps; ++i) A.slots.push_back(all + (size_t)i * n);
+            for (int64_t i = 0; i < nsteps; ++i) {
+                S1.push_back(all + (size_t)(nsteps + 1 + i) * n);
+                S2.push_back(all + (size_t)(2 * nsteps + 1 + i) * n);
+            }
+        }
+    }
+    for (int64_t i = 0; !keep_stages && i < slots; ++i) {
         double* q = get(n);
         if (!q) {
             release();
@@ -495,8 +542,12 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
         }
         if (A.uT_dev) cudaMemcpyAsync(A.uT_dev, A.slots[0], sizeof(double) * n, cudaMemcpyDeviceToDevice, plan->stream);
     } else {
-        std::vector<double*> free(A.slots.begin() + 1, A.slots.end());
-        A.rev(0, nsteps, A.slots[0], free);
+        if (keep_stages) {
+            A.stored_sweep(A.slots.data(), S1.data(), S2.data());
+        } else {
+            std::vector<double*> free(A.slots.begin() + 1, A.slots.end());
+            A.rev(0, nsteps, A.slots[0], free);
+        }
         A.finish();
     }
     A.cap_end();
