@@ -387,6 +387,7 @@ int mol_rhs_vjp(mol_plan* plan, const double* lambda, const double* u, const dou
     int pst = 0;
     const double* pp = p ? (is_device_ptr(p) ? p : nullptr) : (const double*)plan->a64.params;
     if (p && !pp) {
+        plan->a64.params_known = false;
         pst = cuda_check(plan, cudaMemcpyAsync(plan->a64.params, p, sizeof(double) * plan->nparams,
                                                cudaMemcpyHostToDevice, plan->stream), "params");
         if (pst) return pst;

@@ -44,6 +44,19 @@ bool is_device_ptr(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Device-accessible address of pinned (page-locked, registered or cudaHostAlloc'd) host
+// memory, or nullptr for anything else.  On GB300 the GPU reads and writes such memory
+// coherently over NVLink-C2C.
+void* mapped_host_ptr(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int plan_alloc(mol_plan* plan, void** ptr, size_t bytes) {
     *ptr = nullptr;
     if (bytes == 0) bytes = 16;
@@ -258,7 +271,16 @@ template int launch_rhs<float>(mol_plan*, float*, const float*, const float*, do
 
 template <class T>
 int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt) {
+    return launch_ssprk_step_io<T>(plan, u, u, u1, u2, p, dt);
+}
+template int launch_ssprk_step<double>(mol_plan*, double*, double*, double*, const double*, double);
+template int launch_ssprk_step<float>(mol_plan*, float*, float*, float*, const float*, double);
+
+// One SSPRK33 step from uin to uout (which may be the same array).
+template <class T>
+int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, const T* p, double dt) {
     const DevProb<T>& P = prob<T>(plan);
+    const T* u = uin;
     g_launches += 3;
     if (plan->use_jit) {
         const bool is64 = std::is_same<T, double>::value;
@@ -273,17 +295,17 @@ int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt)
         if (e == cudaSuccess)
             e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, P, cu1, cu, u2, p, plan->d_state, dt, nan);
         if (e == cudaSuccess)
-            e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, P, cu2, cu, u, p, plan->d_state, dt, nan);
+            e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, P, cu2, cu, uout, p, plan->d_state, dt, nan);
         return cuda_check(plan, e, "ssprk launch");
     }
     const double nan = std::nan("");
     k_ssprk_t<T, InterpCell, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt, nan);
     k_ssprk_t<T, InterpCell, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt, nan);
-    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, u, p, plan->d_state, dt, nan);
+    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, uout, p, plan->d_state, dt, nan);
     return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
 }
-template int launch_ssprk_step<double>(mol_plan*, double*, double*, double*, const double*, double);
-template int launch_ssprk_step<float>(mol_plan*, float*, float*, float*, const float*, double);
+template int launch_ssprk_step_io<double>(mol_plan*, const double*, double*, double*, double*, const double*, double);
+template int launch_ssprk_step_io<float>(mol_plan*, const float*, float*, float*, float*, const float*, double);
 
 }  // namespace mol
 
@@ -498,6 +520,9 @@ static int build_prec(mol_plan* plan, const mol_problem_desc* d, PlanArrays& A, 
     if ((st = cuda_check(plan, cudaMemcpy(A.bc, bc.data(), sizeof(DevBC<T>) * bc.size(), cudaMemcpyHostToDevice), "bc")))
         return st;
     if ((st = upload<T>(plan, &A.params, d->params, d->nparams))) return st;
+    A.params_host.assign(d->nparams, 0.0);
+    for (int i = 0; i < d->nparams; ++i) A.params_host[i] = (double)(T)d->params[i];
+    A.params_known = true;
     P.ndim = d->ndim;
     P.nfields = d->nfields;
     P.nparams = d->nparams;
@@ -798,8 +823,14 @@ const T* params_ptr(mol_plan* plan, const T* p, int* st) {
     PlanArrays& A = std::is_same<T, double>::value ? plan->a64 : plan->a32;
     if (!p) return (const T*)A.params;
     if (is_device_ptr(p)) return p;
-    *st = cuda_check(plan, cudaMemcpyAsync(A.params, p, sizeof(T) * (size_t)std::max(plan->nparams, 0),
-                                           cudaMemcpyHostToDevice, plan->stream), "params H2D");
+    const int np = std::max(plan->nparams, 0);
+    bool same = A.params_known && (int)A.params_host.size() == np;
+    for (int i = 0; same && i < np; ++i) same = (double)p[i] == A.params_host[i];
+    if (same) return (const T*)A.params;
+    *st = cuda_check(plan, cudaMemcpyAsync(A.params, p, sizeof(T) * (size_t)np, cudaMemcpyHostToDevice, plan->stream),
+                     "params H2D");
+    A.params_host.assign(p, p + np);
+    A.params_known = !*st;
     return (const T*)A.params;
 }
 
@@ -847,6 +878,15 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     Staged<T> su;
     const bool host = !is_device_ptr(u);
     T* ud = host ? ws[0] : u;
+    // Pinned host state: the last stage writes the result straight into it over the coherent
+    // host link instead of a bulk copy after the steps (stores do not stall the SMs, so the
+    // write-back hides under the FP64-bound stage; reading the input that way measured slower
+    // than the bulk copy, whose loads would stall).  MOL_ZERO_COPY=0 keeps both copies.
+    T* hz = nullptr;
+    if (host && nsteps > 0) {
+        const char* zc = getenv("MOL_ZERO_COPY");
+        if (!(zc && zc[0] == '0')) hz = (T*)mapped_host_ptr(u);
+    }
     if (host && (st = cuda_check(plan, cudaMemcpyAsync(ud, u, sizeof(T) * (size_t)plan->nunk, cudaMemcpyHostToDevice,
                                                        plan->stream), "H2D")))
         return st;
@@ -860,6 +900,7 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     ++g_launches;
     T* u1 = ws[1];
     T* u2 = ws[2];
+    const int64_t nmid = hz ? nsteps - 1 : nsteps;  // steps that stay in the device buffer ud
     // chunks of `chunk` steps replayed as one CUDA graph; the tail is launched directly
     const int chunk = plan->g_chunk;
     const bool is64 = std::is_same<T, double>::value;
@@ -870,7 +911,7 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     int64_t done = 0;
     // the legacy default stream cannot be captured: launch directly there
     const bool can_capture = plan->stream != nullptr && plan->stream != cudaStreamLegacy;
-    if (nsteps >= chunk && can_capture) {
+    if (nmid >= chunk && can_capture) {
         // the state buffer, parameter pointer and dt are baked into the captured graph
         if (gx && (gdt != dt || gp != (const void*)ud || gpp != (const void*)pp)) {
             cudaGraphExecDestroy(gx);
@@ -892,13 +933,17 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
             gp = (const void*)ud;
             gpp = (const void*)pp;
         }
-        for (; done + chunk <= nsteps; done += chunk) {
+        for (; done + chunk <= nmid; done += chunk) {
             if ((st = cuda_check(plan, cudaGraphLaunch(gx, plan->stream), "graph launch"))) return st;
             g_launches += 3 * chunk;
         }
     }
-    for (; done < nsteps; ++done)
+    for (; done < nmid; ++done)
         if ((st = launch_ssprk_step<T>(plan, ud, u1, u2, pp, dt))) return st;
+    if (hz) {
+        if ((st = launch_ssprk_step_io<T>(plan, ud, hz, u1, u2, pp, dt))) return st;
+        return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+    }
     if (host) {
         if ((st = cuda_check(plan, cudaMemcpyAsync(u, ud, sizeof(T) * (size_t)plan->nunk, cudaMemcpyDeviceToHost,
                                                    plan->stream), "D2H")))

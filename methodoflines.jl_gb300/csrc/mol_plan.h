@@ -23,6 +23,10 @@ struct PlanArrays {
     void* coords[3] = {nullptr, nullptr, nullptr};
     void* bc = nullptr;
     void* params = nullptr;
+    // host copy of what `params` holds (valid when params_known), so a call passing the
+    // same host parameters again skips the upload
+    std::vector<double> params_host;
+    bool params_known = false;
 };
 
 struct mol_plan_impl;
@@ -110,5 +114,8 @@ template <class T>
 int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t);
 template <class T>
 int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt);
+template <class T>
+int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, const T* p, double dt);
+void* mapped_host_ptr(const void* p);
 
 }  // namespace mol

@@ -65,6 +65,11 @@ def test_rhs_parameters_runtime(gpu_lib):
     du = np.zeros(lw.n_unknowns)
     plan.rhs(du, u, p, 0.2)
     assert _rel(du, orc.rhs(u, 0.2, p)) < RHS_TOL
+    # the plan skips re-uploading unchanged host parameters: alternate values must all land
+    for val in (3.5, 7.25, 7.25, 3.5, None):
+        plan.rhs(du, u, None if val is None else np.array([val]), 0.2)
+        ref = orc.rhs(u, 0.2, np.array([3.5 if val is None else val]))
+        assert _rel(du, ref) < RHS_TOL, val
 
 
 TRAJ = [
@@ -184,3 +189,29 @@ def test_generated_rhs_matches_interpreter(gpu_lib, name, kw, monkeypatch):
     gen.step_ssprk33(x, dt, 20)
     interp.step_ssprk33(y, dt, 20)
     assert _rel(x, y) < 1e-12
+
+
+@pytest.mark.parametrize("nsteps", [1, 2, 5, 40])
+def test_pinned_host_state_zero_copy(gpu_lib, monkeypatch, nsteps):
+    """The last stage writes a pinned host state's result straight over the host link (no
+    bulk copy back); the result equals stepping a device array, and equals the copy path
+    (MOL_ZERO_COPY=0), bit for bit."""
+    torch = pytest.importorskip("torch")
+    sys_, disc, ex = problems.brusselator(N=48)
+    lw = lower(sys_.to_spec(disc))
+    plan = Plan(lw)
+    st = torch.cuda.Stream()
+    plan.set_stream(st.cuda_stream)
+    dt = ex["dt_ssprk"]
+    dev = torch.tensor(lw.u0, device="cuda")
+    plan.step_ssprk33(dev, dt, nsteps, t0=1.05)
+    st.synchronize()
+    ref = dev.cpu().numpy()
+    for zc in ("1", "0"):
+        monkeypatch.setenv("MOL_ZERO_COPY", zc)
+        pinned = torch.empty(lw.n_unknowns, dtype=torch.float64, pin_memory=True)
+        pinned.copy_(torch.from_numpy(lw.u0))
+        hnp = pinned.numpy()
+        plan.step_ssprk33(hnp, dt, nsteps, t0=1.05)
+        assert np.array_equal(hnp, ref), (zc, nsteps)
+    plan.close()
