@@ -46,6 +46,8 @@ struct mol_batch {
     unsigned long long* d_sync = nullptr;
     long long* d_tile_pre = nullptr;
     int tile_cells_uploaded = 0;
+    long long tiles_total = 0;               // tiles of one round at the uploaded tile size
+    unsigned long long inject_ticket = 0;     // host value for the injected first ticket
     const double** d_par64 = nullptr;
     const float** d_par32 = nullptr;
     double* s64[3] = {nullptr, nullptr, nullptr};  // state (staging), u1, u2
@@ -94,7 +96,10 @@ int upload_tiles(mol_batch* b, int tile_cells) {
     int st = bcheck(b, cudaMemcpyAsync(b->d_tile_pre, pre.data(), sizeof(long long) * (b->n + 1),
                                        cudaMemcpyHostToDevice, b->stream), "tile table");
     if (!st) st = bcheck(b, cudaStreamSynchronize(b->stream), "tile table");
-    if (!st) b->tile_cells_uploaded = tile_cells;
+    if (!st) {
+        b->tile_cells_uploaded = tile_cells;
+        b->tiles_total = pre[b->n];
+    }
     return st;
 }
 
@@ -118,11 +123,22 @@ int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, 
     sync.ticket = b->d_sync;
     sync.status = (int*)(b->d_sync + 1);
     sync.done = b->d_sync + 2;
+    sync.spin_limit = MOL_BATCH_SPIN_LIMIT;
+    // Host-side injection of a dependency that is never met, for tests of the bounded waits:
+    // MOL_BATCH_INJECT_SKIP_ROUND=1 starts the ticket after round 0, so every tile of round 1
+    // waits for round-0 tiles that no CTA will run; MOL_BATCH_SPIN_LIMIT shortens the budget.
+    unsigned long long first_ticket = 0;
+    if (const char* lim = getenv("MOL_BATCH_SPIN_LIMIT"))
+        if (atoll(lim) > 0) sync.spin_limit = atoll(lim);
+    if (tiled && getenv("MOL_BATCH_INJECT_SKIP_ROUND") && getenv("MOL_BATCH_INJECT_SKIP_ROUND")[0] == '1')
+        first_ticket = (unsigned long long)b->tiles_total;
     const size_t sync_bytes = sizeof(unsigned long long) * (2 + (size_t)b->n);
     auto enqueue = [&]() -> cudaError_t {
         if (tiled) {
             // the status word survives replays so a failed run stays visible to mol_batch_check
-            cudaError_t e = cudaMemsetAsync(b->d_sync, 0, sizeof(unsigned long long), b->stream);
+            cudaError_t e = first_ticket ? cudaMemcpyAsync(b->d_sync, &b->inject_ticket, sizeof(unsigned long long),
+                                                           cudaMemcpyHostToDevice, b->stream)
+                                         : cudaMemsetAsync(b->d_sync, 0, sizeof(unsigned long long), b->stream);
             if (e == cudaSuccess)
                 e = cudaMemsetAsync(b->d_sync + 2, 0, sync_bytes - 2 * sizeof(unsigned long long), b->stream);
             if (e != cudaSuccess) return e;
@@ -138,7 +154,9 @@ int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, 
     const bool key_ok = b->graph && b->g_key[0] == (const void*)U && b->g_key[1] == (const void*)k &&
                         b->g_steps == nsteps && b->g_t0 == t0 && b->g_cfg[0] == threads && b->g_cfg[1] == ctas &&
                         b->g_cfg[2] == tile_cells;
-    const bool can_capture = b->stream != nullptr && b->stream != cudaStreamLegacy;
+    b->inject_ticket = first_ticket;
+    const bool can_capture = b->stream != nullptr && b->stream != cudaStreamLegacy && !first_ticket &&
+                             sync.spin_limit == MOL_BATCH_SPIN_LIMIT;
     if (!key_ok && can_capture) {
         if (b->graph) {
             cudaGraphExecDestroy(b->graph);

@@ -1130,6 +1130,18 @@ std::vector<std::string> jit_options(int min_blocks) {
     o.push_back("-DMOL_MIN_BLOCKS=" + std::to_string(minb));
     // MOL_JIT_VERBOSE=1: ptxas resource report (registers, stack, spills) on stderr
     if (getenv("MOL_JIT_VERBOSE")) o.push_back("--ptxas-options=-v");
+    // MOL_JIT_DEFINES="A B=1": extra preprocessor definitions for the generated modules
+    if (const char* defs = getenv("MOL_JIT_DEFINES")) {
+        std::string all(defs), tok;
+        for (size_t i = 0; i <= all.size(); ++i) {
+            if (i == all.size() || all[i] == ' ') {
+                if (!tok.empty()) o.push_back("-D" + tok);
+                tok.clear();
+            } else {
+                tok += all[i];
+            }
+        }
+    }
     return o;
 }
 

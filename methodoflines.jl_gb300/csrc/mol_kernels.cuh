@@ -263,6 +263,7 @@ struct BatchSync {
     unsigned long long* ticket;   // next work item
     unsigned long long* done;     // [instance] tiles finished, all rounds so far
     int* status;                  // 0 ok, 1 a wait ran out of budget
+    long long spin_limit;         // polls before a wait gives up (MOL_BATCH_SPIN_LIMIT by default)
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
@@ -317,7 +318,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_tiles_t(const DevProb<T>*
                     ok = 0;
                     break;
                 }
-                if (++polls > MOL_BATCH_SPIN_LIMIT) {
+                if (++polls > sync.spin_limit) {
                     atomicExch(sync.status, 1);
                     ok = 0;
                     break;

@@ -105,3 +105,33 @@ def test_batch_tiled_device_arrays_repeat(gpu_lib):
         Plan(lw).step_ssprk33(ref, dts[i], 14, t0=0.0)
         got = got_all[batch.offsets[i]:batch.offsets[i + 1]]
         assert np.allclose(got, ref, rtol=1e-13, atol=1e-15), i
+
+
+def test_batch_bounded_wait_reports_abandoned_run(gpu_lib, monkeypatch):
+    """Failure detection without a GPU fault: a dependency that is never met (the host starts
+    the ticket after round 0, so round-1 tiles wait for tiles no CTA runs) makes the bounded
+    waits run out; every CTA leaves, mol_batch_check reports the abandoned run, and the
+    ensemble works normally afterwards."""
+    torch = pytest.importorskip("torch")
+    from molgpu._lib import MolError
+    lws, dts = _members(SPECS)
+    batch = Batch(lws)
+    batch.tune(128, 2, 64)
+    st = torch.cuda.Stream()
+    batch.set_stream(st.cuda_stream)
+    u = torch.tensor(batch.pack([lw.u0 for lw in lws]), device="cuda")
+    monkeypatch.setenv("MOL_BATCH_INJECT_SKIP_ROUND", "1")
+    monkeypatch.setenv("MOL_BATCH_SPIN_LIMIT", "2000")
+    batch.step_ssprk33(u, dts, 3)
+    with pytest.raises(MolError, match="poll budget"):
+        batch.check()
+    monkeypatch.delenv("MOL_BATCH_INJECT_SKIP_ROUND")
+    monkeypatch.delenv("MOL_BATCH_SPIN_LIMIT")
+    u = torch.tensor(batch.pack([lw.u0 for lw in lws]), device="cuda")
+    batch.step_ssprk33(u, dts, 6)
+    batch.check()
+    got_all = u.cpu().numpy()
+    for i, lw in enumerate(lws):
+        ref = lw.u0.copy()
+        Plan(lw).step_ssprk33(ref, dts[i], 6, t0=0.0)
+        assert np.allclose(got_all[batch.offsets[i]:batch.offsets[i + 1]], ref, rtol=1e-13, atol=1e-15), i
