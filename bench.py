@@ -472,10 +472,12 @@ def batched(args, dev, stream):
         seq_ms += _time(lambda: p.step_ssprk33(ui, dts[i], steps), stream, 1, warm=False)
         p.close()
     seq_ms *= count / len(idx)
+    sched = batch.config
     batch.close()
     return {"instances": count, "unknowns": total, "steps": steps, "setup_s": setup,
             "batched_ms": ms, "batched_Mcell_s": total * steps / ms / 1e3,
             "f32state_batched_ms": ms32, "f32state_rel_err_vs_f64": f32err,
+            "schedule": sched,
             "sequential_plain_ms_estimated": seq_ms,
             "sequential_sample": f"{len(idx)} of {count} instances, scaled by {count / len(idx):.1f}",
             "batched_vs_sequential": seq_ms / ms}

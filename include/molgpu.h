@@ -278,6 +278,9 @@ int mol_batch_tune(mol_batch* batch, int32_t threads, int32_t ctas_per_sm, int64
  * dependency wait ran out of its poll budget (MOL_ERR_CUDA; the flag is then cleared).
  * Steps on host arrays call it themselves. */
 int mol_batch_check(mol_batch* batch);
+/* The schedule in use (after autotuning, once a step has run): threads per CTA, CTAs per SM,
+ * tile cells (-1: one CTA per instance). */
+int mol_batch_config(const mol_batch* batch, int32_t* threads, int32_t* ctas_per_sm, int64_t* tile_cells);
 
 #ifdef __cplusplus
 }

@@ -44,7 +44,8 @@ struct mol_batch {
     unsigned* d_ticket = nullptr;
     // tiled schedule: [ticket u64][status i32 + pad][done u64 x n] in one allocation
     unsigned long long* d_sync = nullptr;
-    long long* d_tile_pre = nullptr;
+    TileRef* d_tiles = nullptr;              // per tile of a round: instance, index, count
+    size_t d_tiles_cap = 0;
     int tile_cells_uploaded = 0;
     long long tiles_total = 0;               // tiles of one round at the uploaded tile size
     unsigned long long inject_ticket = 0;     // host value for the injected first ticket
@@ -85,20 +86,34 @@ int balloc(mol_batch* b, void** p, size_t bytes) {
     return MOL_OK;
 }
 
-// Tile prefix sums of the instances in slot order for a tile size.
+// The tile table of one round for a tile size: tiles of the instances in slot order
+// (largest first), each with its instance, its index within the instance and the instance's
+// tile count.
 int upload_tiles(mol_batch* b, int tile_cells) {
     if (b->tile_cells_uploaded == tile_cells) return MOL_OK;
-    std::vector<long long> pre(b->n + 1, 0);
+    std::vector<TileRef> t;
     for (int s = 0; s < b->n; ++s) {
-        const long long nc = b->plans[b->order[s]]->ncell;
-        pre[s + 1] = pre[s] + (nc + tile_cells - 1) / tile_cells;
+        const int inst = b->order[s];
+        const long long nc = b->plans[inst]->ncell;
+        const long long k = (nc + tile_cells - 1) / tile_cells;
+        for (long long j = 0; j < k; ++j) t.push_back(TileRef{inst, (int)j, (int)k, 0});
     }
-    int st = bcheck(b, cudaMemcpyAsync(b->d_tile_pre, pre.data(), sizeof(long long) * (b->n + 1),
-                                       cudaMemcpyHostToDevice, b->stream), "tile table");
+    int st = MOL_OK;
+    if (t.size() > b->d_tiles_cap) {
+        if (b->d_tiles) cudaFree(b->d_tiles);
+        b->d_tiles = nullptr;
+        b->d_tiles_cap = 0;
+        void* q = nullptr;
+        if ((st = bcheck(b, cudaMalloc(&q, sizeof(TileRef) * t.size()), "tile table"))) return st;
+        b->d_tiles = (TileRef*)q;
+        b->d_tiles_cap = t.size();
+    }
+    st = bcheck(b, cudaMemcpyAsync(b->d_tiles, t.data(), sizeof(TileRef) * t.size(), cudaMemcpyHostToDevice,
+                                   b->stream), "tile table");
     if (!st) st = bcheck(b, cudaStreamSynchronize(b->stream), "tile table");
     if (!st) {
         b->tile_cells_uploaded = tile_cells;
-        b->tiles_total = pre[b->n];
+        b->tiles_total = (long long)t.size();
     }
     return st;
 }
@@ -142,7 +157,7 @@ int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, 
             if (e == cudaSuccess)
                 e = cudaMemsetAsync(b->d_sync + 2, 0, sync_bytes - 2 * sizeof(unsigned long long), b->stream);
             if (e != cudaSuccess) return e;
-            return launch_k(k, grid, threads, b->stream, probs, off, order, (const long long*)b->d_tile_pre, ninst,
+            return launch_k(k, grid, threads, b->stream, probs, off, (const TileRef*)b->d_tiles, b->tiles_total,
                             tile_cells, U, U1, U2, params, (const double*)b->d_dt, t0, nsteps, sync);
         }
         cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned), b->stream);
@@ -209,7 +224,7 @@ int tune(mol_batch* b, T* U, long long probe_steps) {
                 if (c > maxc) continue;
                 if (!tiled) cand.push_back({th, c, 0});
                 else
-                    for (int per : {4, 16}) cand.push_back({th, c, th * per});
+                    for (int per : {4, 16, 64, 256}) cand.push_back({th, c, th * per});
             }
         }
     }
@@ -345,7 +360,6 @@ int mol_batch_create(const mol_problem_desc* const* descs, int32_t n, mol_batch*
                      [&](int a, int c) { return b->plans[a]->ncell > b->plans[c]->ncell; });
     b->order = order;
     if ((st = balloc(b, (void**)&b->d_sync, sizeof(unsigned long long) * (2 + (size_t)n)))) return st;
-    if ((st = balloc(b, (void**)&b->d_tile_pre, sizeof(long long) * (n + 1)))) return st;
     cudaMemset(b->d_sync, 0, sizeof(unsigned long long) * (2 + (size_t)n));
     if ((st = balloc(b, (void**)&b->d_p64, sizeof(DevProb<double>) * n))) return st;
     if ((st = balloc(b, (void**)&b->d_p32, sizeof(DevProb<float>) * n))) return st;
@@ -368,6 +382,7 @@ int mol_batch_destroy(mol_batch* b) {
     if (!b) return MOL_ERR_INVALID;
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->d_tiles) cudaFree(b->d_tiles);
     for (mol_plan* p : b->plans) mol_plan_destroy(p);
     for (void* p : b->allocs) cudaFree(p);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -401,6 +416,14 @@ int mol_batch_step_ssprk33(mol_batch* b, double* u, const double* dts, double t0
 
 int mol_batch_step_ssprk33_f32state(mol_batch* b, float* u, const double* dts, double t0, int64_t nsteps) {
     return step_impl<float>(b, u, dts, t0, nsteps);
+}
+
+int mol_batch_config(const mol_batch* b, int32_t* threads, int32_t* ctas_per_sm, int64_t* tile_cells) {
+    if (!b) return MOL_ERR_INVALID;
+    if (threads) *threads = b->threads;
+    if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+    if (tile_cells) *tile_cells = b->tile_cells > 0 ? b->tile_cells : -1;
+    return MOL_OK;
 }
 
 int mol_batch_check(mol_batch* b) {

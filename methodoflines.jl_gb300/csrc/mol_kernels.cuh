@@ -276,59 +276,64 @@ __device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsig
     asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Tile g of a round: its instance (slot order already resolved), its index within the
+// instance and the instance's tile count.
+struct TileRef {
+    int inst, tile, ntiles, pad;
+};
+
 template <class T, class G>
 __global__ void __launch_bounds__(kThreads, 1) k_batch_tiles_t(const DevProb<T>* __restrict__ probs,
                                                             const long long* __restrict__ off,
-                                                            const int* __restrict__ order,
-                                                            const long long* __restrict__ tile_pre, int ninst,
-                                                            int tile_cells, T* U, T* U1, T* U2,
+                                                            const TileRef* __restrict__ tiles,
+                                                            long long ntiles, int tile_cells, T* U, T* U1, T* U2,
                                                             const T* const* __restrict__ params,
                                                             const double* __restrict__ dts, double t0,
                                                             long long nsteps, BatchSync sync) {
     __shared__ long long s_item;
+    __shared__ TileRef s_ref;
     __shared__ int s_ok;
-    const long long ntiles = tile_pre[ninst];
     const long long nitems = 3 * nsteps * ntiles;
     T out[MOL_MAX_FIELDS];
     typename G::template Uniform<T> UN;
+    // thread 0 takes the next ticket while the CTA works on the current tile; the held ticket
+    // is larger than the one being worked on, so the lowest unfinished unit still always runs
+    long long next = 0;
+    if (threadIdx.x == 0) next = *(volatile int*)sync.status ? nitems : (long long)atomicAdd(sync.ticket, 1ull);
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0)
-            s_item = *(volatile int*)sync.status ? nitems : (long long)atomicAdd(sync.ticket, 1ull);
-        __syncthreads();
-        const long long item = s_item;
-        if (item >= nitems) return;
-        const long long r = item / ntiles;
-        const long long g = item - r * ntiles;
-        int lo = 0, hi = ninst;  // tile_pre[lo] <= g < tile_pre[hi]
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (tile_pre[mid] <= g) lo = mid;
-            else hi = mid;
-        }
-        const int i = order[lo];
-        const long long tiles_i = tile_pre[lo + 1] - tile_pre[lo];
-        const long long j = g - tile_pre[lo];
         if (threadIdx.x == 0) {
-            const unsigned long long need = (unsigned long long)(r * tiles_i);
+            const long long item = next;
+            s_item = item;
             int ok = 1;
-            long long polls = 0;
-            while (ld_acquire_u64(sync.done + i) < need) {
-                if (*(volatile int*)sync.status != 0) {
-                    ok = 0;
-                    break;
+            if (item < nitems) {
+                const long long r = item / ntiles;
+                const TileRef ref = tiles[item - r * ntiles];
+                s_ref = ref;
+                const unsigned long long need = (unsigned long long)(r * ref.ntiles);
+                long long polls = 0;
+                while (ld_acquire_u64(sync.done + ref.inst) < need) {
+                    if (*(volatile int*)sync.status != 0) {
+                        ok = 0;
+                        break;
+                    }
+                    if (++polls > sync.spin_limit) {
+                        atomicExch(sync.status, 1);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(64);
                 }
-                if (++polls > sync.spin_limit) {
-                    atomicExch(sync.status, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
+                if (ok) next = *(volatile int*)sync.status ? nitems : (long long)atomicAdd(sync.ticket, 1ull);
             }
             s_ok = ok;
         }
         __syncthreads();
-        if (!s_ok) return;
+        const long long item = s_item;
+        if (item >= nitems || !s_ok) return;
+        const long long r = item / ntiles;
+        const int i = s_ref.inst;
+        const long long j = s_ref.tile;
         const DevProb<T>& P = probs[i];
         T* u = U + off[i];
         T* u1 = U1 + off[i];

@@ -121,6 +121,7 @@ _PROTOS = {
     "mol_batch_step_ssprk33_f32state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int64]),
     "mol_batch_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64]),
     "mol_batch_check": (C.c_int, [C.c_void_p]),
+    "mol_batch_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
 }
 
 EXPORTED = sorted(_PROTOS)

@@ -223,6 +223,13 @@ class Batch:
         """tile_cells > 0: tiled schedule with that tile; < 0: one CTA per instance; all 0: autotune."""
         L.check(L.lib().mol_batch_tune(self._h, int(threads), int(ctas_per_sm), int(tile_cells)), batch=self._h)
 
+    @property
+    def config(self):
+        """The schedule in use: threads per CTA, CTAs per SM, tile cells (-1: one CTA per instance)."""
+        th, cps, tc = C.c_int32(), C.c_int32(), C.c_int64()
+        L.check(L.lib().mol_batch_config(self._h, C.byref(th), C.byref(cps), C.byref(tc)), batch=self._h)
+        return {"threads": th.value, "ctas_per_sm": cps.value, "tile_cells": tc.value}
+
     def check(self):
         """Waits for the stream; raises if a run was abandoned after a dependency wait ran out."""
         L.check(L.lib().mol_batch_check(self._h), batch=self._h)
