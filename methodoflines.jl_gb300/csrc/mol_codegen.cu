@@ -498,7 +498,7 @@ void emit_weno(Emitter& e, const mol_problem_desc* d, int k) {
 // Nonlinear Laplacian.  The face value a(x~, u~) * (D_inner u) at half point Ih
 // is emitted twice: with compile-time offsets for interior cells and with
 // runtime tap tables for the rest.
-void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
+void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot) {
     const mol_term& tm = d->terms[k];
     const mol_op1d& oo = d->ops[tm.op];
     const mol_op1d& oi = d->ops[tm.op2];
@@ -597,10 +597,9 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
                    : "(long long)(" + std::to_string(x) + ") * s";
     };
     // fast path helpers: relative face offsets r = omin_outer + m - 1 (outer stencil sits at II - 1)
-    auto fast_face = [&](int m, bool vjp) {
-        const int r = oo.omin + m - 1;
-        const std::string tag = "f" + std::to_string(m) + "_";
-        e << "    {\n";
+    // statements computing the face at relative half point r: tag du, tag uf<f>, the face
+    // program; leaves tag a and tag du
+    auto face_body = [&](int r, const std::string& tag, bool vjp) {
         // inner derivative
         for (size_t q = 0; q < nzi.size(); ++q) {
             const int t_ = nzi[q];
@@ -628,11 +627,25 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
             if (vjp) e << "    T " << tag << "gfa" << j << " = T(0);\n";
         }
         face_forward(tag);
+    };
+    // face r of this cell from the face pass: the left face of cell I + r + 1 along D, when that
+    // cell is an unknown reached without a wrap
+    const std::string FQ = std::to_string(face_slot);
+    auto from_pass = [&](int r) {
+        return "P.faces && I[" + D + "] + (" + std::to_string(r + 1) + ") > P.lo[" + D + "] && I[" + D + "] + (" +
+               std::to_string(r + 1) + ") <= P.n[" + D + "] - P.up[" + D + "]";
+    };
+    auto fast_face = [&](int m, bool vjp) {
+        const int r = oo.omin + m - 1;
+        const std::string tag = "f" + std::to_string(m) + "_";
+        e << "    {\n";
         if (!vjp) {
+            face_body(r, tag, false);
             e << "    const T " << tag << "F = " << tag << "a * " << tag << "du;\n";
             e << "    acc = started ? fma(wo[" << m << "], " << tag << "F, acc) : wo[" << m << "] * " << tag << "F;\n"
               << "    started = true;\n";
         } else {
+            face_body(r, tag, true);
             e << "    const T " << tag << "g = g * wo[" << m << "];\n";
             e << "    { const T gd = " << tag << "g * " << tag << "a;\n";
             for (int t_ : nzi)
@@ -675,8 +688,27 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
           << "    const T* __restrict__ wp = P.w + P.ops[" << opp << "].w_int;\n"
           << "    const T* __restrict__ bF = u + (long long)" << F << " * P.ncell + c;\n"
           << "    const long long s = gstride(P, " << D << ");\n";
-        if (!vjp) e << "    T acc = T(0);\n    bool started = false;\n";
-        else e << "    T* lF = lam_u + (long long)" << F << " * P.ncell + c;\n";
+        if (!vjp) {
+            // every face of the warp's cells from the face pass: a warp-uniform branch, so the
+            // face arithmetic below is not issued at all (FP64 instructions cost the same
+            // predicated off)
+            std::string all_owned = "P.faces";
+            for (int m : nzo) all_owned += " && " + from_pass(oo.omin + m - 1);
+            e << "    if (warp_all(" << all_owned << ")) {\n"
+              << "    const T* __restrict__ fq = P.faces + (long long)" << FQ << " * P.ncell + c;\n";
+            bool first = true;
+            for (int m : nzo) {
+                const int r = oo.omin + m - 1;
+                const std::string Fv = "fq[(long long)(" + std::to_string(r + 1) + ") * s]";
+                if (first) e << "    T acc = wo[" << m << "] * " << Fv << ";\n";
+                else e << "    acc = fma(wo[" << m << "], " << Fv << ", acc);\n";
+                first = false;
+            }
+            e << "    return " << (nzo.empty() ? "T(0)" : "acc") << ";\n    }\n";
+            e << "    T acc = T(0);\n    bool started = false;\n";
+        } else {
+            e << "    T* lF = lam_u + (long long)" << F << " * P.ncell + c;\n";
+        }
         for (int m : nzo) fast_face(m, vjp);
         if (!vjp) e << "    return acc;\n    }\n";
         else e << "    return;\n    }\n";
@@ -688,12 +720,42 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k) {
           << "        if (q >= so.cnt) break;\n"
           << "        const T w_ = P.w[so.woff + q];\n        if (w_ == T(0)) continue;\n";
         if (!vjp)
-            e << "        const T F_ = gface" << K << "<T>(P, u, c, I, so.first + q, t, p);\n"
+            e << "        const int Ih = so.first + q;\n"
+              << "        T F_;\n"
+              << "        if (P.faces && Ih + 1 > P.lo[" << D << "] && Ih + 1 <= P.n[" << D << "] - P.up[" << D << "])\n"
+              << "            F_ = P.faces[(long long)" << FQ << " * P.ncell + c + (long long)(Ih + 1 - I[" << D
+              << "]) * gstride(P, " << D << ")];\n"
+              << "        else\n"
+              << "            F_ = gface" << K << "<T>(P, u, c, I, Ih, t, p);\n"
               << "        acc = started ? fma(w_, F_, acc) : w_ * F_;\n        started = true;\n    }\n    return acc;\n";
         else
             e << "        gface" << K << "_vjp<T>(P, u, c, I, so.first + q, t, p, g * w_, lam_u, lp, lam_aux);\n    }\n";
         e << "}\n";
     }
+    // the face pass: the left face (half point I - 1/2) of this cell
+    int reach_left = 0;
+    for (int t_ : nzi) reach_left = std::max(reach_left, std::abs(-1 + oi.omin + t_));
+    for (int t_ : nzp) reach_left = std::max(reach_left, std::abs(-1 + op.omin + t_));
+    std::string lcond;
+    if (per) {
+        lcond = "wrap_line_ok(P, " + F + ", " + D + ", " + std::to_string(reach_left) + ")";
+        for (int f : used_fields)
+            if (f != tm.field)
+                lcond += " && wrap_line_ok(P, " + std::to_string(f) + ", " + D + ", " + std::to_string(reach_left) + ")";
+    } else {
+        lcond = "warp_all(fast_line(P, P.ops[" + opi + "], " + F + ", " + D + ", I[" + D + "] - 1) && fast_line(P, P.ops[" +
+                opp + "], " + F + ", " + D + ", I[" + D + "] - 1))";
+    }
+    e << "template <class T>\n__device__ __forceinline__ T gfl" << K
+      << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) {\n"
+      << "    if (" << lcond << ") {\n"
+      << "    const T* __restrict__ wi = P.w + P.ops[" << opi << "].w_int;\n"
+      << "    const T* __restrict__ wp = P.w + P.ops[" << opp << "].w_int;\n"
+      << "    const T* __restrict__ bF = u + (long long)" << F << " * P.ncell + c;\n"
+      << "    const long long s = gstride(P, " << D << ");\n";
+    face_body(-1, "fl_", false);
+    e << "    return fl_a * fl_du;\n    }\n"
+      << "    return gface" << K << "<T>(P, u, c, I, I[" << D << "] - 1, t, p);\n}\n";
 }
 
 }  // namespace
@@ -996,12 +1058,13 @@ std::string generate_source(const mol_problem_desc* d, std::string& why) {
     e << "// generated by libmolgpu for one problem structure\n"
       << "#include \"mol_kernels.cuh\"\n"
       << "namespace mol {\n";
+    int nface = 0;  // nonlinear-Laplacian terms: slots of the face pass
     for (int k = 0; k < d->nterms; ++k) {
         switch (d->terms[k].kind) {
             case MOL_TERM_LINEAR: emit_linear(e, d, k); break;
             case MOL_TERM_MIXED: emit_mixed(e, d, k); break;
             case MOL_TERM_WENO: emit_weno(e, d, k); break;
-            case MOL_TERM_NONLINLAP: emit_nonlinlap(e, d, k); break;
+            case MOL_TERM_NONLINLAP: emit_nonlinlap(e, d, k, nface++); break;
             default: why = "unknown term"; return "";
         }
     }
@@ -1042,8 +1105,21 @@ std::string generate_source(const mol_problem_desc* d, std::string& why) {
     for (int f = 0; f < d->nfields; ++f)
         e << "    atomicAdd(lam_u + (long long)" << f << " * P.ncell + c, own" << f << ");\n";
     e << "}\n";
+    // the face pass: left faces of every nonlinear-Laplacian term, slot order = term order
+    e << "template <class T>\n__device__ __forceinline__ void gen_faces(const DevProb<T>& P, const T* __restrict__ u, "
+         "long long c, const int* I, T t, const T* __restrict__ p, T* out) {\n";
+    {
+        int q = 0;
+        for (int k = 0; k < d->nterms; ++k)
+            if (d->terms[k].kind == MOL_TERM_NONLINLAP)
+                e << "    out[" << q++ << "] = gfl" << k << "<T>(P, u, c, I, t, p);\n";
+    }
+    e << "}\n";
     e << "struct GenCell {\n"
       << "static constexpr int kFields = " << d->nfields << ";\n"
+      << "static constexpr int kFaceTerms = " << nface << ";\n"
+      << "template <class T>\nstatic __device__ __forceinline__ void faces(const DevProb<T>& P, const T* __restrict__ u, "
+         "long long c, const int* I, T t, const T* __restrict__ p, T* out) { gen_faces<T>(P, u, c, I, t, p, out); }\n"
          "template <class T> using Uniform = GenUniform<T>;\n"
          "template <class T>\nstatic __device__ __forceinline__ void uniform(const DevProb<T>& P, T t, const T* "
          "__restrict__ p, GenUniform<T>& U) { gen_uniform<T>(P, t, p, U); }\n"
@@ -1227,11 +1303,12 @@ std::vector<std::string> jit_kernel_names(int nparams, int group) {
         case JIT_FWD64:
             n = {"&mol::k_rhs_t<double, mol::GenCell>", "&mol::k_ssprk_t<double, mol::GenCell, 1>",
                  "&mol::k_ssprk_t<double, mol::GenCell, 2>", "&mol::k_ssprk_t<double, mol::GenCell, 3>",
-                 "&mol::k_tsit_stage_t<double, mol::GenCell>"};
+                 "&mol::k_tsit_stage_t<double, mol::GenCell>", "&mol::k_faces_t<double, mol::GenCell>"};
             break;
         case JIT_FWD32:
             n = {"&mol::k_rhs_t<float, mol::GenCell>", "&mol::k_ssprk_t<float, mol::GenCell, 1>",
-                 "&mol::k_ssprk_t<float, mol::GenCell, 2>", "&mol::k_ssprk_t<float, mol::GenCell, 3>"};
+                 "&mol::k_ssprk_t<float, mol::GenCell, 2>", "&mol::k_ssprk_t<float, mol::GenCell, 3>",
+                 "&mol::k_faces_t<float, mol::GenCell>"};
             break;
         case JIT_BATCH:
             n = {"&mol::k_batch_ssprk_t<double, mol::GenCell>", "&mol::k_batch_ssprk_t<float, mol::GenCell>",
@@ -1342,12 +1419,14 @@ int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k
             k->ssp64[1] = got[2];
             k->ssp64[2] = got[3];
             k->tsit64 = got[4];
+            k->faces64 = got[5];
             break;
         case JIT_FWD32:
             k->rhs32 = got[0];
             k->ssp32[0] = got[1];
             k->ssp32[1] = got[2];
             k->ssp32[2] = got[3];
+            k->faces32 = got[4];
             break;
         case JIT_BATCH:
             k->batch64 = got[0];

@@ -24,6 +24,7 @@ struct JitKernels {
     cudaKernel_t rhs32 = nullptr, ssp32[3] = {nullptr, nullptr, nullptr}, batch32 = nullptr, tsit32 = nullptr;
     cudaKernel_t vjp64 = nullptr;
     cudaKernel_t tiles64 = nullptr, tiles32 = nullptr;
+    cudaKernel_t faces64 = nullptr, faces32 = nullptr;  // face pass (nonlinear Laplacian)
 };
 
 std::string generate_source(const mol_problem_desc* d, std::string& why);

@@ -64,6 +64,8 @@ struct DevProb {
     const T* aux;
     const long long* aux_off;     // naux + 1 offsets into aux
     int naux;
+    // left faces of the nonlinear-Laplacian terms from the face pass ([slot][cell]), or null
+    const T* faces;
 };
 
 __device__ __forceinline__ int wrap_periodic(int i, int l) {

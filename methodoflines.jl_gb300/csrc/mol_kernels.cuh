@@ -30,6 +30,9 @@ __device__ __forceinline__ float div3m(float x) { return x / 3.0f; }
 
 struct InterpCell {
     static constexpr int kFields = 0;  // field count known only at run time
+    static constexpr int kFaceTerms = 0;  // the interpreter evaluates every face in the cell
+    template <class T>
+    static __device__ __forceinline__ void faces(const DevProb<T>&, const T*, long long, const int*, T, const T*, T*) {}
     template <class T>
     struct Uniform {};
     template <class T>
@@ -62,6 +65,30 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_rhs_t(const __grid
         G::cell(P, u, c, I, T(t), p, U, out);
         #pragma unroll
         for (int f = 0; f < nfields_of<G>(P); ++f) du[(long long)f * P.ncell + c] = out[f];
+    }
+}
+
+// The face pass: for every cell, the left face (half point I - 1/2 along the term's
+// dimension) of each nonlinear-Laplacian term, so the cell kernel that follows reads a face
+// computed once instead of evaluating it for both cells that share it.  The time is
+// S->t (tfix NaN) or tfix, plus toff, exactly as the stage kernel forms its stage time.
+template <class T, class G>
+__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_faces_t(const __grid_constant__ DevProb<T> P,
+                                                                      const T* __restrict__ u,
+                                                                      const T* __restrict__ p, const SolverState* S,
+                                                                      double toff, double tfix, T* __restrict__ faces) {
+    constexpr int NQ = G::kFaceTerms > 0 ? G::kFaceTerms : 1;
+    if (G::kFaceTerms == 0) return;
+    const double t0 = (tfix == tfix) ? tfix : S->t;
+    const double t = toff == 0.0 ? t0 : t0 + toff;
+    T out[NQ];
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        G::faces(P, u, c, I, T(t), p, out);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) faces[(long long)q * P.ncell + c] = out[q];
     }
 }
 

@@ -252,15 +252,51 @@ __global__ void k_set_time(SolverState* S, double t) {
 // launch helpers
 // ----------------------------------------------------------------------------
 
+// Face buffer of the face pass (allocated on first use, before any graph capture).
+template <class T>
+T*& face_buf(mol_plan* plan);
+template <>
+double*& face_buf<double>(mol_plan* plan) { return plan->faces64; }
+template <>
+float*& face_buf<float>(mol_plan* plan) { return plan->faces32; }
+
+template <class T>
+int ensure_faces(mol_plan* plan) {
+    if (!plan->face_pass || face_buf<T>(plan)) return MOL_OK;
+    void* q = nullptr;
+    int st = plan_alloc(plan, &q, sizeof(T) * (size_t)plan->nface * (size_t)plan->ncell);
+    if (!st) face_buf<T>(plan) = (T*)q;
+    return st;
+}
+
+// The face pass on state u at S->t + toff (tfix NaN) or tfix + toff; returns the problem
+// view the following cell kernel takes (faces set), or the plain view without a face pass.
+template <class T>
+DevProb<T> with_faces(mol_plan* plan, const T* u, const T* p, double toff, double tfix, cudaError_t* e) {
+    DevProb<T> P = prob<T>(plan);
+    *e = cudaSuccess;
+    T* fb = face_buf<T>(plan);
+    cudaKernel_t k = std::is_same<T, double>::value ? plan->jit.faces64 : plan->jit.faces32;
+    if (!plan->face_pass || !plan->use_jit || !fb || !k) return P;
+    *e = launch_k(k, plan->nblocks, plan->nthreads, plan->stream, P, u, p, (const SolverState*)plan->d_state, toff,
+                  tfix, fb);
+    ++g_launches;
+    P.faces = fb;
+    return P;
+}
+
 template <class T>
 int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t) {
     const bool is64 = std::is_same<T, double>::value;
     if (plan->use_jit) {
         int st = jit_ensure(&plan->jit, is64 ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
         if (st) return set_err(plan, st, plan->jit_err);
+        cudaError_t e;
+        const DevProb<T> Pf = with_faces<T>(plan, u, p, 0.0, t, &e);
+        if (e != cudaSuccess) return cuda_check(plan, e, "face pass launch");
         ++g_launches;
         return cuda_check(plan, launch_k(is64 ? plan->jit.rhs64 : plan->jit.rhs32, plan->nblocks, plan->nthreads,
-                                         plan->stream, prob<T>(plan), u, du, p, t), "rhs launch");
+                                         plan->stream, Pf, u, du, p, t), "rhs launch");
     }
     k_rhs_t<T, InterpCell><<<plan->nblocks, kThreads, 0, plan->stream>>>(prob<T>(plan), u, du, p, t);
     ++g_launches;
@@ -291,11 +327,16 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
         const T* cu1 = u1;
         const T* cu2 = u2;
         const double nan = std::nan("");
-        cudaError_t e = launch_k(k[0], plan->nblocks, plan->nthreads, plan->stream, P, cu, cu, u1, p, plan->d_state, dt, nan);
+        cudaError_t e;
+        DevProb<T> Pf = with_faces<T>(plan, cu, p, 0.0, nan, &e);
         if (e == cudaSuccess)
-            e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, P, cu1, cu, u2, p, plan->d_state, dt, nan);
+            e = launch_k(k[0], plan->nblocks, plan->nthreads, plan->stream, Pf, cu, cu, u1, p, plan->d_state, dt, nan);
+        if (e == cudaSuccess) Pf = with_faces<T>(plan, cu1, p, dt, nan, &e);
         if (e == cudaSuccess)
-            e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, P, cu2, cu, uout, p, plan->d_state, dt, nan);
+            e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, Pf, cu1, cu, u2, p, plan->d_state, dt, nan);
+        if (e == cudaSuccess) Pf = with_faces<T>(plan, cu2, p, dt / 2, nan, &e);
+        if (e == cudaSuccess)
+            e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, Pf, cu2, cu, uout, p, plan->d_state, dt, nan);
         return cuda_check(plan, e, "ssprk launch");
     }
     const double nan = std::nan("");
@@ -778,6 +819,13 @@ int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member
             } else {
                 cudaGetLastError();
             }
+            // Face pass for nonlinear-Laplacian terms: each face is evaluated once per stage
+            // instead of once for each of the two cells sharing it.  An extra launch per stage,
+            // so by default only from 32768 cells on; MOL_FACE_PASS=0/1 forces it off/on.
+            for (int k = 0; k < d->nterms; ++k)
+                if (d->terms[k].kind == MOL_TERM_NONLINLAP) ++plan->nface;
+            const char* fp = getenv("MOL_FACE_PASS");
+            plan->face_pass = plan->nface > 0 && (fp && fp[0] ? fp[0] == '1' : ncell >= 32768);
         }
         if (!plan->use_jit) {
             const char* req = getenv("MOL_REQUIRE_CODEGEN");
@@ -858,6 +906,7 @@ int rhs_impl(mol_plan* plan, T* du, const T* u, const T* p, double t) {
     if ((st = stage_in<T>(plan, du, 11, sdu, false))) return st;
     const T* pp = params_ptr<T>(plan, p, &st);
     if (st) return st;
+    if ((st = ensure_faces<T>(plan))) return st;
     if ((st = launch_rhs<T>(plan, sdu.ptr, su.ptr, pp, t))) return st;
     if (sdu.host) {
         if ((st = cuda_check(plan, cudaMemcpyAsync(du, sdu.ptr, sizeof(T) * (size_t)plan->nunk, cudaMemcpyDeviceToHost,
@@ -874,6 +923,7 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     DeviceGuard g(plan->dev);
     int st;
     if ((st = ensure_ws<T>(plan, 3))) return st;
+    if ((st = ensure_faces<T>(plan))) return st;
     T** ws = workspace<T>(plan);
     Staged<T> su;
     const bool host = !is_device_ptr(u);

@@ -79,6 +79,11 @@ struct mol_plan {
     mol::JitKernels jit;
     bool use_jit = false;
     std::string jit_src, jit_err;
+    // face pass for nonlinear-Laplacian terms: nface slots of ncell left faces per precision
+    int nface = 0;
+    bool face_pass = false;
+    double* faces64 = nullptr;
+    float* faces32 = nullptr;
 };
 
 namespace mol {
