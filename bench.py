@@ -576,6 +576,16 @@ def run_case(name, args):
         torch.cuda.synchronize()
         out.update(codegen=plan.uses_codegen, norm=float(torch.linalg.norm(du)))
         plan.close()
+    elif name == "fp64_lanes":
+        # the FP64 pipe: warp FMA instructions per second with 32..1 active lanes per warp
+        import ctypes as C
+        from molgpu import _lib as L
+        rows = []
+        for act in (32, 16, 8, 4, 2, 1):
+            w, t = C.c_double(), C.c_double()
+            L.check(L.lib().mol_diag_fp64_rate(act, C.byref(w), C.byref(t)))
+            rows.append({"active_lanes": act, "warp_fma_G_per_s": w.value / 1e9, "lane_tflops": t.value})
+        out.update(rows=rows)
     elif name == "adr3d_rhs":
         # one RHS of the 3-D ADR problem at 128^3
         sys_, disc, _ = problems.adr3d(N=128, nz_pts=130)
@@ -605,7 +615,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None,
                     choices=["burgers_adjoint", "ensemble", "brusselator_rhs_generated",
-                             "brusselator_rhs_interpreted", "adr3d_rhs"],
+                             "brusselator_rhs_interpreted", "adr3d_rhs", "fp64_lanes"],
                     help="run one small single-path case (for profiling) and exit")
     args = ap.parse_args()
     if args.case:

@@ -282,6 +282,12 @@ int mol_batch_check(mol_batch* batch);
  * tile cells (-1: one CTA per instance). */
 int mol_batch_config(const mol_batch* batch, int32_t* threads, int32_t* ctas_per_sm, int64_t* tile_cells);
 
+/* ---- diagnostics (no reference counterpart) ---- */
+/* FP64 pipe on the current device: warp-level FMA instructions per second when `active_lanes`
+ * (1..32) lanes of every warp run eight independent FMA chains, and the lane-level TFLOP/s
+ * (optional).  On GB300 the warp rate does not depend on the number of active lanes. */
+int mol_diag_fp64_rate(int32_t active_lanes, double* warp_fma_per_s, double* lane_tflops);
+
 #ifdef __cplusplus
 }
 #endif

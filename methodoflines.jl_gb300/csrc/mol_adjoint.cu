@@ -144,11 +144,15 @@ struct Adj {
 
     void stage(int which, const double* uin, const double* u0, double* uout, double t) {
         if (err) return;
-        const DevProb<double>& P = plan->P64;
         const double* cu = uin;
         cap_begin();
-        cudaError_t e = launch_k(plan->jit.ssp64[which - 1], plan->nblocks, plan->nthreads, plan->stream, P, cu, u0, uout,
-                                 p, plan->d_state, dt, t);
+        // the stage's time offset, as the stage kernel forms it from t
+        const double toff = which == 1 ? 0.0 : (which == 2 ? dt : dt / 2);
+        cudaError_t e;
+        const DevProb<double> P = with_faces<double>(plan, cu, p, toff, t, &e);
+        if (e == cudaSuccess)
+            e = launch_k(plan->jit.ssp64[which - 1], plan->nblocks, plan->nthreads, plan->stream, P, cu, u0, uout, p,
+                         plan->d_state, dt, t);
         ++g_launches;
         ck(e, "stage launch");
         counted();
@@ -427,6 +431,7 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
         return MOL_ERR_INVALID;
     int st = need_vjp(plan);
     if (st) return st;
+    if ((st = ensure_faces<double>(plan))) return st;
     const long long n = plan->nunk;
     // working buffers
     std::vector<void*> mine;

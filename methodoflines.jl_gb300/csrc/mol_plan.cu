@@ -262,7 +262,7 @@ float*& face_buf<float>(mol_plan* plan) { return plan->faces32; }
 
 template <class T>
 int ensure_faces(mol_plan* plan) {
-    if (!plan->face_pass || face_buf<T>(plan)) return MOL_OK;
+    if (!std::is_same<T, double>::value || !plan->face_pass || face_buf<T>(plan)) return MOL_OK;
     void* q = nullptr;
     int st = plan_alloc(plan, &q, sizeof(T) * (size_t)plan->nface * (size_t)plan->ncell);
     if (!st) face_buf<T>(plan) = (T*)q;
@@ -277,13 +277,19 @@ DevProb<T> with_faces(mol_plan* plan, const T* u, const T* p, double toff, doubl
     *e = cudaSuccess;
     T* fb = face_buf<T>(plan);
     cudaKernel_t k = std::is_same<T, double>::value ? plan->jit.faces64 : plan->jit.faces32;
-    if (!plan->face_pass || !plan->use_jit || !fb || !k) return P;
+    // FP32 arithmetic is not the bound of the Float32-state kernels: no face pass there
+    if (!std::is_same<T, double>::value || !plan->face_pass || !plan->use_jit || !fb || !k) return P;
     *e = launch_k(k, plan->nblocks, plan->nthreads, plan->stream, P, u, p, (const SolverState*)plan->d_state, toff,
                   tfix, fb);
     ++g_launches;
     P.faces = fb;
     return P;
 }
+
+template int ensure_faces<double>(mol_plan*);
+template int ensure_faces<float>(mol_plan*);
+template DevProb<double> with_faces<double>(mol_plan*, const double*, const double*, double, double, cudaError_t*);
+template DevProb<float> with_faces<float>(mol_plan*, const float*, const float*, double, double, cudaError_t*);
 
 template <class T>
 int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t) {

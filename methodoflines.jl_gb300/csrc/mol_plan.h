@@ -122,5 +122,11 @@ int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt)
 template <class T>
 int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, const T* p, double dt);
 void* mapped_host_ptr(const void* p);
+// The face pass of nonlinear-Laplacian terms (see k_faces_t): buffer allocation (before any
+// capture) and the launch, returning the problem view the next cell kernel takes.
+template <class T>
+int ensure_faces(mol_plan* plan);
+template <class T>
+DevProb<T> with_faces(mol_plan* plan, const T* u, const T* p, double toff, double tfix, cudaError_t* e);
 
 }  // namespace mol

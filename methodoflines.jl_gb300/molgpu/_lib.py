@@ -122,6 +122,7 @@ _PROTOS = {
     "mol_batch_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64]),
     "mol_batch_check": (C.c_int, [C.c_void_p]),
     "mol_batch_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    "mol_diag_fp64_rate": (C.c_int, [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 EXPORTED = sorted(_PROTOS)

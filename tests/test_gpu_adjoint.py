@@ -172,3 +172,21 @@ def test_adjoint_graph_capture_matches_stream_launches(gpu_lib, monkeypatch, nsn
     assert np.array_equal(a[4], b[4])
     assert np.allclose(a[2], b[2], rtol=1e-12, atol=1e-15 * np.max(np.abs(b[2])))
     assert np.allclose(a[3], b[3], rtol=1e-12)
+
+
+def test_adjoint_with_face_pass_matches(gpu_lib, monkeypatch):
+    """The adjoint's forward stages through the face pass give the gradient of the stages
+    evaluating their own faces (3-D ADR, dL/dK on the faces)."""
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("MOL_FACE_PASS", mode)
+        plan, lw, ex = _plan("adr3d", N=8, nz_pts=10)
+        target = np.random.default_rng(5).standard_normal(lw.n_unknowns) * 1e-3
+        gaux = np.zeros(sum(plan.aux_sizes))
+        g = np.zeros(lw.n_unknowns)
+        loss, _ = plan.adjoint_ssprk33(lw.u0, ex["dt"], 6, target, nsnap=3, dLdu0=g, dLdaux=gaux)
+        out[mode] = (loss, g, gaux)
+        plan.close()
+    assert out["1"][0] == out["0"][0]
+    assert np.allclose(out["1"][1], out["0"][1], rtol=1e-12, atol=1e-18)
+    assert np.allclose(out["1"][2], out["0"][2], rtol=1e-12, atol=1e-18)

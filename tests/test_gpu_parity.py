@@ -238,3 +238,17 @@ def test_face_pass_matches_faces_in_cell(gpu_lib, monkeypatch, name, kw):
         plan.close()
     assert np.array_equal(out["1"][0], out["0"][0])
     assert np.array_equal(out["1"][1], out["0"][1])
+
+
+def test_fp64_warp_rate_independent_of_active_lanes(gpu_lib):
+    """The hardware fact the kernels are built around (mol_diag_fp64_rate): an FP64 warp
+    instruction costs the same with 32 or 1 active lanes."""
+    import ctypes as C
+    from molgpu import _lib as L
+    rates = {}
+    for act in (32, 1):
+        w, t = C.c_double(), C.c_double()
+        assert L.lib().mol_diag_fp64_rate(act, C.byref(w), C.byref(t)) == 0
+        assert w.value > 0 and t.value > 0
+        rates[act] = w.value
+    assert 0.8 < rates[1] / rates[32] < 1.25, rates
