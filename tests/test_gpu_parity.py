@@ -252,3 +252,21 @@ def test_fp64_warp_rate_independent_of_active_lanes(gpu_lib):
         assert w.value > 0 and t.value > 0
         rates[act] = w.value
     assert 0.8 < rates[1] / rates[32] < 1.25, rates
+
+
+def test_readme_example_heat_equation(gpu_lib):
+    """The README's example, end to end through the MethodOfLines-style API: discretize and
+    solve with SSPRK33; the result decays like exp(-pi^2 t) sin(pi x)."""
+    from molgpu import (Differential, Eq, Field, Interval, IV, MOLFiniteDifference, PDESystem, SSPRK33,
+                        discretize, sin, solve)
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dxx = Differential(t), Differential(x) ** 2
+    eq = Eq(Dt(u(x, t)), Dxx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), sin(math.pi * x)), Eq(u(0.0, t), 0.0), Eq(u(1.0, t), 0.0)]
+    pdesys = PDESystem([eq], bcs, [(t, Interval(0.0, 0.1)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [])
+    prob = discretize(pdesys, MOLFiniteDifference({x: 0.01}, t, approx_order=2))
+    sol = solve(prob, SSPRK33(), dt=2e-5)
+    xs = np.arange(1, 100) * 0.01
+    exact = np.exp(-math.pi ** 2 * 0.1) * np.sin(math.pi * xs)
+    assert np.max(np.abs(sol.u - exact)) < 1e-3 * np.max(np.abs(exact))
