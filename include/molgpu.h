@@ -72,9 +72,14 @@ typedef enum mol_status {
  *   i <= nlo (non-periodic)        -> low table i-1, taps 1 .. bLlo
  *   i >  len - nhi (non-periodic)  -> high table (len - i - hi_base), taps len-bLhi+1 .. len
  *   otherwise                      -> interior weights, taps i+omin .. i+omin+L-1 (wrapped if periodic)
- * Weights are offsets into mol_problem_desc.weights. */
+ * Weights are offsets into mol_problem_desc.weights.  nrows = 0: one interior row shared by
+ * every interior point.  nrows > 0 (a nonuniform grid, centered_diff_weights.jl:77-153 and
+ * the DX <: AbstractVector method of centered_difference.jl:32-56): one row of L weights per
+ * interior point, row (i - nlo - 1) at w_int + (i - nlo - 1) * L; then nrows must equal
+ * len - nlo - nhi, the dimension must not be periodic, and only LINEAR terms may use the
+ * operator (MOL_ERR_UNSUPPORTED otherwise). */
 typedef struct mol_op1d {
-    int32_t L, omin, nlo, bLlo, nhi, bLhi, hi_base, reserved;
+    int32_t L, omin, nlo, bLlo, nhi, bLhi, hi_base, nrows;
     int64_t w_int, w_lo, w_hi;
 } mol_op1d;
 

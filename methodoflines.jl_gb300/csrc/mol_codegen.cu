@@ -340,10 +340,18 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
     const mol_term& tm = d->terms[k];
     const mol_op1d& o = d->ops[tm.op];
     const std::string K = std::to_string(k), F = std::to_string(tm.field), D = std::to_string(tm.dim);
+    // taps whose weight is zero in every interior row are left out
     std::vector<int> nz;
-    for (int m = 0; m < o.L; ++m)
-        if (!zero_w(d, o.w_int + m)) nz.push_back(m);
+    for (int m = 0; m < o.L; ++m) {
+        bool z = true;
+        for (int r = 0; r < std::max(1, o.nrows) && z; ++r) z = zero_w(d, o.w_int + (int64_t)r * o.L + m);
+        if (!z) nz.push_back(m);
+    }
     const bool per = periodic_dim(d, tm.field, tm.dim);
+    // nonuniform grid: the interior row of the cell's own point (never periodic)
+    const std::string wrow = o.nrows > 0 ? " + (long long)(I[" + D + "] - " + std::to_string(o.nlo + 1) + ") * " +
+                                               std::to_string(o.L)
+                                         : std::string();
     const std::string cond = per ? "wrap_line_ok(P, " + F + ", " + D + ", " + std::to_string(reach_of(o)) + ")"
                                  : "warp_all(fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + D +
                                        ", I[" + D + "]))";
@@ -355,7 +363,7 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
     e << "template <class T>\n__device__ __forceinline__ T gt" << K
       << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) {\n"
       << "    if (" << cond << ") {\n"
-      << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int;\n"
+      << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int" << wrow << ";\n"
       << "        const T* __restrict__ b = u + (long long)" << F << " * P.ncell + c;\n"
       << "        const long long s = gstride(P, " << D << ");\n";
     if (nz.empty()) {
@@ -377,7 +385,7 @@ void emit_linear(Emitter& e, const mol_problem_desc* d, int k) {
       << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p, "
          "T g, T* lam_u, T* lp, T* lam_aux, T& own) {\n"
       << "    if (" << cond << ") {\n"
-      << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int;\n"
+      << "        const T* __restrict__ w = P.w + P.ops[" << tm.op << "].w_int" << wrow << ";\n"
       << "        T* b = lam_u + (long long)" << F << " * P.ncell + c;\n"
       << "        const long long s = gstride(P, " << D << ");\n";
     if (!nz.empty()) {
@@ -805,7 +813,8 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
         LinInfo L;
         if (in.op == MOL_OP_TERM) {
             const mol_term& tm = d->terms[in.imm];
-            if (tm.kind == MOL_TERM_LINEAR || tm.kind == MOL_TERM_MIXED) {
+            // per-point rows (nonuniform grid) have no compile-time tap weights: not fused
+            if ((tm.kind == MOL_TERM_LINEAR && d->ops[tm.op].nrows == 0) || tm.kind == MOL_TERM_MIXED) {
                 L.ok = true;
                 L.field = tm.field;
                 L.coef[in.imm] = "T(1)";

@@ -444,9 +444,10 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
     if (d->nops < 0 || (d->nops && !d->ops)) return set_err(plan, MOL_ERR_INVALID, "ops");
     for (int i = 0; i < d->nops; ++i) {
         const mol_op1d& o = d->ops[i];
-        if (o.L < 0 || o.nlo < 0 || o.nhi < 0 || o.bLlo < 0 || o.bLhi < 0 || o.hi_base < 0 || o.hi_base > 1)
+        if (o.L < 0 || o.nlo < 0 || o.nhi < 0 || o.bLlo < 0 || o.bLhi < 0 || o.hi_base < 0 || o.hi_base > 1 ||
+            o.nrows < 0)
             return set_err(plan, MOL_ERR_INVALID, "operator sizes");
-        if (o.w_int < 0 || o.w_int + o.L > d->nweights || o.w_lo < 0 ||
+        if (o.w_int < 0 || o.w_int + (long long)std::max(1, o.nrows) * o.L > d->nweights || o.w_lo < 0 ||
             o.w_lo + (long long)o.nlo * o.bLlo > d->nweights || o.w_hi < 0 ||
             o.w_hi + (long long)o.nhi * o.bLhi > d->nweights)
             return set_err(plan, MOL_ERR_INVALID, "operator weights out of the pool");
@@ -457,11 +458,23 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
         if (t.field < 0 || t.field >= d->nfields || t.dim < 0 || t.dim >= d->ndim)
             return set_err(plan, MOL_ERR_INVALID, "term field/dim");
         auto opok = [&](int o) { return o >= 0 && o < d->nops; };
+        auto rows = [&](int o) { return opok(o) && d->ops[o].nrows > 0; };
         switch (t.kind) {
-            case MOL_TERM_LINEAR: if (!opok(t.op)) return set_err(plan, MOL_ERR_INVALID, "term op"); break;
+            case MOL_TERM_LINEAR:
+                if (!opok(t.op)) return set_err(plan, MOL_ERR_INVALID, "term op");
+                if (rows(t.op)) {
+                    const mol_op1d& o = d->ops[t.op];
+                    if (d->bc[t.field][t.dim][0].kind == MOL_BC_PERIODIC)
+                        return set_err(plan, MOL_ERR_UNSUPPORTED, "per-point operator rows on a periodic dimension");
+                    if (o.nrows != d->npts[t.dim] - o.nlo - o.nhi)
+                        return set_err(plan, MOL_ERR_INVALID, "operator rows do not match the grid");
+                }
+                break;
             case MOL_TERM_MIXED:
                 if (!opok(t.op) || !opok(t.op2) || t.dim2 < 0 || t.dim2 >= d->ndim || t.dim2 == t.dim)
                     return set_err(plan, MOL_ERR_INVALID, "mixed term");
+                if (rows(t.op) || rows(t.op2))
+                    return set_err(plan, MOL_ERR_UNSUPPORTED, "mixed derivatives with per-point operator rows");
                 break;
             case MOL_TERM_WENO:
                 if (!(t.dx > 0)) return set_err(plan, MOL_ERR_INVALID, "weno dx");
@@ -473,6 +486,8 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
                 break;
             case MOL_TERM_NONLINLAP:
                 if (!opok(t.op) || !opok(t.op2) || !opok(t.op3)) return set_err(plan, MOL_ERR_INVALID, "nonlinlap ops");
+                if (rows(t.op) || rows(t.op2) || rows(t.op3))
+                    return set_err(plan, MOL_ERR_UNSUPPORTED, "nonlinear Laplacian with per-point operator rows");
                 if (t.prog >= 0) {
                     int st = validate_prog(plan, d, t.prog, 1, MOL_MAX_REGS, 0, &t);
                     if (st) return st;

@@ -35,7 +35,7 @@ LOSS_MISFIT, LOSS_LAMBDA = 0, 1
 
 class mol_op1d(C.Structure):
     _fields_ = [("L", C.c_int32), ("omin", C.c_int32), ("nlo", C.c_int32), ("bLlo", C.c_int32),
-                ("nhi", C.c_int32), ("bLhi", C.c_int32), ("hi_base", C.c_int32), ("reserved", C.c_int32),
+                ("nhi", C.c_int32), ("bLhi", C.c_int32), ("hi_base", C.c_int32), ("nrows", C.c_int32),
                 ("w_int", C.c_int64), ("w_lo", C.c_int64), ("w_hi", C.c_int64)]
 
 

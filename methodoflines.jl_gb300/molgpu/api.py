@@ -44,7 +44,11 @@ class WENOScheme:
 
 class MOLFiniteDifference:
     """``MOLFiniteDifference(dxs, time; approx_order, advection_scheme, grid_align, ...)``
-    (src/interface/MOLFiniteDifference.jl:31-76).  Only the options the GPU path honours are kept."""
+    (src/interface/MOLFiniteDifference.jl:31-76).  Only the options the GPU path honours are kept.
+
+    ``dxs`` maps each spatial variable to a number of points (int), a step (float) or the
+    grid's points (a sequence, a nonuniform grid: centered derivatives and boundary rows
+    along it use per-point weights, centered_diff_weights.jl:77-153)."""
 
     def __init__(self, dxs, time: Optional[IV] = None, approx_order: int = 2, advection_scheme=None,
                  grid_align: str = "center", **kwargs):

@@ -26,7 +26,7 @@ from typing import Dict, List, Optional, Tuple
 import numpy as np
 
 from . import _lib as L
-from .weights import Operator, centered, half_centered, select, upwind, wrap
+from .weights import Operator, centered, centered_nonuniform, half_centered, select, upwind, wrap
 
 # ------------------------------------------------------------------------------------
 # grids (Julia Float64 ranges)
@@ -75,17 +75,30 @@ def grid_points(lo: float, step: float, hi: float) -> np.ndarray:
     return np.array([float(flo + k * fst) for k in range(n)])
 
 
-def make_axis(lo: float, hi: float, dxspec) -> Tuple[np.ndarray, float]:
+def make_axis(lo: float, hi: float, dxspec) -> Tuple[np.ndarray, float, bool]:
+    """One dimension's grid (``discretize_space``, discretize_vars.jl:218-233): (points, step,
+    uniform).
+
+    An integer is a number of points and a float a step; the grid is then ``lo:dx:hi`` and
+    its operators are the uniform tables.  When the step does not reach ``hi`` exactly the
+    reference appends ``hi``; the grid is then a Vector, and so is a grid given as a
+    sequence of points: every operator along it is built from the points themselves
+    (differential_discretizer.jl:45-58, centered_diff_weights.jl:77-153)."""
     if isinstance(dxspec, (int, np.integer)) and not isinstance(dxspec, bool):
         dx = (hi - lo) / (int(dxspec) - 1)
-    else:
+    elif isinstance(dxspec, (float, np.floating)):
         dx = float(dxspec)
+    else:
+        g = np.array([float(v) for v in dxspec], dtype=np.float64)
+        if g.ndim != 1 or len(g) < 2 or not np.all(np.diff(g) > 0):
+            raise ValueError("a grid given as points must be strictly increasing, with at least two points")
+        if g[-1] != hi:
+            g = np.append(g, hi)
+        return g, float(g[1] - g[0]), False
     g = grid_points(lo, dx, hi)
     if g[-1] != hi:
-        raise NotImplementedError(
-            "dx does not divide the domain; the reference then appends the end point and the grid becomes "
-            "nonuniform (nonuniform grids are not built)")
-    return g, dx
+        return np.append(g, hi), dx, False
+    return g, dx, True
 
 
 # ------------------------------------------------------------------------------------
@@ -331,6 +344,7 @@ class Lowered:
     bcs: Dict[tuple, dict] = field(default_factory=dict)
     u0: Optional[np.ndarray] = None
     spec: Optional[dict] = None
+    uniform: List[bool] = field(default_factory=list)
 
     # -- registries
     def const(self, v: float) -> int:
@@ -348,7 +362,13 @@ class Lowered:
         key = (kind, j, d, p)
         if key not in self.op_keys:
             dx = self.dx[j]
-            if kind == "centered":
+            if self.uniform and not self.uniform[j]:
+                if kind != "centered":
+                    raise NotImplementedError(
+                        f"{kind} operators on the nonuniform grid of {self.ivs[j]} are not built "
+                        "(centered derivatives and boundary rows are)")
+                o = centered_nonuniform(d, self.order, self.grids[j])
+            elif kind == "centered":
                 o = centered(d, self.order, dx)
             elif kind == "wind_pos":       # offside d+p-1: backward taps (windmap[2])
                 o = upwind(d, p, dx, d + p - 1)
@@ -436,12 +456,13 @@ class _Lowerer:
         disc = spec["disc"]
         if disc.get("grid_align", "center") != "center":
             raise NotImplementedError("only center-aligned grids are built")
-        grids, dxs = [], []
+        grids, dxs, uniform = [], [], []
         for x in ivs:
             lo, hi = spec["domain"][x]
-            g, dx = make_axis(float(lo), float(hi), disc["dxs"][x])
+            g, dx, uni = make_axis(float(lo), float(hi), disc["dxs"][x])
             grids.append(g)
             dxs.append(dx)
+            uniform.append(uni)
         npts = [len(g) for g in grids]
         periodic = {f: [False] * len(ivs) for f in fields}
         bcs = {}
@@ -466,7 +487,11 @@ class _Lowerer:
                           param_values=np.array([float(p[1]) for p in params], dtype=np.float64),
                           grids=grids, dx=dxs, npts=npts, lower=lower, upper=upper, periodic=periodic,
                           functions=dict(spec.get("functions", {})), order=int(disc.get("approx_order", 2)),
-                          adv=adv, spec=spec)
+                          adv=adv, spec=spec, uniform=uniform)
+        for j in range(len(ivs)):
+            if not uniform[j] and any(periodic[f][j] for f in fields):
+                # centered_difference.jl:36 asserts that no interface boundary meets a nonuniform dimension
+                raise NotImplementedError(f"periodic boundaries on the nonuniform grid of {ivs[j]}")
         self.bcs = bcs
         if self.lw.order % 2:
             # MOLFiniteDifference warns and keeps the odd order (MOLFiniteDifference.jl:56-58)
@@ -482,6 +507,8 @@ class _Lowerer:
             if d % 2 == 0:
                 return lw.term(kind=L.TERM_LINEAR, field=f, dim=j, op=lw.op("centered", j, d))
             if lw.adv[0] == "weno" and d == 1:
+                if not lw.uniform[j]:
+                    raise NotImplementedError(f"WENO on the nonuniform grid of {x} is not built")
                 return lw.term(kind=L.TERM_WENO, field=f, dim=j, eps=float(lw.adv[1]), dx=lw.dx[j])
             # bare odd derivative: positive wind (upwind_difference.jl:278-302)
             p = int(lw.adv[1]) if lw.adv[0] == "upwind" else 1
@@ -489,6 +516,8 @@ class _Lowerer:
         if arg[0] == "D" and d == 1 and arg[2] == 1 and arg[3][0] == "field":
             k = lw.ivs.index(arg[1])
             f = lw.fields.index(arg[3][1])
+            if not (lw.uniform[j] and lw.uniform[k]):
+                raise NotImplementedError("mixed derivatives on a nonuniform grid are not built")
             return lw.term(kind=L.TERM_MIXED, field=f, dim=j, dim2=k, op=lw.op("centered", j, 1),
                            op2=lw.op("centered", k, 1))
         if d == 1:
@@ -783,7 +812,12 @@ class Descriptor:
             r = ops[i]
             r.L, r.omin, r.nlo, r.bLlo, r.nhi, r.bLhi, r.hi_base = o.L, o.omin, o.nlo, o.bLlo, o.nhi, o.bLhi, o.hi_base
             r.w_int = len(pool)
-            pool += list(o.interior)
+            if o.rows is not None:          # nonuniform grid: one interior row per interior point
+                r.nrows = len(o.rows)
+                for w in o.rows:
+                    pool += list(w)
+            else:
+                pool += list(o.interior)
             r.w_lo = len(pool)
             for w in o.low:
                 pool += list(w)

@@ -10,6 +10,12 @@ come from ``numpy.random.Generator(PCG64(seed))`` in Float64.
 3. burgers       u_t = -u u_x + nu u_xx, periodic, WENO5 (Convection_WENO tests)
 4. nonlinear_diffusion   u_t = div(u^2 grad u) + k u (1-u), Neumann 0 (ensemble member)
 5. adr3d         u_t = div(K grad u) + 0.3 u_xy - c.grad u - lambda u^2, periodic x,y, Dirichlet z
+6. stretched_reaction_diffusion   u_t = u_xx - k u^2 + s(x), grid clustered at both ends
+                 (a grid given as points), Robin left, Neumann right
+7. neumann_cosine                 u_t = u_xx on [0, pi], homogeneous Neumann, u0 = cos x
+                 (test/Diffusion/MOL_1D_Linear_Diffusion.jl, Test 03), points given as a vector
+8. stretched_2d                   u_t = u_xx + u_yy + 0.1 u, x stretched (Robin/Neumann),
+                 y uniform (Dirichlet with data)
 """
 from __future__ import annotations
 
@@ -196,3 +202,60 @@ def adr3d(N: int = 256, nz_pts: int = 258, seed_k: int = 11, target_seed: int = 
     dt = 0.4 / (1.5 / dx + 2 * (3 * kmax + 0.3) / min(dx, dz) ** 2)
     rt = _rng(target_seed)
     return sys, disc, {"dt": float(dt), "target_seed": target_seed, "K": Kfun, "rng_target": rt}
+
+
+def stretched_points(n: int, lo: float = 0.0, hi: float = 1.0, beta: float = 2.5) -> np.ndarray:
+    """n points on [lo, hi] clustered towards both ends (tanh stretching of k / (n - 1))."""
+    s = np.arange(n, dtype=np.float64) / (n - 1)
+    x = lo + (hi - lo) * 0.5 * (1.0 + np.tanh(beta * (s - 0.5)) / math.tanh(0.5 * beta))
+    x[0], x[-1] = lo, hi
+    return x
+
+
+def stretched_reaction_diffusion(n: int = 201, order: int = 2, beta: float = 2.5):
+    """Reaction-diffusion on a grid given as points (nonuniform centered operators,
+    centered_diff_weights.jl:77-153), Robin row at x = 0 and Neumann row at x = 1."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dxx = Differential(t), Differential(x), Differential(x) ** 2
+    k = Param("k", 2.0)
+    eq = Eq(Dt(u(x, t)), Dxx(u(x, t)) - k * u(x, t) * u(x, t) + sin(math.pi * x))
+    bcs = [Eq(u(x, 0.0), 1.0 + 0.5 * cos(3.0 * x)), Eq(2.0 * u(0.0, t) + 3.0 * Dx(u(0.0, t)), k * t),
+           Eq(Dx(u(1.0, t)), 0.5)]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [k])
+    pts = stretched_points(n, 0.0, 1.0, beta)
+    disc = MOLFiniteDifference({x: pts}, t, approx_order=order)
+    h = float(np.min(np.diff(pts)))
+    return sys, disc, {"dt": 0.1 * h * h, "points": pts}
+
+
+def neumann_cosine(n: int = 300, order: int = 8):
+    """u_t = u_xx, u0 = cos x, u_x = 0 at both ends of [0, pi]: the reference's linear-diffusion
+    Test 03 (exact solution exp(-t) cos x), with the grid given as its n points."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dxx = Differential(t), Differential(x), Differential(x) ** 2
+    eq = Eq(Dt(u(x, t)), Dxx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), cos(x)), Eq(Dx(u(0.0, t)), 0.0), Eq(Dx(u(math.pi, t)), 0.0)]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, math.pi))], [t, x], [u(x, t)], [])
+    pts = np.array([math.pi * k / (n - 1) for k in range(n)])
+    disc = MOLFiniteDifference({x: pts}, t, approx_order=order)
+    h = math.pi / (n - 1)
+    return sys, disc, {"dt": 0.05 * h * h, "points": pts}
+
+
+def stretched_2d(nx: int = 48, ny: int = 40, order: int = 2, beta: float = 2.0):
+    """2-D diffusion with x on stretched points (nonuniform) and y uniform."""
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dxx, Dyy = Differential(t), Differential(x), Differential(x) ** 2, Differential(y) ** 2
+    eq = Eq(Dt(u(x, y, t)), Dxx(u(x, y, t)) + Dyy(u(x, y, t)) + 0.1 * u(x, y, t))
+    bcs = [Eq(u(x, y, 0.0), 1.0 + 0.3 * cos(2.0 * x) * sin(3.0 * y)),
+           Eq(u(0.0, y, t) + 0.5 * Dx(u(0.0, y, t)), 1.0), Eq(Dx(u(1.0, y, t)), 0.0),
+           Eq(u(x, 0.0, t), 1.0), Eq(u(x, 1.0, t), 1.0 + t)]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0))],
+                    [t, x, y], [u(x, y, t)], [])
+    pts = stretched_points(nx, 0.0, 1.0, beta)
+    disc = MOLFiniteDifference({x: pts, y: 1.0 / (ny - 1)}, t, approx_order=order)
+    h = min(float(np.min(np.diff(pts))), 1.0 / (ny - 1))
+    return sys, disc, {"dt": 0.1 * h * h, "points": pts}

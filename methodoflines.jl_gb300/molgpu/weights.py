@@ -12,7 +12,7 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 from fractions import Fraction
-from typing import List, Sequence, Tuple
+from typing import Optional, List, Sequence, Tuple
 
 
 def fornberg(m: int, z: float, nodes: Sequence[float]) -> List[float]:
@@ -78,6 +78,9 @@ class Operator:
     bLlo: int
     bLhi: int
     hi_base: int = 0
+    # nonuniform grids: one interior row per interior position (rows[k] at position nlo+1+k);
+    # `interior` is then rows[0]
+    rows: Optional[List[List[float]]] = None
 
     @property
     def nlo(self):
@@ -98,6 +101,34 @@ def centered(d: int, p: int, dx: float) -> Operator:
     sg = -1.0 if d % 2 else 1.0
     high = [[sg * w for w in lw[::-1]] for lw in low]
     return Operator(L, -h, inner, low, high, bl, bl, 0)
+
+
+def centered_nonuniform(d: int, p: int, x: Sequence[float]) -> Operator:
+    """``CompleteCenteredDifference(d, p, x::AbstractVector)``
+    (centered_difference/centered_diff_weights.jl:77-153): Fornberg weights on the grid's own
+    nodes, one interior row per interior point; boundary rows on the first / last bL nodes
+    taken relative to the first (resp. the one before the last bL) node, as the reference's
+    cumulative sums of the spacings give them."""
+    x = [float(v) for v in x]
+    L = d + p - 1 + (d + p) % 2
+    bl = d + p
+    h = L // 2
+    n = len(x)
+    if n < bl + 1 or n < L:
+        raise NotImplementedError("nonuniform grid too short for the stencil")
+    dxv = [x[i + 1] - x[i] for i in range(n - 1)]
+    rows = [fornberg(d, x[i], x[i - h:i + h + 1]) for i in range(h, n - h)]
+    low_x = [0.0]
+    for v in dxv[:bl - 1]:
+        low_x.append(low_x[-1] + v)
+    high_x = []
+    acc = 0.0
+    for k, v in enumerate(dxv[n - 1 - bl:]):
+        acc = v if k == 0 else acc + v
+        high_x.append(acc)
+    low = [fornberg(d, low_x[i], low_x) for i in range(h)]
+    high = [fornberg(d, high_x[bl - 1 - i], high_x) for i in range(h)]
+    return Operator(L, -h, rows[0], low, high, bl, bl, 0, rows)
 
 
 def upwind(d: int, p: int, dx: float, offside: int) -> Operator:
@@ -132,7 +163,8 @@ def select(op: Operator, i: int, length: int, periodic: bool) -> Tuple[List[floa
         return op.low[i - 1], list(range(1, op.bLlo + 1))
     if not periodic and i > length - op.nhi:
         return op.high[length - i - op.hi_base], list(range(length - op.bLhi + 1, length + 1))
-    return op.interior, list(range(i + op.omin, i + op.omin + op.L))
+    w = op.rows[i - op.nlo - 1] if op.rows is not None else op.interior
+    return w, list(range(i + op.omin, i + op.omin + op.L))
 
 
 def wrap(i: int, l: int) -> int:

@@ -127,6 +127,40 @@ def complete_centered_difference(d: int, p: int, dx: float) -> DerivativeOperato
     return DerivativeOperator(d, p, dx, L, stencil, bL, bpc, low, high, 0, "centered")
 
 
+def complete_centered_difference_nonuniform(d: int, p: int, x: Sequence[float]) -> DerivativeOperator:
+    """``CompleteCenteredDifference(d, p, x::AbstractVector)``,
+    ``centered_difference/centered_diff_weights.jl:77-153``.
+
+    ``stencil_coefs`` is then a list with one row per interior point (points
+    bpc+1 .. len-bpc, 1-based), each the Fornberg weights at x[i] on x[i-bpc .. i+bpc].
+    The boundary rows use node coordinates rebuilt from the spacings: the low rows
+    ``[0; cumsum(dx[1:bL-1])]`` evaluated at their first bpc nodes, the high rows
+    ``cumsum(dx[end-bL+1:end])`` evaluated at their last bpc nodes, last node first.
+    ``cumsum`` of a Vector is a sequential left fold.  No 1/dx^d scaling: the nodes carry
+    the physical coordinates.
+    """
+    x = [float(v) for v in x]
+    L = d + p - 1 + (d + p) % 2
+    bL = d + p
+    bpc = L // 2
+    n = len(x)
+    dxs = [x[i + 1] - x[i] for i in range(n - 1)]
+
+    def cumsum(v):
+        out, acc = [], None
+        for a in v:
+            acc = a if acc is None else acc + a
+            out.append(acc)
+        return out
+
+    low_x = [0.0] + cumsum(dxs[:bL - 1])
+    high_x = cumsum(dxs[len(dxs) - bL:])
+    stencil = [calculate_weights(d, x[i - 1], x[i - 1 - bpc:i + bpc]) for i in range(bpc + 1, n - bpc + 1)]
+    low = [calculate_weights(d, low_x[k], low_x) for k in range(bpc)]
+    high = [calculate_weights(d, high_x[len(high_x) - 1 - k], high_x) for k in range(bpc)]
+    return DerivativeOperator(d, p, float("nan"), L, stencil, bL, bpc, low, high, 0, "centered_nonuniform")
+
+
 def complete_upwind_difference(d: int, p: int, dx: float, offside: int = 0) -> DerivativeOperator:
     """``CompleteUpwindDifference``, ``upwind_difference/upwind_diff_weights.jl:4-91``."""
     assert offside > -1

@@ -17,7 +17,8 @@ from typing import Dict, List, Tuple
 
 import numpy as np
 
-from .fornberg import (complete_centered_difference, complete_half_centered_difference,
+from .fornberg import (complete_centered_difference, complete_centered_difference_nonuniform,
+                       complete_half_centered_difference,
                        complete_upwind_difference)
 
 # --------------------------------------------------------------------------------------
@@ -74,16 +75,25 @@ def julia_float_range(start: float, step: float, stop: float) -> np.ndarray:
     return np.array([float(fs + k * fst) for k in range(ln)])
 
 
-def make_grid(lo: float, hi: float, dx_spec) -> Tuple[np.ndarray, float]:
-    """``discretize_space`` + ``prepare_dx`` for a center-aligned grid."""
+def make_grid(lo: float, hi: float, dx_spec) -> Tuple[np.ndarray, float, bool]:
+    """``discretize_space`` + ``prepare_dx`` for a center-aligned grid
+    (discretize_vars.jl:218-233, :283-285): (points, step, uniform).  A step that does not
+    reach ``hi`` gets ``hi`` appended, and a grid given as points is taken as it is (with
+    ``hi`` appended the same way); both are Vectors, whose operators the reference builds
+    from the points (differential_discretizer.jl:45-58)."""
     if isinstance(dx_spec, (int, np.integer)) and not isinstance(dx_spec, bool):
         dx = (hi - lo) / (int(dx_spec) - 1)
-    else:
+    elif isinstance(dx_spec, (float, np.floating)):
         dx = float(dx_spec)
+    else:
+        g = np.array([float(v) for v in dx_spec])
+        if g[-1] != hi:
+            g = np.append(g, hi)
+        return g, float("nan"), False
     g = julia_float_range(lo, dx, hi)
     if g[-1] != hi:
-        g = np.append(g, hi)
-    return g, dx
+        return np.append(g, hi), dx, False
+    return g, dx, True
 
 
 # --------------------------------------------------------------------------------------
@@ -111,6 +121,9 @@ def central_taps(D, i: int, n: int, periodic: bool):
         return list(D.high_boundary_coefs[n - i]), [n - bL + 1 + k for k in range(bL)]
     half = D.stencil_length // 2
     taps = [i + k for k in range(-half, half + 1)]
+    if D.kind == "centered_nonuniform":   # centered_difference.jl:51-53: the point's own row
+        assert not periodic, "interface boundaries are not supported on nonuniform dimensions"
+        return list(D.stencil_coefs[i - bpc - 1]), taps
     if periodic:
         taps = [wrap_periodic(t, n) for t in taps]
     return list(D.stencil_coefs), taps
@@ -242,9 +255,11 @@ class OracleProblem:
         # grids
         self.grid = []
         self.dx = []
+        self.uniform = []
         for x in self.ivs:
             lo, hi = spec["domain"][x]
-            g, dx = make_grid(float(lo), float(hi), disc["dxs"][x])
+            g, dx, uni = make_grid(float(lo), float(hi), disc["dxs"][x])
+            self.uniform.append(uni)
             self.grid.append(g)
             self.dx.append(dx)
         self.npts = [len(g) for g in self.grid]
@@ -289,7 +304,11 @@ class OracleProblem:
         key = (kind, j, d, extra)
         if key not in self._ops:
             dx = self.dx[j]
-            if kind == "centered":
+            if not self.uniform[j]:
+                if kind != "centered":
+                    raise NotImplementedError(f"oracle: {kind} operators on a nonuniform grid")
+                D = complete_centered_difference_nonuniform(d, self.order, self.grid[j])
+            elif kind == "centered":
                 D = complete_centered_difference(d, self.order, dx)
             elif kind == "wind_neg":        # windmap[1]: offside 0, used when !ispositive
                 D = complete_upwind_difference(d, int(extra), dx, 0)

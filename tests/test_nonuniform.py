@@ -1,0 +1,237 @@
+"""Nonuniform grids (a grid given as points, or a step that does not reach the domain's end):
+per-point centered weight rows and their boundary rows, against the oracle's restatement of
+CompleteCenteredDifference(d, p, x::AbstractVector) (centered_diff_weights.jl:77-153) and the
+nonuniform tap selection (centered_difference.jl:32-56).  CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+from desc_interp import DescInterp
+from molgpu import lower, problems
+from molgpu import _lib as L
+from molgpu.lowering import make_axis
+from molgpu.weights import centered, centered_nonuniform
+from oracle.fornberg import calculate_weights, complete_centered_difference_nonuniform
+from oracle.mol_oracle import OracleProblem, make_grid
+
+
+def _jittered(n, seed):
+    r = np.random.default_rng(seed)
+    x = np.concatenate([[0.0], np.cumsum(r.uniform(0.4, 1.6, n - 1))])
+    return x / x[-1]
+
+
+@pytest.mark.parametrize("d", [1, 2, 3, 4])
+@pytest.mark.parametrize("p", [2, 4, 6, 8])
+def test_nonuniform_tables_bit_identical_to_oracle(d, p):
+    for seed in (0, 1):
+        x = _jittered(40, seed)
+        a = centered_nonuniform(d, p, x)
+        b = complete_centered_difference_nonuniform(d, p, x)
+        assert a.rows == b.stencil_coefs
+        assert a.low == b.low_boundary_coefs and a.high == b.high_boundary_coefs
+        assert a.interior == b.stencil_coefs[0]
+        assert len(a.rows) == len(x) - 2 * (a.L // 2)
+
+
+@pytest.mark.parametrize("d,p", [(1, 2), (2, 2), (2, 4), (2, 8), (3, 4), (4, 6)])
+def test_integer_grid_reduces_to_uniform_tables(d, p):
+    """On the points 0, 1, ..., n-1 every interior row is the uniform interior row bit for
+    bit (the same differences enter Fornberg's recursion) and the low rows are the uniform
+    low rows; the high rows equal the uniform (mirrored) ones to rounding."""
+    a = centered_nonuniform(d, p, list(range(30)))
+    u = centered(d, p, 1.0)
+    assert all(r == u.interior for r in a.rows)
+    assert a.low == u.low
+    for ra, ru in zip(a.high, u.high):
+        assert np.allclose(ra, ru, rtol=0, atol=1e-11 * max(map(abs, ru)))
+
+
+@pytest.mark.parametrize("d,p", [(1, 2), (1, 4), (2, 2), (2, 4), (2, 6)])
+def test_rows_are_exact_on_polynomials(d, p):
+    """Each row differentiates polynomials of degree below its tap count exactly (to rounding)
+    at its own point: interior rows at x_i, low rows at the first nodes, high rows at the last."""
+    x = _jittered(25, 3)
+    op = centered_nonuniform(d, p, x)
+    h = op.L // 2
+    deg = op.L - 1
+    c = np.random.default_rng(5).standard_normal(deg + 1)
+    poly = np.polynomial.Polynomial(c)
+    dpoly = poly.deriv(d)
+    for k, row in enumerate(op.rows):
+        i = h + k
+        got = float(np.dot(row, poly(x[i - h:i + h + 1])))
+        assert abs(got - dpoly(x[i])) <= 1e-7 * (1 + abs(dpoly(x[i]))), (k, got, dpoly(x[i]))
+    bl = op.bLlo
+    degb = bl - 1
+    cb = np.random.default_rng(6).standard_normal(degb + 1)
+    pb = np.polynomial.Polynomial(cb)
+    dpb = pb.deriv(d)
+    for k, row in enumerate(op.low):
+        got = float(np.dot(row, pb(x[:bl] - x[0])))
+        assert abs(got - dpb(x[k] - x[0])) <= 1e-6 * (1 + abs(dpb(x[k] - x[0])))
+    n = len(x)
+    for k, row in enumerate(op.high):     # high[k]: point n-1-k (0-based), nodes n-bl .. n-1
+        base = x[n - 1 - bl]
+        got = float(np.dot(row, pb(x[n - bl:] - base)))
+        want = dpb(x[n - 1 - k] - base)
+        assert abs(got - want) <= 1e-6 * (1 + abs(want))
+
+
+def test_fornberg_golden_values_on_given_nodes():
+    """The reference's own known answers for calculate_weights on explicit node vectors
+    (test/Components/MOLfornberg_weights.jl:5-31), which the nonuniform rows are made of."""
+    assert calculate_weights(2, 0.0, [-1, 0, 1.0]) == [1, -2, 1]
+    assert calculate_weights(1, 0.0, [-1.0, 1.0]) == [-0.5, 0.5]
+    assert calculate_weights(1, 0.0, [0, 1]) == [-1, 1]
+    assert calculate_weights(1, 1.0, [0, 1]) == [-1, 1]
+    assert calculate_weights(3, 0.0, [0, 1, 2, 3, 4, 5]) == [-17 / 4, 71 / 4, -59 / 2, 49 / 2, -41 / 4, 7 / 4]
+
+
+def test_grid_forms():
+    """An integer or a dividing step gives the uniform grid; a step that misses the end gets
+    the end appended (a nonuniform grid, discretize_vars.jl:224-230); points are taken as
+    given, with the end appended when missing."""
+    g, dx, uni = make_axis(0.0, 1.0, 11)
+    assert uni and len(g) == 11
+    g, dx, uni = make_axis(0.0, 1.0, 0.03)
+    assert not uni and g[-1] == 1.0 and g[-2] == pytest.approx(0.99) and len(g) == 35
+    g2, _, uni2 = make_grid(0.0, 1.0, 0.03)
+    assert not uni2 and np.array_equal(g, g2)
+    g, _, uni = make_axis(0.0, 1.0, [0.0, 0.1, 0.5, 0.7])
+    assert not uni and list(g) == [0.0, 0.1, 0.5, 0.7, 1.0]
+    with pytest.raises(ValueError):
+        make_axis(0.0, 1.0, [0.0, 0.5, 0.4, 1.0])
+
+
+def _appended_end():
+    from molgpu.api import MOLFiniteDifference
+    from molgpu.symbolic import Differential, Eq, Field, Interval, IV, PDESystem, sin
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    s = PDESystem([Eq(Differential(t)(u(x, t)), (Differential(x) ** 2)(u(x, t)))],
+                  [Eq(u(x, 0.0), sin(math.pi * x)), Eq(u(0.0, t), 0.0), Eq(u(1.0, t), t)],
+                  [(t, Interval(0, 1)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)])
+    return s.to_spec(MOLFiniteDifference({x: 0.03}, t, approx_order=4))
+
+
+CASES = {
+    "stretched_o2": lambda: problems.stretched_reaction_diffusion(n=41, order=2)[:2],
+    "stretched_o4": lambda: problems.stretched_reaction_diffusion(n=41, order=4)[:2],
+    "stretched_o6": lambda: problems.stretched_reaction_diffusion(n=41, order=6)[:2],
+    "neumann_cosine_o8": lambda: problems.neumann_cosine(n=40, order=8)[:2],
+    "stretched_2d": lambda: problems.stretched_2d(nx=14, ny=11)[:2],
+}
+
+
+def _spec(name):
+    if name == "appended_end":
+        return _appended_end()
+    s, d = CASES[name]()
+    return s.to_spec(d)
+
+
+@pytest.mark.parametrize("name", sorted(CASES) + ["appended_end"])
+def test_descriptor_semantics_match_oracle_nonuniform(name):
+    spec = _spec(name)
+    lw = lower(spec)
+    orc = OracleProblem(spec)
+    assert not all(lw.uniform)
+    assert lw.n_unknowns == orc.n_unknowns
+    assert np.array_equal(lw.u0, orc.initial_condition())
+    assert any(o.rows is not None for o in lw.ops)
+    di = DescInterp(lw)
+    u = lw.u0 + 0.01 * np.random.default_rng(0).standard_normal(lw.n_unknowns)
+    for t in (0.3, 1.5):
+        a, b = orc.rhs(u, t), di.rhs(u, t)
+        assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a), (name, t)
+
+
+def test_neumann_cosine_tracks_exact_solution():
+    """Order 8 on 40 given points: the semi-discrete RHS of cos x is -cos x to high accuracy
+    (the reference's Test 03 compares the solution with exp(-t) cos x)."""
+    s, d, _ = problems.neumann_cosine(n=40, order=8)
+    spec = s.to_spec(d)
+    orc = OracleProblem(spec)
+    lw = lower(spec)
+    x = lw.grids[0][lw.lower[0]:lw.npts[0] - lw.upper[0]]
+    du = DescInterp(lw).rhs(np.cos(x), 0.0)
+    assert np.max(np.abs(du + np.cos(x))) < 1e-6
+    assert np.allclose(orc.rhs(np.cos(x), 0.0), du, rtol=0, atol=1e-12)
+
+
+def test_descriptor_carries_rows():
+    from molgpu import Descriptor
+    s, d, _ = problems.stretched_reaction_diffusion(n=41, order=4)
+    lw = lower(s.to_spec(d))
+    D = Descriptor(lw)
+    ops = [D.desc.ops[i] for i in range(D.desc.nops)]
+    rows = [o for o in ops if o.nrows > 0]
+    assert rows and all(o.nrows == lw.npts[0] - o.nlo - o.nhi for o in rows)
+    o = rows[0]
+    assert D.weights[o.w_int + o.L] == lw.ops[[i for i, q in enumerate(ops) if q.nrows][0]].rows[1][0]
+
+
+def _unsupported(kind):
+    from molgpu.api import MOLFiniteDifference, WENOScheme
+    from molgpu.symbolic import Differential, Eq, Field, Interval, IV, PDESystem, sin
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u = Field("u")
+    Dt, Dx = Differential(t), Differential(x)
+    pts = problems.stretched_points(21)
+    if kind == "upwind":
+        eq, scheme = Eq(Dt(u(x, t)), -Dx(u(x, t))), None
+    elif kind == "weno":
+        eq, scheme = Eq(Dt(u(x, t)), -Dx(u(x, t))), WENOScheme()
+    elif kind == "nonlinlap":
+        eq, scheme = Eq(Dt(u(x, t)), Dx(u(x, t) * Dx(u(x, t)))), None
+    elif kind == "periodic":
+        eq, scheme = Eq(Dt(u(x, t)), (Dx ** 2)(u(x, t))), None
+    if kind == "mixed":
+        Dy = Differential(y)
+        s = PDESystem([Eq(Dt(u(x, y, t)), Dx(Dy(u(x, y, t))))],
+                      [Eq(u(x, y, 0.0), sin(x)), Eq(u(0.0, y, t), 0.0), Eq(u(1.0, y, t), 0.0),
+                       Eq(u(x, 0.0, t), 0.0), Eq(u(x, 1.0, t), 0.0)],
+                      [(t, Interval(0, 1)), (x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0))], [t, x, y],
+                      [u(x, y, t)])
+        return s.to_spec(MOLFiniteDifference({x: pts, y: 0.1}, t))
+    bcs = [Eq(u(x, 0.0), sin(x))]
+    bcs += [Eq(u(0.0, t), u(1.0, t))] if kind == "periodic" else [Eq(u(0.0, t), 0.0), Eq(u(1.0, t), 0.0)]
+    s = PDESystem([eq], bcs, [(t, Interval(0, 1)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)])
+    return s.to_spec(MOLFiniteDifference({x: pts}, t, advection_scheme=scheme))
+
+
+@pytest.mark.parametrize("kind", ["upwind", "weno", "nonlinlap", "periodic", "mixed"])
+def test_schemes_not_built_on_nonuniform_grids_are_refused(kind):
+    with pytest.raises(NotImplementedError):
+        lower(_unsupported(kind))
+
+
+def test_plan_validation_of_rows():
+    """A descriptor whose per-point rows do not match the grid fails at plan creation."""
+    from molgpu import Plan
+    s, d, _ = problems.stretched_reaction_diffusion(n=41, order=2)
+    lw = lower(s.to_spec(d))
+    op = [o for o in lw.ops if o.rows is not None][0]
+    op.rows = op.rows[:-1]
+    with pytest.raises(L.MolError) as e:
+        Plan(lw)
+    assert e.value.status == -1 and "rows" in str(e.value)
+
+
+def test_generated_code_reads_the_point_row():
+    """The generated interior fast path offsets the weights by the cell's own row, and the
+    code compiles for sm_103a (NVRTC, no device needed)."""
+    import ctypes as C
+    from molgpu import Descriptor
+    s, d, _ = problems.stretched_2d(nx=12, ny=9)
+    D = Descriptor(lower(s.to_spec(d)))
+    need = C.c_int64()
+    assert L.lib().mol_generate_code(C.byref(D.desc), None, 0, C.byref(need)) == 0
+    buf = C.create_string_buffer(need.value)
+    assert L.lib().mol_generate_code(C.byref(D.desc), buf, need.value, C.byref(need)) == 0
+    src = buf.value.decode()
+    assert ".w_int + (long long)(I[0] - 2) * 3" in src
+    log = C.create_string_buffer(1 << 16)
+    assert L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16) == 0, log.value.decode()
