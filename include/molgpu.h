@@ -114,7 +114,13 @@ typedef struct mol_bc {
     int32_t kind;
     int32_t prog;       /* -1: a,b,g below are constants; else program with outputs 0:a 1:b 2:g */
     int32_t op;         /* centered first-derivative operator whose boundary table the row uses */
-    int32_t reserved;
+    int32_t extrap;     /* 0, or 1 + the operator holding the extrapolation table of the point
+                           next to this boundary point (generate_extrap_eqs!, generate_bc_eqs.jl:
+                           336-392): when the interior stops two points from the end (WENO on a
+                           bounded uniform dimension, WENO.jl:94), point 2 (or n-1) is observed as
+                           sum_k w_k u[k] over the first (last) bL points with the second low (high)
+                           row of that operator, the boundary point through this row, which must
+                           then be a Dirichlet row (b == 0)                                     */
     double a, b, g;
 } mol_bc;
 

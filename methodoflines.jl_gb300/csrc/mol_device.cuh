@@ -35,10 +35,12 @@ struct SolverState {
 
 // One boundary row.  For rows with constant coefficients (prog < 0) the host also
 // stores inv = 1 / (a + b w_kb) (Robin/Neumann: the boundary value is
-// (g - b sum_{k != kb} w_k u_k) * inv) and c0 = g / a (Dirichlet, b == 0).
+// (g - b sum_{k != kb} w_k u_k) * inv) and c0 = g / a (Dirichlet, b == 0).  xop >= 0: the
+// point next to the boundary point is observed too, through row 1 of that operator's
+// low (high) extrapolation table (generate_extrap_eqs!, generate_bc_eqs.jl:336-392).
 template <class T>
 struct DevBC {
-    int kind, prog, op, pad;
+    int kind, prog, op, xop;
     T a, b, g;
     T inv, c0;
 };
@@ -165,9 +167,49 @@ __device__ __forceinline__ T load_pt(const DevProb<T>& P, const T* u, int f, int
 }
 
 template <class T>
+__device__ __noinline__ T bc_row_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t,
+                                       const T* p);
+
+// Extrapolation row of the point next to the boundary point (point 2, or n-1): the
+// second low (high) row of BoundaryInterpolatorExtrapolator(q) over the first (last) q
+// points, its own slot zero, the boundary point through its (Dirichlet) row
+// (generate_extrap_eqs!, generate_bc_eqs.jl:336-392; extrapolation_weights.jl:1-60).
+template <class T>
+__device__ __forceinline__ T extrap_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t,
+                                          const T* p) {
+    const DevBC<T>& B = P.bc[(f * 3 + dout) * 2 + side];
+    const mol_op1d& x = P.ops[B.xop];
+    const int n = P.n[dout], self = I[dout];
+    const T* w = side == 0 ? P.w + x.w_lo + x.bLlo : P.w + x.w_hi + x.bLhi;
+    const int first = side == 0 ? 1 : n - x.bLhi + 1;
+    const int cnt = side == 0 ? x.bLlo : x.bLhi;
+    const int qb = side == 0 ? 1 : n;
+    int J[3] = {I[0], I[1], I[2]};
+    T acc = T(0);
+    bool started = false;
+    for (int k = 0; k < cnt; ++k) {
+        const int q = first + k;
+        if (q == self) continue;
+        J[dout] = q;
+        const T v = q == qb ? bc_row_value(P, u, f, J, dout, side, t, p) : load_interior(P, u, f, J);
+        acc = started ? fma(w[k], v, acc) : w[k] * v;
+        started = true;
+    }
+    return acc;
+}
+
+template <class T>
 __device__ __noinline__ T bc_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t, const T* p) {
-    // boundary rows exist only on the boundary points themselves
-    if ((side == 0 && I[dout] != 1) || (side == 1 && I[dout] != P.n[dout])) return T(0);
+    const int i = I[dout], n = P.n[dout];
+    if ((side == 0 && i == 1) || (side == 1 && i == n)) return bc_row_value(P, u, f, I, dout, side, t, p);
+    if (P.bc[(f * 3 + dout) * 2 + side].xop >= 0 && ((side == 0 && i == 2) || (side == 1 && i == n - 1)))
+        return extrap_value(P, u, f, I, dout, side, t, p);
+    return T(0);
+}
+
+template <class T>
+__device__ __noinline__ T bc_row_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t,
+                                       const T* p) {
     const DevBC<T> B = P.bc[(f * 3 + dout) * 2 + side];
     if (B.kind != MOL_BC_ROBIN) return T(0);
     const bool dyn = B.prog >= 0;
@@ -304,6 +346,36 @@ __device__ __noinline__ T bc_line_value(const DevProb<T>& P, const T* __restrict
     return (B.g - B.b * acc) * B.inv;
 }
 
+// Extrapolated point next to the boundary point of the line through the cell (extrap_value
+// restricted to D).
+template <class T, int D, bool DYN>
+__device__ __noinline__ T extrap_line_value(const DevProb<T>& P, const T* __restrict__ u, int f, int i0, int i1,
+                                            int i2, long long c, int side, T t, const T* __restrict__ p) {
+    const int iD = D == 0 ? i0 : (D == 1 ? i1 : i2);
+    const DevBC<T>& B = P.bc[(f * 3 + D) * 2 + side];
+    if (B.xop < 0) return T(0);
+    const mol_op1d& x = P.ops[B.xop];
+    const int n = P.n[D];
+    const T* __restrict__ w = side == 0 ? P.w + x.w_lo + x.bLlo : P.w + x.w_hi + x.bLhi;
+    const int first = side == 0 ? 1 : n - x.bLhi + 1;
+    const int cnt = side == 0 ? x.bLlo : x.bLhi;
+    const int self = side == 0 ? 2 : n - 1, qb = side == 0 ? 1 : n;
+    const long long s = gstride(P, D);
+    const T* __restrict__ uf = u + (long long)f * P.ncell + c;
+    T acc = T(0);
+    bool started = false;
+    for (int k = 0; k < cnt; ++k) {
+        const int q = first + k;
+        if (q == self) continue;
+        T v;
+        if (q == qb) v = bc_line_value<T, D, DYN>(P, u, f, i0, i1, i2, c, side, t, p);
+        else v = (q > P.lo[D] && q <= n - P.up[D]) ? uf[(long long)(q - iD) * s] : T(0);
+        acc = started ? fma(w[k], v, acc) : w[k] * v;
+        started = true;
+    }
+    return acc;
+}
+
 // Field f at full-grid position q of the line through the cell (load_pt restricted to D).
 template <class T, int D, bool DYN>
 __device__ __forceinline__ T line_pt(const DevProb<T>& P, const T* __restrict__ u, int f, const int* I, long long c,
@@ -312,8 +384,12 @@ __device__ __forceinline__ T line_pt(const DevProb<T>& P, const T* __restrict__ 
     if ((P.permask[f] >> D) & 1) q = wrap_periodic(q, n);
     if (q > P.lo[D] && q <= n - P.up[D])
         return u[(long long)f * P.ncell + c + (long long)(q - I[D]) * gstride(P, D)];
-    if (q <= P.lo[D]) return q == 1 ? bc_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 0, t, p) : T(0);
-    return q == n ? bc_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 1, t, p) : T(0);
+    if (q <= P.lo[D]) {
+        if (q == 1) return bc_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 0, t, p);
+        return q == 2 ? extrap_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 0, t, p) : T(0);
+    }
+    if (q == n) return bc_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 1, t, p);
+    return q == n - 1 ? extrap_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 1, t, p) : T(0);
 }
 
 // apply_op_at restricted to D: sum_k w_k u[tap_k] at position `pos` of a line of `len` points.
@@ -339,7 +415,7 @@ template <class T, int D, bool DYN>
 __device__ __forceinline__ void weno_taps_line(const DevProb<T>& P, int f, const T* __restrict__ u, const int* I,
                                                long long c, T t, const T* __restrict__ p, T v[5]) {
 #pragma unroll
-    for (int k = 0; k < 5; ++k) v[k] = line_pt<T, D, DYN>(P, u, f, I, c, wrap_periodic(I[D] - 2 + k, P.n[D]), t, p);
+    for (int k = 0; k < 5; ++k) v[k] = line_pt<T, D, DYN>(P, u, f, I, c, I[D] - 2 + k, t, p);
 }
 
 // True when operator `o` at position i of dimension d uses its interior weights and
@@ -354,7 +430,7 @@ __device__ __forceinline__ bool fast_line(const DevProb<T>& P, const mol_op1d& o
 
 template <class T>
 __device__ __forceinline__ bool fast_weno(const DevProb<T>& P, int f, int d, int i) {
-    return ((P.permask[f] >> d) & 1) && i - 2 > P.lo[d] && i + 2 <= P.n[d];
+    return i - 2 > P.lo[d] && i + 2 <= P.n[d] - P.up[d];
 }
 
 // Nonlinear Laplacian at i: the outer half-offset stencil (position i-1 on n-1 points) uses
@@ -460,11 +536,11 @@ __device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps
 template <class T>
 __device__ __forceinline__ void weno_taps(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, T t,
                                           const T* p, T v[5]) {
-    const int f = tm.field, d = tm.dim, n = P.n[d];
+    const int f = tm.field, d = tm.dim;
     int J[3] = {I[0], I[1], I[2]};
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-        J[d] = wrap_periodic(I[d] - 2 + k, n);
+        J[d] = I[d] - 2 + k;  // load_pt wraps along periodic dimensions
         v[k] = load_pt(P, u, f, J[0], J[1], J[2], t, p);
     }
 }

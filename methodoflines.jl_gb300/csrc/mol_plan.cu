@@ -478,10 +478,14 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
                 break;
             case MOL_TERM_WENO:
                 if (!(t.dx > 0)) return set_err(plan, MOL_ERR_INVALID, "weno dx");
-                for (int f = 0; f < d->nfields; ++f) (void)f;
-                if (d->bc[t.field][t.dim][0].kind != MOL_BC_PERIODIC)
+                // bounded dimension: the interior stops two points from each end and the points
+                // next to the boundary points are extrapolated (WENO.jl:94, generate_bc_eqs.jl:336-392);
+                // with no boundary row at an end the reference uses its near-wall WENO stencils
+                if (d->bc[t.field][t.dim][0].kind != MOL_BC_PERIODIC &&
+                    !(d->bc[t.field][t.dim][0].extrap > 0 && d->bc[t.field][t.dim][1].extrap > 0))
                     return set_err(plan, MOL_ERR_UNSUPPORTED,
-                                   "WENO on a non-periodic dimension needs the nonuniform boundary stencils (not built)");
+                                   "WENO on a bounded dimension needs extrapolation rows at both ends "
+                                   "(the near-wall nonuniform WENO stencils are not built)");
                 if (d->npts[t.dim] - 1 < 5) return set_err(plan, MOL_ERR_INVALID, "WENO needs at least 6 grid points to wrap");
                 break;
             case MOL_TERM_NONLINLAP:
@@ -507,6 +511,23 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
             if (per && d->lower[q] != 1) return set_err(plan, MOL_ERR_INVALID, "periodic dims clip exactly the low point");
             for (int s = 0; s < 2; ++s) {
                 const mol_bc& b = d->bc[f][q][s];
+                const int clip = s == 0 ? d->lower[q] : d->upper[q];
+                if (b.extrap < 0 || b.extrap > d->nops) return set_err(plan, MOL_ERR_INVALID, "extrapolation operator");
+                if (b.extrap > 0) {
+                    const mol_op1d& x = d->ops[b.extrap - 1];
+                    const int rows = s == 0 ? x.nlo : x.nhi, len = s == 0 ? x.bLlo : x.bLhi;
+                    if (rows < 2 || len < 3 || len > d->npts[q])
+                        return set_err(plan, MOL_ERR_INVALID, "extrapolation table lacks a second row");
+                    if (clip != 2 || per)
+                        return set_err(plan, MOL_ERR_INVALID, "an extrapolated point needs the interior two points from the end");
+                    if (b.kind != MOL_BC_ROBIN)
+                        return set_err(plan, MOL_ERR_UNSUPPORTED, "an extrapolated point needs a boundary row at the end point");
+                    if (b.prog < 0 && b.b != 0.0)
+                        return set_err(plan, MOL_ERR_UNSUPPORTED,
+                                       "an extrapolated point next to a Neumann/Robin row (a coupled pair of rows) is not built");
+                } else if (clip > 1 && !per) {
+                    return set_err(plan, MOL_ERR_UNSUPPORTED, "interior stops more than one point from the end without an extrapolation row");
+                }
                 if (b.kind == MOL_BC_ROBIN) {
                     if (b.op < 0 || b.op >= d->nops) return set_err(plan, MOL_ERR_INVALID, "bc operator");
                     const mol_op1d& o = d->ops[b.op];
@@ -555,11 +576,13 @@ static int build_prec(mol_plan* plan, const mol_problem_desc* d, PlanArrays& A, 
         for (int q = 0; q < 3; ++q)
             for (int s = 0; s < 2; ++s) {
                 DevBC<T> b{};
+                b.xop = -1;
                 if (f < d->nfields && q < d->ndim) {
                     const mol_bc& src = d->bc[f][q][s];
                     b.kind = src.kind;
                     b.prog = src.prog;
                     b.op = src.op;
+                    b.xop = src.extrap - 1;
                     b.a = (T)src.a;
                     b.b = (T)src.b;
                     b.g = (T)src.g;

@@ -13,9 +13,8 @@
 namespace mol {
 
 template <class T>
-__device__ __noinline__ void bc_scatter(const DevProb<T>& P, T* lam, int f, const int* I, int dout, int side, T g,
-                                        T t, const T* p) {
-    if ((side == 0 && I[dout] != 1) || (side == 1 && I[dout] != P.n[dout])) return;
+__device__ __noinline__ void bc_row_scatter(const DevProb<T>& P, T* lam, int f, const int* I, int dout, int side,
+                                            T g, T t, const T* p) {
     const DevBC<T> B = P.bc[(f * 3 + dout) * 2 + side];
     if (B.kind != MOL_BC_ROBIN) return;
     T a = B.a, b = B.b;
@@ -39,6 +38,39 @@ __device__ __noinline__ void bc_scatter(const DevProb<T>& P, T* lam, int f, cons
 #pragma unroll
         for (int d = 0; d < 3; ++d) in &= (J[d] > P.lo[d]) & (J[d] <= P.n[d] - P.up[d]);
         if (in) atomicAdd(lam + (long long)f * P.ncell + flat_interior(P, J[0], J[1], J[2]), s * w[k]);
+    }
+}
+
+// Transpose of bc_value: the boundary point's row, or the extrapolation row of the point
+// next to it (extrap_value), whose boundary-point share goes on through the row.
+template <class T>
+__device__ __noinline__ void bc_scatter(const DevProb<T>& P, T* lam, int f, const int* I, int dout, int side, T g,
+                                        T t, const T* p) {
+    const int i = I[dout], n = P.n[dout];
+    if ((side == 0 && i == 1) || (side == 1 && i == n)) {
+        bc_row_scatter(P, lam, f, I, dout, side, g, t, p);
+        return;
+    }
+    const DevBC<T>& B = P.bc[(f * 3 + dout) * 2 + side];
+    if (B.xop < 0 || !((side == 0 && i == 2) || (side == 1 && i == n - 1))) return;
+    const mol_op1d& x = P.ops[B.xop];
+    const T* w = side == 0 ? P.w + x.w_lo + x.bLlo : P.w + x.w_hi + x.bLhi;
+    const int first = side == 0 ? 1 : n - x.bLhi + 1;
+    const int cnt = side == 0 ? x.bLlo : x.bLhi;
+    const int qb = side == 0 ? 1 : n;
+    int J[3] = {I[0], I[1], I[2]};
+    for (int k = 0; k < cnt; ++k) {
+        const int q = first + k;
+        if (q == i) continue;
+        J[dout] = q;
+        if (q == qb) {
+            bc_row_scatter(P, lam, f, J, dout, side, g * w[k], t, p);
+            continue;
+        }
+        bool in = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) in &= (J[d] > P.lo[d]) & (J[d] <= P.n[d] - P.up[d]);
+        if (in) atomicAdd(lam + (long long)f * P.ncell + flat_interior(P, J[0], J[1], J[2]), g * w[k]);
     }
 }
 
@@ -139,6 +171,29 @@ __device__ __noinline__ void scatter_bc_line(const DevProb<T>& P, T* lam, int f,
     }
 }
 
+// Transpose of extrap_line_value.
+template <class T, int D, bool DYN>
+__device__ __noinline__ void scatter_extrap_line(const DevProb<T>& P, T* lam, int f, int i0, int i1, int i2,
+                                                 long long c, int side, T g, T t, const T* __restrict__ p) {
+    const int iD = D == 0 ? i0 : (D == 1 ? i1 : i2);
+    const DevBC<T>& B = P.bc[(f * 3 + D) * 2 + side];
+    if (B.xop < 0) return;
+    const mol_op1d& x = P.ops[B.xop];
+    const int n = P.n[D];
+    const T* __restrict__ w = side == 0 ? P.w + x.w_lo + x.bLlo : P.w + x.w_hi + x.bLhi;
+    const int first = side == 0 ? 1 : n - x.bLhi + 1;
+    const int cnt = side == 0 ? x.bLlo : x.bLhi;
+    const int self = side == 0 ? 2 : n - 1, qb = side == 0 ? 1 : n;
+    const long long s = gstride(P, D);
+    T* lf = lam + (long long)f * P.ncell + c;
+    for (int k = 0; k < cnt; ++k) {
+        const int q = first + k;
+        if (q == self) continue;
+        if (q == qb) scatter_bc_line<T, D, DYN>(P, lam, f, i0, i1, i2, c, side, g * w[k], t, p);
+        else if (q > P.lo[D] && q <= n - P.up[D]) atomicAdd(lf + (long long)(q - iD) * s, g * w[k]);
+    }
+}
+
 template <class T, int D, bool DYN>
 __device__ __forceinline__ void scatter_line_pt(const DevProb<T>& P, T* lam, int f, const int* I, long long c, int q,
                                                 T g, T t, const T* __restrict__ p) {
@@ -150,8 +205,11 @@ __device__ __forceinline__ void scatter_line_pt(const DevProb<T>& P, T* lam, int
     }
     if (q <= P.lo[D]) {
         if (q == 1) scatter_bc_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 0, g, t, p);
+        else if (q == 2) scatter_extrap_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 0, g, t, p);
     } else if (q == n) {
         scatter_bc_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 1, g, t, p);
+    } else if (q == n - 1) {
+        scatter_extrap_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 1, g, t, p);
     }
 }
 
@@ -170,7 +228,7 @@ __device__ __forceinline__ void scatter_weno_taps_line(const DevProb<T>& P, int 
                                                        const T* gv, T t, const T* __restrict__ p) {
 #pragma unroll
     for (int k = 0; k < 5; ++k)
-        scatter_line_pt<T, D, DYN>(P, lam, f, I, c, wrap_periodic(I[D] - 2 + k, P.n[D]), gv[k], t, p);
+        scatter_line_pt<T, D, DYN>(P, lam, f, I, c, I[D] - 2 + k, gv[k], t, p);
 }
 
 // Transpose of one interior stencil line: adds v[m] to the adjoint at offset
@@ -318,11 +376,11 @@ __device__ __forceinline__ void weno5_grad(T um2, T um1, T u0, T up1, T up2, T e
 template <class T>
 __device__ __forceinline__ void scatter_weno_taps(const DevProb<T>& P, const mol_term& tm, T* lam, const int* I,
                                                   const T* gv, T t, const T* p) {
-    const int f = tm.field, d = tm.dim, n = P.n[d];
+    const int f = tm.field, d = tm.dim;
     int J[3] = {I[0], I[1], I[2]};
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-        J[d] = wrap_periodic(I[d] - 2 + k, n);
+        J[d] = I[d] - 2 + k;  // scatter_pt wraps along periodic dimensions
         scatter_pt(P, lam, f, J[0], J[1], J[2], gv[k], t, p);
     }
 }

@@ -47,7 +47,7 @@ class mol_term(C.Structure):
 
 
 class mol_bc(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("prog", C.c_int32), ("op", C.c_int32), ("reserved", C.c_int32),
+    _fields_ = [("kind", C.c_int32), ("prog", C.c_int32), ("op", C.c_int32), ("extrap", C.c_int32),
                 ("a", C.c_double), ("b", C.c_double), ("g", C.c_double)]
 
 

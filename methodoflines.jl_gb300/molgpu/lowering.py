@@ -26,7 +26,8 @@ from typing import Dict, List, Optional, Tuple
 import numpy as np
 
 from . import _lib as L
-from .weights import Operator, centered, centered_nonuniform, half_centered, select, upwind, wrap
+from .weights import (Operator, centered, centered_nonuniform, extrapolator, half_centered, select, upwind,
+                      wrap)
 
 # ------------------------------------------------------------------------------------
 # grids (Julia Float64 ranges)
@@ -378,6 +379,8 @@ class Lowered:
                 o = half_centered(d, self.order, dx)
             elif kind == "interp":
                 o = half_centered(0, max(4, self.order), dx)
+            elif kind == "extrap":          # BoundaryInterpolatorExtrapolator(max(6, order), dx)
+                o = extrapolator(max(6, self.order))
             else:
                 raise ValueError(kind)
             self.op_keys[key] = len(self.ops)
@@ -418,6 +421,22 @@ def _split_add(t, sign=1.0):
     if k == "neg":
         return _split_add(t[1], -sign)
     return [(sign, t)]
+
+
+def _deriv_orders(t, x) -> set:
+    """Orders of the derivatives along x anywhere in the expression (``d_orders``)."""
+    out = set()
+    if isinstance(t, tuple) and t:
+        if t[0] == "D" and t[1] == x:
+            out.add(t[2])
+        for a in t[1:]:
+            if isinstance(a, tuple):
+                out |= _deriv_orders(a, x)
+    return out
+
+
+def _is_zero(t) -> bool:
+    return _leaves(t) <= {"num"} and float(host_eval(t, {}, {})) == 0.0
 
 
 def _split_mul(t):
@@ -472,16 +491,39 @@ class _Lowerer:
                 periodic[b["field"]][j] = True
             else:
                 bcs[(b["field"], j, b["side"])] = b
+        adv = list(disc.get("advection", ["upwind", 1]))
         lower = None
         upper = None
+        self.extrap_dims = set()
         for f in fields:
             lo_ = [1 if periodic[f][j] else int((f, j, "lo") in bcs) for j in range(len(ivs))]
             up_ = [0 if periodic[f][j] else int((f, j, "hi") in bcs) for j in range(len(ivs))]
+            if adv[0] == "weno":
+                # stencil extents (interior_map.jl:83-90, :117-139): WENO along a bounded uniform
+                # dimension reaches 2 (WENO.jl:94), so the interior of an equation with a first
+                # derivative along it stops two points from each end and point 2 (n-1) is
+                # extrapolated (generate_extrap_eqs!, generate_bc_eqs.jl:336-392)
+                for j, x in enumerate(ivs):
+                    if periodic[f][j] or 1 not in _deriv_orders(spec["eqs"][f], x):
+                        continue
+                    if not uniform[j]:
+                        raise NotImplementedError(f"WENO on the nonuniform grid of {x} is not built")
+                    for side, arr in (("lo", lo_), ("hi", up_)):
+                        b = bcs.get((f, j, side))
+                        if b is None:
+                            raise NotImplementedError(
+                                f"WENO along {x} with no boundary row at one end (two coupled extrapolated points) "
+                                "is not built")
+                        if not _is_zero(b["b"]):
+                            raise NotImplementedError(
+                                f"WENO along {x} next to a Neumann/Robin row (a coupled boundary/extrapolation "
+                                "pair) is not built")
+                        arr[j] = max(arr[j], 2)
+                    self.extrap_dims.add((f, j))
             if lower is None:
                 lower, upper = lo_, up_
             elif lo_ != lower or up_ != upper:
                 raise NotImplementedError("all fields must share one interior box")
-        adv = list(disc.get("advection", ["upwind", 1]))
         params = spec.get("params", [])
         self.lw = Lowered(ivs=ivs, fields=fields, param_names=[p[0] for p in params],
                           param_values=np.array([float(p[1]) for p in params], dtype=np.float64),
@@ -722,7 +764,8 @@ class _Lowerer:
         # boundary rows
         for (f, j, side), b in self.bcs.items():
             a, bb, g = b["a"], b["b"], b["g"]
-            entry = {"kind": L.BC_ROBIN, "op": lw.op("centered", j, 1), "prog": -1, "a": 0.0, "b": 0.0, "g": 0.0}
+            entry = {"kind": L.BC_ROBIN, "op": lw.op("centered", j, 1), "prog": -1, "a": 0.0, "b": 0.0, "g": 0.0,
+                     "extrap": 1 + lw.op("extrap", j, 0) if (f, j) in self.extrap_dims else 0}
             lv = _leaves(a) | _leaves(bb) | _leaves(g)
             if lv <= {"num"}:
                 entry["a"] = float(host_eval(a, {}, {}))
@@ -805,6 +848,7 @@ class Descriptor:
             b.prog = e["prog"]
             b.op = e["op"]
             b.a, b.b, b.g = e["a"], e["b"], e["g"]
+            b.extrap = e.get("extrap", 0)
         # operators and the weight pool
         pool: List[float] = []
         ops = (L.mol_op1d * max(1, len(lw.ops)))()

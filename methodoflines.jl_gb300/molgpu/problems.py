@@ -16,6 +16,11 @@ come from ``numpy.random.Generator(PCG64(seed))`` in Float64.
                  (test/Diffusion/MOL_1D_Linear_Diffusion.jl, Test 03), points given as a vector
 8. stretched_2d                   u_t = u_xx + u_yy + 0.1 u, x stretched (Robin/Neumann),
                  y uniform (Dirichlet with data)
+9. burgers_weno_dirichlet         u_t = -u u_x, u0 = x, Dirichlet x/(t+1) at both ends, WENO
+                 (test/Burgers/burgers_eq.jl:56-104; exact solution x/(t+1))
+10. viscous_burgers_weno_bounded  u_t = -u u_x + nu u_xx, Dirichlet data, WENO on [0, 1]
+11. burgers_weno_channel          2-D u_t = -u u_x - 0.5 u_y + nu lap u, WENO, x bounded
+                 (Dirichlet), y periodic
 """
 from __future__ import annotations
 
@@ -259,3 +264,51 @@ def stretched_2d(nx: int = 48, ny: int = 40, order: int = 2, beta: float = 2.0):
     disc = MOLFiniteDifference({x: pts, y: 1.0 / (ny - 1)}, t, approx_order=order)
     h = min(float(np.min(np.diff(pts))), 1.0 / (ny - 1))
     return sys, disc, {"dt": 0.1 * h * h, "points": pts}
+
+
+def burgers_weno_dirichlet(dx: float = 0.05):
+    """Inviscid Burgers with WENO on a bounded interval: the interior stops two points from
+    each end and points 2 and n-1 are extrapolated (WENO.jl:94, generate_bc_eqs.jl:336-392)."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx = Differential(t), Differential(x)
+    eq = Eq(Dt(u(x, t)), -u(x, t) * Dx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), 1.0 * x), Eq(u(0.0, t), 0.0 / (t + 1.0)), Eq(u(1.0, t), 1.0 / (t + 1.0))]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 6.0)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [])
+    disc = MOLFiniteDifference({x: dx}, t, advection_scheme=WENOScheme())
+    return sys, disc, {"dt": 0.2 * dx}
+
+
+def viscous_burgers_weno_bounded(n: int = 257, nu: float = 2e-3, order: int = 2):
+    """u_t = -u u_x + nu u_xx on [0, 1], u0 = 0.5 + 0.4 sin(2 pi x) with time-dependent
+    Dirichlet data at both ends, WENO advection."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dxx = Differential(t), Differential(x), Differential(x) ** 2
+    nup = Param("nu", nu)
+    eq = Eq(Dt(u(x, t)), -u(x, t) * Dx(u(x, t)) + nup * Dxx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), 0.5 + 0.4 * sin(2.0 * math.pi * x)), Eq(u(0.0, t), 0.5 + 0.2 * t),
+           Eq(u(1.0, t), 0.5 - 0.1 * t)]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [nup])
+    disc = MOLFiniteDifference({x: n}, t, approx_order=order, advection_scheme=WENOScheme())
+    h = 1.0 / (n - 1)
+    return sys, disc, {"dt": 0.4 / (1.0 / h + 2.0 * nu / h ** 2)}
+
+
+def burgers_weno_channel(nx: int = 65, ny: int = 49, nu: float = 2e-3):
+    """2-D WENO advection with x bounded (Dirichlet, extrapolated points 2 and n-1) and y
+    periodic."""
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dy = Differential(t), Differential(x), Differential(y)
+    Dxx, Dyy = Differential(x) ** 2, Differential(y) ** 2
+    eq = Eq(Dt(u(x, y, t)), -u(x, y, t) * Dx(u(x, y, t)) - 0.5 * Dy(u(x, y, t))
+            + nu * (Dxx(u(x, y, t)) + Dyy(u(x, y, t))))
+    bcs = [Eq(u(x, y, 0.0), 0.6 + 0.3 * sin(2.0 * math.pi * x) * cos(2.0 * math.pi * y)),
+           Eq(u(0.0, y, t), 0.6), Eq(u(1.0, y, t), 0.6 + 0.1 * t),
+           Eq(u(x, 0.0, t), u(x, 1.0, t))]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0))],
+                    [t, x, y], [u(x, y, t)], [])
+    disc = MOLFiniteDifference({x: nx, y: ny}, t, advection_scheme=WENOScheme())
+    h = min(1.0 / (nx - 1), 1.0 / (ny - 1))
+    return sys, disc, {"dt": 0.3 / (1.5 / h + 4.0 * nu / h ** 2)}

@@ -157,6 +157,24 @@ def half_centered(d: int, p: int, dx: float) -> Operator:
     return Operator(L, 1 - e, inner, low, high, bl, bl, 1)
 
 
+def extrapolator(q: int) -> Operator:
+    """``BoundaryInterpolatorExtrapolator(q, dx)`` (extrapolation_weights.jl:1-60): row k of the
+    low table gives the value at node k (0-based) of the first q nodes from the other q - 1
+    (order-0 Fornberg weights, a zero in its own slot); the high rows are the low rows
+    reversed.  No dx scaling: interpolation weights do not depend on the spacing."""
+    L = q - 1 + q % 2
+    h = L // 2
+    low = []
+    for x0 in range(h):
+        others = [float(v) for v in range(q) if v != x0]
+        w = fornberg(0, float(x0), others)
+        low.append(w[:x0] + [0.0] + w[x0:])
+    mid = [float(v) for v in range(-h, h + 1) if v != 0]
+    wi = fornberg(0, 0.0, mid)
+    interior = wi[:h] + [0.0] + wi[h:]
+    return Operator(L, -h, interior, low, [lw[::-1] for lw in low], q, q, 0)
+
+
 def select(op: Operator, i: int, length: int, periodic: bool) -> Tuple[List[float], List[int]]:
     """(weights, unwrapped taps) of `op` at 1-based position i on a line of `length` points."""
     if not periodic and i <= op.nlo:

@@ -161,6 +161,32 @@ def complete_centered_difference_nonuniform(d: int, p: int, x: Sequence[float]) 
     return DerivativeOperator(d, p, float("nan"), L, stencil, bL, bpc, low, high, 0, "centered_nonuniform")
 
 
+def boundary_interpolator_extrapolator(q: int, dx: float) -> DerivativeOperator:
+    """``BoundaryInterpolatorExtrapolator(q, dx)``, ``extrapolation_weights.jl:1-60``.
+
+    ``remove`` drops the node itself from the node list and ``insert`` puts a zero weight
+    back in its slot; the high rows are the low rows reversed.
+    """
+    L = q - 1 + q % 2
+    bL = q
+    half = L // 2
+    dummy_x = list(range(-half, half + 1))
+    left_x = list(range(0, bL))
+    bpc = half
+
+    def remove(v, x):
+        return [a for a in v if a != x]
+
+    def insert(v, i, val):          # Julia's insert!(v, i, val), 1-based i
+        return list(v[:i - 1]) + [val] + list(v[i - 1:])
+
+    stencil = insert(calculate_weights(0, 0.0, remove(dummy_x, 0)), dummy_x.index(0) + 1, 0.0)
+    low = [insert(calculate_weights(0, 1.0 * x0, remove(left_x, x0)), i, 0.0)
+           for i, x0 in enumerate(left_x[:bpc], start=1)]
+    high = [list(reversed(v)) for v in low]
+    return DerivativeOperator(0, q, dx, L, stencil, bL, bpc, low, high, 0, "extrapolation")
+
+
 def complete_upwind_difference(d: int, p: int, dx: float, offside: int = 0) -> DerivativeOperator:
     """``CompleteUpwindDifference``, ``upwind_difference/upwind_diff_weights.jl:4-91``."""
     assert offside > -1

@@ -17,8 +17,8 @@ from typing import Dict, List, Tuple
 
 import numpy as np
 
-from .fornberg import (complete_centered_difference, complete_centered_difference_nonuniform,
-                       complete_half_centered_difference,
+from .fornberg import (boundary_interpolator_extrapolator, complete_centered_difference,
+                       complete_centered_difference_nonuniform, complete_half_centered_difference,
                        complete_upwind_difference)
 
 # --------------------------------------------------------------------------------------
@@ -206,6 +206,18 @@ def _split_add(t, sign=1.0):
     return [(sign, t)]
 
 
+def _deriv_orders(t, x):
+    """Orders of the derivatives along x anywhere in the expression (``d_orders``)."""
+    out = set()
+    if isinstance(t, tuple) and t:
+        if t[0] == "D" and t[1] == x:
+            out.add(t[2])
+        for a in t[1:]:
+            if isinstance(a, tuple):
+                out |= _deriv_orders(a, x)
+    return out
+
+
 def _split_mul(t):
     """Multiplicative factors (numerator list, denominator list)."""
     k = t[0]
@@ -288,6 +300,21 @@ class OracleProblem:
                     up[j] += int(bj["hi"] is not None)
             self.lower[f] = lo
             self.upper[f] = up
+        # stencil extents (interior_map.jl:83-90, :117-139): the advection scheme's extent
+        # along every dimension where the equation has a first derivative and no periodic
+        # boundary; WENO reaches 2 on a uniform grid and 0 on a nonuniform one (WENO.jl:94-95).
+        # The points between the boundary row and the interior are then extrapolated
+        # (generate_extrap_eqs!, generate_bc_eqs.jl:336-392).
+        self.clip_lower = {f: list(self.lower[f]) for f in self.fields}
+        self.clip_upper = {f: list(self.upper[f]) for f in self.fields}
+        if self.adv_kind == "weno":
+            for f in self.fields:
+                for j, x in enumerate(self.ivs):
+                    if self.bc[f][j]["periodic"] or 1 not in _deriv_orders(spec["eqs"][f], x):
+                        continue
+                    ext = 2 if self.uniform[j] else 0
+                    self.lower[f][j] = max(self.lower[f][j], ext)
+                    self.upper[f][j] = max(self.upper[f][j], ext)
         self.shape = {f: tuple(self.npts[j] - self.lower[f][j] - self.upper[f][j] for j in range(self.nd))
                       for f in self.fields}
         self.size = {f: int(np.prod(self.shape[f])) for f in self.fields}
@@ -316,6 +343,8 @@ class OracleProblem:
                 D = complete_upwind_difference(d, int(extra), dx, d + int(extra) - 1)
             elif kind == "half":
                 D = complete_half_centered_difference(d, self.order, dx)
+            elif kind == "extrap":
+                D = boundary_interpolator_extrapolator(max(6, self.order), dx)
             elif kind == "interp":
                 D = complete_half_centered_difference(0, max(4, self.order), dx)
             else:
@@ -436,8 +465,39 @@ class OracleProblem:
                     if b is None:
                         continue
                     self._fill_robin(F, f, j, side, b, t, p)
+            for j in range(self.nd):
+                self._fill_extrapolated(F, f, j)
             self._zero_corners(F, f)
         return full
+
+    def _fill_extrapolated(self, F, f, j):
+        """``generate_extrap_eqs!`` (generate_bc_eqs.jl:336-392): the points between the boundary
+        row and the interior, on the interior's edge slice, are ``central_difference`` of the
+        extrapolator ``BoundaryInterpolatorExtrapolator(max(6, order), dx)`` at that point."""
+        n = self.npts[j]
+        for side in ("lo", "hi"):
+            ext = self.lower[f][j] if side == "lo" else self.upper[f][j]
+            clip = self.clip_lower[f][j] if side == "lo" else self.clip_upper[f][j]
+            if ext <= clip:
+                continue
+            if clip == 0:
+                raise NotImplementedError("oracle: extrapolated points with no boundary row at that end")
+            Dx = self.op("extrap", j, 0)
+            sl = self._other_interior_slices(f, j)
+            for m in range(clip + 1, ext + 1):
+                i = m if side == "lo" else n + 1 - m
+                w, taps = central_taps(Dx, i, n, False)
+                acc = None
+                for wk, tp in zip(w, taps):
+                    if wk == 0.0:
+                        continue
+                    s = list(sl)
+                    s[j] = tp - 1
+                    term = wk * F[tuple(s)]
+                    acc = term if acc is None else acc + term
+                s = list(sl)
+                s[j] = i - 1
+                F[tuple(s)] = acc
 
     def _other_interior_slices(self, f, j):
         sl = []
@@ -652,13 +712,14 @@ class OracleProblem:
         """``weno_f_uniform`` (WENO.jl:6-57) with taps from ``get_f_taps_coords`` (function_scheme.jl:1-34)."""
         n = self.npts[j]
         per = self.bc[f][j]["periodic"]
-        if not per:
-            raise NotImplementedError("oracle WENO covers periodic dimensions only")
+        idx = self.interior_index(f, j)
+        if not per and (idx[0] <= 2 or idx[-1] > n - 2):
+            # get_f_taps_coords picks the near-wall functions there (function_scheme.jl:6-16)
+            raise NotImplementedError("oracle: near-wall WENO stencils")
         eps = float(self.adv_param)
         dx = self.dx[j]
         sl = [slice(self.lower[f][k], self.npts[k] - self.upper[f][k]) for k in range(self.nd)]
-        idx = self.interior_index(f, j)
-        taps = [[wrap_periodic(int(i) + o, n) for i in idx] for o in (-2, -1, 0, 1, 2)]
+        taps = [[wrap_periodic(int(i) + o, n) if per else int(i) + o for i in idx] for o in (-2, -1, 0, 1, 2)]
         def tap(o):
             s = list(sl)
             s[j] = np.array(taps[o + 2]) - 1

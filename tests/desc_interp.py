@@ -46,9 +46,25 @@ class DescInterp:
         if len(out) > 1:
             return 0.0
         d, side = out[0]
+        e = self.lw.bcs.get((f, d, side))
+        nxt = 2 if side == 0 else self.n[d] - 1
+        if e is not None and e.get("extrap", 0) and I[d] == nxt:
+            # extrapolated point next to the boundary point (extrap_value)
+            xo = self.lw.ops[e["extrap"] - 1]
+            w = xo.low[1] if side == 0 else xo.high[1]
+            first = 1 if side == 0 else self.n[d] - xo.bLhi + 1
+            acc = None
+            for k, wk in enumerate(w):
+                q = first + k
+                if q == I[d]:
+                    continue
+                J = list(I)
+                J[d] = q
+                term = wk * self.load(u, f, J, t, p)
+                acc = term if acc is None else acc + term
+            return acc
         if (side == 0 and I[d] != 1) or (side == 1 and I[d] != self.n[d]):
             return 0.0
-        e = self.lw.bcs.get((f, d, side))
         if e is None or e["kind"] != L.BC_ROBIN:
             return 0.0
         a, b, g = e["a"], e["b"], e["g"]
@@ -111,7 +127,7 @@ class DescInterp:
             v = []
             for o in range(-2, 3):
                 J = list(I)
-                J[d] = wrap(I[d] + o, self.n[d])
+                J[d] = I[d] + o  # load wraps along periodic dimensions
                 v.append(self.load(u, f, J, t, p))
             return _weno(*v, tm["eps"], tm["dx"])
         if kind == L.TERM_NONLINLAP:

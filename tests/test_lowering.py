@@ -146,21 +146,6 @@ def test_invalid_descriptor_rejected_before_device_work():
     assert e.value.status == -1 and "constant" in str(e.value)
 
 
-def test_weno_on_bounded_dimension_is_unsupported():
-    from molgpu import Plan
-    from molgpu.symbolic import Differential, Eq, Field, Interval, IV, PDESystem, sin
-    from molgpu.api import MOLFiniteDifference, WENOScheme
-    x, t = IV("x"), IV("t")
-    u = Field("u")
-    s = PDESystem([Eq(Differential(t)(u(x, t)), -u(x, t) * Differential(x)(u(x, t)))],
-                  [Eq(u(x, 0.0), sin(x)), Eq(u(0.0, t), 0.0), Eq(u(1.0, t), 0.0)],
-                  [(t, Interval(0, 1)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)])
-    lw = lower(s.to_spec(MOLFiniteDifference({x: 0.05}, t, advection_scheme=WENOScheme())))
-    with pytest.raises(L.MolError) as e:
-        Plan(lw)
-    assert e.value.status == -6
-
-
 def test_register_allocation_reuses_registers():
     """A long pointwise program fits in the 64-register file through reuse."""
     from molgpu.lowering import ProgramBuilder
