@@ -97,8 +97,14 @@ def test_weno_bounded_adjoint_matches_finite_differences(gpu_lib):
     g = np.zeros(lw.n_unknowns)
     plan.adjoint_ssprk33(lw.u0, dt, n, target, nsnap=4, dLdu0=g)
     w = np.random.default_rng(9).standard_normal(lw.n_unknowns)
-    h = 1e-6
-    fd = (loss(lw.u0 + h * w) - loss(lw.u0 - h * w)) / (2 * h)
+
+    def cd(h):
+        return (loss(lw.u0 + h * w) - loss(lw.u0 - h * w)) / (2 * h)
+
+    # WENO's weights have large third derivatives near the extrema of this state (central
+    # differences at h = 1e-6 are off by ~6e-6 relative, converging as h^2), so the check uses
+    # the Richardson extrapolation of two central differences
+    fd = (4.0 * cd(5e-7) - cd(1e-6)) / 3.0
     assert abs(g @ w - fd) <= 1e-6 * abs(fd), (g @ w, fd)
     plan.close()
 
