@@ -43,7 +43,7 @@ typedef unsigned long long uint64_t;
 extern "C" {
 #endif
 
-#define MOL_ABI_VERSION 1
+#define MOL_ABI_VERSION 2
 #define MOL_MAX_DIMS 3
 #define MOL_MAX_FIELDS 8
 #define MOL_MAX_REGS 64
@@ -107,7 +107,12 @@ typedef struct mol_term {
 typedef enum mol_bc_kind {
     MOL_BC_NONE = 0,      /* no boundary row on this face (interior extends to the end)     */
     MOL_BC_PERIODIC = 1,  /* u[1] ~ u[l] (generate_bc_eqs.jl:35-58, interface_boundary.jl:33-42) */
-    MOL_BC_ROBIN = 2      /* a*u + b*Dx(u) = g at the face, solved for the boundary value     */
+    MOL_BC_ROBIN = 2,     /* a*u + b*Dx(u) = g at the face, solved for the boundary value     */
+    MOL_BC_EDGE = 3       /* edge-aligned grid: a*I(u) + b*H(u) = g at the face half-way between
+                             the ghost point and the first (last) unknown, I the interpolation
+                             table `iop` and H the half-offset first-derivative table `op` at
+                             position 1 (n-1), solved for the ghost point (boundary_value_maps for
+                             EdgeAlignedGrid, generate_bc_eqs.jl:80-160)                       */
 } mol_bc_kind;
 
 typedef struct mol_bc {
@@ -122,6 +127,8 @@ typedef struct mol_bc {
                            row of that operator, the boundary point through this row, which must
                            then be a Dirichlet row (b == 0)                                     */
     double a, b, g;
+    int32_t iop;        /* MOL_BC_EDGE: the half-offset interpolation operator              */
+    int32_t pad;
 } mol_bc;
 
 /* Register-machine instruction of the pointwise programs. */

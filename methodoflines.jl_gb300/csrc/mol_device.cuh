@@ -41,6 +41,7 @@ struct SolverState {
 template <class T>
 struct DevBC {
     int kind, prog, op, xop;
+    int iop, pad;  // MOL_BC_EDGE: interpolation operator (op: half-offset first derivative)
     T a, b, g;
     T inv, c0;
 };
@@ -110,6 +111,34 @@ __device__ __forceinline__ T load_interior(const DevProb<T>& P, const T* u, int 
     for (int d = 0; d < 3; ++d) in &= (I[d] > P.lo[d]) & (I[d] <= P.n[d] - P.up[d]);
     if (!in) return T(0);
     return u[(long long)f * P.ncell + flat_interior(P, I[0], I[1], I[2])];
+}
+
+struct TapSel {
+    long long woff;
+    int first, cnt;
+    bool wrap;
+};
+
+// Tap selection of one 1-D operator at position i of a line of `len` points.
+__device__ __forceinline__ TapSel select_taps(const mol_op1d& op, int i, int len, bool per) {
+    TapSel s;
+    if (!per && i <= op.nlo) {
+        const int ti = i < 1 ? 0 : i - 1;  // positions below 1 only occur in malformed descriptors
+        s.woff = op.w_lo + (long long)ti * op.bLlo; s.first = 1; s.cnt = op.bLlo; s.wrap = false;
+    } else if (!per && i > len - op.nhi) {
+        int ti = len - i - op.hi_base;
+        ti = ti < 0 ? 0 : ti;
+        s.woff = op.w_hi + (long long)ti * op.bLhi; s.first = len - op.bLhi + 1;
+        s.cnt = op.bLhi; s.wrap = false;
+    } else {
+        s.woff = op.w_int; s.first = i + op.omin; s.cnt = op.L; s.wrap = per;
+        if (op.nrows > 0) {  // nonuniform grid: the row of point i (validated: nrows == len - nlo - nhi)
+            int r = i - op.nlo - 1;
+            r = r < 0 ? 0 : (r >= op.nrows ? op.nrows - 1 : r);
+            s.woff += (long long)r * op.L;
+        }
+    }
+    return s;
 }
 
 // Small straight-line program used by boundary rows (a, b, g may depend on t, x, p).
@@ -207,10 +236,46 @@ __device__ __noinline__ T bc_value(const DevProb<T>& P, const T* u, int f, int* 
     return T(0);
 }
 
+// Edge-aligned grid: a * sum_k c_k u_k + b * sum_k d_k u_k = g at the face between the ghost
+// point and the first (last) unknown, c the interpolation and d the half-offset derivative
+// table at position 1 (n-1), solved for the ghost point (boundary_value_maps for
+// EdgeAlignedGrid, generate_bc_eqs.jl:80-160; tables selected as in
+// half_offset_centred_difference.jl:9-37).
+template <class T>
+__device__ __noinline__ T edge_row_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t,
+                                         const T* p) {
+    const DevBC<T>& B = P.bc[(f * 3 + dout) * 2 + side];
+    T a = B.a, b = B.b, g = B.g;
+    if (B.prog >= 0) {
+        a = run_bc_prog(P, B.prog, 0, I, t, p);
+        b = run_bc_prog(P, B.prog, 1, I, t, p);
+        g = run_bc_prog(P, B.prog, 2, I, t, p);
+    }
+    const int n = P.n[dout], pos = side == 0 ? 1 : n - 1, ghost = side == 0 ? 1 : n;
+    const TapSel si = select_taps(P.ops[B.iop], pos, n, false);
+    const TapSel sd = select_taps(P.ops[B.op], pos, n, false);
+    int J[3] = {I[0], I[1], I[2]};
+    T sum_i = T(0), sum_d = T(0), wi = T(0), wd = T(0);
+    for (int k = 0; k < si.cnt; ++k) {
+        const int q = si.first + k;
+        if (q == ghost) { wi = P.w[si.woff + k]; continue; }
+        J[dout] = q;
+        sum_i = fma(P.w[si.woff + k], load_interior(P, u, f, J), sum_i);
+    }
+    for (int k = 0; k < sd.cnt; ++k) {
+        const int q = sd.first + k;
+        if (q == ghost) { wd = P.w[sd.woff + k]; continue; }
+        J[dout] = q;
+        sum_d = fma(P.w[sd.woff + k], load_interior(P, u, f, J), sum_d);
+    }
+    return (g - a * sum_i - b * sum_d) / (a * wi + b * wd);
+}
+
 template <class T>
 __device__ __noinline__ T bc_row_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t,
                                        const T* p) {
     const DevBC<T> B = P.bc[(f * 3 + dout) * 2 + side];
+    if (B.kind == MOL_BC_EDGE) return edge_row_value(P, u, f, I, dout, side, t, p);
     if (B.kind != MOL_BC_ROBIN) return T(0);
     const bool dyn = B.prog >= 0;
     T a = B.a, b = B.b, g = B.g;
@@ -237,34 +302,6 @@ __device__ __noinline__ T bc_row_value(const DevProb<T>& P, const T* u, int f, i
         started = true;
     }
     return dyn ? (g - b * acc) / (a + b * w[kb]) : (g - b * acc) * B.inv;
-}
-
-struct TapSel {
-    long long woff;
-    int first, cnt;
-    bool wrap;
-};
-
-// Tap selection of one 1-D operator at position i of a line of `len` points.
-__device__ __forceinline__ TapSel select_taps(const mol_op1d& op, int i, int len, bool per) {
-    TapSel s;
-    if (!per && i <= op.nlo) {
-        const int ti = i < 1 ? 0 : i - 1;  // positions below 1 only occur in malformed descriptors
-        s.woff = op.w_lo + (long long)ti * op.bLlo; s.first = 1; s.cnt = op.bLlo; s.wrap = false;
-    } else if (!per && i > len - op.nhi) {
-        int ti = len - i - op.hi_base;
-        ti = ti < 0 ? 0 : ti;
-        s.woff = op.w_hi + (long long)ti * op.bLhi; s.first = len - op.bLhi + 1;
-        s.cnt = op.bLhi; s.wrap = false;
-    } else {
-        s.woff = op.w_int; s.first = i + op.omin; s.cnt = op.L; s.wrap = per;
-        if (op.nrows > 0) {  // nonuniform grid: the row of point i (validated: nrows == len - nlo - nhi)
-            int r = i - op.nlo - 1;
-            r = r < 0 ? 0 : (r >= op.nrows ? op.nrows - 1 : r);
-            s.woff += (long long)r * op.L;
-        }
-    }
-    return s;
 }
 
 // sum_k w_k u[tap_k] along dimension d at position `pos` of a line of `len` points
@@ -317,6 +354,11 @@ __device__ __noinline__ T bc_line_value(const DevProb<T>& P, const T* __restrict
                                         long long c, int side, T t, const T* __restrict__ p) {
     const int iD = D == 0 ? i0 : (D == 1 ? i1 : i2);
     const DevBC<T>& B = P.bc[(f * 3 + D) * 2 + side];
+    if (B.kind == MOL_BC_EDGE) {
+        int J[3] = {i0, i1, i2};
+        J[D] = side == 0 ? 1 : P.n[D];
+        return edge_row_value(P, u, f, J, D, side, t, p);
+    }
     if (B.kind != MOL_BC_ROBIN) return T(0);
     if (DYN && B.prog >= 0) {
         int J[3] = {i0, i1, i2};

@@ -537,6 +537,27 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
                         st = validate_prog(plan, d, b.prog, 2, 16, 0, nullptr);
                         if (st) return st;
                     }
+                } else if (b.kind == MOL_BC_EDGE) {
+                    if (per || b.extrap) return set_err(plan, MOL_ERR_INVALID, "edge row on a periodic or extrapolated end");
+                    const int n = (int)d->npts[q], pos = s == 0 ? 1 : n - 1, ghost = s == 0 ? 1 : n;
+                    for (int o : {b.op, b.iop}) {
+                        if (o < 0 || o >= d->nops) return set_err(plan, MOL_ERR_INVALID, "edge bc operator");
+                        // the tap window the device selects (select_taps at pos on n points) must hold
+                        // the ghost point and otherwise unknowns of this line only
+                        const mol_op1d& x = d->ops[o];
+                        int first, cnt;
+                        if (pos <= x.nlo) { first = 1; cnt = x.bLlo; }
+                        else if (pos > n - x.nhi) { first = n - x.bLhi + 1; cnt = x.bLhi; }
+                        else { first = pos + x.omin; cnt = x.L; }
+                        const int last = first + cnt - 1;
+                        if (cnt < 1 || ghost < first || ghost > last || first < 1 || last > n ||
+                            (s == 0 && last > n - d->upper[q]) || (s == 1 && first <= d->lower[q]))
+                            return set_err(plan, MOL_ERR_INVALID, "edge bc stencil leaves the line");
+                    }
+                    if (b.prog >= 0) {
+                        st = validate_prog(plan, d, b.prog, 2, 16, 0, nullptr);
+                        if (st) return st;
+                    }
                 } else if (b.kind != MOL_BC_NONE && b.kind != MOL_BC_PERIODIC) {
                     return set_err(plan, MOL_ERR_INVALID, "bc kind");
                 }
@@ -583,6 +604,7 @@ static int build_prec(mol_plan* plan, const mol_problem_desc* d, PlanArrays& A, 
                     b.prog = src.prog;
                     b.op = src.op;
                     b.xop = src.extrap - 1;
+                    b.iop = src.iop;
                     b.a = (T)src.a;
                     b.b = (T)src.b;
                     b.g = (T)src.g;

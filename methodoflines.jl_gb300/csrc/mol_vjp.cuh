@@ -12,10 +12,49 @@
 
 namespace mol {
 
+// Transpose of edge_row_value: d u_ghost / d u_k = -(a c_k + b d_k) / (a c_ghost + b d_ghost).
+template <class T>
+__device__ __noinline__ void edge_row_scatter(const DevProb<T>& P, T* lam, int f, const int* I, int dout, int side,
+                                              T g, T t, const T* p) {
+    const DevBC<T>& B = P.bc[(f * 3 + dout) * 2 + side];
+    T a = B.a, b = B.b;
+    if (B.prog >= 0) {
+        a = run_bc_prog(P, B.prog, 0, I, t, p);
+        b = run_bc_prog(P, B.prog, 1, I, t, p);
+    }
+    const int n = P.n[dout], pos = side == 0 ? 1 : n - 1, ghost = side == 0 ? 1 : n;
+    const TapSel si = select_taps(P.ops[B.iop], pos, n, false);
+    const TapSel sd = select_taps(P.ops[B.op], pos, n, false);
+    T wi = T(0), wd = T(0);
+    for (int k = 0; k < si.cnt; ++k)
+        if (si.first + k == ghost) wi = P.w[si.woff + k];
+    for (int k = 0; k < sd.cnt; ++k)
+        if (sd.first + k == ghost) wd = P.w[sd.woff + k];
+    const T s = -g / (a * wi + b * wd);
+    int J[3] = {I[0], I[1], I[2]};
+    for (int pass = 0; pass < 2; ++pass) {
+        const TapSel& ts = pass == 0 ? si : sd;
+        const T coef = pass == 0 ? a : b;
+        for (int k = 0; k < ts.cnt; ++k) {
+            const int q = ts.first + k;
+            if (q == ghost) continue;
+            J[dout] = q;
+            bool in = true;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) in &= (J[d] > P.lo[d]) & (J[d] <= P.n[d] - P.up[d]);
+            if (in) atomicAdd(lam + (long long)f * P.ncell + flat_interior(P, J[0], J[1], J[2]), s * coef * P.w[ts.woff + k]);
+        }
+    }
+}
+
 template <class T>
 __device__ __noinline__ void bc_row_scatter(const DevProb<T>& P, T* lam, int f, const int* I, int dout, int side,
                                             T g, T t, const T* p) {
     const DevBC<T> B = P.bc[(f * 3 + dout) * 2 + side];
+    if (B.kind == MOL_BC_EDGE) {
+        edge_row_scatter(P, lam, f, I, dout, side, g, t, p);
+        return;
+    }
     if (B.kind != MOL_BC_ROBIN) return;
     T a = B.a, b = B.b;
     if (B.prog >= 0) {
@@ -146,6 +185,12 @@ __device__ __noinline__ void scatter_bc_line(const DevProb<T>& P, T* lam, int f,
                                              int side, T g, T t, const T* __restrict__ p) {
     const int iD = D == 0 ? i0 : (D == 1 ? i1 : i2);
     const DevBC<T>& B = P.bc[(f * 3 + D) * 2 + side];
+    if (B.kind == MOL_BC_EDGE) {
+        int J[3] = {i0, i1, i2};
+        J[D] = side == 0 ? 1 : P.n[D];
+        edge_row_scatter(P, lam, f, J, D, side, g, t, p);
+        return;
+    }
     if (B.kind != MOL_BC_ROBIN) return;
     if (DYN && B.prog >= 0) {
         int J[3] = {i0, i1, i2};

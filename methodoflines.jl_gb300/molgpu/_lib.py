@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libmolgpu.so")
 MOL_MAX_DIMS = 3
 MOL_MAX_FIELDS = 8
 MOL_MAX_REGS = 64
-MOL_ABI_VERSION = 1
+MOL_ABI_VERSION = 2
 
 STATUS = {
     0: "MOL_OK", -1: "MOL_ERR_INVALID", -2: "MOL_ERR_OOM", -3: "MOL_ERR_NONFINITE",
@@ -24,7 +24,7 @@ STATUS = {
 
 # term kinds, bc kinds, opcodes (mirror of the header enums)
 TERM_LINEAR, TERM_MIXED, TERM_WENO, TERM_NONLINLAP = 1, 2, 3, 4
-BC_NONE, BC_PERIODIC, BC_ROBIN = 0, 1, 2
+BC_NONE, BC_PERIODIC, BC_ROBIN, BC_EDGE = 0, 1, 2, 3
 (OP_CONST, OP_PARAM, OP_FIELD, OP_AUX, OP_COORD, OP_TIME, OP_TERM, OP_UPWIND, OP_ADD, OP_SUB, OP_MUL,
  OP_DIV, OP_NEG, OP_POWI, OP_POW, OP_FN, OP_CMP, OP_IFELSE, OP_OUT) = range(1, 20)
 FN_IDS = {"sin": 0, "cos": 1, "tan": 2, "exp": 3, "log": 4, "sqrt": 5, "abs": 6, "tanh": 7, "sinh": 8,
@@ -48,7 +48,7 @@ class mol_term(C.Structure):
 
 class mol_bc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("prog", C.c_int32), ("op", C.c_int32), ("extrap", C.c_int32),
-                ("a", C.c_double), ("b", C.c_double), ("g", C.c_double)]
+                ("a", C.c_double), ("b", C.c_double), ("g", C.c_double), ("iop", C.c_int32), ("pad", C.c_int32)]
 
 
 class mol_instr(C.Structure):

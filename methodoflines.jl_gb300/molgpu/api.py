@@ -42,6 +42,10 @@ class WENOScheme:
         return ("weno", self.epsilon)
 
 
+center_align = "center"   # CenterAlignedGrid: the grid points are lo:dx:hi
+edge_align = "edge"       # EdgeAlignedGrid: cell centres plus a ghost point beyond each end
+
+
 class MOLFiniteDifference:
     """``MOLFiniteDifference(dxs, time; approx_order, advection_scheme, grid_align, ...)``
     (src/interface/MOLFiniteDifference.jl:31-76).  Only the options the GPU path honours are kept.
@@ -56,7 +60,7 @@ class MOLFiniteDifference:
         self.time = time
         self.approx_order = int(approx_order)
         self.advection_scheme = advection_scheme if advection_scheme is not None else UpwindScheme()
-        self.grid_align = grid_align
+        self.grid_align = {"center_align": "center", "edge_align": "edge"}.get(grid_align, grid_align)
         self.kwargs = kwargs
 
 

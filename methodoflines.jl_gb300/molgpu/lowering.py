@@ -102,6 +102,22 @@ def make_axis(lo: float, hi: float, dxspec) -> Tuple[np.ndarray, float, bool]:
     return g, dx, True
 
 
+def make_edge_axis(lo: float, hi: float, dxspec) -> Tuple[np.ndarray, float, bool]:
+    """Edge-aligned grid (``generate_grid`` for EdgeAlignedGrid, discretize_vars.jl:373-390):
+    the points ``(lo - dx/2):dx:(hi + dx/2)``, cell centres plus one ghost point beyond each
+    end; an integer is a number of cells (``prepare_dx``, :284)."""
+    if isinstance(dxspec, (int, np.integer)) and not isinstance(dxspec, bool):
+        dx = (hi - lo) / int(dxspec)
+    elif isinstance(dxspec, (float, np.floating)):
+        dx = float(dxspec)
+    else:
+        raise NotImplementedError("edge-aligned grids given as points are not built")
+    edges = grid_points(lo, dx, hi)
+    if edges[-1] != hi:
+        raise NotImplementedError("an edge-aligned grid whose step misses the end (a grid of midpoints) is not built")
+    return grid_points(lo - dx / 2, dx, hi + dx / 2), dx, True
+
+
 # ------------------------------------------------------------------------------------
 # host evaluation of hoisted (coordinate-only) sub-expressions
 # ------------------------------------------------------------------------------------
@@ -435,6 +451,14 @@ def _deriv_orders(t, x) -> set:
     return out
 
 
+def _subst_iv(t, x, val):
+    if not isinstance(t, tuple) or not t:
+        return t
+    if t[0] == "iv" and t[1] == x:
+        return val
+    return tuple(_subst_iv(a, x, val) if isinstance(a, tuple) else a for a in t)
+
+
 def _is_zero(t) -> bool:
     return _leaves(t) <= {"num"} and float(host_eval(t, {}, {})) == 0.0
 
@@ -473,12 +497,17 @@ class _Lowerer:
             raise NotImplementedError("1 to 3 spatial dimensions are supported")
         fields = list(spec["fields"])
         disc = spec["disc"]
-        if disc.get("grid_align", "center") != "center":
-            raise NotImplementedError("only center-aligned grids are built")
+        align = disc.get("grid_align", "center")
+        if align not in ("center", "edge"):
+            raise NotImplementedError(f"grid alignment {align!r} is not built (center and edge are)")
+        self.edge = align == "edge"
         grids, dxs, uniform = [], [], []
         for x in ivs:
             lo, hi = spec["domain"][x]
-            g, dx, uni = make_axis(float(lo), float(hi), disc["dxs"][x])
+            if self.edge:
+                g, dx, uni = make_edge_axis(float(lo), float(hi), disc["dxs"][x])
+            else:
+                g, dx, uni = make_axis(float(lo), float(hi), disc["dxs"][x])
             grids.append(g)
             dxs.append(dx)
             uniform.append(uni)
@@ -506,6 +535,8 @@ class _Lowerer:
                 for j, x in enumerate(ivs):
                     if periodic[f][j] or 1 not in _deriv_orders(spec["eqs"][f], x):
                         continue
+                    if self.edge:
+                        raise NotImplementedError("WENO along a bounded edge-aligned dimension is not built")
                     if not uniform[j]:
                         raise NotImplementedError(f"WENO on the nonuniform grid of {x} is not built")
                     for side, arr in (("lo", lo_), ("hi", up_)):
@@ -531,6 +562,8 @@ class _Lowerer:
                           functions=dict(spec.get("functions", {})), order=int(disc.get("approx_order", 2)),
                           adv=adv, spec=spec, uniform=uniform)
         for j in range(len(ivs)):
+            if self.edge and any(periodic[f][j] for f in fields):
+                raise NotImplementedError("periodic boundaries on an edge-aligned grid are not built")
             if not uniform[j] and any(periodic[f][j] for f in fields):
                 # centered_difference.jl:36 asserts that no interface boundary meets a nonuniform dimension
                 raise NotImplementedError(f"periodic boundaries on the nonuniform grid of {ivs[j]}")
@@ -763,9 +796,17 @@ class _Lowerer:
         lw.cell_prog = len(lw.programs) - 1
         # boundary rows
         for (f, j, side), b in self.bcs.items():
-            a, bb, g = b["a"], b["b"], b["g"]
-            entry = {"kind": L.BC_ROBIN, "op": lw.op("centered", j, 1), "prog": -1, "a": 0.0, "b": 0.0, "g": 0.0,
-                     "extrap": 1 + lw.op("extrap", j, 0) if (f, j) in self.extrap_dims else 0}
+            # the row's own coordinate is the domain's end (axiesvals, discretize_vars.jl:321-330)
+            xe = ("num", float(self.spec["domain"][lw.ivs[j]][0 if side == "lo" else 1]))
+            a, bb, g = (_subst_iv(b[k], lw.ivs[j], xe) for k in ("a", "b", "g"))
+            if self.edge:
+                # the face half-way between the ghost point and the first (last) unknown:
+                # a * interpolation + b * half-offset derivative (generate_bc_eqs.jl:80-160)
+                entry = {"kind": L.BC_EDGE, "op": lw.op("half", j, 1), "iop": lw.op("interp", j, 0), "prog": -1,
+                         "a": 0.0, "b": 0.0, "g": 0.0, "extrap": 0}
+            else:
+                entry = {"kind": L.BC_ROBIN, "op": lw.op("centered", j, 1), "prog": -1, "a": 0.0, "b": 0.0,
+                         "g": 0.0, "extrap": 1 + lw.op("extrap", j, 0) if (f, j) in self.extrap_dims else 0}
             lv = _leaves(a) | _leaves(bb) | _leaves(g)
             if lv <= {"num"}:
                 entry["a"] = float(host_eval(a, {}, {}))
@@ -849,6 +890,7 @@ class Descriptor:
             b.op = e["op"]
             b.a, b.b, b.g = e["a"], e["b"], e["g"]
             b.extrap = e.get("extrap", 0)
+            b.iop = e.get("iop", 0)
         # operators and the weight pool
         pool: List[float] = []
         ops = (L.mol_op1d * max(1, len(lw.ops)))()

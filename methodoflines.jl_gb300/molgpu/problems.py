@@ -21,6 +21,10 @@ come from ``numpy.random.Generator(PCG64(seed))`` in Float64.
 10. viscous_burgers_weno_bounded  u_t = -u u_x + nu u_xx, Dirichlet data, WENO on [0, 1]
 11. burgers_weno_channel          2-D u_t = -u u_x - 0.5 u_y + nu lap u, WENO, x bounded
                  (Dirichlet), y periodic
+12. neumann_cosine_edge           u_t = u_xx on an edge-aligned grid of [0, 1], u_x = 0,
+                 u0 = cos(pi x) (the reference's Test 03 with grid_align = edge_align)
+13. robin_2d_edge                 2-D reaction-diffusion on an edge-aligned grid, time- and
+                 coordinate-dependent Robin, Neumann and Dirichlet rows
 """
 from __future__ import annotations
 
@@ -28,7 +32,7 @@ import math
 
 import numpy as np
 
-from .api import MOLFiniteDifference, UpwindScheme, WENOScheme
+from .api import MOLFiniteDifference, UpwindScheme, WENOScheme, edge_align
 from .symbolic import (Differential, Eq, Field, Interval, IV, Param, PDESystem, cos, exp, register, sin)
 
 
@@ -312,3 +316,35 @@ def burgers_weno_channel(nx: int = 65, ny: int = 49, nu: float = 2e-3):
     disc = MOLFiniteDifference({x: nx, y: ny}, t, advection_scheme=WENOScheme())
     h = min(1.0 / (nx - 1), 1.0 / (ny - 1))
     return sys, disc, {"dt": 0.3 / (1.5 / h + 4.0 * nu / h ** 2)}
+
+
+def neumann_cosine_edge(dx: float = 0.01, order: int = 8):
+    """u_t = u_xx on an edge-aligned grid (cell centres plus ghost points) of [0, 1] with
+    u_x = 0 at both faces; exact solution exp(-pi^2 t) cos(pi x)."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dxx = Differential(t), Differential(x), Differential(x) ** 2
+    eq = Eq(Dt(u(x, t)), Dxx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), cos(math.pi * x)), Eq(Dx(u(0.0, t)), 0.0), Eq(Dx(u(1.0, t)), 0.0)]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [])
+    disc = MOLFiniteDifference({x: dx}, t, approx_order=order, grid_align=edge_align)
+    return sys, disc, {"dt": 0.05 * dx * dx}
+
+
+def robin_2d_edge(dx: float = 0.025, dy: float = 0.03125, order: int = 4):
+    """Reaction-diffusion on an edge-aligned 2-D grid: Robin row with data depending on t and
+    y at x = 0, Neumann at x = 1, Dirichlet with data in y."""
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u = Field("u")
+    Dt, Dx = Differential(t), Differential(x)
+    Dxx, Dyy = Differential(x) ** 2, Differential(y) ** 2
+    k = Param("k", 1.0)
+    eq = Eq(Dt(u(x, y, t)), Dxx(u(x, y, t)) + Dyy(u(x, y, t)) - k * u(x, y, t) * u(x, y, t))
+    bcs = [Eq(u(x, y, 0.0), 1.0 + 0.3 * cos(2.0 * x) * sin(3.0 * y)),
+           Eq(2.0 * u(0.0, y, t) + 0.5 * Dx(u(0.0, y, t)), 1.0 + t * y), Eq(Dx(u(1.0, y, t)), 0.2),
+           Eq(u(x, 0.0, t), 1.0), Eq(u(x, 1.0, t), 1.0 + t)]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0))],
+                    [t, x, y], [u(x, y, t)], [k])
+    disc = MOLFiniteDifference({x: dx, y: dy}, t, approx_order=order, grid_align=edge_align)
+    h = min(dx, dy)
+    return sys, disc, {"dt": 0.1 * h * h}

@@ -96,6 +96,19 @@ def make_grid(lo: float, hi: float, dx_spec) -> Tuple[np.ndarray, float, bool]:
     return g, dx, True
 
 
+def make_edge_grid(lo: float, hi: float, dx_spec) -> Tuple[np.ndarray, float, bool]:
+    """``generate_grid`` for EdgeAlignedGrid (discretize_vars.jl:373-390) on a StepRangeLen
+    axis: ``(lo - dx/2):dx:(hi + dx/2)``; an integer is a number of cells (:284)."""
+    if isinstance(dx_spec, (int, np.integer)) and not isinstance(dx_spec, bool):
+        dx = (hi - lo) / int(dx_spec)
+    else:
+        dx = float(dx_spec)
+    axis = julia_float_range(lo, dx, hi)
+    if axis[-1] != hi:
+        raise NotImplementedError("oracle: edge-aligned grid of midpoints")
+    return julia_float_range(lo - dx / 2, dx, hi + dx / 2), dx, True
+
+
 # --------------------------------------------------------------------------------------
 # tap selection: centered_difference.jl:5-30, upwind_difference.jl:1-28,
 # half_offset_centred_difference.jl:9-37, interface_boundary.jl:26-42
@@ -268,9 +281,13 @@ class OracleProblem:
         self.grid = []
         self.dx = []
         self.uniform = []
+        self.edge = disc.get("grid_align", "center") == "edge"
         for x in self.ivs:
             lo, hi = spec["domain"][x]
-            g, dx, uni = make_grid(float(lo), float(hi), disc["dxs"][x])
+            if self.edge:
+                g, dx, uni = make_edge_grid(float(lo), float(hi), disc["dxs"][x])
+            else:
+                g, dx, uni = make_grid(float(lo), float(hi), disc["dxs"][x])
             self.uniform.append(uni)
             self.grid.append(g)
             self.dx.append(dx)
@@ -464,7 +481,10 @@ class OracleProblem:
                     b = self.bc[f][j][side]
                     if b is None:
                         continue
-                    self._fill_robin(F, f, j, side, b, t, p)
+                    if self.edge:
+                        self._fill_edge(F, f, j, side, b, t, p)
+                    else:
+                        self._fill_robin(F, f, j, side, b, t, p)
             for j in range(self.nd):
                 self._fill_extrapolated(F, f, j)
             self._zero_corners(F, f)
@@ -541,6 +561,50 @@ class OracleProblem:
             term = w[k] * F[at(tp)]
             acc = term if acc is None else acc + term
         F[at(i)] = (g - bb * acc) / (a + bb * w[k_b])
+
+    def _fill_edge(self, F, f, j, side, b, t, p):
+        """Edge-aligned boundary row (``boundary_value_maps`` for EdgeAlignedGrid,
+        generate_bc_eqs.jl:80-160): u and Dx(u) at the face become the half-offset
+        interpolation (``interpmap``) and first derivative (``halfoffsetmap``) at index 1, or
+        ``length - 1`` (``newindex(...; shift = true)``, MOL_utils.jl:75-97), and the equation
+        a*u + b*Dx(u) = g is solved for the ghost point."""
+        n = self.npts[j]
+        pos = 1 if side == "lo" else n - 1
+        ghost = 1 if side == "lo" else n
+        wi, ti = half_offset_taps(self.op("interp", j, 0), pos, n, False)
+        wd, td = half_offset_taps(self.op("half", j, 1), pos, n, False)
+        sl = self._other_interior_slices(f, j)
+
+        def at(idx):
+            s = list(sl)
+            s[j] = idx - 1
+            return tuple(s)
+        cs = {}
+        for k in range(self.nd):
+            if k == j:   # axiesvals (discretize_vars.jl:321-330): the domain's end, not the ghost
+                cs[self.ivs[k]] = float(self.spec["domain"][self.ivs[k]][0 if side == "lo" else 1])
+            else:
+                g = self.grid[k][sl[k]]
+                shp = [1] * self.nd
+                shp[k] = len(g)
+                cs[self.ivs[k]] = g.reshape([s for kk, s in enumerate(shp) if kk != j])
+        env = {"coords": cs, "t": t, "p": p}
+        a = self._eval_point(b["a"], env)
+        bb = self._eval_point(b["b"], env)
+        g = self._eval_point(b["g"], env)
+        si = sd = 0.0
+        ci = cd = 0.0
+        for w, tp in zip(wi, ti):
+            if tp == ghost:
+                ci = w
+            else:
+                si = si + w * F[at(tp)]
+        for w, tp in zip(wd, td):
+            if tp == ghost:
+                cd = w
+            else:
+                sd = sd + w * F[at(tp)]
+        F[at(ghost)] = (g - a * si - bb * sd) / (a * ci + bb * cd)
 
     def _zero_corners(self, F, f):
         if self.nd < 2:

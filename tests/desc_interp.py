@@ -65,11 +65,28 @@ class DescInterp:
             return acc
         if (side == 0 and I[d] != 1) or (side == 1 and I[d] != self.n[d]):
             return 0.0
-        if e is None or e["kind"] != L.BC_ROBIN:
+        if e is None or e["kind"] not in (L.BC_ROBIN, L.BC_EDGE):
             return 0.0
         a, b, g = e["a"], e["b"], e["g"]
         if e["prog"] >= 0:
             a, b, g = self.run_prog(e["prog"], "bc", None, I, t, p, u)
+        if e["kind"] == L.BC_EDGE:
+            # edge_row_value: interpolation and half-offset derivative at the face
+            pos, ghost = (1, 1) if side == 0 else (self.n[d] - 1, self.n[d])
+            sums, cg = [], []
+            for opi in (e["iop"], e["op"]):
+                w, taps = select(self.lw.ops[opi], pos, self.n[d], False)
+                acc, c = 0.0, 0.0
+                for wk, q in zip(w, taps):
+                    if q == ghost:
+                        c = wk
+                        continue
+                    J = list(I)
+                    J[d] = q
+                    acc = acc + wk * u[f * self.ncell + self.flat(J)]
+                sums.append(acc)
+                cg.append(c)
+            return (g - a * sums[0] - b * sums[1]) / (a * cg[0] + b * cg[1])
         if b == 0.0:
             return g / a
         op = self.lw.ops[e["op"]]
