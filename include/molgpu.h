@@ -233,6 +233,15 @@ int mol_plan_launch_config(const mol_plan* plan, int32_t* regs, int32_t* threads
 
 /* f!(du, u, p, t): the generated ODEFunction, called exactly as
  * benchmark/weno/suite.jl:283-289 does.  p may be NULL (descriptor defaults). */
+/* Full-grid values of the state u at time t for every field: the unknowns, the observed
+ * boundary values (boundary rows, extrapolated points, ghost points of edge-aligned grids), the
+ * periodic images (u[1] ~ u[l]) and the corner points (~ 0), field-major with the first
+ * dimension fastest, nfields * npts[0] * npts[1] * npts[2] doubles (unused dimensions count 1).
+ * Replaces the observed-variable reconstruction behind sol[u(t, x)] of the reference's
+ * PDETimeSeriesSolution (src/interface/solution/timedep.jl:19-80).  u, p, full: host or
+ * device; a host `full` is written before the call returns. */
+int mol_fill_grid(mol_plan* plan, const double* u, const double* p, double t, double* full);
+
 int mol_rhs(mol_plan* plan, double* du, const double* u, const double* p, double t);
 int mol_rhs_f32state(mol_plan* plan, float* du, const float* u, const float* p, double t);
 

@@ -354,6 +354,29 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
 template int launch_ssprk_step_io<double>(mol_plan*, const double*, double*, double*, double*, const double*, double);
 template int launch_ssprk_step_io<float>(mol_plan*, const float*, float*, float*, float*, const float*, double);
 
+// Every point of the full grid: unknowns, observed boundary values (boundary rows, extrapolated
+// points, ghost points of edge-aligned grids), periodic images and corner points (0), field-major
+// with the first dimension fastest: the arrays behind sol[u(t, x)] of the reference's
+// PDETimeSeriesSolution (interface/solution/timedep.jl:19-80), resolved exactly as the
+// right-hand side's taps are (load_pt).
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_fill_grid_t(const __grid_constant__ DevProb<T> P,
+                                                          const T* __restrict__ u, const T* __restrict__ p, T t,
+                                                          T* __restrict__ full, long long per_field) {
+    const long long total = per_field * P.nfields;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(g / per_field);
+        long long r = g - (long long)f * per_field;
+        const int i0 = (int)(r % P.n[0]);
+        r /= P.n[0];
+        const int i1 = (int)(r % P.n[1]);
+        const int i2 = (int)(r / P.n[1]);
+        full[g] = load_pt(P, u, f, i0 + 1, i1 + 1, i2 + 1, t, p);
+    }
+}
+
+
 }  // namespace mol
 
 using namespace mol;
@@ -1072,6 +1095,41 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
 }  // namespace
 
 extern "C" {
+
+int mol_fill_grid(mol_plan* plan, const double* u, const double* p, double t, double* full) {
+    if (!plan || !u || !full || !std::isfinite(t)) return MOL_ERR_INVALID;
+    DeviceGuard g(plan->dev);
+    int st;
+    Staged<double> su;
+    if ((st = stage_in<double>(plan, u, 10, su, true))) return st;
+    const double* pp = params_ptr<double>(plan, p, &st);
+    if (st) return st;
+    long long per_field = 1;
+    for (int q = 0; q < plan->desc.ndim; ++q) per_field *= plan->desc.npts[q];
+    const long long total = per_field * plan->nfields;
+    const bool host = !is_device_ptr(full);
+    double* out = full;
+    if (host) {
+        if (plan->grid_cap < total) {
+            void* q = nullptr;
+            if ((st = plan_alloc(plan, &q, sizeof(double) * (size_t)total))) return st;
+            plan->grid_buf = (double*)q;
+            plan->grid_cap = total;
+        }
+        out = plan->grid_buf;
+    }
+    const long long blocks = std::min<long long>((total + kThreads - 1) / kThreads, (long long)plan->sms * 8);
+    k_fill_grid_t<double><<<(unsigned)std::max<long long>(blocks, 1), kThreads, 0, plan->stream>>>(
+        plan->P64, su.ptr, pp, t, out, per_field);
+    if ((st = cuda_check(plan, cudaGetLastError(), "fill_grid"))) return st;
+    if (host) {
+        if ((st = cuda_check(plan, cudaMemcpyAsync(full, out, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost,
+                                                   plan->stream), "D2H")))
+            return st;
+        return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+    }
+    return MOL_OK;
+}
 
 int mol_rhs(mol_plan* plan, double* du, const double* u, const double* p, double t) {
     return rhs_impl<double>(plan, du, u, p, t);

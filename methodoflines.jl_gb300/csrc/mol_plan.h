@@ -84,6 +84,9 @@ struct mol_plan {
     bool face_pass = false;
     double* faces64 = nullptr;
     float* faces32 = nullptr;
+    // device staging of full-grid output (mol_fill_grid) for host destinations
+    double* grid_buf = nullptr;
+    long long grid_cap = 0;
 };
 
 namespace mol {

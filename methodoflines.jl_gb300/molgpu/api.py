@@ -12,6 +12,7 @@ Arrays may be numpy (host) or any object exposing ``data_ptr()`` on the GPU
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 from typing import Optional
 
@@ -19,7 +20,7 @@ import numpy as np
 
 from . import _lib as L
 from .lowering import Descriptor, Lowered, lower
-from .symbolic import IV, PDESystem
+from .symbolic import IV, Field, FieldApp, PDESystem
 
 
 class UpwindScheme:
@@ -120,6 +121,24 @@ class Plan:
         fn = L.lib().mol_rhs_f32state if f32 else L.lib().mol_rhs
         L.check(fn(self._h, pd, pu, pp, float(t)), self._h)
         return du
+
+    def fill_grid(self, u, t: float = 0.0, p=None, out=None):
+        """Every grid point of every field at state u and time t (``mol_fill_grid``): the
+        unknowns plus the observed boundary values, extrapolated and ghost points, periodic
+        images and corners, as sol[u(t, x)] holds them.  Host arrays give an array of shape
+        (nfields, *npts); a device ``out`` (nfields * prod(npts) doubles) is filled in place."""
+        lw = self.lowered
+        per = int(np.prod(lw.npts))
+        host_out = out is None or not hasattr(out, "data_ptr")
+        buf = np.empty(len(lw.fields) * per) if out is None else out
+        pu, _ = _ptr(u)
+        pp, _ = _ptr(p)
+        po, _ = _ptr(buf)
+        L.check(L.lib().mol_fill_grid(self._h, pu, pp, float(t), po), self._h)
+        if not host_out:
+            return buf
+        return np.stack([np.asarray(buf[k * per:(k + 1) * per]).reshape(lw.npts, order="F")
+                         for k in range(len(lw.fields))])
 
     def step_ssprk33(self, u, dt: float, nsteps: int, t0: float = 0.0, p=None):
         pu, f32 = _ptr(u)
@@ -287,25 +306,89 @@ class Tsit5:
     """Tsitouras 5(4) with the PI controller, adaptive on the device."""
 
 
-@dataclass
 class Solution:
-    u: np.ndarray
-    t: float
-    stats: dict
+    """Result of ``solve``: the final state ``u`` at time ``t`` with the integrator's ``stats``,
+    and the states saved at ``ts`` (``us``).
+
+    ``sol[u]`` (a Field, an applied field ``u(x, t)`` or a field name) gives that field on the
+    full grid at every saved time, an array (len(ts), *npts) whose boundary, extrapolated,
+    ghost, periodic-image and corner points are the observed values, filled in on the device
+    (``mol_fill_grid``), as sol[u(t, x)] of the reference's PDETimeSeriesSolution
+    (src/interface/solution/timedep.jl:19-80) holds them; ``sol[x]`` (an IV or its name) gives
+    the grid's coordinates along x, and ``sol.grid`` all of them."""
+
+    def __init__(self, u, t, stats, prob=None, ts=None, us=None):
+        self.u = u
+        self.t = t
+        self.stats = stats
+        self.prob = prob
+        self.ts = np.array([t] if ts is None else ts, dtype=np.float64)
+        self.us = [u] if us is None else us
+        self._cache = {}
+
+    @property
+    def grid(self):
+        lw = self.prob.lowered
+        return {x: g.copy() for x, g in zip(lw.ivs, lw.grids)}
+
+    def __getitem__(self, key):
+        lw = self.prob.lowered
+        name = key.name if isinstance(key, (IV, Field)) else (key.field.name if isinstance(key, FieldApp) else key)
+        if name in lw.ivs:
+            return lw.grids[lw.ivs.index(name)].copy()
+        if name not in lw.fields:
+            raise KeyError(name)
+        if "full" not in self._cache:
+            p = self.prob.p
+            self._cache["full"] = np.stack([self.prob.plan.fill_grid(v, tt, p) for v, tt in zip(self.us, self.ts)])
+        return self._cache["full"][:, lw.fields.index(name)]
 
 
 def solve(prob: ODEProblem, alg, dt: Optional[float] = None, abstol: float = 1e-6, reltol: float = 1e-3,
-          adaptive: Optional[bool] = None, u0=None, p=None) -> Solution:
+          adaptive: Optional[bool] = None, u0=None, p=None, saveat=None) -> Solution:
+    """Solve on the device.  ``saveat``: a step between saved times or the times themselves
+    (within tspan); the start and end of tspan are saved by default.  SSPRK33 needs save
+    times on its step grid; Tsit5 stops at each save time and continues from it (no
+    dense-output interpolation between steps)."""
     u = np.array(prob.u0 if u0 is None else u0, dtype=np.float64, copy=True)
     t0, t1 = float(prob.tspan[0]), float(prob.tspan[1])
     p = prob.p if p is None else np.ascontiguousarray(p, dtype=np.float64)
+    if saveat is None:
+        marks = [t1]
+    elif np.ndim(saveat) == 0:
+        step = float(saveat)
+        k = int(math.floor((t1 - t0) / step + 1e-9))
+        marks = [t0 + i * step for i in range(1, k + 1)]
+        if not marks or abs(marks[-1] - t1) > 1e-12 * max(1.0, abs(t1)):
+            marks.append(t1)
+    else:
+        marks = sorted(float(v) for v in saveat if float(v) > t0)
+    ts, us = [t0], [u.copy()]
     if isinstance(alg, SSPRK33) or alg is SSPRK33:
         if dt is None:
             raise ValueError("SSPRK33 needs dt")
-        n = int(round((t1 - t0) / dt))
-        prob.plan.step_ssprk33(u, dt, n, t0=t0, p=p)
-        return Solution(u, t0 + n * dt, {"nsteps": n})
+        done, total = 0, 0
+        for tm in marks:
+            n = int(round((tm - t0) / dt))
+            if abs(t0 + n * dt - tm) > 1e-9 * max(1.0, abs(tm)):
+                raise ValueError(f"save time {tm} is not on the SSPRK33 step grid")
+            prob.plan.step_ssprk33(u, dt, n - done, t0=t0 + done * dt, p=p)
+            done = n
+            ts.append(t0 + n * dt)
+            us.append(u.copy())
+            total = n
+        return Solution(u, t0 + total * dt, {"nsteps": total}, prob, ts, us)
     if isinstance(alg, Tsit5) or alg is Tsit5:
-        stats = prob.plan.solve_tsit5(u, t0, t1, abstol, reltol, p=p, dt0=dt or 0.0)
-        return Solution(u, stats["t"], stats)
+        stats, ta = {}, t0
+        agg = {"naccept": 0, "nreject": 0, "nf": 0}
+        for tm in marks:
+            stats = prob.plan.solve_tsit5(u, ta, tm, abstol, reltol, p=p, dt0=dt or 0.0)
+            for k in agg:
+                agg[k] += int(stats.get(k, 0))
+            ta = stats["t"]
+            ts.append(ta)
+            us.append(u.copy())
+        out = dict(stats)
+        out.update(agg)
+        return Solution(u, ta, out, prob, ts, us)
     raise ValueError(f"unsupported algorithm {alg}")
