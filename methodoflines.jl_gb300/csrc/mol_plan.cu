@@ -372,7 +372,14 @@ __global__ void __launch_bounds__(kThreads) k_fill_grid_t(const __grid_constant_
         r /= P.n[0];
         const int i1 = (int)(r % P.n[1]);
         const int i2 = (int)(r / P.n[1]);
-        full[g] = load_pt(P, u, f, i0 + 1, i1 + 1, i2 + 1, t, p);
+        // outside the interior box in two or more dimensions, periodic images included, is a
+        // corner (~ 0): the periodic and boundary rows cover only the interior's edge slices
+        // (generate_bc_eqs.jl:35-58, :396-459)
+        const int I[3] = {i0 + 1, i1 + 1, i2 + 1};
+        int nout = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) nout += (I[d] <= P.lo[d]) | (I[d] > P.n[d] - P.up[d]);
+        full[g] = nout > 1 ? T(0) : load_pt(P, u, f, I[0], I[1], I[2], t, p);
     }
 }
 
