@@ -519,6 +519,26 @@ class OracleProblem:
                 s[j] = i - 1
                 F[tuple(s)] = acc
 
+    def solution_arrays(self, u: np.ndarray, t: float, p: np.ndarray) -> Dict[str, np.ndarray]:
+        """The arrays behind sol[u(t, x)] (interface/solution/timedep.jl:19-80): every discrete
+        variable, the observed ones from their equations.  Periodic rows (generate_bc_eqs.jl:
+        35-58) and boundary rows cover only the interior's edge slices, so a point outside the
+        interior box in two or more dimensions, periodic images included, is a corner row ~ 0
+        (generate_bc_eqs.jl:396-459); ``full_arrays`` instead fills such points of two periodic
+        dimensions with the wrapped value, which is what the right-hand side's wrapped taps
+        read."""
+        full = self.full_arrays(u, t, p)
+        for f in self.fields:
+            outside = np.zeros(self.npts, dtype=np.int32)
+            for j in range(self.nd):
+                idx = np.arange(1, self.npts[j] + 1)
+                m = (idx <= self.lower[f][j]) | (idx > self.npts[j] - self.upper[f][j])
+                shp = [1] * self.nd
+                shp[j] = self.npts[j]
+                outside = outside + m.reshape(shp)
+            full[f][outside >= 2] = 0.0
+        return full
+
     def _other_interior_slices(self, f, j):
         sl = []
         for k in range(self.nd):

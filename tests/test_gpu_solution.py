@@ -32,7 +32,7 @@ def test_fill_grid_matches_oracle_full_arrays(gpu_lib, name):
     v = lw.u0 + 0.02 * np.random.default_rng(2).standard_normal(lw.n_unknowns)
     for t in (0.0, 0.6):
         got = plan.fill_grid(v, t)
-        ref = orc.full_arrays(v, t, lw.param_values)
+        ref = orc.solution_arrays(v, t, lw.param_values)
         for k, f in enumerate(lw.fields):
             assert got[k].shape == tuple(lw.npts)
             assert np.allclose(got[k], ref[f], rtol=1e-12, atol=1e-13), (name, f, t)
