@@ -266,7 +266,9 @@ def test_readme_example_heat_equation(gpu_lib):
     bcs = [Eq(u(x, 0.0), sin(math.pi * x)), Eq(u(0.0, t), 0.0), Eq(u(1.0, t), 0.0)]
     pdesys = PDESystem([eq], bcs, [(t, Interval(0.0, 0.1)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [])
     prob = discretize(pdesys, MOLFiniteDifference({x: 0.01}, t, approx_order=2))
-    sol = solve(prob, SSPRK33(), dt=2e-5)
+    sol = solve(prob, SSPRK33(), dt=2e-5, saveat=0.02)
     xs = np.arange(1, 100) * 0.01
     exact = np.exp(-math.pi ** 2 * 0.1) * np.sin(math.pi * xs)
     assert np.max(np.abs(sol.u - exact)) < 1e-3 * np.max(np.abs(exact))
+    assert sol[u].shape == (6, 101) and np.array_equal(sol[u][-1, 1:-1], sol.u)
+    assert np.array_equal(sol[x], np.arange(101) * 0.01) or np.allclose(sol[x], np.arange(101) * 0.01, atol=1e-15)
