@@ -116,17 +116,19 @@ __device__ __forceinline__ void last_block_advance(SolverState* S, double t_new)
 
 // `tfix` (when not NaN) is the step's start time, used instead of S->t and leaving S alone:
 // the adjoint recomputes single stages at known times without touching the solver state.
+// Cells [cbeg, cend) are processed (stage 1 runs in slabs while the state arrives from the
+// host; every other launch covers all cells).
 template <class T, class G, int STAGE>
 __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_ssprk_t(const __grid_constant__ DevProb<T> P, const T* __restrict__ uin, const T* u0, T* uout,
                                                       const T* __restrict__ p, SolverState* S, double dt,
-                                                      double tfix) {
+                                                      double tfix, long long cbeg, long long cend) {
     const bool from_state = !(tfix == tfix);
     const double t0 = from_state ? S->t : tfix;
     const double ts = STAGE == 1 ? t0 : (STAGE == 2 ? t0 + dt : t0 + dt / 2);
     T out[MOL_MAX_FIELDS];
     typename G::template Uniform<T> U;
     G::uniform(P, T(ts), p, U);
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+    for (long long c = cbeg + blockIdx.x * (long long)blockDim.x + threadIdx.x; c < cend;
          c += (long long)gridDim.x * blockDim.x) {
         int I[3];
         cell_index(P, c, I);

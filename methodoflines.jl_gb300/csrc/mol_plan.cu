@@ -260,6 +260,12 @@ double*& face_buf<double>(mol_plan* plan) { return plan->faces64; }
 template <>
 float*& face_buf<float>(mol_plan* plan) { return plan->faces32; }
 
+// The face pass runs for FP64 state with generated code only.
+template <class T>
+bool face_pass_on(const mol_plan* plan) {
+    return std::is_same<T, double>::value && plan->face_pass && plan->use_jit;
+}
+
 template <class T>
 int ensure_faces(mol_plan* plan) {
     if (!std::is_same<T, double>::value || !plan->face_pass || face_buf<T>(plan)) return MOL_OK;
@@ -320,7 +326,7 @@ template int launch_ssprk_step<float>(mol_plan*, float*, float*, float*, const f
 
 // One SSPRK33 step from uin to uout (which may be the same array).
 template <class T>
-int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, const T* p, double dt) {
+int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, const T* p, double dt, bool skip1) {
     const DevProb<T>& P = prob<T>(plan);
     const T* u = uin;
     g_launches += 3;
@@ -335,24 +341,113 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
         const double nan = std::nan("");
         cudaError_t e;
         DevProb<T> Pf = with_faces<T>(plan, cu, p, 0.0, nan, &e);
-        if (e == cudaSuccess)
-            e = launch_k(k[0], plan->nblocks, plan->nthreads, plan->stream, Pf, cu, cu, u1, p, plan->d_state, dt, nan);
+        const long long c0 = 0, c1 = plan->ncell;
+        if (e == cudaSuccess && !skip1)
+            e = launch_k(k[0], plan->nblocks, plan->nthreads, plan->stream, Pf, cu, cu, u1, p, plan->d_state, dt, nan,
+                         c0, c1);
         if (e == cudaSuccess) Pf = with_faces<T>(plan, cu1, p, dt, nan, &e);
         if (e == cudaSuccess)
-            e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, Pf, cu1, cu, u2, p, plan->d_state, dt, nan);
+            e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, Pf, cu1, cu, u2, p, plan->d_state, dt, nan,
+                         c0, c1);
         if (e == cudaSuccess) Pf = with_faces<T>(plan, cu2, p, dt / 2, nan, &e);
         if (e == cudaSuccess)
-            e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, Pf, cu2, cu, uout, p, plan->d_state, dt, nan);
+            e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, Pf, cu2, cu, uout, p, plan->d_state, dt, nan,
+                         c0, c1);
         return cuda_check(plan, e, "ssprk launch");
     }
     const double nan = std::nan("");
-    k_ssprk_t<T, InterpCell, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt, nan);
-    k_ssprk_t<T, InterpCell, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt, nan);
-    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, uout, p, plan->d_state, dt, nan);
+    const long long c1 = plan->ncell;
+    if (!skip1)
+        k_ssprk_t<T, InterpCell, 1><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u, u, u1, p, plan->d_state, dt, nan,
+                                                                                   0ll, c1);
+    k_ssprk_t<T, InterpCell, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt, nan,
+                                                                               0ll, c1);
+    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, uout, p, plan->d_state, dt, nan,
+                                                                               0ll, c1);
     return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
 }
-template int launch_ssprk_step_io<double>(mol_plan*, const double*, double*, double*, double*, const double*, double);
-template int launch_ssprk_step_io<float>(mol_plan*, const float*, float*, float*, float*, const float*, double);
+
+// Stage 1 of a step whose state is arriving from pinned host memory: the copy runs on a
+// side stream in slabs of whole slices of the slowest interior dimension, and stage 1 of
+// each slab starts as soon as the slabs its stencils reach (`halo` slices either side,
+// wrapped along a periodic dimension) have landed, so the host-to-device copy hides under
+// stage 1 instead of preceding it.  The arithmetic per cell is the unchunked launch's.
+template <class T>
+int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T* p, double dt) {
+    const int D = plan->desc.ndim - 1;
+    const long long nsl = plan->desc.npts[D] - plan->desc.lower[D] - plan->desc.upper[D];
+    const long long S = plan->ncell / nsl;  // cells per slice
+    const int K = plan->h2d_slabs;
+    const long long h = plan->halo;
+    const bool per = plan->per_last;
+    int st;
+    if (!plan->copy_stream) {
+        if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->copy_stream, cudaStreamNonBlocking), "copy stream")))
+            return st;
+        for (int k = 0; k <= kMaxSlabs; ++k)
+            if ((st = cuda_check(plan, cudaEventCreateWithFlags(&plan->slab_ev[k], cudaEventDisableTiming), "slab event")))
+                return st;
+    }
+    // the copies may only overwrite the staging buffer once earlier work on the stream is done
+    if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[kMaxSlabs], plan->stream), "record"))) return st;
+    if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->copy_stream, plan->slab_ev[kMaxSlabs], 0), "wait"))) return st;
+    auto copy = [&](long long s0, long long s1) -> int {
+        for (int f = 0; f < plan->nfields; ++f) {
+            const long long off = (long long)f * plan->ncell + s0 * S;
+            cudaError_t e = cudaMemcpyAsync(ud + off, host + off, sizeof(T) * (size_t)((s1 - s0) * S),
+                                            cudaMemcpyHostToDevice, plan->copy_stream);
+            if (e != cudaSuccess) return cuda_check(plan, e, "H2D slab");
+        }
+        return MOL_OK;
+    };
+    // slab boundaries; along a periodic dimension the last `halo` slices travel first, since
+    // slab 0 reads them through the wrap
+    std::vector<long long> b(K + 1);
+    for (int k = 0; k <= K; ++k) b[k] = nsl * k / K;
+    const long long tail = per ? std::min(h, nsl) : 0;
+    if (tail && (st = copy(nsl - tail, nsl))) return st;
+    std::vector<long long> landed(K);  // slices [0, landed[k]) are on the device after event k
+    for (int k = 0; k < K; ++k) {
+        const long long s1 = std::min(b[k + 1], nsl - tail);
+        const long long s0 = std::min(b[k], s1);
+        if (s1 > s0 && (st = copy(s0, s1))) return st;
+        landed[k] = k == K - 1 ? nsl : s1;
+        if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[k], plan->copy_stream), "record"))) return st;
+    }
+    const DevProb<T>& P = prob<T>(plan);
+    const double nan = std::nan("");
+    const bool is64 = std::is_same<T, double>::value;
+    int waited = -1;
+    for (int k = 0; k < K; ++k) {
+        const long long need = std::min(nsl, b[k + 1] + h);  // slices [0, need) must have landed
+        int j = k;
+        while (j < K - 1 && landed[j] < need) ++j;
+        if (j > waited) {
+            if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[j], 0), "wait slab"))) return st;
+            waited = j;
+        }
+        const long long c0 = b[k] * S, c1 = b[k + 1] * S;
+        if (c1 <= c0) continue;
+        const int thr = plan->use_jit ? plan->nthreads : kThreads;
+        const int blocks = (int)std::min<long long>(plan->nblocks, (c1 - c0 + thr - 1) / thr);
+        ++g_launches;
+        if (plan->use_jit) {
+            cudaKernel_t kk = is64 ? plan->jit.ssp64[0] : plan->jit.ssp32[0];
+            cudaError_t e = launch_k(kk, blocks, plan->nthreads, plan->stream, P, (const T*)ud, (const T*)ud, u1, p,
+                                     plan->d_state, dt, nan, c0, c1);
+            if ((st = cuda_check(plan, e, "stage-1 slab"))) return st;
+        } else {
+            k_ssprk_t<T, InterpCell, 1><<<blocks, kThreads, 0, plan->stream>>>(P, ud, ud, u1, p, plan->d_state, dt, nan,
+                                                                                c0, c1);
+            if ((st = cuda_check(plan, cudaGetLastError(), "stage-1 slab"))) return st;
+        }
+    }
+    // the remaining stages read the whole state: every slab is in once the last event is
+    return cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[K - 1], 0), "wait last slab");
+}
+template int launch_ssprk_step_io<double>(mol_plan*, const double*, double*, double*, double*, const double*, double,
+                                          bool);
+template int launch_ssprk_step_io<float>(mol_plan*, const float*, float*, float*, float*, const float*, double, bool);
 
 // Every point of the full grid: unknowns, observed boundary values (boundary rows, extrapolated
 // points, ghost points of edge-aligned grids), periodic images and corner points (0), field-major
@@ -767,6 +862,12 @@ int mol_plan_destroy(mol_plan* plan) {
     if (plan->g_ssp64) cudaGraphExecDestroy(plan->g_ssp64);
     if (plan->g_ssp32) cudaGraphExecDestroy(plan->g_ssp32);
     for (void* p : plan->allocs) cudaFree(p);
+    if (plan->copy_stream) {
+        cudaStreamSynchronize(plan->copy_stream);
+        cudaStreamDestroy(plan->copy_stream);
+    }
+    for (cudaEvent_t e : plan->slab_ev)
+        if (e) cudaEventDestroy(e);
     if (plan->own_stream && plan->stream) cudaStreamDestroy(plan->stream);
     delete plan;
     return MOL_OK;
@@ -928,6 +1029,23 @@ int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member
             if (req && req[0] == '1') return fail(set_err(plan, st ? st : MOL_ERR_UNSUPPORTED, plan->jit_err));
         }
     }
+    // Slabs of the streamed host-to-device copy: a stencil of any operator (its interior
+    // taps, boundary and extrapolation tables) or a WENO term reaches at most `halo` slices
+    // of the slowest dimension.  Only problems large enough to matter and with at least
+    // 2 * halo + 1 slices per slab stream their state.
+    {
+        const int D = d->ndim - 1;
+        long long reach = 2;
+        for (int i = 0; i < d->nops; ++i) {
+            const mol_op1d& o = d->ops[i];
+            reach = std::max<long long>(reach, std::max({std::abs(o.omin), std::abs(o.omin + o.L - 1), o.bLlo, o.bLhi}));
+        }
+        plan->halo = reach + 1;
+        for (int f = 0; f < d->nfields; ++f) plan->per_last |= d->bc[f][D][0].kind == MOL_BC_PERIODIC;
+        const long long nsl = d->npts[D] - d->lower[D] - d->upper[D];
+        const long long k = std::min<long long>(kMaxSlabs, nsl / (2 * plan->halo + 1));
+        plan->h2d_slabs = (plan->ncell >= (1ll << 16) && k >= 2) ? (int)k : 0;
+    }
     *out = plan;
     return MOL_OK;
 }
@@ -1033,8 +1151,17 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
         const char* zc = getenv("MOL_ZERO_COPY");
         if (!(zc && zc[0] == '0')) hz = (T*)mapped_host_ptr(u);
     }
-    if (host && (st = cuda_check(plan, cudaMemcpyAsync(ud, u, sizeof(T) * (size_t)plan->nunk, cudaMemcpyHostToDevice,
-                                                       plan->stream), "H2D")))
+    // Pinned host state and a problem that slabs along its slowest dimension: the first step's
+    // stage 1 runs slab by slab behind the host-to-device copy (launch_stage1_streamed).
+    // MOL_H2D_SLABS=0 copies first, then steps.
+    bool streamed = false;
+    if (host && nsteps > 0 && plan->h2d_slabs >= 2 && !face_pass_on<T>(plan) && mapped_host_ptr(u)) {
+        const char* hs = getenv("MOL_H2D_SLABS");
+        streamed = !(hs && hs[0] == '0');
+    }
+    if (host && !streamed &&
+        (st = cuda_check(plan, cudaMemcpyAsync(ud, u, sizeof(T) * (size_t)plan->nunk, cudaMemcpyHostToDevice,
+                                               plan->stream), "H2D")))
         return st;
     const T* pp = params_ptr<T>(plan, p, &st);
     if (st) return st;
@@ -1046,6 +1173,14 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     ++g_launches;
     T* u1 = ws[1];
     T* u2 = ws[2];
+    if (streamed) {
+        if ((st = launch_stage1_streamed<T>(plan, u, ud, u1, pp, dt))) return st;
+        T* out1 = (nsteps == 1 && hz) ? hz : ud;
+        if ((st = launch_ssprk_step_io<T>(plan, ud, out1, u1, u2, pp, dt, true))) return st;
+        --nsteps;
+        if (nsteps == 0 && hz) return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+    }
+    if (nsteps == 0) hz = nullptr;  // nothing left to step: the state goes back by copy below
     const int64_t nmid = hz ? nsteps - 1 : nsteps;  // steps that stay in the device buffer ud
     // chunks of `chunk` steps replayed as one CUDA graph; the tail is launched directly
     const int chunk = plan->g_chunk;

@@ -31,6 +31,8 @@ struct PlanArrays {
 
 struct mol_plan_impl;
 
+constexpr int kMaxSlabs = 8;  // slabs of the streamed host-to-device copy
+
 }  // namespace mol
 
 struct mol_plan {
@@ -87,6 +89,13 @@ struct mol_plan {
     // device staging of full-grid output (mol_fill_grid) for host destinations
     double* grid_buf = nullptr;
     long long grid_cap = 0;
+    // host-to-device copy of a pinned state in slabs of the slowest dimension, overlapped
+    // with stage 1 (h2d_slabs < 2: one copy before the step)
+    int h2d_slabs = 0;
+    long long halo = 0;      // slices a stencil reaches along the slowest dimension
+    bool per_last = false;   // the slowest dimension is periodic
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t slab_ev[mol::kMaxSlabs + 1] = {nullptr};
 };
 
 namespace mol {
@@ -123,7 +132,8 @@ int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t);
 template <class T>
 int launch_ssprk_step(mol_plan* plan, T* u, T* u1, T* u2, const T* p, double dt);
 template <class T>
-int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, const T* p, double dt);
+int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, const T* p, double dt,
+                         bool skip1 = false);
 void* mapped_host_ptr(const void* p);
 // The face pass of nonlinear-Laplacian terms (see k_faces_t): buffer allocation (before any
 // capture) and the launch, returning the problem view the next cell kernel takes.
