@@ -34,7 +34,9 @@ def test_streamed_first_step_bit_identical(gpu_lib, monkeypatch, name, nsteps, c
     h = pinned.numpy()
     plan.step_ssprk33(h, dt, nsteps, t0=0.2)
     dev = torch.tensor(lw.u0, device="cuda")
+    torch.cuda.synchronize()
     plan.step_ssprk33(dev, dt, nsteps, t0=0.2)
+    torch.cuda.synchronize()   # the plan's own stream does not order with torch's
     assert np.array_equal(h, dev.cpu().numpy()), name
     monkeypatch.setenv("MOL_H2D_SLABS", "0")
     pinned.copy_(torch.from_numpy(lw.u0))
