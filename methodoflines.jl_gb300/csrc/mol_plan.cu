@@ -373,11 +373,10 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
 // wrapped along a periodic dimension) have landed, so the host-to-device copy hides under
 // stage 1 instead of preceding it.  The arithmetic per cell is the unchunked launch's.
 template <class T>
-int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T* p, double dt) {
+int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T* p, double dt, int K) {
     const int D = plan->desc.ndim - 1;
     const long long nsl = plan->desc.npts[D] - plan->desc.lower[D] - plan->desc.upper[D];
     const long long S = plan->ncell / nsl;  // cells per slice
-    const int K = plan->h2d_slabs;
     const long long h = plan->halo;
     const bool per = plan->per_last;
     int st;
@@ -391,55 +390,51 @@ int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T*
     // the copies may only overwrite the staging buffer once earlier work on the stream is done
     if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[kMaxSlabs], plan->stream), "record"))) return st;
     if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->copy_stream, plan->slab_ev[kMaxSlabs], 0), "wait"))) return st;
+    // slices [s0, s1) of every field in one strided copy (fields are ncell apart)
     auto copy = [&](long long s0, long long s1) -> int {
-        for (int f = 0; f < plan->nfields; ++f) {
-            const long long off = (long long)f * plan->ncell + s0 * S;
-            cudaError_t e = cudaMemcpyAsync(ud + off, host + off, sizeof(T) * (size_t)((s1 - s0) * S),
-                                            cudaMemcpyHostToDevice, plan->copy_stream);
-            if (e != cudaSuccess) return cuda_check(plan, e, "H2D slab");
-        }
-        return MOL_OK;
+        if (s1 <= s0) return MOL_OK;
+        const size_t pitch = sizeof(T) * (size_t)plan->ncell;
+        cudaError_t e = cudaMemcpy2DAsync(ud + s0 * S, pitch, host + s0 * S, pitch, sizeof(T) * (size_t)((s1 - s0) * S),
+                                          (size_t)plan->nfields, cudaMemcpyHostToDevice, plan->copy_stream);
+        return e == cudaSuccess ? MOL_OK : cuda_check(plan, e, "H2D slab");
     };
-    // slab boundaries; along a periodic dimension the last `halo` slices travel first, since
-    // slab 0 reads them through the wrap
-    std::vector<long long> b(K + 1);
-    for (int k = 0; k <= K; ++k) b[k] = nsl * k / K;
-    const long long tail = per ? std::min(h, nsl) : 0;
-    if (tail && (st = copy(nsl - tail, nsl))) return st;
-    std::vector<long long> landed(K);  // slices [0, landed[k]) are on the device after event k
-    for (int k = 0; k < K; ++k) {
-        const long long s1 = std::min(b[k + 1], nsl - tail);
-        const long long s0 = std::min(b[k], s1);
-        if (s1 > s0 && (st = copy(s0, s1))) return st;
-        landed[k] = k == K - 1 ? nsl : s1;
-        if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[k], plan->copy_stream), "record"))) return st;
-    }
     const DevProb<T>& P = prob<T>(plan);
     const double nan = std::nan("");
     const bool is64 = std::is_same<T, double>::value;
-    int waited = -1;
-    for (int k = 0; k < K; ++k) {
-        const long long need = std::min(nsl, b[k + 1] + h);  // slices [0, need) must have landed
-        int j = k;
-        while (j < K - 1 && landed[j] < need) ++j;
-        if (j > waited) {
-            if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[j], 0), "wait slab"))) return st;
-            waited = j;
-        }
-        const long long c0 = b[k] * S, c1 = b[k + 1] * S;
-        if (c1 <= c0) continue;
+    auto stage1 = [&](long long c0, long long c1) -> int {
+        if (c1 <= c0) return MOL_OK;
         const int thr = plan->use_jit ? plan->nthreads : kThreads;
         const int blocks = (int)std::min<long long>(plan->nblocks, (c1 - c0 + thr - 1) / thr);
         ++g_launches;
         if (plan->use_jit) {
             cudaKernel_t kk = is64 ? plan->jit.ssp64[0] : plan->jit.ssp32[0];
-            cudaError_t e = launch_k(kk, blocks, plan->nthreads, plan->stream, P, (const T*)ud, (const T*)ud, u1, p,
-                                     plan->d_state, dt, nan, c0, c1);
-            if ((st = cuda_check(plan, e, "stage-1 slab"))) return st;
-        } else {
-            k_ssprk_t<T, InterpCell, 1><<<blocks, kThreads, 0, plan->stream>>>(P, ud, ud, u1, p, plan->d_state, dt, nan,
-                                                                                c0, c1);
-            if ((st = cuda_check(plan, cudaGetLastError(), "stage-1 slab"))) return st;
+            return cuda_check(plan, launch_k(kk, blocks, plan->nthreads, plan->stream, P, (const T*)ud, (const T*)ud, u1,
+                                             p, plan->d_state, dt, nan, c0, c1), "stage-1 slab");
+        }
+        k_ssprk_t<T, InterpCell, 1><<<blocks, kThreads, 0, plan->stream>>>(P, ud, ud, u1, p, plan->d_state, dt, nan,
+                                                                            c0, c1);
+        return cuda_check(plan, cudaGetLastError(), "stage-1 slab");
+    };
+    // slab boundaries; along a periodic dimension the last `halo` slices travel first, since
+    // slab 0 reads them through the wrap.  Copies and stage-1 launches are issued interleaved,
+    // each launch right after the copy that completes what its stencils reach.
+    std::vector<long long> b(K + 1);
+    for (int k = 0; k <= K; ++k) b[k] = nsl * k / K;
+    const long long tail = per ? std::min(h, nsl) : 0;
+    if ((st = copy(nsl - tail, nsl))) return st;
+    int next = 0;
+    for (int k = 0; k < K; ++k) {
+        const long long s1 = std::min(b[k + 1], nsl - tail);
+        if ((st = copy(std::min(b[k], s1), s1))) return st;
+        const long long landed = k == K - 1 ? nsl : s1;  // slices [0, landed) are on the device
+        if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[k], plan->copy_stream), "record"))) return st;
+        bool waited = false;
+        while (next < K && std::min(nsl, b[next + 1] + h) <= landed) {
+            if (!waited && (st = cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[k], 0), "wait slab")))
+                return st;
+            waited = true;
+            if ((st = stage1(b[next] * S, b[next + 1] * S))) return st;
+            ++next;
         }
     }
     // the remaining stages read the whole state: every slab is in once the last event is
@@ -1154,11 +1149,12 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     // Pinned host state and a problem that slabs along its slowest dimension: the first step's
     // stage 1 runs slab by slab behind the host-to-device copy (launch_stage1_streamed).
     // MOL_H2D_SLABS=0 copies first, then steps.
-    bool streamed = false;
+    int slabs = 0;
     if (host && nsteps > 0 && plan->h2d_slabs >= 2 && !face_pass_on<T>(plan) && mapped_host_ptr(u)) {
-        const char* hs = getenv("MOL_H2D_SLABS");
-        streamed = !(hs && hs[0] == '0');
+        const char* hs = getenv("MOL_H2D_SLABS");  // a slab count (0: copy first, then step)
+        slabs = std::min(plan->h2d_slabs, (hs && hs[0]) ? std::max(0, atoi(hs)) : 4);
     }
+    const bool streamed = slabs >= 2;
     if (host && !streamed &&
         (st = cuda_check(plan, cudaMemcpyAsync(ud, u, sizeof(T) * (size_t)plan->nunk, cudaMemcpyHostToDevice,
                                                plan->stream), "H2D")))
@@ -1174,7 +1170,7 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     T* u1 = ws[1];
     T* u2 = ws[2];
     if (streamed) {
-        if ((st = launch_stage1_streamed<T>(plan, u, ud, u1, pp, dt))) return st;
+        if ((st = launch_stage1_streamed<T>(plan, u, ud, u1, pp, dt, slabs))) return st;
         T* out1 = (nsteps == 1 && hz) ? hz : ud;
         if ((st = launch_ssprk_step_io<T>(plan, ud, out1, u1, u2, pp, dt, true))) return st;
         --nsteps;
