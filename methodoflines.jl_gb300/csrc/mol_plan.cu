@@ -415,27 +415,22 @@ int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T*
                                                                             c0, c1);
         return cuda_check(plan, cudaGetLastError(), "stage-1 slab");
     };
-    // slab boundaries; along a periodic dimension the last `halo` slices travel first, since
-    // slab 0 reads them through the wrap.  Copies and stage-1 launches are issued interleaved,
-    // each launch right after the copy that completes what its stencils reach.
+    // Slab boundaries b[k]; along a periodic dimension the last `halo` slices travel first,
+    // since the first slices read them through the wrap.  Stage 1 of the window
+    // [b[k] - halo, b[k+1] - halo) reads slices below b[k+1] only, so it runs as soon as slab k
+    // has landed (the last window runs to the end): each launch is issued right behind its
+    // copy, and only the last window waits for the whole state.
     std::vector<long long> b(K + 1);
     for (int k = 0; k <= K; ++k) b[k] = nsl * k / K;
     const long long tail = per ? std::min(h, nsl) : 0;
     if ((st = copy(nsl - tail, nsl))) return st;
-    int next = 0;
     for (int k = 0; k < K; ++k) {
         const long long s1 = std::min(b[k + 1], nsl - tail);
         if ((st = copy(std::min(b[k], s1), s1))) return st;
-        const long long landed = k == K - 1 ? nsl : s1;  // slices [0, landed) are on the device
         if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[k], plan->copy_stream), "record"))) return st;
-        bool waited = false;
-        while (next < K && std::min(nsl, b[next + 1] + h) <= landed) {
-            if (!waited && (st = cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[k], 0), "wait slab")))
-                return st;
-            waited = true;
-            if ((st = stage1(b[next] * S, b[next + 1] * S))) return st;
-            ++next;
-        }
+        if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[k], 0), "wait slab"))) return st;
+        const long long w0 = std::max(0ll, b[k] - h), w1 = k == K - 1 ? nsl : std::max(0ll, b[k + 1] - h);
+        if ((st = stage1(w0 * S, w1 * S))) return st;
     }
     // the remaining stages read the whole state: every slab is in once the last event is
     return cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[K - 1], 0), "wait last slab");
