@@ -367,57 +367,6 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
     return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
 }
 
-// One SSPRK33 stage over cells [c0, c1) (no face pass): generated code or the interpreter.
-template <class T>
-int launch_stage(mol_plan* plan, int which, const T* uin, const T* u0, T* uout, const T* p, double dt, double tfix,
-                 long long c0, long long c1) {
-    if (c1 <= c0) return MOL_OK;
-    const DevProb<T>& P = prob<T>(plan);
-    const int thr = plan->use_jit ? plan->nthreads : kThreads;
-    const int blocks = (int)std::min<long long>(plan->nblocks, (c1 - c0 + thr - 1) / thr);
-    ++g_launches;
-    if (plan->use_jit) {
-        const bool is64 = std::is_same<T, double>::value;
-        cudaKernel_t kk = (is64 ? plan->jit.ssp64 : plan->jit.ssp32)[which - 1];
-        return cuda_check(plan, launch_k(kk, blocks, plan->nthreads, plan->stream, P, uin, u0, uout, p, plan->d_state,
-                                         dt, tfix, c0, c1), "stage launch");
-    }
-    if (which == 1)
-        k_ssprk_t<T, InterpCell, 1><<<blocks, kThreads, 0, plan->stream>>>(P, uin, u0, uout, p, plan->d_state, dt, tfix,
-                                                                            c0, c1);
-    else if (which == 2)
-        k_ssprk_t<T, InterpCell, 2><<<blocks, kThreads, 0, plan->stream>>>(P, uin, u0, uout, p, plan->d_state, dt, tfix,
-                                                                            c0, c1);
-    else
-        k_ssprk_t<T, InterpCell, 3><<<blocks, kThreads, 0, plan->stream>>>(P, uin, u0, uout, p, plan->d_state, dt, tfix,
-                                                                            c0, c1);
-    return cuda_check(plan, cudaGetLastError(), "stage launch");
-}
-
-// Stage 3 of the last step of a call on a pinned host state, in slabs of the slowest
-// dimension: each slab's result goes back to the host on the copy stream while the next
-// slab computes (stage 3 reads only the complete stage-2 state, so slabs have no halo).
-// Runs at the explicit start time t of the step and leaves the solver's time alone.
-template <class T>
-int launch_stage3_streamed(mol_plan* plan, T* host, T* ud, const T* u2, const T* p, double dt, double t, int K) {
-    const int D = plan->desc.ndim - 1;
-    const long long nsl = plan->desc.npts[D] - plan->desc.lower[D] - plan->desc.upper[D];
-    const long long S = plan->ncell / nsl;
-    const size_t pitch = sizeof(T) * (size_t)plan->ncell;
-    int st;
-    for (int k = 0; k < K; ++k) {
-        const long long s0 = nsl * k / K, s1 = nsl * (k + 1) / K;
-        if ((st = launch_stage<T>(plan, 3, u2, ud, ud, p, dt, t, s0 * S, s1 * S))) return st;
-        if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[k], plan->stream), "record"))) return st;
-        if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->copy_stream, plan->slab_ev[k], 0), "wait"))) return st;
-        if ((st = cuda_check(plan, cudaMemcpy2DAsync(host + s0 * S, pitch, ud + s0 * S, pitch,
-                                                     sizeof(T) * (size_t)((s1 - s0) * S), (size_t)plan->nfields,
-                                                     cudaMemcpyDeviceToHost, plan->copy_stream), "D2H slab")))
-            return st;
-    }
-    return cuda_check(plan, cudaStreamSynchronize(plan->copy_stream), "sync copies");
-}
-
 // Stage 1 of a step whose state is arriving from pinned host memory: the copy runs on a
 // side stream in slabs of whole slices of the slowest interior dimension, and stage 1 of
 // each slab starts as soon as the slabs its stencils reach (`halo` slices either side,
@@ -1215,17 +1164,6 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     ++g_launches;
     T* u1 = ws[1];
     T* u2 = ws[2];
-    if (streamed && nsteps == 1) {
-        // one step: stage 1 behind the slabbed copy in, stage 3 ahead of the slabbed copy out
-        // (MOL_D2H_SLABS=0 writes stage 3 straight into the pinned state instead)
-        const char* ds = getenv("MOL_D2H_SLABS");
-        if (!(ds && ds[0] == '0')) {
-            if ((st = launch_stage1_streamed<T>(plan, u, ud, u1, pp, dt, slabs))) return st;
-            if ((st = launch_stage<T>(plan, 2, u1, ud, u2, pp, dt, std::nan(""), 0, plan->ncell))) return st;
-            if ((st = launch_stage3_streamed<T>(plan, u, ud, u2, pp, dt, t0, slabs))) return st;
-            return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
-        }
-    }
     if (streamed) {
         if ((st = launch_stage1_streamed<T>(plan, u, ud, u1, pp, dt, slabs))) return st;
         T* out1 = (nsteps == 1 && hz) ? hz : ud;
