@@ -1,7 +1,7 @@
 """The first step of a call on a pinned host state streams the host-to-device copy in slabs
-of the slowest dimension and runs stage 1 slab by slab behind it: the result equals stepping a device copy of
-the state bit for bit (periodic, bounded and 3-D slowest dimensions, one and several steps,
-generated code and interpreter)."""
+of the slowest dimension and runs stage 1 slab by slab behind it: the result equals stepping
+a device copy of the state bit for bit (periodic, bounded and 3-D slowest dimensions, one
+and several steps, generated code and interpreter)."""
 import numpy as np
 import pytest
 
