@@ -75,9 +75,12 @@ typedef enum mol_status {
  * Weights are offsets into mol_problem_desc.weights.  nrows = 0: one interior row shared by
  * every interior point.  nrows > 0 (a nonuniform grid, centered_diff_weights.jl:77-153 and
  * the DX <: AbstractVector method of centered_difference.jl:32-56): one row of L weights per
- * interior point, row (i - nlo - 1) at w_int + (i - nlo - 1) * L; then nrows must equal
- * len - nlo - nhi, the dimension must not be periodic, and only LINEAR terms may use the
- * operator (MOL_ERR_UNSUPPORTED otherwise). */
+ * interior point, row (i - nlo - 1) at w_int + (i - nlo - 1) * L; then every interior
+ * position that reads an interior row needs one (nrows >= min(len - upper, len - nhi) - nlo),
+ * the dimension must not be periodic, and only LINEAR terms may use the operator
+ * (MOL_ERR_UNSUPPORTED otherwise).  The reference's nonuniform upwind operators
+ * (upwind_diff_weights.jl:93-171 with the selection of upwind_difference.jl:131-162) are
+ * expressed this way too. */
 typedef struct mol_op1d {
     int32_t L, omin, nlo, bLlo, nhi, bLhi, hi_base, nrows;
     int64_t w_int, w_lo, w_hi;

@@ -581,7 +581,10 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
                     const mol_op1d& o = d->ops[t.op];
                     if (d->bc[t.field][t.dim][0].kind == MOL_BC_PERIODIC)
                         return set_err(plan, MOL_ERR_UNSUPPORTED, "per-point operator rows on a periodic dimension");
-                    if (o.nrows != d->npts[t.dim] - o.nlo - o.nhi)
+                    // every interior point that reads an interior row has one: rows up to
+                    // position min(n - upper, n - nhi) (row index = position - nlo - 1)
+                    const long long n = d->npts[t.dim];
+                    if (o.nrows < std::min<long long>(n - d->upper[t.dim], n - o.nhi) - o.nlo)
                         return set_err(plan, MOL_ERR_INVALID, "operator rows do not match the grid");
                 }
                 break;

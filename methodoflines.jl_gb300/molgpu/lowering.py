@@ -27,7 +27,7 @@ import numpy as np
 
 from . import _lib as L
 from .weights import (Operator, centered, centered_nonuniform, extrapolator, half_centered, select, upwind,
-                      wrap)
+                      upwind_nonuniform, wrap)
 
 # ------------------------------------------------------------------------------------
 # grids (Julia Float64 ranges)
@@ -380,11 +380,15 @@ class Lowered:
         if key not in self.op_keys:
             dx = self.dx[j]
             if self.uniform and not self.uniform[j]:
-                if kind != "centered":
+                if kind == "centered":
+                    o = centered_nonuniform(d, self.order, self.grids[j])
+                elif kind in ("wind_pos", "wind_neg") and d + p == 2:
+                    # the reference's nonuniform tables reach every interior point only for L = 2
+                    o = upwind_nonuniform(d, p, self.grids[j], d + p - 1 if kind == "wind_pos" else 0)
+                else:
                     raise NotImplementedError(
-                        f"{kind} operators on the nonuniform grid of {self.ivs[j]} are not built "
-                        "(centered derivatives and boundary rows are)")
-                o = centered_nonuniform(d, self.order, self.grids[j])
+                        f"{kind} operators (order {d}, upwind order {p}) on the nonuniform grid of {self.ivs[j]} "
+                        "are not built (centered derivatives, first-order upwinding and boundary rows are)")
             elif kind == "centered":
                 o = centered(d, self.order, dx)
             elif kind == "wind_pos":       # offside d+p-1: backward taps (windmap[2])

@@ -25,6 +25,8 @@ come from ``numpy.random.Generator(PCG64(seed))`` in Float64.
                  u0 = cos(pi x) (the reference's Test 03 with grid_align = edge_align)
 13. robin_2d_edge                 2-D reaction-diffusion on an edge-aligned grid, time- and
                  coordinate-dependent Robin, Neumann and Dirichlet rows
+14. convection_nonuniform         u_t = -v u_x on clustered grids (first-order upwinding on a
+                 nonuniform grid; test/Convection_NU/MOL_1D_Linear_Convection_NonUniform.jl)
 """
 from __future__ import annotations
 
@@ -348,3 +350,42 @@ def robin_2d_edge(dx: float = 0.025, dy: float = 0.03125, order: int = 4):
     disc = MOLFiniteDifference({x: dx, y: dy}, t, approx_order=order, grid_align=edge_align)
     h = min(dx, dy)
     return sys, disc, {"dt": 0.1 * h * h}
+
+
+def cluster_grid(kind: str, n: int = 101, a: float = 0.0, b: float = 1.0) -> np.ndarray:
+    """Clustered grids of the reference's nonuniform convection tests: "symmetric" (sinh
+    stretching 7), "left"/"right" (geometric spacing, ratio 1000) and "chebyshev" nodes."""
+    if kind == "symmetric":
+        xi = np.array([-1.0 + 2.0 * k / (n - 1) for k in range(n)])
+        x = a + (b - a) * (np.sinh(7.0 * xi) / math.sinh(7.0) + 1.0) / 2.0
+    elif kind in ("left", "right"):
+        m = n - 1
+        r = 1000.0 ** (1.0 / (m - 1))
+        dx = np.array([r ** k for k in range(m)])
+        if kind == "right":
+            dx = dx[::-1]
+        dx = dx * ((b - a) / np.sum(dx))
+        x = a + np.concatenate([[0.0], np.cumsum(dx)])
+    elif kind == "chebyshev":
+        k = np.arange(1, n + 1)
+        x = np.sort((a + b) / 2 + (b - a) / 2 * np.cos(math.pi * (2 * k - 1) / (2 * n)))
+    else:
+        raise ValueError(kind)
+    x[0], x[-1] = a, b
+    return x
+
+
+def convection_nonuniform(kind: str = "symmetric", n: int = 101, v: float = 1.0):
+    """u_t = -v u_x, u0 = sin(2 pi x), exact translating-sine data at both ends, first-order
+    upwinding on a clustered grid given as points."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx = Differential(t), Differential(x)
+    vp = Param("v", v)
+    eq = Eq(Dt(u(x, t)), -vp * Dx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), sin(2.0 * math.pi * x)), Eq(u(0.0, t), sin(2.0 * math.pi * (0.0 - v * t))),
+           Eq(u(1.0, t), sin(2.0 * math.pi * (1.0 - v * t)))]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 0.25)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [vp])
+    pts = cluster_grid(kind, n)
+    disc = MOLFiniteDifference({x: pts}, t, advection_scheme=UpwindScheme())
+    return sys, disc, {"dt": 0.25 * float(np.min(np.diff(pts))) / abs(v), "points": pts}

@@ -145,6 +145,27 @@ def upwind(d: int, p: int, dx: float, offside: int) -> Operator:
     return Operator(L, -offside, inner, low, high, bl, bl, 0)
 
 
+def upwind_nonuniform(d: int, p: int, x: Sequence[float], offside: int) -> Operator:
+    """``CompleteUpwindDifference(d, p, x::AbstractVector, offside)``
+    (upwind_difference/upwind_diff_weights.jl:93-171) in the form its tap selection reads it
+    (upwind_difference.jl:131-162): the reference returns the operator with offside 0, so a
+    point i uses the i-th table row (built for the point i + offside) with taps i .. i+L-1
+    (offside 0) or i-L+1 .. i (offside L-1), and only the offside-0 operator has high rows
+    (weights at the last L-1 points, in grid order, on the last bL nodes, the first of them
+    used at the last point).  Rows as in the reference; only L = 2 reaches no further than
+    its table on every interior point."""
+    x = [float(v) for v in x]
+    L = d + p
+    bl = d + p
+    nlo = offside
+    nhi = L - 1 - offside
+    n = len(x)
+    rows = [fornberg(d, x[i - 1], x[i - 1 - offside:i - 1 + L - offside]) for i in range(nlo + 1, n - nhi + 1)]
+    high = [fornberg(d, x0, x[n - bl:]) for x0 in x[n - nhi:]] if (offside == 0 and nhi > 0) else []
+    omin = 0 if offside == 0 else -(L - 1)
+    return Operator(L, omin, rows[0], [], high, bl, bl, 0, rows)
+
+
 def half_centered(d: int, p: int, dx: float) -> Operator:
     L = p + 2 * (d // 2) + (p % 2)
     bl = d + p

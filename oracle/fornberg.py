@@ -216,6 +216,32 @@ def complete_upwind_difference(d: int, p: int, dx: float, offside: int = 0) -> D
     return DerivativeOperator(d, p, dx, L, stencil, bL, nhi, low, high, offside, "upwind")
 
 
+def complete_upwind_difference_nonuniform(d: int, p: int, x: Sequence[float], offside: int = 0) -> DerivativeOperator:
+    """``CompleteUpwindDifference(d, p, x::AbstractVector, offside)``,
+    ``upwind_difference/upwind_diff_weights.jl:93-171``.
+
+    ``stencil_coefs[k]`` (0-based) holds the weights at x[i] on x[i - offside .. i + L - 1 -
+    offside] for the grid point i = offside + 1 + k (1-based); the high rows are the weights
+    at the last L - 1 - offside points, in grid order, on the last bL nodes.  As the
+    reference returns it, the operator's ``offside`` is 0 and its boundary point count the
+    high count: its tap selection (``_upwind_difference`` for DX <: AbstractVector,
+    upwind_difference.jl:131-162) then reads ``stencil_coefs[II]`` for a point II, i.e. the
+    row built for point II + offside.
+    """
+    x = [float(v) for v in x]
+    L = d + p
+    bL = d + p
+    nlo = offside
+    nhi = L - 1 - offside
+    n = len(x)
+    stencil = [calculate_weights(d, x[i - 1], x[i - 1 - offside:i - 1 + L - offside]) for i in range(nlo + 1, n - nhi + 1)]
+    low_x = x[:bL]
+    high_x = x[n - bL:]
+    low = [calculate_weights(d, x0, low_x) for x0 in x[:nlo]]
+    high = [calculate_weights(d, x0, high_x) for x0 in x[n - nhi:]] if nhi > 0 else []
+    return DerivativeOperator(d, p, float("nan"), L, stencil, bL, nhi, low, high, 0, "upwind_nonuniform")
+
+
 def complete_half_centered_difference(d: int, p: int, dx: float) -> DerivativeOperator:
     """``CompleteHalfCenteredDifference``, ``half_offset_weights.jl:4-70``."""
     assert p > 1

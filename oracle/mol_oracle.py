@@ -19,6 +19,7 @@ import numpy as np
 
 from .fornberg import (boundary_interpolator_extrapolator, complete_centered_difference,
                        complete_centered_difference_nonuniform, complete_half_centered_difference,
+                       complete_upwind_difference_nonuniform,
                        complete_upwind_difference)
 
 # --------------------------------------------------------------------------------------
@@ -143,9 +144,18 @@ def central_taps(D, i: int, n: int, periodic: bool):
 
 
 def upwind_taps(D, i: int, n: int, periodic: bool, ispositive: bool):
-    """``_upwind_difference`` (uniform dx)."""
+    """``_upwind_difference`` (uniform dx, upwind_difference.jl:1-28; a nonuniform grid without
+    interfaces, :131-162)."""
     L = D.stencil_length
     bL = D.boundary_stencil_length
+    if D.kind == "upwind_nonuniform":
+        assert not periodic, "interfaces on nonuniform upwind dimensions are not restated"
+        if not ispositive:
+            if i > n - D.boundary_point_count:
+                return list(D.high_boundary_coefs[n - i]), [n - bL + 1 + k for k in range(bL)]
+            return list(D.stencil_coefs[i - 1]), [i + k for k in range(0, L)]
+        # D.offside is 0 as the reference returns the operator: never the low rows
+        return list(D.stencil_coefs[i - 1]), [i + k for k in range(-L + 1, 1)]
     if not ispositive:
         if i > n - D.boundary_point_count and not periodic:
             return list(D.high_boundary_coefs[n - i]), [n - bL + 1 + k for k in range(bL)]
@@ -349,9 +359,14 @@ class OracleProblem:
         if key not in self._ops:
             dx = self.dx[j]
             if not self.uniform[j]:
-                if kind != "centered":
+                if kind == "centered":
+                    D = complete_centered_difference_nonuniform(d, self.order, self.grid[j])
+                elif kind == "wind_neg":
+                    D = complete_upwind_difference_nonuniform(d, int(extra), self.grid[j], 0)
+                elif kind == "wind_pos":
+                    D = complete_upwind_difference_nonuniform(d, int(extra), self.grid[j], d + int(extra) - 1)
+                else:
                     raise NotImplementedError(f"oracle: {kind} operators on a nonuniform grid")
-                D = complete_centered_difference_nonuniform(d, self.order, self.grid[j])
             elif kind == "centered":
                 D = complete_centered_difference(d, self.order, dx)
             elif kind == "wind_neg":        # windmap[1]: offside 0, used when !ispositive

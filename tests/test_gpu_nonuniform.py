@@ -115,3 +115,50 @@ def test_nonuniform_f32state(gpu_lib):
     plan.step_ssprk33(u32, ex["dt"], 20)
     assert _rel(u32.astype(np.float64), u64) < 1e-5
     plan.close()
+
+
+@pytest.mark.parametrize("kind", ["symmetric", "left", "right", "chebyshev"])
+def test_nonuniform_upwind_rhs_trajectory_and_boundedness(gpu_lib, kind):
+    """First-order upwinding on the reference's clustered grids (stretching up to 1000): RHS
+    and SSPRK33 trajectory against the oracle, and the reference test's boundedness over
+    t in [0, 0.25] (test/Convection_NU/MOL_1D_Linear_Convection_NonUniform.jl)."""
+    s, d, ex = problems.convection_nonuniform(kind, n=101)
+    spec = s.to_spec(d)
+    lw, orc = lower(spec), OracleProblem(spec)
+    plan = Plan(lw)
+    v = lw.u0 + 0.05 * np.random.default_rng(4).standard_normal(lw.n_unknowns)
+    for t in (0.0, 0.11):
+        du = np.zeros(lw.n_unknowns)
+        plan.rhs(du, v, None, t)
+        ref = orc.rhs(v, t)
+        assert _rel(du, ref) <= 1e-12, (kind, t)
+    u = lw.u0.copy()
+    plan.step_ssprk33(u, ex["dt"], 40, t0=0.0)
+    ref, _ = ssprk33(lambda w, tt: orc.rhs(w, tt), lw.u0, 0.0, ex["dt"], 40)
+    assert _rel(u, ref) <= 1e-10, kind
+    nsteps = int(round(0.25 / ex["dt"]))
+    u = lw.u0.copy()
+    plan.step_ssprk33(u, ex["dt"], nsteps, t0=0.0)
+    assert np.all(np.isfinite(u)) and np.max(np.abs(u)) < 5
+    plan.close()
+
+
+def test_nonuniform_upwind_adjoint_matches_finite_differences(gpu_lib):
+    s, d, ex = problems.convection_nonuniform("chebyshev", n=101)
+    lw = lower(s.to_spec(d))
+    plan = Plan(lw)
+    dt, n = ex["dt"], 30
+    target = np.zeros(lw.n_unknowns)
+
+    def loss(u0):
+        u = u0.copy()
+        plan.step_ssprk33(u, dt, n, t0=0.0)
+        return 0.5 * float(np.sum((u - target) ** 2))
+
+    g = np.zeros(lw.n_unknowns)
+    plan.adjoint_ssprk33(lw.u0, dt, n, target, nsnap=4, dLdu0=g)
+    w = np.random.default_rng(9).standard_normal(lw.n_unknowns)
+    h = 1e-6
+    fd = (loss(lw.u0 + h * w) - loss(lw.u0 - h * w)) / (2 * h)
+    assert abs(g @ w - fd) <= 1e-6 * abs(fd), (g @ w, fd)
+    plan.close()

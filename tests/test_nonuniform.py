@@ -174,14 +174,14 @@ def test_descriptor_carries_rows():
 
 
 def _unsupported(kind):
-    from molgpu.api import MOLFiniteDifference, WENOScheme
+    from molgpu.api import MOLFiniteDifference, UpwindScheme, WENOScheme
     from molgpu.symbolic import Differential, Eq, Field, Interval, IV, PDESystem, sin
     x, y, t = IV("x"), IV("y"), IV("t")
     u = Field("u")
     Dt, Dx = Differential(t), Differential(x)
     pts = problems.stretched_points(21)
-    if kind == "upwind":
-        eq, scheme = Eq(Dt(u(x, t)), -Dx(u(x, t))), None
+    if kind == "upwind":       # second-order upwinding: the reference's table is too short
+        eq, scheme = Eq(Dt(u(x, t)), -Dx(u(x, t))), UpwindScheme(2)
     elif kind == "weno":
         eq, scheme = Eq(Dt(u(x, t)), -Dx(u(x, t))), WENOScheme()
     elif kind == "nonlinlap":
@@ -235,3 +235,51 @@ def test_generated_code_reads_the_point_row():
     assert ".w_int + (long long)(I[0] - 2) * 3" in src
     log = C.create_string_buffer(1 << 16)
     assert L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16) == 0, log.value.decode()
+
+
+UPWIND_GRIDS = ["symmetric", "left", "right", "chebyshev"]
+
+
+@pytest.mark.parametrize("kind", UPWIND_GRIDS)
+def test_nonuniform_upwind_tables_and_selection(kind):
+    """First-order upwind tables on a nonuniform grid (upwind_diff_weights.jl:93-171) and the
+    reference's selection (upwind_difference.jl:131-162): product and oracle agree bit for bit
+    at every interior point, in both wind directions."""
+    from molgpu.weights import select, upwind_nonuniform
+    from oracle.fornberg import complete_upwind_difference_nonuniform
+    from oracle.mol_oracle import upwind_taps
+    x = problems.cluster_grid(kind, 41)
+    n = len(x)
+    for off, positive in ((0, False), (1, True)):
+        a = upwind_nonuniform(1, 1, x, off)
+        b = complete_upwind_difference_nonuniform(1, 1, x, off)
+        assert a.rows == b.stencil_coefs and a.high == b.high_boundary_coefs
+        for i in range(2, n):
+            assert list(select(a, i, n, False)) == list(upwind_taps(b, i, n, False, positive)), (off, i)
+
+
+def test_nonuniform_positive_wind_row_is_the_next_points():
+    """Pinned reference behaviour: the operator comes back with offside 0, so the positive-wind
+    difference at point i uses the row built for point i + 1 on taps i-1, i, i.e.
+    (u_i - u_{i-1}) / (x_{i+1} - x_i)."""
+    from molgpu.weights import select, upwind_nonuniform
+    x = problems.cluster_grid("left", 21)
+    op = upwind_nonuniform(1, 1, x, 1)
+    for i in range(2, len(x)):
+        w, taps = select(op, i, len(x), False)
+        h = x[i] - x[i - 1]          # x_{i+1} - x_i in 1-based terms
+        assert taps == [i - 1, i]
+        assert np.allclose(w, [-1.0 / h, 1.0 / h], rtol=1e-14)
+
+
+@pytest.mark.parametrize("kind", UPWIND_GRIDS)
+def test_descriptor_semantics_match_oracle_nonuniform_upwind(kind):
+    s, d, _ = problems.convection_nonuniform(kind, n=41)
+    spec = s.to_spec(d)
+    lw = lower(spec)
+    orc = OracleProblem(spec)
+    di = DescInterp(lw)
+    u = lw.u0 + 0.01 * np.random.default_rng(0).standard_normal(lw.n_unknowns)
+    for t in (0.05, 0.2):
+        a, b = orc.rhs(u, t), di.rhs(u, t)
+        assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a), (kind, t)
