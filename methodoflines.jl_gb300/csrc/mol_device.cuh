@@ -141,6 +141,49 @@ __device__ __forceinline__ TapSel select_taps(const mol_op1d& op, int i, int len
     return s;
 }
 
+// Elementary functions, comparisons and integer powers of the programs.
+template <class T>
+__device__ __forceinline__ T apply_fn(int fn, T x) {
+    switch (fn) {
+        case MOL_FN_SIN: return sin(x);
+        case MOL_FN_COS: return cos(x);
+        case MOL_FN_TAN: return tan(x);
+        case MOL_FN_EXP: return exp(x);
+        case MOL_FN_LOG: return log(x);
+        case MOL_FN_SQRT: return sqrt(x);
+        case MOL_FN_ABS: return fabs(x);
+        case MOL_FN_TANH: return tanh(x);
+        case MOL_FN_SINH: return sinh(x);
+        case MOL_FN_COSH: return cosh(x);
+        case MOL_FN_ATAN: return atan(x);
+        default: return x;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ T apply_cmp(int c, T a, T b) {
+    bool r;
+    switch (c) {
+        case MOL_CMP_LE: r = a <= b; break;
+        case MOL_CMP_LT: r = a < b; break;
+        case MOL_CMP_GE: r = a >= b; break;
+        case MOL_CMP_GT: r = a > b; break;
+        default: r = a == b; break;
+    }
+    return r ? T(1) : T(0);
+}
+
+template <class T>
+__device__ __forceinline__ T powi(T x, int n) {
+    if (n == 2) return x * x;
+    if (n == 3) return x * x * x;
+    if (n == 1) return x;
+    if (n == 0) return T(1);
+    if (n == -1) return T(1) / x;
+    if (n == -2) return T(1) / (x * x);
+    return pow(x, T(n));
+}
+
 // Small straight-line program used by boundary rows (a, b, g may depend on t, x, p).
 template <class T>
 __device__ T run_bc_prog(const DevProb<T>& P, int prog, int out_index, const int* I, T t, const T* p) {
@@ -160,6 +203,11 @@ __device__ T run_bc_prog(const DevProb<T>& P, int prog, int out_index, const int
             case MOL_OP_MUL: r[dst] = r[in.a & 15] * r[in.b & 15]; break;
             case MOL_OP_DIV: r[dst] = r[in.a & 15] / r[in.b & 15]; break;
             case MOL_OP_NEG: r[dst] = -r[in.a & 15]; break;
+            case MOL_OP_POWI: r[dst] = powi(r[in.a & 15], in.imm); break;
+            case MOL_OP_POW: r[dst] = pow(r[in.a & 15], r[in.b & 15]); break;
+            case MOL_OP_FN: r[dst] = apply_fn(in.imm, r[in.a & 15]); break;
+            case MOL_OP_CMP: r[dst] = apply_cmp(in.imm, r[in.a & 15], r[in.b & 15]); break;
+            case MOL_OP_IFELSE: r[dst] = r[in.a & 15] != T(0) ? r[in.b & 15] : r[in.c & 15]; break;
             case MOL_OP_OUT: if (in.imm == out_index) res = r[in.a & 15]; break;
             default: break;
         }
@@ -593,48 +641,6 @@ __device__ T apply_weno(const DevProb<T>& P, const mol_term& tm, const T* u, con
     weno_taps(P, tm, u, I, t, p, v);
     // the device copy of a WENO term stores 1/dx in `dx`
     return weno5_point<T>(v[0], v[1], v[2], v[3], v[4], T(tm.eps), T(tm.dx));
-}
-
-template <class T>
-__device__ __forceinline__ T apply_fn(int fn, T x) {
-    switch (fn) {
-        case MOL_FN_SIN: return sin(x);
-        case MOL_FN_COS: return cos(x);
-        case MOL_FN_TAN: return tan(x);
-        case MOL_FN_EXP: return exp(x);
-        case MOL_FN_LOG: return log(x);
-        case MOL_FN_SQRT: return sqrt(x);
-        case MOL_FN_ABS: return fabs(x);
-        case MOL_FN_TANH: return tanh(x);
-        case MOL_FN_SINH: return sinh(x);
-        case MOL_FN_COSH: return cosh(x);
-        case MOL_FN_ATAN: return atan(x);
-        default: return x;
-    }
-}
-
-template <class T>
-__device__ __forceinline__ T apply_cmp(int c, T a, T b) {
-    bool r;
-    switch (c) {
-        case MOL_CMP_LE: r = a <= b; break;
-        case MOL_CMP_LT: r = a < b; break;
-        case MOL_CMP_GE: r = a >= b; break;
-        case MOL_CMP_GT: r = a > b; break;
-        default: r = a == b; break;
-    }
-    return r ? T(1) : T(0);
-}
-
-template <class T>
-__device__ __forceinline__ T powi(T x, int n) {
-    if (n == 2) return x * x;
-    if (n == 3) return x * x * x;
-    if (n == 1) return x;
-    if (n == 0) return T(1);
-    if (n == -1) return T(1) / x;
-    if (n == -2) return T(1) / (x * x);
-    return pow(x, T(n));
 }
 
 // Face value a(x_{I+1/2}, u~) * (D_inner u)_{I+1/2} of a nonlinear Laplacian term

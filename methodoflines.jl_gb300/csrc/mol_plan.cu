@@ -524,14 +524,12 @@ static int validate_prog(mol_plan* plan, const mol_problem_desc* d, int prog, in
                 break;
             case MOL_OP_ADD: case MOL_OP_SUB: case MOL_OP_MUL: case MOL_OP_DIV: case MOL_OP_NEG:
             case MOL_OP_POWI: case MOL_OP_POW: case MOL_OP_IFELSE:
-                if (kind == 2 && (in.op == MOL_OP_POWI || in.op == MOL_OP_POW || in.op == MOL_OP_IFELSE))
-                    return set_err(plan, MOL_ERR_UNSUPPORTED, "boundary programs support + - * / only");
                 break;
             case MOL_OP_FN:
-                if (kind == 2 || in.imm < 0 || in.imm > MOL_FN_ATAN) return set_err(plan, MOL_ERR_INVALID, "function id");
+                if (in.imm < 0 || in.imm > MOL_FN_ATAN) return set_err(plan, MOL_ERR_INVALID, "function id");
                 break;
             case MOL_OP_CMP:
-                if (kind == 2 || in.imm < 0 || in.imm > MOL_CMP_EQ) return set_err(plan, MOL_ERR_INVALID, "comparison id");
+                if (in.imm < 0 || in.imm > MOL_CMP_EQ) return set_err(plan, MOL_ERR_INVALID, "comparison id");
                 break;
             case MOL_OP_OUT:
                 if (kind == 0 && (in.imm < 0 || in.imm >= d->nfields)) return set_err(plan, MOL_ERR_INVALID, "output index");
