@@ -135,3 +135,27 @@ def test_batch_bounded_wait_reports_abandoned_run(gpu_lib, monkeypatch):
         ref = lw.u0.copy()
         Plan(lw).step_ssprk33(ref, dts[i], 6, t0=0.0)
         assert np.allclose(got_all[batch.offsets[i]:batch.offsets[i + 1]], ref, rtol=1e-13, atol=1e-15), i
+
+
+@pytest.mark.parametrize("family", ["stretched", "weno_bounded", "edge"])
+def test_batch_members_with_grid_variants(gpu_lib, family):
+    """Ensembles of members on nonuniform grids (per-point rows), with WENO on a bounded
+    dimension (extrapolated points) and on edge-aligned grids (ghost rows) step like their
+    plans."""
+    if family == "stretched":
+        made = [problems.stretched_reaction_diffusion(n=n, order=4) for n in (41, 97, 200)]
+    elif family == "weno_bounded":
+        made = [problems.viscous_burgers_weno_bounded(n=n, order=2) for n in (33, 65, 129)]
+    else:
+        made = [problems.neumann_cosine_edge(dx=dx, order=4) for dx in (0.05, 0.02, 0.01)]
+    lws = [lower(s.to_spec(d)) for s, d, _ in made]
+    dts = np.array([ex["dt"] for _, _, ex in made])
+    batch = Batch(lws)
+    batch.tune(128, 2, 64)
+    u = batch.pack([lw.u0 for lw in lws])
+    batch.step_ssprk33(u, dts, 12, t0=0.0)
+    batch.check()
+    for i, lw in enumerate(lws):
+        ref = lw.u0.copy()
+        Plan(lw).step_ssprk33(ref, dts[i], 12, t0=0.0)
+        assert np.allclose(u[batch.offsets[i]:batch.offsets[i + 1]], ref, rtol=1e-13, atol=1e-15), (family, i)
