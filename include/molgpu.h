@@ -99,10 +99,20 @@ typedef struct mol_term {
     int32_t dim, dim2;  /* dimension(s), 0-based                                        */
     int32_t op, op2, op3; /* LINEAR: op. MIXED: op (dim), op2 (dim2).
                            NONLINLAP: op = outer half-offset d1, op2 = inner half-offset d1,
-                           op3 = half-offset interpolation (order 0)                    */
+                           op3 = half-offset interpolation (order 0).
+                           WENO with variant 1: op holds the per-point geometry rows      */
     int32_t prog;       /* NONLINLAP: face program (outputs a at the half point)        */
     int32_t aux0;       /* NONLINLAP: first face-aux array used by the face program      */
-    int32_t reserved0, reserved1, reserved2;
+    int32_t reserved0;  /* filled by the library                                         */
+    int32_t variant;    /* WENO: 0 uniform Jiang-Shu (WENO.jl:6-57); 1 node-centred Lagrange
+                           WENO-5 on a nonuniform dimension (nonuniform_weno.jl:1-212): op's
+                           row i-1 (nrows = npts, L = 56) holds point i's geometry: dx/6, dx,
+                           dx^3, per substencil the first-derivative weights at the target,
+                           the Simpson cell's ends and middle and the second-derivative
+                           weights at the middle, then dp_k/sigma_p, dm_k/sigma_m, sigma_p,
+                           sigma_m; taps 1..5 (points 1, 2), n-4..n (points n-1, n) or
+                           i-2..i+2                                                       */
+    int32_t reserved2;
     double eps;         /* WENO epsilon                                                  */
     double dx;          /* WENO grid spacing                                             */
 } mol_term;

@@ -461,6 +461,19 @@ void emit_mixed(Emitter& e, const mol_problem_desc* d, int k) {
 void emit_weno(Emitter& e, const mol_problem_desc* d, int k) {
     const mol_term& tm = d->terms[k];
     const std::string K = std::to_string(k), F = std::to_string(tm.field), D = std::to_string(tm.dim);
+    if (tm.variant == 1) {
+        // nonuniform dimension: per-point geometry rows, taps through the line helpers
+        const std::string DYN = dyn_bc(d, tm.field, tm.dim);
+        e << "template <class T>\n__device__ __forceinline__ T gt" << K
+          << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) "
+             "{\n    return weno_nu_line<T, "
+          << D << ", " << DYN << ">(P, P.terms[" << K << "], u, " << F << ", I, c, t, p);\n}\n";
+        e << "template <class T>\n__device__ __forceinline__ void gt" << K
+          << "_vjp(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, "
+             "const T* __restrict__ p, T g, T* lam_u, T* lp, T* lam_aux, T& own) {\n    weno_nu_line_vjp<T, "
+          << D << ", " << DYN << ">(P, P.terms[" << K << "], u, " << F << ", I, c, t, p, g, lam_u);\n}\n";
+        return;
+    }
     const std::string cond = "warp_all(fast_weno(P, " + F + ", " + D + ", I[" + D + "]))";
     const char* W = warp_scatter() ? "true" : "false";
     const std::string DY = dyn_bc(d, tm.field, tm.dim);
@@ -1104,7 +1117,7 @@ std::string generate_source(const mol_problem_desc* d, std::string& why) {
             }
         }
         for (int k = 0; k < d->nterms; ++k)
-            if (d->terms[k].kind == MOL_TERM_WENO && refs[k] == 1) {
+            if (d->terms[k].kind == MOL_TERM_WENO && d->terms[k].variant == 0 && refs[k] == 1) {
                 VL.split.push_back(k);
                 e << "    bool fw" << k << " = false;\n    T gw" << k << "[5];\n";
             }

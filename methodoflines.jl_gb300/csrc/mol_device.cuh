@@ -635,9 +635,120 @@ __device__ __forceinline__ void weno_taps(const DevProb<T>& P, const mol_term& t
     }
 }
 
+// ---------------------------------------------------------------------------
+// Node-centred Lagrange WENO-5 on a nonuniform dimension (nonuniform_weno.jl:120-163).
+// `g` is the point's geometry row (56 values, see mol_term.variant); v the five taps.
+// Per substencil k on taps k..k+2: r_k the derivative at the target, beta_k the Simpson
+// smoothness indicator max(dx (dx/6)(pL^2 + 4 pM^2 + pR^2) + dx^3 dx pp^2, 0); the split
+// ideal weights give the result sigma_p R_p - sigma_m R_m.
+
+template <class T>
+__device__ __forceinline__ T dot3(const T* w, const T* a) { return w[0] * a[0] + w[1] * a[1] + w[2] * a[2]; }
+
+template <class T>
+__device__ __forceinline__ T weno5nu_point(const T* __restrict__ g, const T v[5], T eps) {
+    T b[3], r[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T* m = g + 3 + 15 * k;
+        const T* a = v + k;
+        r[k] = dot3(m, a);
+        const T pL = dot3(m + 3, a), pM = dot3(m + 6, a), pR = dot3(m + 9, a), pp = dot3(m + 12, a);
+        const T I1 = g[0] * (pL * pL + T(4) * (pM * pM) + pR * pR);
+        const T I2 = g[1] * (pp * pp);
+        const T val = g[1] * I1 + g[2] * I2;
+        b[k] = val > T(0) ? val : T(0);
+    }
+    T ap[3], am[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T e = eps + b[k];
+        const T e2 = e * e;
+        ap[k] = g[48 + k] / e2;
+        am[k] = g[51 + k] / e2;
+    }
+    const T sp = ap[0] + ap[1] + ap[2], sm = am[0] + am[1] + am[2];
+    const T Rp = (ap[0] / sp) * r[0] + (ap[1] / sp) * r[1] + (ap[2] / sp) * r[2];
+    const T Rm = (am[0] / sm) * r[0] + (am[1] / sm) * r[1] + (am[2] / sm) * r[2];
+    return g[54] * Rp - g[55] * Rm;
+}
+
+// Value and gradient with respect to the five taps (reverse mode through the nonlinear
+// weights: dF/dr_k = sp w+_k - sm w-_k, dF/dbeta_k = -2/(eps + beta_k) (sp w+_k (r_k - R+) -
+// sm w-_k (r_k - R-)), beta_k quadratic in its three taps, zero where clipped).
+template <class T>
+__device__ __forceinline__ T weno5nu_valgrad(const T* __restrict__ g, const T v[5], T eps, T gr[5]) {
+    T b[3], r[3], pl[3], pm[3], pr[3], pq[3];
+    bool clip[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T* m = g + 3 + 15 * k;
+        const T* a = v + k;
+        r[k] = dot3(m, a);
+        pl[k] = dot3(m + 3, a);
+        pm[k] = dot3(m + 6, a);
+        pr[k] = dot3(m + 9, a);
+        pq[k] = dot3(m + 12, a);
+        const T I1 = g[0] * (pl[k] * pl[k] + T(4) * (pm[k] * pm[k]) + pr[k] * pr[k]);
+        const T I2 = g[1] * (pq[k] * pq[k]);
+        const T val = g[1] * I1 + g[2] * I2;
+        clip[k] = !(val > T(0));
+        b[k] = clip[k] ? T(0) : val;
+    }
+    T ap[3], am[3], ie[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T e = eps + b[k];
+        ie[k] = T(1) / e;
+        const T e2 = e * e;
+        ap[k] = g[48 + k] / e2;
+        am[k] = g[51 + k] / e2;
+    }
+    const T sp = ap[0] + ap[1] + ap[2], sm = am[0] + am[1] + am[2];
+    T wp[3], wm[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        wp[k] = ap[k] / sp;
+        wm[k] = am[k] / sm;
+    }
+    const T Rp = wp[0] * r[0] + wp[1] * r[1] + wp[2] * r[2];
+    const T Rm = wm[0] * r[0] + wm[1] * r[1] + wm[2] * r[2];
+    const T SP = g[54], SM = g[55];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) gr[q] = T(0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T* m = g + 3 + 15 * k;
+        const T dr = SP * wp[k] - SM * wm[k];
+        const T db = clip[k] ? T(0)
+                             : T(-2) * ie[k] * (SP * wp[k] * (r[k] - Rp) - SM * wm[k] * (r[k] - Rm));
+        // d beta / d a = dx (dx/6) (2 pL m1L + 8 pM m1M + 2 pR m1R) + dx^3 dx 2 pp m2M
+        const T cL = db * g[1] * g[0] * T(2) * pl[k], cM = db * g[1] * g[0] * T(8) * pm[k];
+        const T cR = db * g[1] * g[0] * T(2) * pr[k], cQ = db * g[2] * g[1] * T(2) * pq[k];
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            gr[k + j] += dr * m[j] + cL * m[3 + j] + cM * m[6 + j] + cR * m[9 + j] + cQ * m[12 + j];
+    }
+    return SP * Rp - SM * Rm;
+}
+
+// First tap of the nonuniform WENO stencil at point i of n (the two one-sided targets at
+// each end, get_f_taps_coords with the scheme's boundary functions, WENO.jl:84-85).
+__device__ __forceinline__ int weno_nu_first(int i, int n) { return i <= 2 ? 1 : (i > n - 2 ? n - 4 : i - 2); }
+
 template <class T>
 __device__ T apply_weno(const DevProb<T>& P, const mol_term& tm, const T* u, const int* I, T t, const T* p) {
     T v[5];
+    if (tm.variant == 1) {
+        const int d = tm.dim, n = P.n[d], q0 = weno_nu_first(I[d], n);
+        int J[3] = {I[0], I[1], I[2]};
+        for (int k = 0; k < 5; ++k) {
+            J[d] = q0 + k;
+            v[k] = load_pt(P, u, tm.field, J[0], J[1], J[2], t, p);
+        }
+        const mol_op1d& o = P.ops[tm.op];
+        return weno5nu_point<T>(P.w + o.w_int + (long long)(I[d] - 1) * o.L, v, T(tm.eps));
+    }
     weno_taps(P, tm, u, I, t, p, v);
     // the device copy of a WENO term stores 1/dx in `dx`
     return weno5_point<T>(v[0], v[1], v[2], v[3], v[4], T(tm.eps), T(tm.dx));

@@ -594,6 +594,15 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
                 break;
             case MOL_TERM_WENO:
                 if (!(t.dx > 0)) return set_err(plan, MOL_ERR_INVALID, "weno dx");
+                if (t.variant == 1) {  // nonuniform: geometry rows for every point, no wrap
+                    if (!opok(t.op) || d->ops[t.op].L != 56 || d->ops[t.op].nrows != d->npts[t.dim] ||
+                        d->npts[t.dim] < 5)
+                        return set_err(plan, MOL_ERR_INVALID, "nonuniform WENO geometry rows");
+                    if (d->bc[t.field][t.dim][0].kind == MOL_BC_PERIODIC)
+                        return set_err(plan, MOL_ERR_UNSUPPORTED, "nonuniform WENO on a periodic dimension");
+                    break;
+                }
+                if (t.variant != 0) return set_err(plan, MOL_ERR_INVALID, "weno variant");
                 // bounded dimension: the interior stops two points from each end and the points
                 // next to the boundary points are extrapolated (WENO.jl:94, generate_bc_eqs.jl:336-392);
                 // with no boundary row at an end the reference uses its near-wall WENO stencils

@@ -417,6 +417,33 @@ __device__ __forceinline__ void weno5_grad(T um2, T um1, T u0, T up1, T up2, T e
     (void)weno5_valgrad<T>(um2, um1, u0, up1, up2, eps, inv_dx, gr);
 }
 
+// Nonuniform WENO along a compile-time dimension D: the five taps of the point, its
+// geometry row, and the transpose (used by the generated code).
+template <class T, int D, bool DYN>
+__device__ __forceinline__ T weno_nu_line(const DevProb<T>& P, const mol_term& tm, const T* __restrict__ u, int f,
+                                          const int* I, long long c, T t, const T* __restrict__ p) {
+    const int n = P.n[D], q0 = weno_nu_first(I[D], n);
+    T v[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) v[k] = line_pt<T, D, DYN>(P, u, f, I, c, q0 + k, t, p);
+    const mol_op1d& o = P.ops[tm.op];
+    return weno5nu_point<T>(P.w + o.w_int + (long long)(I[D] - 1) * o.L, v, T(tm.eps));
+}
+
+template <class T, int D, bool DYN>
+__device__ __forceinline__ void weno_nu_line_vjp(const DevProb<T>& P, const mol_term& tm, const T* __restrict__ u,
+                                                 int f, const int* I, long long c, T t, const T* __restrict__ p, T g,
+                                                 T* lam) {
+    const int n = P.n[D], q0 = weno_nu_first(I[D], n);
+    T v[5], gr[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) v[k] = line_pt<T, D, DYN>(P, u, f, I, c, q0 + k, t, p);
+    const mol_op1d& o = P.ops[tm.op];
+    (void)weno5nu_valgrad<T>(P.w + o.w_int + (long long)(I[D] - 1) * o.L, v, T(tm.eps), gr);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) scatter_line_pt<T, D, DYN>(P, lam, f, I, c, q0 + k, g * gr[k], t, p);
+}
+
 // Transpose of weno_taps: gv[k] goes to tap k through the generic path.
 template <class T>
 __device__ __forceinline__ void scatter_weno_taps(const DevProb<T>& P, const mol_term& tm, T* lam, const int* I,
@@ -434,6 +461,22 @@ template <class T>
 __device__ __noinline__ void scatter_weno(const DevProb<T>& P, const mol_term& tm, const T* u, T* lam, const int* I, T g,
                                           T t, const T* p) {
     T v[5];
+    if (tm.variant == 1) {  // nonuniform: taps q0..q0+4, geometry row of the point
+        const int d = tm.dim, n = P.n[d], q0 = weno_nu_first(I[d], n);
+        int J[3] = {I[0], I[1], I[2]};
+        for (int k = 0; k < 5; ++k) {
+            J[d] = q0 + k;
+            v[k] = load_pt(P, u, tm.field, J[0], J[1], J[2], t, p);
+        }
+        const mol_op1d& o = P.ops[tm.op];
+        T gr[5];
+        (void)weno5nu_valgrad<T>(P.w + o.w_int + (long long)(I[d] - 1) * o.L, v, T(tm.eps), gr);
+        for (int k = 0; k < 5; ++k) {
+            J[d] = q0 + k;
+            scatter_pt(P, lam, tm.field, J[0], J[1], J[2], g * gr[k], t, p);
+        }
+        return;
+    }
     weno_taps(P, tm, u, I, t, p, v);
     T gr[5];
     weno5_grad<T>(v[0], v[1], v[2], v[3], v[4], T(tm.eps), T(tm.dx), gr);

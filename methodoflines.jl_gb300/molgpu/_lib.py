@@ -42,7 +42,7 @@ class mol_op1d(C.Structure):
 class mol_term(C.Structure):
     _fields_ = [("kind", C.c_int32), ("field", C.c_int32), ("dim", C.c_int32), ("dim2", C.c_int32),
                 ("op", C.c_int32), ("op2", C.c_int32), ("op3", C.c_int32), ("prog", C.c_int32),
-                ("aux0", C.c_int32), ("reserved0", C.c_int32), ("reserved1", C.c_int32),
+                ("aux0", C.c_int32), ("reserved0", C.c_int32), ("variant", C.c_int32),
                 ("reserved2", C.c_int32), ("eps", C.c_double), ("dx", C.c_double)]
 
 

@@ -26,8 +26,8 @@ from typing import Dict, List, Optional, Tuple
 import numpy as np
 
 from . import _lib as L
-from .weights import (Operator, centered, centered_nonuniform, extrapolator, half_centered, select, upwind,
-                      upwind_nonuniform, wrap)
+from .weights import (WENO_NU_ROW, Operator, centered, centered_nonuniform, extrapolator, half_centered, select,
+                      upwind, upwind_nonuniform, weno_nonuniform_rows, wrap)
 
 # ------------------------------------------------------------------------------------
 # grids (Julia Float64 ranges)
@@ -379,7 +379,10 @@ class Lowered:
         key = (kind, j, d, p)
         if key not in self.op_keys:
             dx = self.dx[j]
-            if self.uniform and not self.uniform[j]:
+            if kind == "weno_nu":            # per-point WENO geometry (nonuniform_weno.jl)
+                rows = weno_nonuniform_rows(self.grids[j])
+                o = Operator(WENO_NU_ROW, 0, rows[0], [], [], 0, 0, 0, rows)
+            elif self.uniform and not self.uniform[j]:
                 if kind == "centered":
                     o = centered_nonuniform(d, self.order, self.grids[j])
                 elif kind in ("wind_pos", "wind_neg") and d + p == 2:
@@ -542,7 +545,7 @@ class _Lowerer:
                     if self.edge:
                         raise NotImplementedError("WENO along a bounded edge-aligned dimension is not built")
                     if not uniform[j]:
-                        raise NotImplementedError(f"WENO on the nonuniform grid of {x} is not built")
+                        continue        # extent 0 on a nonuniform grid (WENO.jl:95): no extrapolation
                     for side, arr in (("lo", lo_), ("hi", up_)):
                         b = bcs.get((f, j, side))
                         if b is None:
@@ -587,7 +590,9 @@ class _Lowerer:
                 return lw.term(kind=L.TERM_LINEAR, field=f, dim=j, op=lw.op("centered", j, d))
             if lw.adv[0] == "weno" and d == 1:
                 if not lw.uniform[j]:
-                    raise NotImplementedError(f"WENO on the nonuniform grid of {x} is not built")
+                    # node-centred Lagrange WENO-5 from the grid's coordinates (nonuniform_weno.jl)
+                    return lw.term(kind=L.TERM_WENO, field=f, dim=j, eps=float(lw.adv[1]), dx=1.0,
+                                   op=lw.op("weno_nu", j, 0), variant=1)
                 return lw.term(kind=L.TERM_WENO, field=f, dim=j, eps=float(lw.adv[1]), dx=lw.dx[j])
             # bare odd derivative: positive wind (upwind_difference.jl:278-302)
             p = int(lw.adv[1]) if lw.adv[0] == "upwind" else 1
@@ -934,6 +939,7 @@ class Descriptor:
             r.aux0 = t.get("aux0", 0)
             r.eps = t.get("eps", 0.0)
             r.dx = t.get("dx", 0.0)
+            r.variant = t.get("variant", 0)
         keep.append(terms)
         d.nterms = len(lw.terms)
         d.terms = C.cast(terms, C.POINTER(L.mol_term))

@@ -27,6 +27,10 @@ come from ``numpy.random.Generator(PCG64(seed))`` in Float64.
                  coordinate-dependent Robin, Neumann and Dirichlet rows
 14. convection_nonuniform         u_t = -v u_x on clustered grids (first-order upwinding on a
                  nonuniform grid; test/Convection_NU/MOL_1D_Linear_Convection_NonUniform.jl)
+15. weno_convection_mms           u_t = -v u_x with WENO on grids given as points (uniform points,
+                 sinh, tanh): test/Convection_WENO/MOL_1D_WENO_NU_Convergence.jl
+16. burgers_nonuniform_upwind     u_t = -u u_x, u0 = x, first-order upwinding on a perturbed
+                 grid (test/Burgers/burgers_eq.jl:106-152)
 """
 from __future__ import annotations
 
@@ -389,3 +393,60 @@ def convection_nonuniform(kind: str = "symmetric", n: int = 101, v: float = 1.0)
     pts = cluster_grid(kind, n)
     disc = MOLFiniteDifference({x: pts}, t, advection_scheme=UpwindScheme())
     return sys, disc, {"dt": 0.25 * float(np.min(np.diff(pts))) / abs(v), "points": pts}
+
+
+WENO_MMS_ALPHA = 0.15
+
+
+def weno_mms_exact(x, t, v=1.0, L=2 * math.pi):
+    return np.sin(2 * math.pi * (x - v * t) / L) + WENO_MMS_ALPHA * np.sin(4 * math.pi * (x - v * t) / L)
+
+
+def weno_grid(kind: str, n: int, a: float = 0.0, b: float = 2 * math.pi) -> np.ndarray:
+    """Grids of the reference's nonuniform WENO convergence test: "uniform" (the points of
+    range(a, b, length = n) given as a vector), "sinh" (stretch 4), "tanh" (stretch 2)."""
+    xi = np.array([-1.0 + 2.0 * k / (n - 1) for k in range(n)])
+    if kind == "uniform":
+        x = a + (b - a) * (xi + 1.0) / 2.0
+    elif kind == "sinh":
+        x = a + (b - a) * (np.sinh(4.0 * xi) / math.sinh(4.0) + 1.0) / 2.0
+    elif kind == "tanh":
+        x = a + (b - a) * (np.tanh(2.0 * xi) / math.tanh(2.0) + 1.0) / 2.0
+    else:
+        raise ValueError(kind)
+    x[0], x[-1] = a, b
+    return x
+
+
+def weno_convection_mms(kind: str = "sinh", n: int = 81, v: float = 1.0):
+    """u_t = -v u_x on [0, 2 pi] with WENO on a grid given as points and the manufactured
+    solution sin(2 pi (x - v t)/L) + 0.15 sin(4 pi (x - v t)/L) as Dirichlet data."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx = Differential(t), Differential(x)
+    L = 2 * math.pi
+    a = WENO_MMS_ALPHA
+
+    def ex(xx, tt):
+        return sin(2 * math.pi * (xx - v * tt) / L) + a * sin(4 * math.pi * (xx - v * tt) / L)
+    eq = Eq(Dt(u(x, t)), -v * Dx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), ex(x, 0.0)), Eq(u(0.0, t), ex(0.0, t)), Eq(u(L, t), ex(L, t))]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 0.05)), (x, Interval(0.0, L))], [t, x], [u(x, t)], [])
+    pts = weno_grid(kind, n)
+    disc = MOLFiniteDifference({x: pts}, t, advection_scheme=WENOScheme())
+    return sys, disc, {"dt": 0.01 * float(np.min(np.diff(pts))) / abs(v), "points": pts}
+
+
+def burgers_nonuniform_upwind(seed: int = 0):
+    """The reference's nonuniform Burgers test: 0:0.05:1 with the inner points moved by
+    +-0.001 (seeded here with PCG64), u0 = x, Dirichlet x/(t+1), first-order upwinding."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx = Differential(t), Differential(x)
+    eq = Eq(Dt(u(x, t)), -u(x, t) * Dx(u(x, t)))
+    bcs = [Eq(u(x, 0.0), 1.0 * x), Eq(u(0.0, t), 0.0 / (t + 1.0)), Eq(u(1.0, t), 1.0 / (t + 1.0))]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)], [])
+    pts = np.array([k * 0.05 for k in range(21)])
+    pts[1:-1] += _rng(seed).choice([0.001, -0.001], size=19)
+    disc = MOLFiniteDifference({x: pts}, t, advection_scheme=UpwindScheme(1))
+    return sys, disc, {"dt": 0.2 * float(np.min(np.diff(pts))), "points": pts}

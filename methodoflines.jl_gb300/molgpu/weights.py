@@ -196,6 +196,95 @@ def extrapolator(q: int) -> Operator:
     return Operator(L, -h, interior, low, [lw[::-1] for lw in low], q, q, 0)
 
 
+# ---------------------------------------------------------------------------------------
+# Node-centred Lagrange WENO-5 on nonuniform grids (WENO/nonuniform_weno.jl:1-212): the
+# geometry of every point (Fornberg three-point weights of the Simpson cell, the cell width,
+# the split ideal weights) depends on the grid only and is tabulated here, in the
+# reference's operation order; the device forms the smoothness indicators and nonlinear
+# weights from the state.
+
+WENO_NU_ROW = 56   # dx/6, dx, dx^3, then per substencil m1(xi), m1(xL), m1(xM), m1(xph), m2(xM),
+                   # then dp_k/sigma_p, dm_k/sigma_m (k = 0..2), sigma_p, sigma_m
+
+
+def _fb3(a, xt):
+    """Three-point Fornberg weights (m = 1 and m = 2) at xt, _fornberg3_weights's order."""
+    a0, a1, a2 = a
+    c2 = a1 - a0
+    r1 = 1.0 / c2
+    tA = a1 - xt
+    p1 = [(tA * 1.0) / c2, (tA * 0.0 - 1.0) / c2, (tA * 0.0 - 2 * 0.0) / c2]
+    sB = a0 - xt
+    p2 = [r1 * (-(sB) * 1.0), r1 * (1.0 - sB * 0.0), r1 * (2 * 0.0 - sB * 0.0)]
+    c1 = c2
+    c2 = (a2 - a0) * (a2 - a1)
+    r2 = c1 / c2
+    c3a, c3b = a2 - a0, a2 - a1
+    tA2 = a2 - xt
+    b1 = [(tA2 * p1[0]) / c3a, (tA2 * p1[1] - p1[0]) / c3a, (tA2 * p1[2] - 2 * p1[1]) / c3a]
+    b2 = [(tA2 * p2[0]) / c3b, (tA2 * p2[1] - p2[0]) / c3b, (tA2 * p2[2] - 2 * p2[1]) / c3b]
+    sB2 = a1 - xt
+    b3 = [r2 * (-(sB2) * p2[0]), r2 * (p2[0] - sB2 * p2[1]), r2 * (2 * p2[1] - sB2 * p2[2])]
+    return [b1[1], b2[1], b3[1]], [b1[2], b2[2], b3[2]]
+
+
+def weno_nonuniform_target(i: int, n: int) -> Tuple[int, int]:
+    """(first tap, target) at 1-based point i of n: two one-sided targets at each end, the
+    centre elsewhere (get_f_taps_coords, function_scheme.jl:1-34; WENO.jl:84-85)."""
+    if i <= 2:
+        return 1, i
+    if i > n - 2:
+        return n - 4, 5 - (n - i)
+    return i - 2, 3
+
+
+def weno_nonuniform_rows(x: Sequence[float]) -> List[List[float]]:
+    """One WENO_NU_ROW-vector per grid point (1-based point i in row i-1)."""
+    x = [float(v) for v in x]
+    n = len(x)
+    rows = []
+    for i in range(1, n + 1):
+        q0, tg = weno_nonuniform_target(i, n)
+        x1, x2, x3, x4, x5 = x[q0 - 1:q0 + 4]
+        xi, xL, xph = {1: (x1, x1, (x1 + x2) / 2), 2: (x2, (x1 + x2) / 2, (x2 + x3) / 2),
+                       3: (x3, (x2 + x3) / 2, (x3 + x4) / 2), 4: (x4, (x3 + x4) / 2, (x4 + x5) / 2),
+                       5: (x5, (x4 + x5) / 2, x5)}[tg]
+        dx = xph - xL
+        xM = (xL + xph) / 2
+        row = [dx / 6, dx, dx * dx * dx]
+        for al in ((x1, x2, x3), (x2, x3, x4), (x3, x4, x5)):
+            m1i, _ = _fb3(al, xi)
+            m1L, _ = _fb3(al, xL)
+            m1M, m2M = _fb3(al, xM)
+            m1R, _ = _fb3(al, xph)
+            row += m1i + m1L + m1M + m1R + m2M
+        if tg == 3:
+            d0 = ((x3 - x4) * (x3 - x5)) / ((x1 - x4) * (x1 - x5))
+            d2 = ((x3 - x1) * (x3 - x2)) / ((x5 - x1) * (x5 - x2))
+        elif tg == 1:
+            d0 = (((2 * x1 - x2 - x3) * (x1 - x4) * (x1 - x5) + (x1 - x3) * (x1 - x5) * (x1 - x2)
+                   + (x1 - x3) * (x1 - x4) * (x1 - x2)) / ((2 * x1 - x2 - x3) * (x1 - x4) * (x1 - x5)))
+            d2 = ((x1 - x3) * (x1 - x4) * (x1 - x2)) / ((-x1 + x5) * (2 * x1 - x3 - x4) * (-x2 + x5))
+        elif tg == 2:
+            d0 = ((x2 - x4) * (x2 - x5)) / ((x1 - x4) * (x1 - x5))
+            d2 = ((-x1 + x2) * (x2 - x3) * (x2 - x4)) / ((-x1 + x5) * (2 * x2 - x3 - x4) * (-x2 + x5))
+        elif tg == 4:
+            d0 = ((-x2 + x4) * (-x3 + x4) * (x4 - x5)) / ((x1 - x4) * (x1 - x5) * (-x2 - x3 + 2 * x4))
+            d2 = ((-x1 + x4) * (-x2 + x4)) / ((-x1 + x5) * (-x2 + x5))
+        else:
+            d0 = ((-x2 + x5) * (-x3 + x5) * (-x4 + x5)) / ((x1 - x4) * (x1 - x5) * (-x2 - x3 + 2 * x5))
+            d2 = (((-x1 - x4 + 2 * x5) * (-x2 + x5) * (-x3 + x5) + (-x1 + x5) * (-x2 - x3 + 2 * x5) * (-x4 + x5))
+                  / ((-x1 + x5) * (-x2 + x5) * (-x3 - x4 + 2 * x5)))
+        d1 = 1.0 - d0 - d2
+        dp = [0.5 * (d + 3.0 * abs(d)) for d in (d0, d1, d2)]
+        dm = [dp[0] - d0, dp[1] - d1, dp[2] - d2]
+        sp_ = dp[0] + dp[1] + dp[2]
+        sm_ = dm[0] + dm[1] + dm[2]
+        row += [v / sp_ for v in dp] + [v / sm_ for v in dm] + [sp_, sm_]
+        rows.append(row)
+    return rows
+
+
 def select(op: Operator, i: int, length: int, periodic: bool) -> Tuple[List[float], List[int]]:
     """(weights, unwrapped taps) of `op` at 1-based position i on a line of `length` points."""
     if not periodic and i <= op.nlo:

@@ -17,6 +17,7 @@ from typing import Dict, List, Tuple
 
 import numpy as np
 
+from .weno_nonuniform import taps_and_target, weno_f_nonuniform
 from .fornberg import (boundary_interpolator_extrapolator, complete_centered_difference,
                        complete_centered_difference_nonuniform, complete_half_centered_difference,
                        complete_upwind_difference_nonuniform,
@@ -812,6 +813,8 @@ class OracleProblem:
         n = self.npts[j]
         per = self.bc[f][j]["periodic"]
         idx = self.interior_index(f, j)
+        if not self.uniform[j]:
+            return self._weno_nonuniform(F, f, j)
         if not per and (idx[0] <= 2 or idx[-1] > n - 2):
             # get_f_taps_coords picks the near-wall functions there (function_scheme.jl:6-16)
             raise NotImplementedError("oracle: near-wall WENO stencils")
@@ -825,6 +828,25 @@ class OracleProblem:
             return F[tuple(s)]
         u_m2, u_m1, u_0, u_p1, u_p2 = tap(-2), tap(-1), tap(0), tap(1), tap(2)
         return weno5(u_m2, u_m1, u_0, u_p1, u_p2, eps, dx)
+
+    def _weno_nonuniform(self, F, f, j):
+        """``function_scheme`` with the WENO scheme on a nonuniform dimension (function_scheme.jl:
+        36-76): every point uses ``weno_f_nonuniform`` on the grid coordinates of its five taps,
+        the two points at each end the one-sided targets (WENO.jl:84-85)."""
+        n = self.npts[j]
+        eps = float(self.adv_param)
+        sl = [slice(self.lower[f][k], self.npts[k] - self.upper[f][k]) for k in range(self.nd)]
+        out = []
+        for i in self.interior_index(f, j):
+            taps, tg = taps_and_target(int(i), n)
+            vals = []
+            for q in taps:
+                s = list(sl)
+                s[j] = q - 1
+                vals.append(F[tuple(s)])
+            xs = [self.grid[j][q - 1] for q in taps]
+            out.append(weno_f_nonuniform(vals, eps, xs, tg))
+        return np.stack(out, axis=j)
 
     def _nonlinlap(self, coef_num, coef_den, g, f, j, full, env):
         """``cartesian_nonlinear_laplacian`` (nonlinear_laplacian.jl:28-103)."""

@@ -141,6 +141,15 @@ class DescInterp:
                     acc += wa * wb * self.load(u, f, J, t, p)
             return acc
         if kind == L.TERM_WENO:
+            if tm.get("variant", 0) == 1:
+                from molgpu.weights import weno_nonuniform_target
+                q0, _ = weno_nonuniform_target(I[d], self.n[d])
+                v = []
+                for k in range(5):
+                    J = list(I)
+                    J[d] = q0 + k
+                    v.append(self.load(u, f, J, t, p))
+                return _weno_nu(self.lw.ops[tm["op"]].rows[I[d] - 1], v, tm["eps"])
             v = []
             for o in range(-2, 3):
                 J = list(I)
@@ -251,3 +260,24 @@ def _weno(um2, um1, u0, up1, up2, eps, dx):
     hm = [(11 * u0 - 7 * up1 + 2 * up2) / 6, (5 * u0 - up1 + 2 * um1) / 6, (2 * u0 + 5 * um1 - um2) / 6]
     hp = [(2 * u0 + 5 * up1 - up2) / 6, (5 * u0 + 2 * up1 - um1) / 6, (11 * u0 - 7 * um1 + 2 * um2) / 6]
     return (sum(a * b for a, b in zip(wp, hp)) / sum(wp) - sum(a * b for a, b in zip(wm, hm)) / sum(wm)) / dx
+
+
+def _weno_nu(g, v, eps):
+    """weno5nu_point: the nonuniform WENO from a point's geometry row."""
+    b, r = [], []
+    for k in range(3):
+        m = g[3 + 15 * k:3 + 15 * (k + 1)]
+        a = v[k:k + 3]
+
+        def d3(w):
+            return w[0] * a[0] + w[1] * a[1] + w[2] * a[2]
+        rr, pL, pM, pR, pp = d3(m[0:3]), d3(m[3:6]), d3(m[6:9]), d3(m[9:12]), d3(m[12:15])
+        val = g[1] * (g[0] * (pL * pL + 4 * (pM * pM) + pR * pR)) + g[2] * (g[1] * (pp * pp))
+        b.append(max(val, 0.0))
+        r.append(rr)
+    ap = [g[48 + k] / ((eps + b[k]) * (eps + b[k])) for k in range(3)]
+    am = [g[51 + k] / ((eps + b[k]) * (eps + b[k])) for k in range(3)]
+    sp, sm = ap[0] + ap[1] + ap[2], am[0] + am[1] + am[2]
+    Rp = (ap[0] / sp) * r[0] + (ap[1] / sp) * r[1] + (ap[2] / sp) * r[2]
+    Rm = (am[0] / sm) * r[0] + (am[1] / sm) * r[1] + (am[2] / sm) * r[2]
+    return g[54] * Rp - g[55] * Rm

@@ -8,7 +8,7 @@ import math
 import numpy as np
 import pytest
 
-from molgpu import Plan, lower, problems
+from molgpu import Plan, Tsit5, discretize, lower, problems, solve
 from molgpu import _lib as L
 from oracle.integrators import ssprk33, tsit5
 from oracle.mol_oracle import OracleProblem
@@ -162,3 +162,97 @@ def test_nonuniform_upwind_adjoint_matches_finite_differences(gpu_lib):
     fd = (loss(lw.u0 + h * w) - loss(lw.u0 - h * w)) / (2 * h)
     assert abs(g @ w - fd) <= 1e-6 * abs(fd), (g @ w, fd)
     plan.close()
+
+
+WENO_KINDS = ["uniform", "sinh", "tanh"]
+
+
+@pytest.mark.parametrize("kind", WENO_KINDS)
+def test_nonuniform_weno_rhs_and_trajectory(gpu_lib, kind):
+    """Node-centred Lagrange WENO-5 on grids given as points (nonuniform_weno.jl): RHS and
+    SSPRK33 trajectory against the oracle, generated code against the interpreter."""
+    s, d, ex = problems.weno_convection_mms(kind, 161)
+    spec = s.to_spec(d)
+    lw, orc = lower(spec), OracleProblem(spec)
+    plan = Plan(lw)
+    assert L.lib().mol_plan_uses_codegen(plan.handle) == 1
+    v = lw.u0 + 0.05 * np.random.default_rng(4).standard_normal(lw.n_unknowns)
+    for t in (0.0, 0.03):
+        du = np.zeros(lw.n_unknowns)
+        plan.rhs(du, v, None, t)
+        ref = orc.rhs(v, t)
+        assert _rel(du, ref) <= 1e-12, (kind, t)
+    u = lw.u0.copy()
+    plan.step_ssprk33(u, ex["dt"], 40, t0=0.0)
+    ref, _ = ssprk33(lambda w, tt: orc.rhs(w, tt), lw.u0, 0.0, ex["dt"], 40)
+    assert _rel(u, ref) <= 1e-10, kind
+    plan.close()
+
+
+def test_nonuniform_weno_generated_matches_interpreter(gpu_lib, monkeypatch):
+    s, d, ex = problems.weno_convection_mms("sinh", 161)
+    lw = lower(s.to_spec(d))
+    gen = Plan(lw)
+    monkeypatch.setenv("MOL_DISABLE_CODEGEN", "1")
+    interp = Plan(lw)
+    u = lw.u0 * 1.01
+    a, b = np.zeros_like(u), np.zeros_like(u)
+    gen.rhs(a, u, None, 0.02)
+    interp.rhs(b, u, None, 0.02)
+    assert _rel(a, b) < 1e-13
+
+
+def test_nonuniform_weno_solution_converges(gpu_lib):
+    """The reference's MMS convergence run on the uniform points (CFL 0.01 to t = 0.05, SSPRK33;
+    its assertion: observed order above 3.75)."""
+    errs = []
+    for n in (81, 161):
+        s, d, ex = problems.weno_convection_mms("uniform", n)
+        lw = lower(s.to_spec(d))
+        plan = Plan(lw)
+        nsteps = int(math.ceil(0.05 / ex["dt"]))
+        dt = 0.05 / nsteps
+        u = lw.u0.copy()
+        plan.step_ssprk33(u, dt, nsteps, t0=0.0)
+        xs = lw.grids[0]
+        full = plan.fill_grid(u, 0.05)[0]
+        w = np.concatenate([np.diff(xs), [xs[-1] - xs[-2]]])
+        ue = problems.weno_mms_exact(xs, 0.05)
+        errs.append(math.sqrt(np.sum(w * (full - ue) ** 2)) / math.sqrt(np.sum(w * ue ** 2)))
+        plan.close()
+    assert math.log(errs[0] / errs[1]) / math.log(160 / 80) > 3.75, errs
+
+
+def test_nonuniform_weno_adjoint_matches_finite_differences(gpu_lib):
+    s, d, ex = problems.weno_convection_mms("tanh", 81)
+    lw = lower(s.to_spec(d))
+    plan = Plan(lw)
+    dt, n = ex["dt"] * 20, 25
+    target = np.zeros(lw.n_unknowns)
+
+    def loss(u0):
+        u = u0.copy()
+        plan.step_ssprk33(u, dt, n, t0=0.0)
+        return 0.5 * float(np.sum((u - target) ** 2))
+
+    g = np.zeros(lw.n_unknowns)
+    plan.adjoint_ssprk33(lw.u0, dt, n, target, nsnap=4, dLdu0=g)
+    w = np.random.default_rng(9).standard_normal(lw.n_unknowns)
+
+    def cd(h):
+        return (loss(lw.u0 + h * w) - loss(lw.u0 - h * w)) / (2 * h)
+
+    fd = (4.0 * cd(5e-7) - cd(1e-6)) / 3.0
+    assert abs(g @ w - fd) <= 1e-6 * abs(fd), (g @ w, fd)
+    plan.close()
+
+
+def test_burgers_nonuniform_upwind_tsit5(gpu_lib):
+    """The reference's nonuniform Burgers test (first-order upwinding on a perturbed grid,
+    Tsit5 to t = 1; burgers_eq.jl:106-152 asserts atol 10^-2.5 against x/(t+1))."""
+    s, d, _ = problems.burgers_nonuniform_upwind()
+    prob = discretize(s, d)
+    sol = solve(prob, Tsit5(), abstol=1e-8, reltol=1e-8, saveat=0.25)
+    x = sol["x"]
+    for i, t in enumerate(sol.ts):
+        assert np.max(np.abs(sol["u"][i] - x / (t + 1))) < 10 ** -2.5, t
