@@ -331,6 +331,25 @@ class Solution:
         lw = self.prob.lowered
         return {x: g.copy() for x, g in zip(lw.ivs, lw.grids)}
 
+    def __call__(self, t, *coords, var=None):
+        """Multilinear interpolation of a field over (t, x, ...) through the saved full-grid
+        arrays, as the reference's ``Gridded(Linear())`` interpolation of each dependent
+        variable (interface/solution/solution_utils.jl:3-32).  ``var`` names the field (a
+        Field, applied field or name); it may be left out when there is only one."""
+        from scipy.interpolate import RegularGridInterpolator
+        lw = self.prob.lowered
+        if var is None:
+            if len(lw.fields) != 1:
+                raise ValueError("several fields: name one with var=")
+            var = lw.fields[0]
+        vals = self[var]
+        if len(self.ts) < 2:
+            raise ValueError("interpolation in t needs at least two saved times")
+        f = RegularGridInterpolator((self.ts,) + tuple(lw.grids), vals, method="linear")
+        pts = np.broadcast_arrays(np.asarray(t, dtype=np.float64), *[np.asarray(c, dtype=np.float64) for c in coords])
+        out = f(np.stack([p.ravel() for p in pts], axis=-1))
+        return out.reshape(pts[0].shape) if pts[0].shape else float(out[0])
+
     def __getitem__(self, key):
         lw = self.prob.lowered
         name = key.name if isinstance(key, (IV, Field)) else (key.field.name if isinstance(key, FieldApp) else key)

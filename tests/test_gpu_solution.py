@@ -65,3 +65,18 @@ def test_burgers_weno_solution_on_full_grid(gpu_lib):
     assert u.shape == (7, len(x))
     for i, t in enumerate(sol.ts):
         assert np.max(np.abs(u[i] - x / (t + 1))) < 1e-8, t
+
+
+def test_solution_interpolation(gpu_lib):
+    """sol(t, x): linear in t and x through the saved full-grid arrays (the reference's
+    Gridded(Linear()) interpolation)."""
+    s, d, _ = problems.heat1d(n=101)
+    prob = discretize(s, d)
+    sol = solve(prob, SSPRK33(), dt=2e-5, saveat=0.02)
+    u = sol["u"]
+    x = sol["x"]
+    assert sol(0.04, x[37]) == pytest.approx(u[2, 37], rel=1e-14)
+    mid = sol(0.03, 0.5 * (x[10] + x[11]))
+    want = 0.25 * (u[1, 10] + u[1, 11] + u[2, 10] + u[2, 11])
+    assert mid == pytest.approx(want, rel=1e-12)
+    assert sol([0.0, 0.1], [0.0, 1.0]).shape == (2,)
