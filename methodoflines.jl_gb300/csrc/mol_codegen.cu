@@ -1075,10 +1075,39 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
     e << "}\n";
 }
 
+// True when some boundary program uses an elementary function, a power, a comparison or a
+// select (the generated module then compiles those cases into run_bc_prog).
+bool bc_full_ops(const mol_problem_desc* d) {
+    for (int f = 0; f < d->nfields; ++f)
+        for (int q = 0; q < d->ndim; ++q)
+            for (int s = 0; s < 2; ++s) {
+                const mol_bc& b = d->bc[f][q][s];
+                if (b.prog < 0 || b.prog >= d->nprogs) continue;
+                const int start = d->prog_ranges[2 * b.prog], len = d->prog_ranges[2 * b.prog + 1];
+                for (int pc = start; pc < start + len; ++pc) {
+                    const int op = d->code[pc].op;
+                    if (op == MOL_OP_POWI || op == MOL_OP_POW || op == MOL_OP_FN || op == MOL_OP_CMP ||
+                        op == MOL_OP_IFELSE)
+                        return true;
+                }
+            }
+    return false;
+}
+
 std::string generate_source(const mol_problem_desc* d, std::string& why) {
     Emitter e;
-    e << "// generated by libmolgpu for one problem structure\n"
-      << "#include \"mol_kernels.cuh\"\n"
+    e << "// generated by libmolgpu for one problem structure\n";
+    if (bc_full_ops(d)) e << "#define MOL_BC_FULL_OPS 1\n";
+    bool edge_rows = false, extrap_rows = false;
+    for (int f = 0; f < d->nfields; ++f)
+        for (int q = 0; q < d->ndim; ++q)
+            for (int s = 0; s < 2; ++s) {
+                edge_rows |= d->bc[f][q][s].kind == MOL_BC_EDGE;
+                extrap_rows |= d->bc[f][q][s].extrap > 0;
+            }
+    if (edge_rows) e << "#define MOL_HAS_EDGE_ROWS 1\n";
+    if (extrap_rows) e << "#define MOL_HAS_EXTRAP_ROWS 1\n";
+    e << "#include \"mol_kernels.cuh\"\n"
       << "namespace mol {\n";
     int nface = 0;  // nonlinear-Laplacian terms: slots of the face pass
     for (int k = 0; k < d->nterms; ++k) {

@@ -18,6 +18,21 @@
 
 #include "molgpu.h"
 
+// Generated modules compile the rows their problem has: edge-aligned face rows and
+// extrapolated points only when some boundary row uses them (each adds out-of-line code
+// that the stage kernels' register allocation pays for).  The library's own kernels
+// (the interpreter) always have both.
+#ifndef MOL_JIT
+#define MOL_HAS_EDGE_ROWS 1
+#define MOL_HAS_EXTRAP_ROWS 1
+#endif
+#ifndef MOL_HAS_EDGE_ROWS
+#define MOL_HAS_EDGE_ROWS 0
+#endif
+#ifndef MOL_HAS_EXTRAP_ROWS
+#define MOL_HAS_EXTRAP_ROWS 0
+#endif
+
 namespace mol {
 
 // Device-resident integrator state; kernels read t/dt from here so a captured
@@ -203,11 +218,16 @@ __device__ T run_bc_prog(const DevProb<T>& P, int prog, int out_index, const int
             case MOL_OP_MUL: r[dst] = r[in.a & 15] * r[in.b & 15]; break;
             case MOL_OP_DIV: r[dst] = r[in.a & 15] / r[in.b & 15]; break;
             case MOL_OP_NEG: r[dst] = -r[in.a & 15]; break;
+#if !defined(MOL_JIT) || defined(MOL_BC_FULL_OPS)
+            // Elementary functions in a boundary program: compiled into generated code only when
+            // some boundary program uses them (their range reduction would otherwise raise the
+            // register count of every stage kernel that can reach a boundary row).
             case MOL_OP_POWI: r[dst] = powi(r[in.a & 15], in.imm); break;
             case MOL_OP_POW: r[dst] = pow(r[in.a & 15], r[in.b & 15]); break;
             case MOL_OP_FN: r[dst] = apply_fn(in.imm, r[in.a & 15]); break;
             case MOL_OP_CMP: r[dst] = apply_cmp(in.imm, r[in.a & 15], r[in.b & 15]); break;
             case MOL_OP_IFELSE: r[dst] = r[in.a & 15] != T(0) ? r[in.b & 15] : r[in.c & 15]; break;
+#endif
             case MOL_OP_OUT: if (in.imm == out_index) res = r[in.a & 15]; break;
             default: break;
         }
@@ -279,8 +299,10 @@ template <class T>
 __device__ __noinline__ T bc_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t, const T* p) {
     const int i = I[dout], n = P.n[dout];
     if ((side == 0 && i == 1) || (side == 1 && i == n)) return bc_row_value(P, u, f, I, dout, side, t, p);
+#if MOL_HAS_EXTRAP_ROWS
     if (P.bc[(f * 3 + dout) * 2 + side].xop >= 0 && ((side == 0 && i == 2) || (side == 1 && i == n - 1)))
         return extrap_value(P, u, f, I, dout, side, t, p);
+#endif
     return T(0);
 }
 
@@ -289,9 +311,12 @@ __device__ __noinline__ T bc_value(const DevProb<T>& P, const T* u, int f, int* 
 // table at position 1 (n-1), solved for the ghost point (boundary_value_maps for
 // EdgeAlignedGrid, generate_bc_eqs.jl:80-160; tables selected as in
 // half_offset_centred_difference.jl:9-37).
+// Scalar coordinates (no pointer to a caller's array): the generated stage kernels reach it
+// from their line helpers, and an address-taken array there costs them a stack frame.
 template <class T>
-__device__ __noinline__ T edge_row_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t,
-                                         const T* p) {
+__device__ __noinline__ T edge_row_value(const DevProb<T>& P, const T* u, int f, int i0, int i1, int i2, int dout,
+                                         int side, T t, const T* p) {
+    const int I[3] = {i0, i1, i2};
     const DevBC<T>& B = P.bc[(f * 3 + dout) * 2 + side];
     T a = B.a, b = B.b, g = B.g;
     if (B.prog >= 0) {
@@ -323,7 +348,9 @@ template <class T>
 __device__ __noinline__ T bc_row_value(const DevProb<T>& P, const T* u, int f, int* I, int dout, int side, T t,
                                        const T* p) {
     const DevBC<T> B = P.bc[(f * 3 + dout) * 2 + side];
-    if (B.kind == MOL_BC_EDGE) return edge_row_value(P, u, f, I, dout, side, t, p);
+#if MOL_HAS_EDGE_ROWS
+    if (B.kind == MOL_BC_EDGE) return edge_row_value(P, u, f, I[0], I[1], I[2], dout, side, t, p);
+#endif
     if (B.kind != MOL_BC_ROBIN) return T(0);
     const bool dyn = B.prog >= 0;
     T a = B.a, b = B.b, g = B.g;
@@ -402,11 +429,12 @@ __device__ __noinline__ T bc_line_value(const DevProb<T>& P, const T* __restrict
                                         long long c, int side, T t, const T* __restrict__ p) {
     const int iD = D == 0 ? i0 : (D == 1 ? i1 : i2);
     const DevBC<T>& B = P.bc[(f * 3 + D) * 2 + side];
+#if MOL_HAS_EDGE_ROWS
     if (B.kind == MOL_BC_EDGE) {
-        int J[3] = {i0, i1, i2};
-        J[D] = side == 0 ? 1 : P.n[D];
-        return edge_row_value(P, u, f, J, D, side, t, p);
+        const int e = side == 0 ? 1 : P.n[D];
+        return edge_row_value(P, u, f, D == 0 ? e : i0, D == 1 ? e : i1, D == 2 ? e : i2, D, side, t, p);
     }
+#endif
     if (B.kind != MOL_BC_ROBIN) return T(0);
     if (DYN && B.prog >= 0) {
         int J[3] = {i0, i1, i2};
@@ -466,6 +494,27 @@ __device__ __noinline__ T extrap_line_value(const DevProb<T>& P, const T* __rest
     return acc;
 }
 
+// A point of the line through the cell that is not an unknown: a boundary point, the
+// extrapolated point next to it, or nothing (0).  One out-of-line call per tap, so the
+// generated kernels that inline line_pt keep a single call site per tap.
+template <class T, int D, bool DYN>
+__device__ __noinline__ T line_edge_pt(const DevProb<T>& P, const T* __restrict__ u, int f, int i0, int i1, int i2,
+                                       long long c, int q, T t, const T* __restrict__ p) {
+    const int n = P.n[D];
+    if (q <= P.lo[D]) {
+        if (q == 1) return bc_line_value<T, D, DYN>(P, u, f, i0, i1, i2, c, 0, t, p);
+#if MOL_HAS_EXTRAP_ROWS
+        if (q == 2) return extrap_line_value<T, D, DYN>(P, u, f, i0, i1, i2, c, 0, t, p);
+#endif
+        return T(0);
+    }
+    if (q == n) return bc_line_value<T, D, DYN>(P, u, f, i0, i1, i2, c, 1, t, p);
+#if MOL_HAS_EXTRAP_ROWS
+    if (q == n - 1) return extrap_line_value<T, D, DYN>(P, u, f, i0, i1, i2, c, 1, t, p);
+#endif
+    return T(0);
+}
+
 // Field f at full-grid position q of the line through the cell (load_pt restricted to D).
 template <class T, int D, bool DYN>
 __device__ __forceinline__ T line_pt(const DevProb<T>& P, const T* __restrict__ u, int f, const int* I, long long c,
@@ -474,12 +523,7 @@ __device__ __forceinline__ T line_pt(const DevProb<T>& P, const T* __restrict__ 
     if ((P.permask[f] >> D) & 1) q = wrap_periodic(q, n);
     if (q > P.lo[D] && q <= n - P.up[D])
         return u[(long long)f * P.ncell + c + (long long)(q - I[D]) * gstride(P, D)];
-    if (q <= P.lo[D]) {
-        if (q == 1) return bc_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 0, t, p);
-        return q == 2 ? extrap_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 0, t, p) : T(0);
-    }
-    if (q == n) return bc_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 1, t, p);
-    return q == n - 1 ? extrap_line_value<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, 1, t, p) : T(0);
+    return line_edge_pt<T, D, DYN>(P, u, f, I[0], I[1], I[2], c, q, t, p);
 }
 
 // apply_op_at restricted to D: sum_k w_k u[tap_k] at position `pos` of a line of `len` points.

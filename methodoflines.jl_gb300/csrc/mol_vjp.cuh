@@ -14,8 +14,9 @@ namespace mol {
 
 // Transpose of edge_row_value: d u_ghost / d u_k = -(a c_k + b d_k) / (a c_ghost + b d_ghost).
 template <class T>
-__device__ __noinline__ void edge_row_scatter(const DevProb<T>& P, T* lam, int f, const int* I, int dout, int side,
-                                              T g, T t, const T* p) {
+__device__ __noinline__ void edge_row_scatter(const DevProb<T>& P, T* lam, int f, int i0, int i1, int i2, int dout,
+                                              int side, T g, T t, const T* p) {
+    const int I[3] = {i0, i1, i2};
     const DevBC<T>& B = P.bc[(f * 3 + dout) * 2 + side];
     T a = B.a, b = B.b;
     if (B.prog >= 0) {
@@ -51,10 +52,12 @@ template <class T>
 __device__ __noinline__ void bc_row_scatter(const DevProb<T>& P, T* lam, int f, const int* I, int dout, int side,
                                             T g, T t, const T* p) {
     const DevBC<T> B = P.bc[(f * 3 + dout) * 2 + side];
+#if MOL_HAS_EDGE_ROWS
     if (B.kind == MOL_BC_EDGE) {
-        edge_row_scatter(P, lam, f, I, dout, side, g, t, p);
+        edge_row_scatter(P, lam, f, I[0], I[1], I[2], dout, side, g, t, p);
         return;
     }
+#endif
     if (B.kind != MOL_BC_ROBIN) return;
     T a = B.a, b = B.b;
     if (B.prog >= 0) {
@@ -185,12 +188,13 @@ __device__ __noinline__ void scatter_bc_line(const DevProb<T>& P, T* lam, int f,
                                              int side, T g, T t, const T* __restrict__ p) {
     const int iD = D == 0 ? i0 : (D == 1 ? i1 : i2);
     const DevBC<T>& B = P.bc[(f * 3 + D) * 2 + side];
+#if MOL_HAS_EDGE_ROWS
     if (B.kind == MOL_BC_EDGE) {
-        int J[3] = {i0, i1, i2};
-        J[D] = side == 0 ? 1 : P.n[D];
-        edge_row_scatter(P, lam, f, J, D, side, g, t, p);
+        const int e = side == 0 ? 1 : P.n[D];
+        edge_row_scatter(P, lam, f, D == 0 ? e : i0, D == 1 ? e : i1, D == 2 ? e : i2, D, side, g, t, p);
         return;
     }
+#endif
     if (B.kind != MOL_BC_ROBIN) return;
     if (DYN && B.prog >= 0) {
         int J[3] = {i0, i1, i2};
@@ -239,6 +243,26 @@ __device__ __noinline__ void scatter_extrap_line(const DevProb<T>& P, T* lam, in
     }
 }
 
+// Transpose of line_edge_pt (one out-of-line call per tap).
+template <class T, int D, bool DYN>
+__device__ __noinline__ void scatter_line_edge_pt(const DevProb<T>& P, T* lam, int f, int i0, int i1, int i2,
+                                                  long long c, int q, T g, T t, const T* __restrict__ p) {
+    const int n = P.n[D];
+    if (q <= P.lo[D]) {
+        if (q == 1) scatter_bc_line<T, D, DYN>(P, lam, f, i0, i1, i2, c, 0, g, t, p);
+#if MOL_HAS_EXTRAP_ROWS
+        else if (q == 2) scatter_extrap_line<T, D, DYN>(P, lam, f, i0, i1, i2, c, 0, g, t, p);
+#endif
+    } else if (q == n) {
+        scatter_bc_line<T, D, DYN>(P, lam, f, i0, i1, i2, c, 1, g, t, p);
+    }
+#if MOL_HAS_EXTRAP_ROWS
+    else if (q == n - 1) {
+        scatter_extrap_line<T, D, DYN>(P, lam, f, i0, i1, i2, c, 1, g, t, p);
+    }
+#endif
+}
+
 template <class T, int D, bool DYN>
 __device__ __forceinline__ void scatter_line_pt(const DevProb<T>& P, T* lam, int f, const int* I, long long c, int q,
                                                 T g, T t, const T* __restrict__ p) {
@@ -248,14 +272,7 @@ __device__ __forceinline__ void scatter_line_pt(const DevProb<T>& P, T* lam, int
         atomicAdd(lam + (long long)f * P.ncell + c + (long long)(q - I[D]) * gstride(P, D), g);
         return;
     }
-    if (q <= P.lo[D]) {
-        if (q == 1) scatter_bc_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 0, g, t, p);
-        else if (q == 2) scatter_extrap_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 0, g, t, p);
-    } else if (q == n) {
-        scatter_bc_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 1, g, t, p);
-    } else if (q == n - 1) {
-        scatter_extrap_line<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, 1, g, t, p);
-    }
+    scatter_line_edge_pt<T, D, DYN>(P, lam, f, I[0], I[1], I[2], c, q, g, t, p);
 }
 
 template <class T, int D, int NT, bool DYN>
