@@ -147,7 +147,7 @@ __device__ __forceinline__ TapSel select_taps(const mol_op1d& op, int i, int len
         s.cnt = op.bLhi; s.wrap = false;
     } else {
         s.woff = op.w_int; s.first = i + op.omin; s.cnt = op.L; s.wrap = per;
-        if (op.nrows > 0) {  // nonuniform grid: the row of point i (validated: nrows == len - nlo - nhi)
+        if (op.nrows > 0) {  // per-point rows (nonuniform grid): the row of point i, kept in range
             int r = i - op.nlo - 1;
             r = r < 0 ? 0 : (r >= op.nrows ? op.nrows - 1 : r);
             s.woff += (long long)r * op.L;

