@@ -1255,6 +1255,9 @@ std::vector<std::string> jit_options(int min_blocks) {
     const char* mb = getenv("MOL_JIT_MIN_BLOCKS");
     const int minb = (mb && atoi(mb) > 0) ? atoi(mb) : (min_blocks > 0 ? min_blocks : kDefaultMinBlocks);
     o.push_back("-DMOL_MIN_BLOCKS=" + std::to_string(minb));
+    // MOL_BATCH_MIN_BLOCKS: the same bound for the ensemble kernels (default 1: no cap)
+    const char* bmb = getenv("MOL_BATCH_MIN_BLOCKS");
+    if (bmb && atoi(bmb) > 0) o.push_back("-DMOL_BATCH_MIN_BLOCKS=" + std::to_string(atoi(bmb)));
     // MOL_JIT_VERBOSE=1: ptxas resource report (registers, stack, spills) on stderr
     if (getenv("MOL_JIT_VERBOSE")) o.push_back("--ptxas-options=-v");
     // MOL_JIT_DEFINES="A B=1": extra preprocessor definitions for the generated modules

@@ -13,6 +13,9 @@ constexpr int kThreads = 256;
 
 // Minimum resident CTAs per SM requested from the register allocator for the kernels that
 // evaluate the right-hand side (set for generated modules, MOL_JIT_MIN_BLOCKS).
+#ifndef MOL_BATCH_MIN_BLOCKS
+#define MOL_BATCH_MIN_BLOCKS 1  // ensemble kernels: CTAs of kThreads per SM the register budget must allow
+#endif
 #ifndef MOL_MIN_BLOCKS
 #define MOL_MIN_BLOCKS 1
 #endif
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_vjp_t(const __grid
 // (largest first, dynamic via an atomic ticket) and integrates it for `nsteps`
 // SSPRK33 steps, synchronising only its own threads between stages.
 template <class T, class G>
-__global__ void __launch_bounds__(kThreads, 1) k_batch_ssprk_t(const DevProb<T>* __restrict__ probs,
+__global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_ssprk_t(const DevProb<T>* __restrict__ probs,
                                                             const long long* __restrict__ off,
                                                             const int* __restrict__ order, int ninst, T* U, T* U1,
                                                             T* U2, const T* const* __restrict__ params,
@@ -312,7 +315,7 @@ struct TileRef {
 };
 
 template <class T, class G>
-__global__ void __launch_bounds__(kThreads, 1) k_batch_tiles_t(const DevProb<T>* __restrict__ probs,
+__global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_tiles_t(const DevProb<T>* __restrict__ probs,
                                                             const long long* __restrict__ off,
                                                             const TileRef* __restrict__ tiles,
                                                             long long ntiles, int tile_cells, T* U, T* U1, T* U2,
