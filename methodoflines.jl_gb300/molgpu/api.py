@@ -62,6 +62,10 @@ class MOLFiniteDifference:
         self.approx_order = int(approx_order)
         self.advection_scheme = advection_scheme if advection_scheme is not None else UpwindScheme()
         self.grid_align = {"center_align": "center", "edge_align": "edge"}.get(grid_align, grid_align)
+        if kwargs.get("upwind_order") is not None:
+            # MOLFiniteDifference.jl:53-55: the keyword is accepted and has no effect
+            import warnings
+            warnings.warn("`upwind_order` no longer does anything; use advection_scheme=UpwindScheme(order)")
         self.kwargs = kwargs
 
 
