@@ -43,3 +43,22 @@ def test_streamed_first_step_bit_identical(gpu_lib, monkeypatch, name, nsteps, c
     plan.step_ssprk33(h, dt, nsteps, t0=0.2)
     assert np.array_equal(h, dev.cpu().numpy()), name
     plan.close()
+
+
+def test_streamed_first_step_f32state(gpu_lib, monkeypatch):
+    """The Float32-state variant streams its copy the same way."""
+    torch = pytest.importorskip("torch")
+    s, d, ex = problems.brusselator(N=256)
+    lw = lower(s.to_spec(d))
+    plan = Plan(lw)
+    dt = ex["dt_ssprk"]
+    pinned = torch.empty(lw.n_unknowns, dtype=torch.float32, pin_memory=True)
+    pinned.copy_(torch.from_numpy(lw.u0.astype(np.float32)))
+    h = pinned.numpy()
+    plan.step_ssprk33(h, dt, 2, t0=0.2)
+    dev = torch.tensor(lw.u0.astype(np.float32), device="cuda")
+    torch.cuda.synchronize()
+    plan.step_ssprk33(dev, dt, 2, t0=0.2)
+    torch.cuda.synchronize()
+    assert np.array_equal(h, dev.cpu().numpy())
+    plan.close()
