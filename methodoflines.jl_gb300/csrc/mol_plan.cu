@@ -367,18 +367,6 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
     return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
 }
 
-// The side stream and events of the streamed copy (created outside any stream capture).
-static int ensure_copy_stream(mol_plan* plan) {
-    if (plan->copy_stream) return MOL_OK;
-    int st;
-    if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->copy_stream, cudaStreamNonBlocking), "copy stream")))
-        return st;
-    for (int k = 0; k <= kMaxSlabs; ++k)
-        if ((st = cuda_check(plan, cudaEventCreateWithFlags(&plan->slab_ev[k], cudaEventDisableTiming), "slab event")))
-            return st;
-    return MOL_OK;
-}
-
 // Stage 1 of a step whose state is arriving from pinned host memory: the copy runs on a
 // side stream in slabs of whole slices of the slowest interior dimension, and stage 1 of
 // each slab starts as soon as the slabs its stencils reach (`halo` slices either side,
@@ -392,7 +380,13 @@ int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T*
     const long long h = plan->halo;
     const bool per = plan->per_last;
     int st;
-    if ((st = ensure_copy_stream(plan))) return st;
+    if (!plan->copy_stream) {
+        if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->copy_stream, cudaStreamNonBlocking), "copy stream")))
+            return st;
+        for (int k = 0; k <= kMaxSlabs; ++k)
+            if ((st = cuda_check(plan, cudaEventCreateWithFlags(&plan->slab_ev[k], cudaEventDisableTiming), "slab event")))
+                return st;
+    }
     // the copies may only overwrite the staging buffer once earlier work on the stream is done
     if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[kMaxSlabs], plan->stream), "record"))) return st;
     if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->copy_stream, plan->slab_ev[kMaxSlabs], 0), "wait"))) return st;
@@ -858,7 +852,6 @@ int mol_plan_set_stream(mol_plan* plan, void* stream) {
     plan->stream = (cudaStream_t)stream;
     if (plan->g_ssp64) { cudaGraphExecDestroy(plan->g_ssp64); plan->g_ssp64 = nullptr; }
     if (plan->g_ssp32) { cudaGraphExecDestroy(plan->g_ssp32); plan->g_ssp32 = nullptr; }
-    if (plan->g_io) { cudaGraphExecDestroy(plan->g_io); plan->g_io = nullptr; }
     return MOL_OK;
 }
 
@@ -868,7 +861,6 @@ int mol_plan_destroy(mol_plan* plan) {
     if (plan->stream) cudaStreamSynchronize(plan->stream);
     if (plan->g_ssp64) cudaGraphExecDestroy(plan->g_ssp64);
     if (plan->g_ssp32) cudaGraphExecDestroy(plan->g_ssp32);
-    if (plan->g_io) cudaGraphExecDestroy(plan->g_io);
     for (void* p : plan->allocs) cudaFree(p);
     if (plan->copy_stream) {
         cudaStreamSynchronize(plan->copy_stream);
@@ -1182,46 +1174,6 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     ++g_launches;
     T* u1 = ws[1];
     T* u2 = ws[2];
-    const bool can_capture_io = plan->stream != nullptr && plan->stream != cudaStreamLegacy;
-    const char* gio = getenv("MOL_IO_GRAPH");
-    if (streamed && nsteps == 1 && hz && can_capture_io && !(gio && gio[0] == '0')) {
-        // The whole one-step call as one graph: about twenty copy, event and launch calls
-        // become one launch (the solver time is set outside it, by k_set_time above).
-        const int prec = std::is_same<T, double>::value ? 64 : 32;
-        if (plan->g_io && (plan->g_io_u != (const void*)u || plan->g_io_p != (const void*)pp || plan->g_io_dt != dt ||
-                           plan->g_io_slabs != slabs || plan->g_io_prec != prec)) {
-            cudaGraphExecDestroy(plan->g_io);
-            plan->g_io = nullptr;
-        }
-        if (!plan->g_io) {
-            if ((st = ensure_copy_stream(plan))) return st;
-            cudaGraph_t graph;
-            if ((st = cuda_check(plan, cudaStreamBeginCapture(plan->stream, cudaStreamCaptureModeThreadLocal),
-                                 "capture io")))
-                return st;
-            const long long before = g_launches.load();
-            int cst = launch_stage1_streamed<T>(plan, u, ud, u1, pp, dt, slabs);
-            if (!cst) cst = launch_ssprk_step_io<T>(plan, ud, hz, u1, u2, pp, dt, true);
-            g_launches = before;
-            cudaError_t ce = cudaStreamEndCapture(plan->stream, &graph);
-            if (cst) {
-                if (ce == cudaSuccess) cudaGraphDestroy(graph);
-                return cst;
-            }
-            if ((st = cuda_check(plan, ce, "end capture io"))) return st;
-            st = cuda_check(plan, cudaGraphInstantiate(&plan->g_io, graph, 0), "instantiate io");
-            cudaGraphDestroy(graph);
-            if (st) return st;
-            plan->g_io_u = (const void*)u;
-            plan->g_io_p = (const void*)pp;
-            plan->g_io_dt = dt;
-            plan->g_io_slabs = slabs;
-            plan->g_io_prec = prec;
-        }
-        if ((st = cuda_check(plan, cudaGraphLaunch(plan->g_io, plan->stream), "graph launch io"))) return st;
-        g_launches += slabs + 2;
-        return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
-    }
     if (streamed) {
         if ((st = launch_stage1_streamed<T>(plan, u, ud, u1, pp, dt, slabs))) return st;
         T* out1 = (nsteps == 1 && hz) ? hz : ud;

@@ -96,13 +96,6 @@ struct mol_plan {
     bool per_last = false;   // the slowest dimension is periodic
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t slab_ev[mol::kMaxSlabs + 1] = {nullptr};
-    // one-step calls on a pinned host state, captured as one graph (copies in, stage-1
-    // windows, stages 2 and 3 writing the host state), keyed by what it bakes in
-    cudaGraphExec_t g_io = nullptr;
-    const void* g_io_u = nullptr;
-    const void* g_io_p = nullptr;
-    double g_io_dt = 0;
-    int g_io_slabs = 0, g_io_prec = 0;
 };
 
 namespace mol {
