@@ -367,18 +367,6 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
     return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
 }
 
-// The side stream and events of the streamed copy.
-static int ensure_copy_stream(mol_plan* plan) {
-    if (plan->copy_stream) return MOL_OK;
-    int st;
-    if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->copy_stream, cudaStreamNonBlocking), "copy stream")))
-        return st;
-    for (int k = 0; k <= kMaxSlabs; ++k)
-        if ((st = cuda_check(plan, cudaEventCreateWithFlags(&plan->slab_ev[k], cudaEventDisableTiming), "slab event")))
-            return st;
-    return MOL_OK;
-}
-
 // Stage 1 of a step whose state is arriving from pinned host memory: the copy runs on a
 // side stream in slabs of whole slices of the slowest interior dimension, and stage 1 of
 // each slab starts as soon as the slabs its stencils reach (`halo` slices either side,
@@ -392,7 +380,13 @@ int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T*
     const long long h = plan->halo;
     const bool per = plan->per_last;
     int st;
-    if ((st = ensure_copy_stream(plan))) return st;
+    if (!plan->copy_stream) {
+        if ((st = cuda_check(plan, cudaStreamCreateWithFlags(&plan->copy_stream, cudaStreamNonBlocking), "copy stream")))
+            return st;
+        for (int k = 0; k <= kMaxSlabs; ++k)
+            if ((st = cuda_check(plan, cudaEventCreateWithFlags(&plan->slab_ev[k], cudaEventDisableTiming), "slab event")))
+                return st;
+    }
     // the copies may only overwrite the staging buffer once earlier work on the stream is done
     if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[kMaxSlabs], plan->stream), "record"))) return st;
     if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->copy_stream, plan->slab_ev[kMaxSlabs], 0), "wait"))) return st;
@@ -441,98 +435,6 @@ int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T*
     // the remaining stages read the whole state: every slab is in once the last event is
     return cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[K - 1], 0), "wait last slab");
 }
-// One SSPRK33 stage over cells [c0, c1) at the explicit step start time tfix (no face pass).
-template <class T>
-static int stage_range(mol_plan* plan, int which, const T* uin, const T* u0, T* uout, const T* p, double dt,
-                       double tfix, long long c0, long long c1) {
-    if (c1 <= c0) return MOL_OK;
-    const DevProb<T>& P = prob<T>(plan);
-    const int thr = plan->use_jit ? plan->nthreads : kThreads;
-    const int blocks = (int)std::min<long long>(plan->nblocks, (c1 - c0 + thr - 1) / thr);
-    ++g_launches;
-    if (plan->use_jit) {
-        const bool is64 = std::is_same<T, double>::value;
-        cudaKernel_t kk = (is64 ? plan->jit.ssp64 : plan->jit.ssp32)[which - 1];
-        return cuda_check(plan, launch_k(kk, blocks, plan->nthreads, plan->stream, P, uin, u0, uout, p, plan->d_state,
-                                         dt, tfix, c0, c1), "stage window");
-    }
-    if (which == 1)
-        k_ssprk_t<T, InterpCell, 1><<<blocks, kThreads, 0, plan->stream>>>(P, uin, u0, uout, p, plan->d_state, dt, tfix,
-                                                                            c0, c1);
-    else if (which == 2)
-        k_ssprk_t<T, InterpCell, 2><<<blocks, kThreads, 0, plan->stream>>>(P, uin, u0, uout, p, plan->d_state, dt, tfix,
-                                                                            c0, c1);
-    else
-        k_ssprk_t<T, InterpCell, 3><<<blocks, kThreads, 0, plan->stream>>>(P, uin, u0, uout, p, plan->d_state, dt, tfix,
-                                                                            c0, c1);
-    return cuda_check(plan, cudaGetLastError(), "stage window");
-}
-
-// A whole one-step call on a pinned host state as a wavefront over slabs of the slowest
-// dimension: slab k lands on the side stream, then stage s runs on the window
-// [b[k] - s*halo, b[k+1] - s*halo) of slices (the windows of each stage tile the line; on a
-// bounded line the first starts at 0 and the last runs to the end).  Stage s of window k
-// reads stage s-1 on windows k-1 and k only, so all three stages of a window follow its
-// slab, and the copy in hides under the step instead of preceding it.  On a periodic line
-// the windows wrap: the last 2*halo slices travel first, and stage 2 of window 0 and
-// stage 3 of windows 0 and 1 (which read through the wrap what the last windows write) run
-// after the last slab.  Stage 3 writes straight into the pinned state (hz).  All stages run
-// at the explicit step start time t0 and leave the solver's time alone.
-template <class T>
-int launch_step_streamed(mol_plan* plan, const T* host, T* ud, T* u1, T* u2, T* hz, const T* p, double dt, double t0,
-                         int K) {
-    const int D = plan->desc.ndim - 1;
-    const long long nsl = plan->desc.npts[D] - plan->desc.lower[D] - plan->desc.upper[D];
-    const long long S = plan->ncell / nsl;
-    const long long h = plan->halo;
-    const bool per = plan->per_last;
-    int st;
-    if ((st = ensure_copy_stream(plan))) return st;
-    if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[kMaxSlabs], plan->stream), "record"))) return st;
-    if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->copy_stream, plan->slab_ev[kMaxSlabs], 0), "wait"))) return st;
-    const size_t pitch = sizeof(T) * (size_t)plan->ncell;
-    auto copy = [&](long long s0, long long s1) -> int {
-        if (s1 <= s0) return MOL_OK;
-        cudaError_t e = cudaMemcpy2DAsync(ud + s0 * S, pitch, host + s0 * S, pitch, sizeof(T) * (size_t)((s1 - s0) * S),
-                                          (size_t)plan->nfields, cudaMemcpyHostToDevice, plan->copy_stream);
-        return e == cudaSuccess ? MOL_OK : cuda_check(plan, e, "H2D slab");
-    };
-    std::vector<long long> b(K + 1);
-    for (int k = 0; k <= K; ++k) b[k] = nsl * k / K;
-    auto run = [&](int s, int k) -> int {
-        const T* in = s == 1 ? ud : (s == 2 ? u1 : u2);
-        T* out = s == 1 ? u1 : (s == 2 ? u2 : hz);
-        long long w0 = b[k] - s * h, w1 = b[k + 1] - s * h;
-        if (!per) {
-            if (k == 0) w0 = 0;
-            if (k == K - 1) w1 = nsl;
-            return stage_range<T>(plan, s, in, ud, out, p, dt, t0, w0 * S, w1 * S);
-        }
-        if (w0 < 0) {  // the wrapped part at the top of the line
-            if ((st = stage_range<T>(plan, s, in, ud, out, p, dt, t0, (w0 + nsl) * S, nsl * S))) return st;
-            w0 = 0;
-        }
-        return stage_range<T>(plan, s, in, ud, out, p, dt, t0, w0 * S, w1 * S);
-    };
-    const long long tail = per ? std::min(2 * h, nsl) : 0;
-    if ((st = copy(nsl - tail, nsl))) return st;
-    for (int k = 0; k < K; ++k) {
-        const long long s1 = std::min(b[k + 1], nsl - tail);
-        if ((st = copy(std::min(b[k], s1), s1))) return st;
-        if ((st = cuda_check(plan, cudaEventRecord(plan->slab_ev[k], plan->copy_stream), "record"))) return st;
-        if ((st = cuda_check(plan, cudaStreamWaitEvent(plan->stream, plan->slab_ev[k], 0), "wait slab"))) return st;
-        if ((st = run(1, k))) return st;
-        if ((!per || k >= 1) && (st = run(2, k))) return st;
-        if ((!per || k >= 2) && (st = run(3, k))) return st;
-    }
-    if (per) {
-        if ((st = run(2, 0))) return st;
-        if ((st = run(3, 0))) return st;
-        if ((st = run(3, 1))) return st;
-    }
-    return MOL_OK;
-}
-
 template int launch_ssprk_step_io<double>(mol_plan*, const double*, double*, double*, double*, const double*, double,
                                           bool);
 template int launch_ssprk_step_io<float>(mol_plan*, const float*, float*, float*, float*, const float*, double, bool);
@@ -1143,9 +1045,6 @@ int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member
         const long long nsl = d->npts[D] - d->lower[D] - d->upper[D];
         const long long k = std::min<long long>(kMaxSlabs, nsl / (2 * plan->halo + 1));
         plan->h2d_slabs = (plan->ncell >= (1ll << 16) && k >= 2) ? (int)k : 0;
-        // the whole-step wavefront shifts each stage's windows by another halo
-        const long long kw = std::min<long long>(kMaxSlabs, nsl / (4 * plan->halo + 1));
-        plan->wave_slabs = (plan->h2d_slabs && kw >= 2) ? (int)kw : 0;
     }
     *out = plan;
     return MOL_OK;
@@ -1275,14 +1174,6 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     ++g_launches;
     T* u1 = ws[1];
     T* u2 = ws[2];
-    const char* wf = getenv("MOL_STEP_WAVEFRONT");
-    if (streamed && nsteps == 1 && hz && plan->wave_slabs >= 2 && !(wf && wf[0] == '0')) {
-        const int K = std::min(slabs, plan->wave_slabs);
-        if (K >= 2) {
-            if ((st = launch_step_streamed<T>(plan, u, ud, u1, u2, hz, pp, dt, t0, K))) return st;
-            return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
-        }
-    }
     if (streamed) {
         if ((st = launch_stage1_streamed<T>(plan, u, ud, u1, pp, dt, slabs))) return st;
         T* out1 = (nsteps == 1 && hz) ? hz : ud;

@@ -92,7 +92,6 @@ struct mol_plan {
     // host-to-device copy of a pinned state in slabs of the slowest dimension, overlapped
     // with stage 1 (h2d_slabs < 2: one copy before the step)
     int h2d_slabs = 0;
-    int wave_slabs = 0;      // slabs of the one-step wavefront (all three stages behind the copy)
     long long halo = 0;      // slices a stencil reaches along the slowest dimension
     bool per_last = false;   // the slowest dimension is periodic
     cudaStream_t copy_stream = nullptr;

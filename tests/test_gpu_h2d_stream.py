@@ -1,8 +1,7 @@
 """The first step of a call on a pinned host state streams the host-to-device copy in slabs
-of the slowest dimension and runs stage 1 (several steps) or all three stages (one step,
-a wavefront of windows) behind it: the result equals stepping a device copy of the state
-bit for bit (periodic, bounded and 3-D slowest dimensions, one and several steps, generated
-code and interpreter)."""
+of the slowest dimension and runs stage 1 slab by slab behind it: the result equals stepping
+a device copy of the state bit for bit (periodic, bounded and 3-D slowest dimensions, one
+and several steps, generated code and interpreter)."""
 import numpy as np
 import pytest
 
@@ -39,11 +38,10 @@ def test_streamed_first_step_bit_identical(gpu_lib, monkeypatch, name, nsteps, c
     plan.step_ssprk33(dev, dt, nsteps, t0=0.2)
     torch.cuda.synchronize()   # the plan's own stream does not order with torch's
     assert np.array_equal(h, dev.cpu().numpy()), name
-    for var in ("MOL_STEP_WAVEFRONT", "MOL_H2D_SLABS"):  # stage 1 only behind the copy; no slabs at all
-        monkeypatch.setenv(var, "0")
-        pinned.copy_(torch.from_numpy(lw.u0))
-        plan.step_ssprk33(h, dt, nsteps, t0=0.2)
-        assert np.array_equal(h, dev.cpu().numpy()), (name, var)
+    monkeypatch.setenv("MOL_H2D_SLABS", "0")
+    pinned.copy_(torch.from_numpy(lw.u0))
+    plan.step_ssprk33(h, dt, nsteps, t0=0.2)
+    assert np.array_equal(h, dev.cpu().numpy()), name
     plan.close()
 
 
