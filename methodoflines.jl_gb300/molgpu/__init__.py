@@ -6,14 +6,14 @@ in ``libmolgpu.so`` on the GPU.
 """
 from . import _lib
 from .api import (Batch, MOLFiniteDifference, ODEFunction, ODEProblem, Plan, Solution, SSPRK33, Tsit5, UpwindScheme,
-                  WENOScheme, center_align, discretize, edge_align, solve)
+                  WENOScheme, center_align, chebyspace, discretize, edge_align, solve)
 from .lowering import Descriptor, Lowered, lower
 from .symbolic import (Differential, Eq, Equation, Field, Interval, IV, Param, PDESystem, abs_, atan, cos, cosh,
                        exp, ifelse, log, register, sin, sinh, sqrt, tan, tanh)
 
 __all__ = [
     "Batch", "MOLFiniteDifference", "ODEFunction", "ODEProblem", "Plan", "Solution", "SSPRK33", "Tsit5", "UpwindScheme",
-    "WENOScheme", "center_align", "discretize", "edge_align", "solve", "Descriptor", "Lowered", "lower", "Differential", "Eq", "Equation",
+    "WENOScheme", "center_align", "chebyspace", "discretize", "edge_align", "solve", "Descriptor", "Lowered", "lower", "Differential", "Eq", "Equation",
     "Field", "Interval", "IV", "Param", "PDESystem", "abs_", "atan", "cos", "cosh", "exp", "ifelse", "log",
     "register", "sin", "sinh", "sqrt", "tan", "tanh",
 ]

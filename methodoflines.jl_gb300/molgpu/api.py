@@ -43,6 +43,30 @@ class WENOScheme:
         return ("weno", self.epsilon)
 
 
+def _cospi(z: float) -> float:
+    """cos(pi z), the argument reduced in z first (exact for the rationals chebyspace uses up to
+    the last bit of the final cos/sin)."""
+    r = math.fmod(abs(z), 2.0)
+    if r > 1.0:
+        r = 2.0 - r
+    if r <= 0.25:
+        return math.cos(math.pi * r)
+    if r <= 0.75:
+        return math.sin(math.pi * (0.5 - r))
+    return -math.cos(math.pi * (1.0 - r))
+
+
+def chebyspace(n: int, dom):
+    """``chebyspace(N, dom)`` (src/MOL_utils.jl:112-123): N Chebyshev points of the first kind
+    on the interval of ``dom = (x, Interval(a, b))`` in increasing order, the end points set
+    to a and b; returns ``(x, points)`` for MOLFiniteDifference's dxs."""
+    x, interval = dom
+    a, b = float(interval.lo), float(interval.hi)
+    pts = [(a + b) / 2 + (b - a) / 2 * _cospi((2 * k - 1) / (2 * n)) for k in range(1, n + 1)][::-1]
+    pts[0], pts[-1] = a, b
+    return x, np.array(pts)
+
+
 center_align = "center"   # CenterAlignedGrid: the grid points are lo:dx:hi
 edge_align = "edge"       # EdgeAlignedGrid: cell centres plus a ghost point beyond each end
 

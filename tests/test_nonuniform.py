@@ -341,3 +341,27 @@ def test_descriptor_semantics_match_oracle_burgers_nonuniform_upwind():
     u = lw.u0 + 0.01 * np.random.default_rng(0).standard_normal(lw.n_unknowns)
     a, b = orc.rhs(u, 0.3), DescInterp(lw).rhs(u, 0.3)
     assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a)
+
+
+def test_chebyspace_grid():
+    """chebyspace(N, x in [a, b]) (MOL_utils.jl:112-123): increasing Chebyshev points of the
+    first kind with the end points set; the docs' example (100 points, Dirichlet heat) lowers
+    to a nonuniform grid and matches the oracle."""
+    from molgpu import IV, Interval, MOLFiniteDifference, chebyspace
+    from molgpu.symbolic import Differential, Eq, Field, PDESystem, cos, exp
+    x, t = IV("x"), IV("t")
+    xv, pts = chebyspace(100, (x, Interval(0.0, 1.0)))
+    assert xv is x and len(pts) == 100 and pts[0] == 0.0 and pts[-1] == 1.0
+    assert np.all(np.diff(pts) > 0)
+    k = np.arange(1, 101)
+    assert np.allclose(pts[1:-1], (0.5 + 0.5 * np.cos(np.pi * (2 * k - 1) / 200))[::-1][1:-1], atol=1e-15)
+    u = Field("u")
+    s = PDESystem([Eq(Differential(t)(u(x, t)), (Differential(x) ** 2)(u(x, t)))],
+                  [Eq(u(x, 0.0), cos(x)), Eq(u(0.0, t), exp(-1.0 * t)), Eq(u(1.0, t), exp(-1.0 * t) * math.cos(1.0))],
+                  [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)])
+    spec = s.to_spec(MOLFiniteDifference(dict([chebyspace(100, (x, Interval(0.0, 1.0)))]), t))
+    lw = lower(spec)
+    assert not lw.uniform[0] and lw.npts == [100]
+    v = lw.u0 * 1.01
+    a, b = OracleProblem(spec).rhs(v, 0.2), DescInterp(lw).rhs(v, 0.2)
+    assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a)
