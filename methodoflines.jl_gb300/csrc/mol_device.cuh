@@ -213,6 +213,10 @@ __device__ T run_bc_prog(const DevProb<T>& P, int prog, int out_index, const int
             case MOL_OP_PARAM: r[dst] = p[in.imm]; break;
             case MOL_OP_COORD: r[dst] = P.coords[in.imm][I[in.imm] - 1]; break;
             case MOL_OP_TIME: r[dst] = t; break;
+            case MOL_OP_AUX:  // a full-grid array (host-evaluated registered function) at the point
+                r[dst] = P.aux[P.aux_off[in.imm] + (long long)(I[0] - 1) +
+                               (long long)P.n[0] * ((long long)(I[1] - 1) + (long long)P.n[1] * (I[2] - 1))];
+                break;
             case MOL_OP_ADD: r[dst] = r[in.a & 15] + r[in.b & 15]; break;
             case MOL_OP_SUB: r[dst] = r[in.a & 15] - r[in.b & 15]; break;
             case MOL_OP_MUL: r[dst] = r[in.a & 15] * r[in.b & 15]; break;

@@ -499,11 +499,13 @@ static int validate_prog(mol_plan* plan, const mol_problem_desc* d, int prog, in
                 if (in.imm < 0 || in.imm >= d->nfields) return set_err(plan, MOL_ERR_INVALID, "field index");
                 break;
             case MOL_OP_AUX: {
-                if (kind == 2) return set_err(plan, MOL_ERR_INVALID, "AUX in a boundary program");
                 const int ax = kind == 1 ? term->aux0 + in.imm : in.imm;
                 if (ax < 0 || ax >= d->naux) return set_err(plan, MOL_ERR_INVALID, "aux index");
                 long long need = aux_need_cell;
-                if (kind == 1) {
+                if (kind == 2) {  // boundary programs read full-grid arrays at the boundary point
+                    need = 1;
+                    for (int q = 0; q < d->ndim; ++q) need *= d->npts[q];
+                } else if (kind == 1) {
                     need = 1;
                     for (int q = 0; q < 3; ++q)
                         need *= (q < d->ndim ? d->npts[q] : 1) + (q == term->dim ? 1 : 0);

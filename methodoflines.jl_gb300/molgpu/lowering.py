@@ -671,6 +671,30 @@ class _Lowerer:
             lw.aux.append(np.ascontiguousarray(arr.reshape(-1, order="F")))
         return ("aux", lw.aux_keys[key])
 
+    def _hoist_bc_calls(self, t, j, side):
+        """Registered functions of coordinates in a boundary row (docs: boundary_conditions.md,
+        "Registered User Defined Function") are evaluated on the host at every point of the
+        boundary face (its own coordinate fixed at the domain's end, the others the grid's)
+        into a full-grid array the row's program reads at its boundary point."""
+        if not isinstance(t, tuple) or not t:
+            return t
+        if t[0] == "call" and _leaves(t) <= {"num", "iv"}:
+            lw = self.lw
+            key = ("bc", j, side, t)
+            if key not in lw.aux_keys:
+                grids = np.meshgrid(*lw.grids, indexing="ij")
+                coords = {x: g for x, g in zip(lw.ivs, grids)}
+                v = host_eval(t, coords, lw.functions)
+                arr = np.broadcast_to(np.asarray(v, dtype=np.float64), tuple(lw.npts))
+                lw.aux_keys[key] = len(lw.aux)
+                lw.aux.append(np.ascontiguousarray(arr.reshape(-1, order="F")))
+            return ("aux", lw.aux_keys[key])
+        if t[0] in ("fn", "call"):
+            return t[:2] + tuple(self._hoist_bc_calls(a, j, side) for a in t[2:])
+        if t[0] == "cmp":
+            return t[:2] + tuple(self._hoist_bc_calls(a, j, side) for a in t[2:])
+        return (t[0],) + tuple(self._hoist_bc_calls(a, j, side) if isinstance(a, tuple) else a for a in t[1:])
+
     def hoist_face(self, t, j, f):
         """Hoist coordinate-only parts of a nonlinear-Laplacian coefficient into face arrays.
 
@@ -807,7 +831,7 @@ class _Lowerer:
         for (f, j, side), b in self.bcs.items():
             # the row's own coordinate is the domain's end (axiesvals, discretize_vars.jl:321-330)
             xe = ("num", float(self.spec["domain"][lw.ivs[j]][0 if side == "lo" else 1]))
-            a, bb, g = (_subst_iv(b[k], lw.ivs[j], xe) for k in ("a", "b", "g"))
+            a, bb, g = (self._hoist_bc_calls(_subst_iv(b[k], lw.ivs[j], xe), j, side) for k in ("a", "b", "g"))
             if self.edge:
                 # the face half-way between the ghost point and the first (last) unknown:
                 # a * interpolation + b * half-offset derivative (generate_bc_eqs.jl:80-160)

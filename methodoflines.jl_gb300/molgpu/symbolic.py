@@ -298,7 +298,8 @@ class PDESystem:
                         b[key] = _time_leaf(b[key], tname)
         params = [(p.name, p.default) for p in self.ps]
         funcs = {}
-        for tree in list(eqs.values()) + list(ics.values()):
+        bc_trees = [b[k] for b in uniq for k in ("a", "b", "g") if isinstance(b.get(k), tuple)]
+        for tree in list(eqs.values()) + list(ics.values()) + bc_trees:
             for n in walk(tree):
                 if isinstance(n, tuple) and n and n[0] == "call":
                     funcs[n[1]] = _REGISTRY[n[1]]

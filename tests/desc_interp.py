@@ -195,6 +195,8 @@ class DescInterp:
                     e1 = self.n[1] + (d == 1)
                     j = [Ih if q == d else I[q] - 1 for q in range(3)]
                     r[dst] = self.lw.aux[tm["aux0"] + imm][j[0] + e0 * (j[1] + e1 * j[2])]
+                elif kind == "bc":   # full-grid array, read at the boundary point
+                    r[dst] = self.lw.aux[imm][(I[0] - 1) + self.n[0] * ((I[1] - 1) + self.n[1] * (I[2] - 1))]
                 else:
                     r[dst] = self.lw.aux[imm][c]
             elif op == L.OP_COORD:

@@ -90,3 +90,22 @@ def test_boundary_rows_adjoint_matches_finite_differences(gpu_lib, name):
     fd = (loss(lw.u0 + h * w) - loss(lw.u0 - h * w)) / (2 * h)
     assert abs(g @ w - fd) <= 1e-6 * abs(fd), (g @ w, fd)
     plan.close()
+
+
+def test_registered_function_in_a_boundary_row_gpu(gpu_lib):
+    """A registered function of coordinates in a Dirichlet row (the boundary-condition docs'
+    example), host-evaluated on the boundary face and read by the row's program."""
+    from test_lowering import _registered_bc_problem
+    spec = _registered_bc_problem()
+    lw = lower(spec)
+    orc = OracleProblem(spec)
+    plan = Plan(lw)
+    v = lw.u0 + 0.05 * np.random.default_rng(4).standard_normal(lw.n_unknowns)
+    for t in (0.0, 0.37):
+        du = np.zeros(lw.n_unknowns)
+        plan.rhs(du, v, None, t)
+        ref = orc.rhs(v, t)
+        assert np.linalg.norm(du - ref) <= 1e-12 * np.linalg.norm(ref), t
+    full = plan.fill_grid(v, 0.37)[0]
+    assert np.allclose(full, orc.solution_arrays(v, 0.37, lw.param_values)["u"], rtol=1e-12, atol=1e-13)
+    plan.close()

@@ -178,3 +178,39 @@ def test_generated_code_compiles_for_sm103a(name, kw):
     log = C.create_string_buffer(1 << 16)
     st = L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16)
     assert st == 0, log.value.decode()
+
+
+def _registered_bc_problem():
+    """The boundary-condition docs' example: u(t, x, y_min) ~ f(t, x, y_min) + alpha / g(x, y_min)
+    with f a plain function (traced) and g registered (a conditional on sin(x y) + cos(y))."""
+    import math as _m
+    from molgpu.api import MOLFiniteDifference
+    from molgpu.symbolic import Differential, Eq, Field, Interval, IV, PDESystem, register
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u = Field("u")
+
+    def g_host(xx, yy):
+        z = np.sin(xx * yy) + np.cos(yy)
+        return np.where(z > 0, xx, 1.0)
+    g = register("g_bc_doc", g_host)
+    alpha = 9.0
+
+    def f(tt, xx, yy):
+        return xx * yy - tt
+    Dt, Dxx, Dyy = Differential(t), Differential(x) ** 2, Differential(y) ** 2
+    s = PDESystem([Eq(Dt(u(x, y, t)), Dxx(u(x, y, t)) + Dyy(u(x, y, t)))],
+                  [Eq(u(x, y, 0.0), 1.0 + 0.1 * x * y), Eq(u(x, 0.0, t), f(t, x, 0.0) + alpha / g(x, 0.0)),
+                   Eq(u(x, 1.0, t), 2.0), Eq(u(0.0, y, t), 1.0), Eq(u(1.0, y, t), 1.0 + t)],
+                  [(t, Interval(0, 1)), (x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0))], [t, x, y], [u(x, y, t)])
+    return s.to_spec(MOLFiniteDifference({x: 0.1, y: 0.125}, t))
+
+
+def test_registered_function_in_a_boundary_row():
+    spec = _registered_bc_problem()
+    lw = lower(spec)
+    orc = OracleProblem(spec)
+    assert any(a.size == int(np.prod(lw.npts)) for a in lw.aux)    # host-evaluated on the face
+    u = lw.u0 + 0.01 * np.random.default_rng(0).standard_normal(lw.n_unknowns)
+    for t in (0.0, 0.6):
+        a, b = orc.rhs(u, t), DescInterp(lw).rhs(u, t)
+        assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a), t
