@@ -93,17 +93,41 @@ class MOLFiniteDifference:
         self.kwargs = kwargs
 
 
-def _ptr(a):
-    """(pointer, is_float32) of a numpy array or a CUDA tensor-like object."""
+def _ptr(a, n=None, name="array", f32=None, out=False):
+    """(pointer, is_float32) of a numpy array or a CUDA tensor-like object.
+
+    The library trusts the pointers it is given and reads or writes exactly the element
+    counts its entry points document, so each argument is checked here first: float64 or
+    float32 (``f32`` fixes which when given: the state's precision), contiguous, writable when
+    ``out``, and exactly ``n`` elements when ``n`` is given and not 0."""
     if a is None:
         return None, None
     if hasattr(a, "data_ptr"):
         dt = str(getattr(a, "dtype", ""))
-        return C.c_void_p(a.data_ptr()), ("float32" in dt)
-    arr = a
-    if not (arr.flags["C_CONTIGUOUS"]):
-        raise ValueError("arrays must be contiguous")
-    return C.c_void_p(arr.ctypes.data), arr.dtype == np.float32
+        is32 = dt.endswith("float32")
+        if not (is32 or dt.endswith("float64")):
+            raise TypeError(f"{name}: float64 or float32 elements expected, got {dt or type(a).__name__}")
+        if hasattr(a, "is_contiguous") and not a.is_contiguous():
+            raise ValueError(f"{name}: the array must be contiguous")
+        size = int(a.numel()) if hasattr(a, "numel") else None
+        ptr = C.c_void_p(a.data_ptr())
+    else:
+        if not isinstance(a, np.ndarray):
+            raise TypeError(f"{name}: a numpy array or a CUDA tensor expected, got {type(a).__name__}")
+        if a.dtype not in (np.float64, np.float32):
+            raise TypeError(f"{name}: float64 or float32 elements expected, got {a.dtype}")
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"{name}: the array must be contiguous")
+        if out and not a.flags["WRITEABLE"]:
+            raise ValueError(f"{name}: the array is written and must be writable")
+        is32 = a.dtype == np.float32
+        size = int(a.size)
+        ptr = C.c_void_p(a.ctypes.data)
+    if f32 is not None and bool(is32) != bool(f32):
+        raise TypeError(f"{name}: {'float32' if f32 else 'float64'} elements expected, as the state has")
+    if n and size is not None and size != n:          # n == 0: the pointer is not read
+        raise ValueError(f"{name}: {n} elements expected, got {size}")
+    return ptr, bool(is32)
 
 
 class Plan:
@@ -122,6 +146,8 @@ class Plan:
             self._h = None
             raise L.MolError(st, msg)
         self.n = int(L.lib().mol_plan_n_unknowns(h))
+        self.nparams = len(lowered.param_values)
+        self.naux = int(sum(a.size for a in lowered.aux))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -143,9 +169,9 @@ class Plan:
 
     def rhs(self, du, u, p=None, t: float = 0.0):
         """f!(du, u, p, t)."""
-        pd, f32 = _ptr(du)
-        pu, _ = _ptr(u)
-        pp, _ = _ptr(p)
+        pd, f32 = _ptr(du, self.n, "du", out=True)
+        pu, _ = _ptr(u, self.n, "u", f32)
+        pp, _ = _ptr(p, self.nparams, "p", f32)
         fn = L.lib().mol_rhs_f32state if f32 else L.lib().mol_rhs
         L.check(fn(self._h, pd, pu, pp, float(t)), self._h)
         return du
@@ -159,9 +185,9 @@ class Plan:
         per = int(np.prod(lw.npts))
         host_out = out is None or not hasattr(out, "data_ptr")
         buf = np.empty(len(lw.fields) * per) if out is None else out
-        pu, _ = _ptr(u)
-        pp, _ = _ptr(p)
-        po, _ = _ptr(buf)
+        pu, _ = _ptr(u, self.n, "u", False)
+        pp, _ = _ptr(p, self.nparams, "p", False)
+        po, _ = _ptr(buf, len(lw.fields) * per, "out", False, out=True)
         L.check(L.lib().mol_fill_grid(self._h, pu, pp, float(t), po), self._h)
         if not host_out:
             return buf
@@ -169,22 +195,23 @@ class Plan:
                          for k in range(len(lw.fields))])
 
     def step_ssprk33(self, u, dt: float, nsteps: int, t0: float = 0.0, p=None):
-        pu, f32 = _ptr(u)
-        pp, _ = _ptr(p)
+        pu, f32 = _ptr(u, self.n, "u", out=True)
+        pp, _ = _ptr(p, self.nparams, "p", f32)
         fn = L.lib().mol_step_ssprk33_f32state if f32 else L.lib().mol_step_ssprk33
         L.check(fn(self._h, pu, pp, float(t0), float(dt), int(nsteps)), self._h)
         return u
 
     def step_ssprk33_noalloc(self, u, dt: float, nsteps: int, t0: float = 0.0, p=None):
         """SSPRK33 steps that allocate nothing (device arrays only, at most 2^20 unknowns)."""
-        L.check(L.lib().mol_step_ssprk33_noalloc(self._h, _ptr(u)[0], _ptr(p)[0], float(t0), float(dt), int(nsteps)),
-                self._h)
+        pu, _ = _ptr(u, self.n, "u", False, out=True)
+        pp, _ = _ptr(p, self.nparams, "p", False)
+        L.check(L.lib().mol_step_ssprk33_noalloc(self._h, pu, pp, float(t0), float(dt), int(nsteps)), self._h)
         return u
 
     def solve_tsit5(self, u, t0: float, t1: float, abstol: float, reltol: float, p=None, dt0: float = 0.0,
                     maxiters: int = 0):
-        pu, _ = _ptr(u)
-        pp, _ = _ptr(p)
+        pu, _ = _ptr(u, self.n, "u", False, out=True)
+        pp, _ = _ptr(p, self.nparams, "p", False)
         stats = L.mol_stats()
         L.check(L.lib().mol_solve_tsit5(self._h, pu, pp, float(t0), float(t1), float(abstol), float(reltol),
                                         float(dt0), int(maxiters), C.byref(stats)), self._h)
@@ -205,17 +232,23 @@ class Plan:
         return (L.lib().mol_plan_codegen_source(self._h) or b"").decode()
 
     def vjp(self, lam, u, p=None, t: float = 0.0, lam_u=None, lam_p=None, lam_aux=None):
-        L.check(L.lib().mol_rhs_vjp(self._h, _ptr(lam)[0], _ptr(u)[0], _ptr(p)[0], float(t), _ptr(lam_u)[0],
-                                    _ptr(lam_p)[0], _ptr(lam_aux)[0]), self._h)
+        n, npar, naux = self.n, self.nparams, self.naux
+        L.check(L.lib().mol_rhs_vjp(self._h, _ptr(lam, n, "lam", False)[0], _ptr(u, n, "u", False)[0],
+                                    _ptr(p, npar, "p", False)[0], float(t), _ptr(lam_u, n, "lam_u", False, True)[0],
+                                    _ptr(lam_p, npar, "lam_p", False, True)[0],
+                                    _ptr(lam_aux, naux, "lam_aux", False, True)[0]), self._h)
 
     def adjoint_ssprk33(self, u0, dt: float, nsteps: int, target, t0: float = 0.0, p=None, nsnap: int = 64,
                         loss_kind: int = L.LOSS_MISFIT, uT=None, dLdu0=None, dLdp=None, dLdaux=None):
         loss = np.zeros(1)
         nfw = C.c_int64(0)
-        L.check(L.lib().mol_adjoint_ssprk33(self._h, _ptr(u0)[0], _ptr(p)[0], float(t0), float(dt), int(nsteps),
-                                            int(nsnap), int(loss_kind), _ptr(target)[0], _ptr(uT)[0],
-                                            _ptr(loss)[0], _ptr(dLdu0)[0], _ptr(dLdp)[0], _ptr(dLdaux)[0],
-                                            C.byref(nfw)), self._h)
+        n, npar, naux = self.n, self.nparams, self.naux
+        L.check(L.lib().mol_adjoint_ssprk33(self._h, _ptr(u0, n, "u0", False)[0], _ptr(p, npar, "p", False)[0],
+                                            float(t0), float(dt), int(nsteps), int(nsnap), int(loss_kind),
+                                            _ptr(target, n, "target", False)[0], _ptr(uT, n, "uT", False, True)[0],
+                                            _ptr(loss)[0], _ptr(dLdu0, n, "dLdu0", False, True)[0],
+                                            _ptr(dLdp, npar, "dLdp", False, True)[0],
+                                            _ptr(dLdaux, naux, "dLdaux", False, True)[0], C.byref(nfw)), self._h)
         return float(loss[0]), int(nfw.value)
 
     @property
@@ -268,8 +301,10 @@ class Batch:
         return np.concatenate([np.asarray(p, dtype=np.float64) for p in parts])
 
     def step_ssprk33(self, u, dts, nsteps: int, t0: float = 0.0):
-        pu, f32 = _ptr(u)
+        pu, f32 = _ptr(u, int(self.offsets[-1]), "u", out=True)
         d = np.ascontiguousarray(dts, dtype=np.float64)
+        if d.shape != (self.n,):
+            raise ValueError(f"dts: one step per instance expected ({self.n}), got shape {d.shape}")
         fn = L.lib().mol_batch_step_ssprk33_f32state if f32 else L.lib().mol_batch_step_ssprk33
         L.check(fn(self._h, pu, C.c_void_p(d.ctypes.data), float(t0), int(nsteps)), batch=self._h)
         return u
