@@ -273,7 +273,8 @@ int mol_step_ssprk33_f32state(mol_plan* plan, float* u, const float* p, double t
 int mol_step_ssprk33_noalloc(mol_plan* plan, double* u, const double* p, double t0, double dt, int64_t nsteps);
 
 /* solve(prob, Tsit5(); abstol, reltol) from t0 to t1, in place on u
- * (test/Burgers/burgers_eq.jl:39).  dt0 <= 0 selects the initial step automatically. */
+ * (test/Burgers/burgers_eq.jl:39).  dt0 <= 0 selects the initial step automatically;
+ * maxiters <= 0 allows 10^8 steps.  Non-finite times, tolerances or dt0 give MOL_ERR_INVALID. */
 int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, double t1,
                     double abstol, double reltol, double dt0, int64_t maxiters, mol_stats* stats);
 

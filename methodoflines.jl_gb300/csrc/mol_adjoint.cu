@@ -427,7 +427,8 @@ int mol_rhs_vjp(mol_plan* plan, const double* lambda, const double* u, const dou
 int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, double t0, double dt, int64_t nsteps,
                         int32_t nsnap, int32_t loss_kind, const double* target, double* uT, double* loss,
                         double* dLdu0, double* dLdp, double* dLdaux, int64_t* nforward_steps) {
-    if (!plan || !u0 || !target || nsteps < 0 || !(dt > 0) || (loss_kind != MOL_LOSS_MISFIT && loss_kind != MOL_LOSS_LAMBDA))
+    if (!plan || !u0 || !target || nsteps < 0 || !(dt > 0) || !std::isfinite(dt) || !std::isfinite(t0) ||
+        (loss_kind != MOL_LOSS_MISFIT && loss_kind != MOL_LOSS_LAMBDA))
         return MOL_ERR_INVALID;
     int st = need_vjp(plan);
     if (st) return st;

@@ -1113,7 +1113,7 @@ struct DeviceGuard {
 
 template <class T>
 int rhs_impl(mol_plan* plan, T* du, const T* u, const T* p, double t) {
-    if (!plan || !du || !u) return MOL_ERR_INVALID;
+    if (!plan || !du || !u || !std::isfinite(t)) return MOL_ERR_INVALID;
     DeviceGuard g(plan->dev);
     int st;
     // slots 10 and 11 stage host buffers for f!
@@ -1291,7 +1291,9 @@ int mol_step_ssprk33_f32state(mol_plan* plan, float* u, const float* p, double t
 
 int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, double t1, double abstol, double reltol,
                     double dt0, int64_t maxiters, mol_stats* stats) {
-    if (!plan || !u || !(t1 >= t0) || !(abstol > 0) || !(reltol >= 0)) return MOL_ERR_INVALID;
+    if (!plan || !u || !std::isfinite(t0) || !std::isfinite(t1) || !(t1 >= t0) || !(abstol > 0) ||
+        !std::isfinite(abstol) || !(reltol >= 0) || !std::isfinite(reltol) || !std::isfinite(dt0))
+        return MOL_ERR_INVALID;
     DeviceGuard g(plan->dev);
     int st;
     // slots: 0 u, 1..7 k1..k7, 8 ybuf0, 9 ybuf1
