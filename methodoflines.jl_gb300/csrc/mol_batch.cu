@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -270,7 +271,7 @@ int tune(mol_batch* b, T* U, long long probe_steps) {
 
 template <class T>
 int step_impl(mol_batch* b, T* u, const double* dts, double t0, int64_t nsteps) {
-    if (!b || !u || !dts || nsteps < 0) return MOL_ERR_INVALID;
+    if (!b || !u || !dts || nsteps < 0 || !std::isfinite(t0)) return MOL_ERR_INVALID;
     int st;
     const bool is64 = std::is_same<T, double>::value;
     if ((st = jit_ensure(&b->jit, JIT_BATCH, b->err))) return berr(b, st, b->err);
