@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import warnings
 from dataclasses import dataclass
 from typing import Optional
 
@@ -84,11 +85,16 @@ class MOLFiniteDifference:
         self.dxs = {(k.name if isinstance(k, IV) else k): v for k, v in dict(dxs).items()}
         self.time = time
         self.approx_order = int(approx_order)
+        if self.approx_order % 2 != 0:
+            # MOLFiniteDifference.jl:56-58: a warning only; the odd order is kept and the
+            # tables are built for it
+            warnings.warn(f"Discretization approx_order must be even, rounding up to {self.approx_order + 1}")
+        if self.approx_order < 1:
+            raise ValueError("approx_order must be at least 1")
         self.advection_scheme = advection_scheme if advection_scheme is not None else UpwindScheme()
         self.grid_align = {"center_align": "center", "edge_align": "edge"}.get(grid_align, grid_align)
         if kwargs.get("upwind_order") is not None:
             # MOLFiniteDifference.jl:53-55: the keyword is accepted and has no effect
-            import warnings
             warnings.warn("`upwind_order` no longer does anything; use advection_scheme=UpwindScheme(order)")
         self.kwargs = kwargs
 

@@ -92,6 +92,9 @@ class Operator:
 
 
 def centered(d: int, p: int, dx: float) -> Operator:
+    """``CompleteCenteredDifference(d, p, dx)`` (centered_difference/centered_diff_weights.jl:4-75)."""
+    if p <= 1:
+        raise ValueError("approximation_order must be greater than 1.")    # centered_diff_weights.jl:8
     L = d + p - 1 + (d + p) % 2
     bl = d + p
     h = L // 2

@@ -214,3 +214,42 @@ def test_registered_function_in_a_boundary_row():
     for t in (0.0, 0.6):
         a, b = orc.rhs(u, t), DescInterp(lw).rhs(u, t)
         assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a), t
+
+
+def _third_derivative_problem(order):
+    import math
+    from molgpu.api import MOLFiniteDifference
+    from molgpu.symbolic import Differential, Eq, Field, Interval, IV, PDESystem, sin
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx = Differential(t), Differential(x)
+    s = PDESystem([Eq(Dt(u(x, t)), (Dx ** 2)(u(x, t)) + 0.3 * (Dx ** 3)(u(x, t)))],
+                  [Eq(u(x, 0.0), sin(math.pi * x)), Eq(u(0.0, t), 0.0), Eq(Dx(u(1.0, t)), 0.0)],
+                  [(t, Interval(0, 1)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)])
+    return s.to_spec(MOLFiniteDifference({x: 21}, t, approx_order=order))
+
+
+@pytest.mark.parametrize("order", [3, 5, 7])
+def test_odd_approx_order_warns_and_builds_its_tables(order):
+    """An odd approx_order draws the reference's warning and is kept as given
+    (MOLFiniteDifference.jl:56-58): the tables of that order, equal to the oracle's."""
+    with pytest.warns(UserWarning, match="must be even"):
+        spec = _third_derivative_problem(order)
+    assert spec["disc"]["approx_order"] == order
+    lw = lower(spec)
+    orc = OracleProblem(spec)
+    v = lw.u0 + 0.01 * np.random.default_rng(1).standard_normal(lw.n_unknowns)
+    a, b = orc.rhs(v, 0.2), DescInterp(lw).rhs(v, 0.2)
+    assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a)
+
+
+def test_approx_order_one_is_refused():
+    """approx_order = 1 passes the constructor's bound (>= 1) with the odd-order warning, and
+    the centered tables refuse it (centered_diff_weights.jl:8: approximation_order > 1)."""
+    with pytest.warns(UserWarning):
+        spec = _third_derivative_problem(1)
+    with pytest.raises(ValueError, match="greater than 1"):
+        lower(spec)
+    from molgpu.api import MOLFiniteDifference
+    with pytest.raises(ValueError):
+        MOLFiniteDifference({"x": 11}, None, approx_order=0)
