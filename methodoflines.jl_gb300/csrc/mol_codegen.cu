@@ -694,6 +694,10 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
         for (int f : used_fields)
             if (f != tm.field) cond += " && wrap_line_ok(P, " + std::to_string(f) + ", " + D + ", " + std::to_string(reach) + ")";
     }
+    // per-point rows (nonuniform grid): the compile-time fast path reads one interior row, so
+    // every cell takes the runtime-tap path, whose tap selection picks each position's row
+    const bool rows = oo.nrows > 0 || oi.nrows > 0 || op.nrows > 0;
+    if (rows) cond = "false";
     for (int vjp = 0; vjp < 2; ++vjp) {
         if (!vjp)
             e << "template <class T>\n__device__ __forceinline__ T gt" << K
@@ -767,6 +771,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
         lcond = "warp_all(fast_line(P, P.ops[" + opi + "], " + F + ", " + D + ", I[" + D + "] - 1) && fast_line(P, P.ops[" +
                 opp + "], " + F + ", " + D + ", I[" + D + "] - 1))";
     }
+    if (rows) lcond = "false";
     e << "template <class T>\n__device__ __forceinline__ T gfl" << K
       << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, const T* __restrict__ p) {\n"
       << "    if (" << lcond << ") {\n"

@@ -617,8 +617,21 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
                 break;
             case MOL_TERM_NONLINLAP:
                 if (!opok(t.op) || !opok(t.op2) || !opok(t.op3)) return set_err(plan, MOL_ERR_INVALID, "nonlinlap ops");
-                if (rows(t.op) || rows(t.op2) || rows(t.op3))
-                    return set_err(plan, MOL_ERR_UNSUPPORTED, "nonlinear Laplacian with per-point operator rows");
+                if (rows(t.op) || rows(t.op2) || rows(t.op3)) {
+                    // nonuniform grid (half_offset_centred_difference.jl:39-69): no wrap, and rows
+                    // for every position that reads an interior row: the outer operator at
+                    // II - 1 on the n - 1 half points, the inner ones at half points up to n - 1
+                    if (d->bc[t.field][t.dim][0].kind == MOL_BC_PERIODIC)
+                        return set_err(plan, MOL_ERR_UNSUPPORTED, "per-point operator rows on a periodic dimension");
+                    const long long n = d->npts[t.dim];
+                    const mol_op1d& oo = d->ops[t.op];
+                    const mol_op1d& oi = d->ops[t.op2];
+                    const mol_op1d& oq = d->ops[t.op3];
+                    if ((oo.nrows > 0 && oo.nrows < std::min<long long>(n - 1 - d->upper[t.dim], n - 1 - oo.nhi) - oo.nlo) ||
+                        (oi.nrows > 0 && oi.nrows < std::min<long long>(n - 1, n - oi.nhi) - oi.nlo) ||
+                        (oq.nrows > 0 && oq.nrows < std::min<long long>(n - 1, n - oq.nhi) - oq.nlo))
+                        return set_err(plan, MOL_ERR_INVALID, "operator rows do not match the grid");
+                }
                 if (t.prog >= 0) {
                     int st = validate_prog(plan, d, t.prog, 1, MOL_MAX_REGS, 0, &t);
                     if (st) return st;

@@ -26,8 +26,8 @@ from typing import Dict, List, Optional, Tuple
 import numpy as np
 
 from . import _lib as L
-from .weights import (WENO_NU_ROW, Operator, centered, centered_nonuniform, extrapolator, half_centered, select,
-                      upwind, upwind_nonuniform, weno_nonuniform_rows, wrap)
+from .weights import (WENO_NU_ROW, Operator, centered, centered_nonuniform, extrapolator, half_centered,
+                      half_centered_nonuniform, select, upwind, upwind_nonuniform, weno_nonuniform_rows, wrap)
 
 # ------------------------------------------------------------------------------------
 # grids (Julia Float64 ranges)
@@ -385,13 +385,24 @@ class Lowered:
             elif self.uniform and not self.uniform[j]:
                 if kind == "centered":
                     o = centered_nonuniform(d, self.order, self.grids[j])
+                elif kind in ("half", "interp", "half_outer"):
+                    g = self.grids[j]
+                    if kind == "half_outer":
+                        # differential_discretizer.jl:47-52: the nonlinear Laplacian's outer
+                        # operator is built on the grid's midpoints
+                        o = half_centered_nonuniform(d, self.order, [(g[i + 1] + g[i]) / 2 for i in range(len(g) - 1)])
+                    elif kind == "half":
+                        o = half_centered_nonuniform(d, self.order, g)
+                    else:
+                        o = half_centered_nonuniform(0, max(4, self.order), g)
                 elif kind in ("wind_pos", "wind_neg") and d + p == 2:
                     # the reference's nonuniform tables reach every interior point only for L = 2
                     o = upwind_nonuniform(d, p, self.grids[j], d + p - 1 if kind == "wind_pos" else 0)
                 else:
                     raise NotImplementedError(
                         f"{kind} operators (order {d}, upwind order {p}) on the nonuniform grid of {self.ivs[j]} "
-                        "are not built (centered derivatives, first-order upwinding and boundary rows are)")
+                        "are not built (centered derivatives, first-order upwinding, the nonlinear Laplacian "
+                        "and boundary rows are)")
             elif kind == "centered":
                 o = centered(d, self.order, dx)
             elif kind == "wind_pos":       # offside d+p-1: backward taps (windmap[2])
@@ -631,7 +642,8 @@ class _Lowerer:
             lw.programs.append(pb.finish())
             prog = len(lw.programs) - 1
             aux0 = faux[0] if faux else 0
-        return lw.term(kind=L.TERM_NONLINLAP, field=f, dim=j, op=lw.op("half", j, 1), op2=lw.op("half", j, 1),
+        outer = lw.op("half" if (not lw.uniform or lw.uniform[j]) else "half_outer", j, 1)
+        return lw.term(kind=L.TERM_NONLINLAP, field=f, dim=j, op=outer, op2=lw.op("half", j, 1),
                        op3=lw.op("interp", j, 0), prog=prog, aux0=aux0, key=repr(a))
 
     # ---------------------------------------------------------------- hoisting

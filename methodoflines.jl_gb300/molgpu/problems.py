@@ -39,7 +39,7 @@ import math
 import numpy as np
 
 from .api import MOLFiniteDifference, UpwindScheme, WENOScheme, edge_align
-from .symbolic import (Differential, Eq, Field, Interval, IV, Param, PDESystem, cos, exp, register, sin)
+from .symbolic import (Differential, Eq, Field, Interval, IV, Param, PDESystem, cos, exp, register, sin, sqrt)
 
 
 def _rng(seed):
@@ -450,3 +450,37 @@ def burgers_nonuniform_upwind(seed: int = 0):
     pts[1:-1] += _rng(seed).choice([0.001, -0.001], size=19)
     disc = MOLFiniteDifference({x: pts}, t, advection_scheme=UpwindScheme(1))
     return sys, disc, {"dt": 0.2 * float(np.min(np.diff(pts))), "points": pts}
+
+
+NLD_C, NLD_H = 50.0, 0.5
+
+
+def nonlinear_diffusion_nu_exact(x, t):
+    """u = (x + h) / (2 sqrt(c - t)), the exact solution of u_t = (u^2 u_x)_x the reference's
+    nonuniform nonlinear-diffusion test uses (test/Nonlinear_Diffusion_NU, Test 01a)."""
+    return 0.5 * (np.asarray(x) + NLD_H) / math.sqrt(NLD_C - t)
+
+
+def nonlinear_diffusion_nonuniform(order: int = 2, seed: int = 0, coefficient: str = "u2"):
+    """u_t = Dx(a Dx(u)) on the points of 0:0.01:2 with the inner points moved by +-0.001
+    (seeded here with PCG64), Dirichlet rows from the exact solution at both ends: the
+    nonlinear Laplacian on a nonuniform grid (nonlinear_laplacian.jl:28-103 with the per-point
+    half-offset tables of half_offset_weights.jl:72-150).  coefficient "u2" is the reference
+    test's a = u^2; "x" gives a = 1 + x, a function of the interpolated half-point coordinate."""
+    from .lowering import grid_points
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dt, Dx = Differential(t), Differential(x)
+    a = u(x, t) ** 2 if coefficient == "u2" else 1.0 + x
+    eq = Eq(Dt(u(x, t)), Dx(a * Dx(u(x, t))))
+    k = 0.5 / math.sqrt(NLD_C)
+    bcs = [Eq(u(x, 0.0), k * (x + NLD_H)),
+           Eq(u(0.0, t), 0.5 * (0.0 + NLD_H) / sqrt(NLD_C - t)),
+           Eq(u(2.0, t), 0.5 * (2.0 + NLD_H) / sqrt(NLD_C - t))]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 2.0)), (x, Interval(0.0, 2.0))], [t, x], [u(x, t)], [])
+    pts = np.array(grid_points(0.0, 0.01, 2.0), dtype=np.float64)
+    pts[1:-1] += _rng(seed).choice([0.001, -0.001], size=len(pts) - 2)
+    disc = MOLFiniteDifference({x: pts}, t, approx_order=order)
+    h = float(np.min(np.diff(pts)))
+    amax = 1.0 + 2.0 if coefficient == "x" else (0.5 * (2.0 + NLD_H) / math.sqrt(NLD_C - 2.0)) ** 2
+    return sys, disc, {"dt": 0.2 * h * h / amax, "points": pts}

@@ -181,6 +181,31 @@ def half_centered(d: int, p: int, dx: float) -> Operator:
     return Operator(L, 1 - e, inner, low, high, bl, bl, 1)
 
 
+def half_centered_nonuniform(d: int, p: int, x: Sequence[float]) -> Operator:
+    """``CompleteHalfCenteredDifference(d, p, x::AbstractVector)`` (half_offset_weights.jl:72-150):
+    per-half-point rows on the grid's own nodes.  Half point i (1-based, between nodes i and
+    i+1) sits at (x_i + x_{i+1})/2; its interior row is Fornberg on nodes i-e+1 .. i+e (e half
+    the stencil length), the low rows (half points 1..e) and high rows (the last e, last first)
+    on the first / last d+p nodes.  Tap selection reads row i-e for half point i
+    (half_offset_centred_difference.jl:39-69), the device's row index i - nlo - 1."""
+    if p <= 1:
+        raise ValueError("approximation_order must be greater than 1.")
+    x = [float(v) for v in x]
+    L = p + 2 * (d // 2) + (p % 2)
+    bl = d + p
+    e = L // 2
+    n = len(x)
+    if n < bl or n < L:
+        raise NotImplementedError("nonuniform grid too short for the half-offset stencil")
+    mid = [(x[k] + x[k + 1]) / 2 for k in range(n - 1)]
+    rows = [fornberg(d, mid[i - 1], x[i - e:i + e]) for i in range(e + 1, n - e + 1)]
+    low = [fornberg(d, mid[k], x[:bl]) for k in range(e)]
+    high = [fornberg(d, mid[n - 2 - k], x[n - bl:]) for k in range(e)]
+    if not rows:
+        raise NotImplementedError("nonuniform grid too short for the half-offset stencil")
+    return Operator(L, 1 - e, rows[0], low, high, bl, bl, 1, rows)
+
+
 def extrapolator(q: int) -> Operator:
     """``BoundaryInterpolatorExtrapolator(q, dx)`` (extrapolation_weights.jl:1-60): row k of the
     low table gives the value at node k (0-based) of the first q nodes from the other q - 1

@@ -242,6 +242,30 @@ def complete_upwind_difference_nonuniform(d: int, p: int, x: Sequence[float], of
     return DerivativeOperator(d, p, float("nan"), L, stencil, bL, nhi, low, high, 0, "upwind_nonuniform")
 
 
+def complete_half_centered_difference_nonuniform(d: int, p: int, x: Sequence[float]) -> DerivativeOperator:
+    """``CompleteHalfCenteredDifference(d, p, x::AbstractVector)``, ``half_offset_weights.jl:72-150``.
+
+    With hx[i] = (x[i] + x[i+1]) / 2 the half points (1-based), ``stencil_coefs`` holds one
+    row per half point i = endpoint+1 .. len(x)-endpoint: the Fornberg weights at hx[i] on
+    x[i-endpoint+1 .. i+endpoint].  The low rows are the weights at hx[1..bpc] on the first
+    bL nodes, the high rows the weights at hx[end], hx[end-1], ... on the last bL nodes.  No
+    1/dx^d scaling: the nodes carry the physical coordinates.
+    """
+    assert p > 1
+    x = [float(v) for v in x]
+    L = p + 2 * (d // 2) + (p % 2)
+    bL = d + p
+    endpoint = L // 2
+    n = len(x)
+    hx = [(x[i] + x[i + 1]) / 2 for i in range(n - 1)]
+    stencil = [calculate_weights(d, hx[i - 1], x[i - endpoint:i + endpoint]) for i in range(endpoint + 1, n - endpoint + 1)]
+    low_x = x[:bL]
+    high_x = x[n - bL:]
+    low = [calculate_weights(d, off, low_x) for off in hx[:endpoint]]
+    high = [calculate_weights(d, hx[len(hx) - 1 - k], high_x) for k in range(endpoint)]
+    return DerivativeOperator(d, p, float("nan"), L, stencil, bL, endpoint, low, high, 0, "half_nonuniform")
+
+
 def complete_half_centered_difference(d: int, p: int, dx: float) -> DerivativeOperator:
     """``CompleteHalfCenteredDifference``, ``half_offset_weights.jl:4-70``."""
     assert p > 1

@@ -20,6 +20,7 @@ import numpy as np
 from .weno_nonuniform import taps_and_target, weno_f_nonuniform
 from .fornberg import (boundary_interpolator_extrapolator, complete_centered_difference,
                        complete_centered_difference_nonuniform, complete_half_centered_difference,
+                       complete_half_centered_difference_nonuniform,
                        complete_upwind_difference_nonuniform,
                        complete_upwind_difference)
 
@@ -180,7 +181,11 @@ def half_offset_taps(D, i: int, n: int, periodic: bool, length: int = 0, wrap: b
     if i > ln - bpc and not periodic:
         return list(D.high_boundary_coefs[ln - i - 1]), [ln - bL + 1 + k for k in range(bL)]
     h = D.stencil_length // 2
-    return list(D.stencil_coefs), [i + k for k in range(1 - h, h + 1)]
+    taps = [i + k for k in range(1 - h, h + 1)]
+    if D.kind == "half_nonuniform":     # half_offset_centred_difference.jl:39-69: the point's own row
+        assert not periodic, "interface boundaries are not supported on nonuniform dimensions"
+        return list(D.stencil_coefs[i - bpc - 1]), taps
+    return list(D.stencil_coefs), taps
 
 
 # --------------------------------------------------------------------------------------
@@ -366,6 +371,16 @@ class OracleProblem:
                     D = complete_upwind_difference_nonuniform(d, int(extra), self.grid[j], 0)
                 elif kind == "wind_pos":
                     D = complete_upwind_difference_nonuniform(d, int(extra), self.grid[j], d + int(extra) - 1)
+                elif kind == "half":
+                    D = complete_half_centered_difference_nonuniform(d, self.order, self.grid[j])
+                elif kind == "interp":
+                    D = complete_half_centered_difference_nonuniform(0, max(4, self.order), self.grid[j])
+                elif kind == "half_outer":
+                    # differential_discretizer.jl:47-52: the outer operator of the nonlinear
+                    # Laplacian is built on the midpoints of the grid
+                    g = self.grid[j]
+                    D = complete_half_centered_difference_nonuniform(
+                        d, self.order, [(g[i + 1] + g[i]) / 2 for i in range(len(g) - 1)])
                 else:
                     raise NotImplementedError(f"oracle: {kind} operators on a nonuniform grid")
             elif kind == "centered":
@@ -852,7 +867,7 @@ class OracleProblem:
         """``cartesian_nonlinear_laplacian`` (nonlinear_laplacian.jl:28-103)."""
         n = self.npts[j]
         per = self.bc[f][j]["periodic"]
-        D_outer = self.op("half", j, 1)
+        D_outer = self.op("half" if self.uniform[j] else "half_outer", j, 1)
         D_inner = self.op("half", j, 1)
         interp = self.op("interp", j, 0)
         cliplen = n - 1

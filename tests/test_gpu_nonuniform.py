@@ -256,3 +256,88 @@ def test_burgers_nonuniform_upwind_tsit5(gpu_lib):
     x = sol["x"]
     for i, t in enumerate(sol.ts):
         assert np.max(np.abs(sol["u"][i] - x / (t + 1))) < 10 ** -2.5, t
+
+
+# the nonlinear Laplacian on a nonuniform grid (the reference's test/Nonlinear_Diffusion_NU):
+# per-half-point tables, the outer operator on the grid's midpoints
+NLD_CASES = [(2, "u2"), (4, "u2"), (2, "x"), (6, "x")]
+
+
+@pytest.mark.parametrize("order,coefficient", NLD_CASES)
+def test_nonuniform_nonlinlap_rhs_and_trajectory(gpu_lib, order, coefficient):
+    s, d, ex = problems.nonlinear_diffusion_nonuniform(order, coefficient=coefficient)
+    spec = s.to_spec(d)
+    lw, orc = lower(spec), OracleProblem(spec)
+    plan = Plan(lw)
+    assert L.lib().mol_plan_uses_codegen(plan.handle) == 1
+    v = lw.u0 * (1 + 0.05 * np.random.default_rng(order).standard_normal(lw.n_unknowns))
+    for t in (0.0, 0.7):
+        du = np.zeros(lw.n_unknowns)
+        plan.rhs(du, v, None, t)
+        assert _rel(du, orc.rhs(v, t)) < 1e-12, t
+    u = lw.u0.copy()
+    plan.step_ssprk33(u, ex["dt"], 40, t0=0.1)
+    ref, _ = ssprk33(lambda w, tt: orc.rhs(w, tt), lw.u0, 0.1, ex["dt"], 40)
+    assert _rel(u, ref) < 1e-10
+    plan.close()
+
+
+def test_nonuniform_nonlinlap_generated_matches_interpreter(gpu_lib, monkeypatch):
+    """Generated code without and with the face pass (faces computed once per step by their
+    own kernel) and the interpreter give the same right-hand side."""
+    s, d, ex = problems.nonlinear_diffusion_nonuniform(4, coefficient="x")
+    lw = lower(s.to_spec(d))
+    gen = Plan(lw)
+    monkeypatch.setenv("MOL_FACE_PASS", "1")
+    faced = Plan(lw)
+    monkeypatch.setenv("MOL_DISABLE_CODEGEN", "1")
+    interp = Plan(lw)
+    assert L.lib().mol_plan_uses_codegen(interp.handle) == 0
+    u = lw.u0 * 1.01
+    a, b, c = np.zeros_like(u), np.zeros_like(u), np.zeros_like(u)
+    gen.rhs(a, u, None, 0.9)
+    faced.rhs(c, u, None, 0.9)
+    interp.rhs(b, u, None, 0.9)
+    assert _rel(a, b) < 1e-13 and _rel(c, b) < 1e-13
+    x, y = lw.u0.copy(), lw.u0.copy()
+    gen.step_ssprk33(x, ex["dt"], 20)
+    faced.step_ssprk33(y, ex["dt"], 20)
+    assert _rel(x, y) < 1e-13
+    for pl in (gen, faced, interp):
+        pl.close()
+
+
+def test_nonuniform_nonlinlap_tracks_the_exact_solution(gpu_lib):
+    """The reference's Test 01a (u_t = (u^2 u_x)_x, u = (x + 1/2)/(2 sqrt(50 - t)) on a jittered
+    0:0.01:2) solved on the GPU with Tsit5 to t = 2: within 1e-6 of the exact solution (the
+    reference test's bar is 0.1)."""
+    s, d, ex = problems.nonlinear_diffusion_nonuniform(2)
+    lw = lower(s.to_spec(d))
+    plan = Plan(lw)
+    u = lw.u0.copy()
+    st = plan.solve_tsit5(u, 0.0, 2.0, 1e-8, 1e-8)
+    assert st["t"] == 2.0
+    exact = problems.nonlinear_diffusion_nu_exact(ex["points"][1:-1], 2.0)
+    assert np.max(np.abs(u - exact)) < 1e-6
+    plan.close()
+
+
+def test_nonuniform_nonlinlap_adjoint_matches_finite_differences(gpu_lib):
+    s, d, ex = problems.nonlinear_diffusion_nonuniform(2)
+    lw = lower(s.to_spec(d))
+    plan = Plan(lw)
+    dt, n = ex["dt"], 20
+    target = np.full(lw.n_unknowns, 0.1)
+
+    def loss(u0):
+        u = u0.copy()
+        plan.step_ssprk33(u, dt, n, t0=0.0)
+        return 0.5 * float(np.sum((u - target) ** 2))
+
+    g = np.zeros(lw.n_unknowns)
+    plan.adjoint_ssprk33(lw.u0, dt, n, target, nsnap=4, dLdu0=g)
+    w = np.random.default_rng(9).standard_normal(lw.n_unknowns)
+    h = 1e-6
+    fd = (loss(lw.u0 + h * w) - loss(lw.u0 - h * w)) / (2 * h)
+    assert abs(g @ w - fd) <= 1e-6 * abs(fd), (g @ w, fd)
+    plan.close()

@@ -200,7 +200,7 @@ def _unsupported(kind):
     return s.to_spec(MOLFiniteDifference({x: pts}, t, advection_scheme=scheme))
 
 
-@pytest.mark.parametrize("kind", ["upwind", "nonlinlap", "periodic", "mixed"])
+@pytest.mark.parametrize("kind", ["upwind", "periodic", "mixed"])
 def test_schemes_not_built_on_nonuniform_grids_are_refused(kind):
     with pytest.raises(NotImplementedError):
         lower(_unsupported(kind))
@@ -365,3 +365,98 @@ def test_chebyspace_grid():
     v = lw.u0 * 1.01
     a, b = OracleProblem(spec).rhs(v, 0.2), DescInterp(lw).rhs(v, 0.2)
     assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a)
+
+
+# ---------------------------------------------------------------------------------------
+# the nonlinear Laplacian on a nonuniform grid: per-half-point tables
+# (CompleteHalfCenteredDifference(d, p, x::AbstractVector), half_offset_weights.jl:72-150),
+# the outer operator on the grid's midpoints (differential_discretizer.jl:47-52)
+# ---------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("d", [0, 1, 2])
+@pytest.mark.parametrize("p", [2, 4, 6])
+def test_half_offset_tables_bit_identical_to_oracle(d, p):
+    from molgpu.weights import half_centered_nonuniform
+    from oracle.fornberg import complete_half_centered_difference_nonuniform
+    for seed in (0, 1):
+        x = _jittered(30, seed)
+        a = half_centered_nonuniform(d, p, x)
+        b = complete_half_centered_difference_nonuniform(d, p, x)
+        assert a.rows == b.stencil_coefs
+        assert a.low == b.low_boundary_coefs and a.high == b.high_boundary_coefs
+        assert a.nlo == b.boundary_point_count and len(a.rows) == len(x) - 2 * a.nlo
+
+
+@pytest.mark.parametrize("d", [0, 1, 2])
+@pytest.mark.parametrize("p", [2, 4, 6])
+def test_integer_grid_half_offset_reduces_to_uniform(d, p):
+    """On the points 0..n-1 every interior and low row equals the uniform table bit for bit;
+    the high rows (computed on the last nodes, not reflected) agree to rounding."""
+    from molgpu.weights import half_centered, half_centered_nonuniform
+    nu = half_centered_nonuniform(d, p, np.arange(24, dtype=float))
+    un = half_centered(d, p, 1.0)
+    assert all(r == un.interior for r in nu.rows)
+    assert nu.low == un.low
+    assert np.allclose(nu.high, un.high, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("coefficient", ["u2", "x"])
+def test_descriptor_semantics_match_oracle_nonuniform_nonlinlap(order, coefficient):
+    s, d, ex = problems.nonlinear_diffusion_nonuniform(order, coefficient=coefficient)
+    spec = s.to_spec(d)
+    lw, orc = lower(spec), OracleProblem(spec)
+    v = lw.u0 * (1 + 0.05 * np.random.default_rng(order).standard_normal(lw.n_unknowns))
+    for t in (0.0, 0.7):
+        a, b = orc.rhs(v, t), DescInterp(lw).rhs(v, t)
+        assert np.array_equal(a, b), (order, coefficient, t)
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_nonuniform_nonlinlap_is_exact_at_the_midpoints_of_midpoints(order):
+    """On the reference test's exact solution (linear in x) every table is exact, so the
+    semi-discrete RHS is the exact flux derivative 2 u u_x^2 taken where the outer operator
+    sits: at the midpoint of the two half points around each grid point, (x[i-1] + 2x[i] +
+    x[i+1])/4, not at x[i] (the outer operator is built on the grid's midpoints)."""
+    s, d, ex = problems.nonlinear_diffusion_nonuniform(order)
+    spec = s.to_spec(d)
+    lw, orc = lower(spec), OracleProblem(spec)
+    g = ex["points"]
+    t = 0.7
+    v = problems.nonlinear_diffusion_nu_exact(g[1:-1], t)
+    m = (g[:-1] + g[1:]) / 2
+    hm = (m[:-1] + m[1:]) / 2
+    exact = 0.25 * (hm + problems.NLD_H) / (problems.NLD_C - t) ** 1.5
+    for r in (orc.rhs(v, t), DescInterp(lw).rhs(v, t)):
+        assert np.max(np.abs(r - exact)) <= 1e-9 * np.max(np.abs(exact))
+    xi = 0.25 * (g[1:-1] + problems.NLD_H) / (problems.NLD_C - t) ** 1.5
+    assert np.max(np.abs(exact - xi)) > 1e-4 * np.max(np.abs(xi))   # the offset is visible
+
+
+def test_plan_validation_of_nonlinlap_rows():
+    from molgpu import Plan
+    s, d, _ = problems.nonlinear_diffusion_nonuniform(2)
+    lw = lower(s.to_spec(d))
+    term = [tm for tm in lw.terms if tm["kind"] == L.TERM_NONLINLAP][0]
+    op = lw.ops[term["op"]]
+    op.rows = op.rows[:-2]
+    with pytest.raises(L.MolError) as e:
+        Plan(lw)
+    assert e.value.status == -1 and "rows" in str(e.value)
+
+
+def test_generated_code_nonlinlap_rows_takes_the_runtime_tap_path():
+    """With per-point rows the compile-time interior path (one row) is switched off and the
+    code compiles for sm_103a (NVRTC, no device needed)."""
+    import ctypes as C
+    from molgpu import Descriptor
+    s, d, _ = problems.nonlinear_diffusion_nonuniform(4)
+    D = Descriptor(lower(s.to_spec(d)))
+    need = C.c_int64()
+    assert L.lib().mol_generate_code(C.byref(D.desc), None, 0, C.byref(need)) == 0
+    buf = C.create_string_buffer(need.value)
+    assert L.lib().mol_generate_code(C.byref(D.desc), buf, need.value, C.byref(need)) == 0
+    src = buf.value.decode()
+    assert src.count("if (false) {") >= 3      # forward, adjoint and face-pass fast paths
+    log = C.create_string_buffer(1 << 16)
+    assert L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16) == 0, log.value.decode()
