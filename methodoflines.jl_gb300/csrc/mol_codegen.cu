@@ -417,8 +417,12 @@ void emit_mixed(Emitter& e, const mol_problem_desc* d, int k) {
             if (!zero_w(d, o1.w_int + x) && !zero_w(d, o2.w_int + y)) nz.push_back({x, y});
     // both dimensions periodic: wrapped offsets everywhere (uniform branch)
     const bool per = periodic_dim(d, tm.field, tm.dim) && periodic_dim(d, tm.field, tm.dim2);
+    // per-point rows (nonuniform grid): the precomputed product table is one row's, so every
+    // cell takes apply_mixed, whose tap selection picks each position's row
+    const bool rows = o1.nrows > 0 || o2.nrows > 0;
     const std::string cond =
-        per ? "wrap_line_ok(P, " + F + ", " + D1 + ", " + std::to_string(reach_of(o1)) + ") && wrap_line_ok(P, " + F +
+        rows ? std::string("false")
+        : per ? "wrap_line_ok(P, " + F + ", " + D1 + ", " + std::to_string(reach_of(o1)) + ") && wrap_line_ok(P, " + F +
                   ", " + D2 + ", " + std::to_string(reach_of(o2)) + ")"
             : "warp_all(fast_line(P, P.ops[" + std::to_string(tm.op) + "], " + F + ", " + D1 + ", I[" + D1 +
                   "]) && fast_line(P, P.ops[" + std::to_string(tm.op2) + "], " + F + ", " + D2 + ", I[" + D2 + "]))";
@@ -832,7 +836,8 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
         if (in.op == MOL_OP_TERM) {
             const mol_term& tm = d->terms[in.imm];
             // per-point rows (nonuniform grid) have no compile-time tap weights: not fused
-            if ((tm.kind == MOL_TERM_LINEAR && d->ops[tm.op].nrows == 0) || tm.kind == MOL_TERM_MIXED) {
+            if ((tm.kind == MOL_TERM_LINEAR && d->ops[tm.op].nrows == 0) ||
+                (tm.kind == MOL_TERM_MIXED && d->ops[tm.op].nrows == 0 && d->ops[tm.op2].nrows == 0)) {
                 L.ok = true;
                 L.field = tm.field;
                 L.coef[in.imm] = "T(1)";

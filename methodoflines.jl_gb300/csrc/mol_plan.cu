@@ -591,8 +591,17 @@ static int validate_desc(mol_plan* plan, const mol_problem_desc* d) {
             case MOL_TERM_MIXED:
                 if (!opok(t.op) || !opok(t.op2) || t.dim2 < 0 || t.dim2 >= d->ndim || t.dim2 == t.dim)
                     return set_err(plan, MOL_ERR_INVALID, "mixed term");
-                if (rows(t.op) || rows(t.op2))
-                    return set_err(plan, MOL_ERR_UNSUPPORTED, "mixed derivatives with per-point operator rows");
+                // nonuniform dimensions (centered_difference.jl:32-56 on each): no wrap, and rows
+                // for every interior point that reads an interior row
+                for (int q = 0; q < 2; ++q) {
+                    const int o = q == 0 ? t.op : t.op2, dm = q == 0 ? t.dim : t.dim2;
+                    if (!rows(o)) continue;
+                    if (d->bc[t.field][dm][0].kind == MOL_BC_PERIODIC)
+                        return set_err(plan, MOL_ERR_UNSUPPORTED, "per-point operator rows on a periodic dimension");
+                    const long long n = d->npts[dm];
+                    if (d->ops[o].nrows < std::min<long long>(n - d->upper[dm], n - d->ops[o].nhi) - d->ops[o].nlo)
+                        return set_err(plan, MOL_ERR_INVALID, "operator rows do not match the grid");
+                }
                 break;
             case MOL_TERM_WENO:
                 if (!(t.dx > 0)) return set_err(plan, MOL_ERR_INVALID, "weno dx");

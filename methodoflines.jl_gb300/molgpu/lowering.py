@@ -611,8 +611,6 @@ class _Lowerer:
         if arg[0] == "D" and d == 1 and arg[2] == 1 and arg[3][0] == "field":
             k = lw.ivs.index(arg[1])
             f = lw.fields.index(arg[3][1])
-            if not (lw.uniform[j] and lw.uniform[k]):
-                raise NotImplementedError("mixed derivatives on a nonuniform grid are not built")
             return lw.term(kind=L.TERM_MIXED, field=f, dim=j, dim2=k, op=lw.op("centered", j, 1),
                            op2=lw.op("centered", k, 1))
         if d == 1:

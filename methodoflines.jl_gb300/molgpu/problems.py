@@ -484,3 +484,22 @@ def nonlinear_diffusion_nonuniform(order: int = 2, seed: int = 0, coefficient: s
     h = float(np.min(np.diff(pts)))
     amax = 1.0 + 2.0 if coefficient == "x" else (0.5 * (2.0 + NLD_H) / math.sqrt(NLD_C - 2.0)) ** 2
     return sys, disc, {"dt": 0.2 * h * h / amax, "points": pts}
+
+
+def mixed_nonuniform(nx: int = 21, ny: int = 17, order: int = 2):
+    """u_t = Dxx u + Dyy u + 0.3 Dx(Dy(u)) with x on stretched points and y on a grid clustered
+    at its low end: the mixed derivative as the product of the two dimensions' per-point
+    first-derivative rows (2nd_order_mixed_deriv.jl:5-22 through centered_difference.jl:32-56).
+    Dirichlet rows hold x^2 y^2 on every face, so that state is exact data for the tables."""
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u = Field("u")
+    Dt, Dx, Dy = Differential(t), Differential(x), Differential(y)
+    eq = Eq(Dt(u(x, y, t)), (Dx ** 2)(u(x, y, t)) + (Dy ** 2)(u(x, y, t)) + 0.3 * Dx(Dy(u(x, y, t))))
+    bcs = [Eq(u(x, y, 0.0), x * x * y * y), Eq(u(0.0, y, t), 0.0), Eq(u(1.0, y, t), y * y),
+           Eq(u(x, 0.0, t), 0.0), Eq(u(x, 1.0, t), x * x)]
+    sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0))],
+                    [t, x, y], [u(x, y, t)], [])
+    px, py = stretched_points(nx), cluster_grid("left", ny)
+    disc = MOLFiniteDifference({x: px, y: py}, t, approx_order=order)
+    h = min(float(np.min(np.diff(px))), float(np.min(np.diff(py))))
+    return sys, disc, {"dt": 0.1 * h * h, "points": (px, py)}

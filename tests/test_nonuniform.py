@@ -200,7 +200,7 @@ def _unsupported(kind):
     return s.to_spec(MOLFiniteDifference({x: pts}, t, advection_scheme=scheme))
 
 
-@pytest.mark.parametrize("kind", ["upwind", "periodic", "mixed"])
+@pytest.mark.parametrize("kind", ["upwind", "periodic"])
 def test_schemes_not_built_on_nonuniform_grids_are_refused(kind):
     with pytest.raises(NotImplementedError):
         lower(_unsupported(kind))
@@ -458,5 +458,49 @@ def test_generated_code_nonlinlap_rows_takes_the_runtime_tap_path():
     assert L.lib().mol_generate_code(C.byref(D.desc), buf, need.value, C.byref(need)) == 0
     src = buf.value.decode()
     assert src.count("if (false) {") >= 3      # forward, adjoint and face-pass fast paths
+    log = C.create_string_buffer(1 << 16)
+    assert L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16) == 0, log.value.decode()
+
+
+# ---------------------------------------------------------------------------------------
+# mixed derivatives on nonuniform grids: the product of the two per-point first-derivative rows
+# ---------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_descriptor_semantics_match_oracle_nonuniform_mixed(order):
+    s, d, ex = problems.mixed_nonuniform(order=order)
+    spec = s.to_spec(d)
+    lw, orc = lower(spec), OracleProblem(spec)
+    v = lw.u0 + 0.05 * np.random.default_rng(order).standard_normal(lw.n_unknowns)
+    a, b = orc.rhs(v, 0.3), DescInterp(lw).rhs(v, 0.3)
+    assert np.array_equal(a, b)
+
+
+def test_nonuniform_mixed_is_exact_on_a_biquadratic():
+    """Every order-2 row is exact on quadratics, so on u = x^2 y^2 the RHS is 2y^2 + 2x^2 +
+    0.3 * 4xy at every interior point whose mixed stencil stays off the corners (the corner
+    points read 0, generate_bc_eqs.jl:396-459)."""
+    s, d, ex = problems.mixed_nonuniform(order=2)
+    spec = s.to_spec(d)
+    lw, orc = lower(spec), OracleProblem(spec)
+    px, py = ex["points"]
+    X, Y = np.meshgrid(px[1:-1], py[1:-1], indexing="ij")
+    v = (X * X * Y * Y).reshape(-1, order="F")
+    exact = (2 * Y * Y + 2 * X * X + 1.2 * X * Y)
+    for r in (orc.rhs(v, 0.0), DescInterp(lw).rhs(v, 0.0)):
+        R = r.reshape(X.shape, order="F")
+        assert np.max(np.abs(R[1:-1, 1:-1] - exact[1:-1, 1:-1])) <= 1e-9 * np.max(np.abs(exact))
+
+
+def test_generated_code_mixed_rows_takes_the_runtime_tap_path():
+    import ctypes as C
+    from molgpu import Descriptor
+    s, d, _ = problems.mixed_nonuniform(nx=11, ny=9)
+    D = Descriptor(lower(s.to_spec(d)))
+    need = C.c_int64()
+    assert L.lib().mol_generate_code(C.byref(D.desc), None, 0, C.byref(need)) == 0
+    buf = C.create_string_buffer(need.value)
+    assert L.lib().mol_generate_code(C.byref(D.desc), buf, need.value, C.byref(need)) == 0
+    assert buf.value.decode().count("if (false) {") >= 2
     log = C.create_string_buffer(1 << 16)
     assert L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16) == 0, log.value.decode()
