@@ -174,26 +174,16 @@ def test_descriptor_carries_rows():
 
 
 def _unsupported(kind):
-    from molgpu.api import MOLFiniteDifference, UpwindScheme, WENOScheme
+    from molgpu.api import MOLFiniteDifference, UpwindScheme
     from molgpu.symbolic import Differential, Eq, Field, Interval, IV, PDESystem, sin
-    x, y, t = IV("x"), IV("y"), IV("t")
+    x, t = IV("x"), IV("t")
     u = Field("u")
     Dt, Dx = Differential(t), Differential(x)
     pts = problems.stretched_points(21)
     if kind == "upwind":       # second-order upwinding: the reference's table is too short
         eq, scheme = Eq(Dt(u(x, t)), -Dx(u(x, t))), UpwindScheme(2)
-    elif kind == "nonlinlap":
-        eq, scheme = Eq(Dt(u(x, t)), Dx(u(x, t) * Dx(u(x, t)))), None
-    elif kind == "periodic":
+    else:                      # no periodic boundary on a nonuniform dimension (centered_difference.jl:36)
         eq, scheme = Eq(Dt(u(x, t)), (Dx ** 2)(u(x, t))), None
-    if kind == "mixed":
-        Dy = Differential(y)
-        s = PDESystem([Eq(Dt(u(x, y, t)), Dx(Dy(u(x, y, t))))],
-                      [Eq(u(x, y, 0.0), sin(x)), Eq(u(0.0, y, t), 0.0), Eq(u(1.0, y, t), 0.0),
-                       Eq(u(x, 0.0, t), 0.0), Eq(u(x, 1.0, t), 0.0)],
-                      [(t, Interval(0, 1)), (x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0))], [t, x, y],
-                      [u(x, y, t)])
-        return s.to_spec(MOLFiniteDifference({x: pts, y: 0.1}, t))
     bcs = [Eq(u(x, 0.0), sin(x))]
     bcs += [Eq(u(0.0, t), u(1.0, t))] if kind == "periodic" else [Eq(u(0.0, t), 0.0), Eq(u(1.0, t), 0.0)]
     s = PDESystem([eq], bcs, [(t, Interval(0, 1)), (x, Interval(0.0, 1.0))], [t, x], [u(x, t)])
