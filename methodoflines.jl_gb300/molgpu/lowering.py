@@ -786,6 +786,10 @@ class _Lowerer:
         out = []
         for sign, term in _split_add(self.spec["eqs"][f]):
             num, den = _split_mul(term)
+            sph = self.spherical_tree(num, den)
+            if sph is not None:
+                out.append(("neg", sph) if sign < 0 else sph)
+                continue
             odd = [k for k, a in enumerate(num) if a[0] == "D" and a[3][0] == "field" and a[2] % 2 == 1
                    and not (lw.adv[0] == "weno" and a[2] == 1)]
             if odd:
@@ -812,6 +816,41 @@ class _Lowerer:
                 v = self.subst(term)
                 out.append(("neg", v) if sign < 0 else v)
         return _fold("add", out)
+
+    def spherical_tree(self, num, den):
+        """The spherical Laplacian ``r^-2 Dr(c r^2 Dr(u))`` (generate_spherical_diffusion_rules,
+        spherical_laplacian.jl:42-130): a product whose only denominator is r^2 and which has a
+        factor Dr(inner), inner a product of r^2, Dr(u) and coefficient factors c, becomes the
+        other factors times spherical_diffusion(c) (:10-40), which the reference writes as
+        c(cell) * (D1(u) / r + Dr(c Dr(u))): the centered first derivative over the cell's r
+        plus the nonlinear Laplacian of c.  None when the term does not have that form."""
+        lw = self.lw
+        for kd, a in enumerate(num):
+            if a[0] != "D" or a[2] != 1 or a[3][0] == "field":
+                continue
+            x = a[1]
+            r2 = ("pow", ("iv", x), ("num", 2.0))
+            inum, iden = _split_mul(a[3])
+            if den != [r2] or iden or inum.count(r2) != 1:
+                continue
+            dk = [k for k, q in enumerate(inum) if q[0] == "D" and q[1] == x and q[2] == 1 and q[3][0] == "field"]
+            if len(dk) != 1:
+                continue
+            g = lw.fields.index(inum[dk[0]][3][1])
+            coef = [q for k, q in enumerate(inum) if k != dk[0] and q != r2]
+            j = lw.ivs.index(x)
+            if np.any(np.abs(lw.grids[j][lw.lower[j]:lw.npts[j] - lw.upper[j]]) <= 1e-6):
+                # spherical_laplacian.jl:30-33: 6 c D2(u) at r = 0
+                raise NotImplementedError("a spherical Laplacian with r = 0 as an unknown is not built")
+            here = _fold("mul", [self.subst(c) for c in coef]) if coef else ("num", 1.0)
+            d1 = lw.term(kind=L.TERM_LINEAR, field=g, dim=j, op=lw.op("centered", j, 1))
+            nll = self.nonlinlap_term(coef, [], lw.fields[g], j)
+            v = ("mul", here, ("add", ("div", ("term", d1), ("iv", x)), ("term", nll)))
+            for k, q in enumerate(num):
+                if k != kd:
+                    v = ("mul", self.subst(q), v)
+            return v
+        return None
 
     def subst(self, t):
         k = t[0]

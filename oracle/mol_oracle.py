@@ -702,6 +702,9 @@ class OracleProblem:
         takes the backward stencil when that coefficient is > 0, the forward one otherwise.
         """
         num, den = _split_mul(term)
+        sph = self._spherical(num, den, f, full, env)
+        if sph is not None:
+            return -sph if sign < 0 else sph
         odd = [k for k, a in enumerate(num) if _is_field_deriv(a) and a[2] % 2 == 1
                and not (self.adv_kind == "weno" and a[2] == 1)]
         if odd:
@@ -725,6 +728,50 @@ class OracleProblem:
             return -lhs
         v = self._eval_point(term, env)
         return -v if sign < 0 else v
+
+    def _spherical(self, num, den, f, full, env):
+        """``generate_spherical_diffusion_rules`` / ``spherical_diffusion``
+        (spherical_laplacian.jl:10-40, 42-130).
+
+        A product whose only denominator is r^2 and one of whose factors is Dr(inner), inner a
+        product holding r^2 and Dr(u), is rewritten: the other outer factors times
+        spherical_diffusion(innerexpr), innerexpr the inner product without r^2 and Dr(u).  As
+        the reference writes it, spherical_diffusion is innerexpr at the point times
+        (D1(u) / r + cartesian_nonlinear_laplacian(innerexpr)), D1 the centered first
+        derivative; at a point with |r| <= 1e-6 it is 6 innerexpr D2(u).  Returns None when
+        the term does not have that form."""
+        for kd, a in enumerate(num):
+            if a[0] != "D" or a[2] != 1 or a[3][0] == "field":
+                continue
+            x = a[1]
+            r2 = ("pow", ("iv", x), ("num", 2.0))
+            if den != [r2]:
+                continue
+            inum, iden = _split_mul(a[3])
+            if iden or inum.count(r2) != 1:
+                continue
+            ks = [k for k, q in enumerate(inum) if q[0] == "D" and q[1] == x and q[2] == 1 and q[3][0] == "field"]
+            if len(ks) != 1:
+                continue
+            g = inum[ks[0]][3][1]
+            coef = [q for k, q in enumerate(inum) if k != ks[0] and q != r2]
+            j = self.ivs.index(x)
+            r = self.coords_interior(f)[j]
+            here = 1.0
+            for c in coef:
+                here = here * self._eval_point(c, env)
+            d1 = self._linear(full[g], f, j, "centered", 1)
+            nll = self._nonlinlap(coef, [], g, f, j, full, env)
+            at0 = np.abs(r) <= 1e-6
+            with np.errstate(divide="ignore", invalid="ignore"):
+                v = here * (d1 / r + nll)
+            if np.any(at0):
+                v = np.where(at0, 6 * here * self._linear(full[g], f, j, "centered", 2), v)
+            for k, q in enumerate(num):
+                if k != kd:
+                    v = self._eval_point(q, env) * v
+            return v
+        return None
 
     def _deriv(self, node, f, full, env, ispositive):
         _, x, d, arg = node
