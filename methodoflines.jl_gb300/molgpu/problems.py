@@ -507,14 +507,14 @@ def mixed_nonuniform(nx: int = 21, ny: int = 17, order: int = 2):
 
 def spherical_laplacian(dr: float = 0.1, order: int = 4, scale: float = 1.0):
     """u_t = scale / r^2 * Dr(r^2 Dr(u)) on [0, 1], u0 = sin(r)/r, Dr(u) = 0 at r = 0 and
-    u = e^-t sin(1) at r = 1: the reference's spherical-Laplacian tests
+    u = e^(-scale t) sin(1) at r = 1: the reference's spherical-Laplacian tests
     (test/Diffusion/MOL_1D_Linear_Diffusion.jl, Tests 07 and 08), discretised through its
     spherical_diffusion rule (spherical_laplacian.jl)."""
     r, t = IV("r"), IV("t")
     u = Field("u")
     Dt, Dr = Differential(t), Differential(r)
     eq = Eq(Dt(u(r, t)), scale / r ** 2 * Dr(r ** 2 * Dr(u(r, t))))
-    bcs = [Eq(u(r, 0.0), sin(r) / r), Eq(Dr(u(0.0, t)), 0.0), Eq(u(1.0, t), exp(-t) * math.sin(1.0))]
+    bcs = [Eq(u(r, 0.0), sin(r) / r), Eq(Dr(u(0.0, t)), 0.0), Eq(u(1.0, t), exp(-scale * t) * math.sin(1.0))]
     sys = PDESystem([eq], bcs, [(t, Interval(0.0, 1.0)), (r, Interval(0.0, 1.0))], [t, r], [u(r, t)], [])
     disc = MOLFiniteDifference({r: dr}, t, approx_order=order)
     return sys, disc, {"dt": 0.1 * dr * dr / scale}

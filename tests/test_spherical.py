@@ -62,17 +62,22 @@ def test_spherical_rule_value_on_a_quadratic():
         assert np.allclose(rhs, 4.0, rtol=0, atol=1e-10)
 
 
-def test_reference_test07_bar():
-    """The reference's Test 07 (order 4, dr = 0.1) holds the solution within 0.06 of
-    e^-t sin(r)/r over t in [0, 1]; the restated rule, integrated with Tsit5, stays inside it."""
-    s, d, ex = problems.spherical_laplacian()
+@pytest.mark.parametrize("scale,order", [(1.0, 4), (4.0, 2)])
+def test_reference_tests_07_and_08_bars(scale, order):
+    """The reference's Tests 07 (order 4) and 08 (scale 4, order 2) hold every unknown within
+    0.06 of e^(-scale t) sin(r)/r at the save times 0.1, ..., 1 (dr = 0.1).  The restated rule
+    integrated with Tsit5 stays inside by a small margin (0.0555 at worst), where the
+    continuous operator's error would be near 1e-5: the bar was set for this scheme."""
+    s, d, ex = problems.spherical_laplacian(dr=0.1, order=order, scale=scale)
     spec = s.to_spec(d)
     lw, orc = lower(spec), OracleProblem(spec)
     g = lw.grids[0][1:-1]
     u = lw.u0.copy()
-    for t0, t1 in ((0.0, 0.5), (0.5, 1.0)):
-        u, _ = tsit5(lambda w, tt: orc.rhs(w, tt), u, t0, t1, 1e-8, 1e-8)
-        assert np.max(np.abs(u - math.exp(-t1) * np.sin(g) / g)) < 0.06
+    worst = 0.0
+    for k in range(10):
+        u, _ = tsit5(lambda w, tt: orc.rhs(w, tt), u, 0.1 * k, 0.1 * (k + 1), 1e-8, 1e-8)
+        worst = max(worst, float(np.max(np.abs(u - math.exp(-scale * 0.1 * (k + 1)) * np.sin(g) / g))))
+    assert 0.05 < worst < 0.06
 
 
 def test_spherical_rule_with_r0_as_an_unknown_is_refused():
