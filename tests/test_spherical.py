@@ -89,3 +89,20 @@ def test_spherical_rule_with_r0_as_an_unknown_is_refused():
                   [(t, Interval(0, 1)), (r, Interval(-1.0, 1.0))], [t, r], [u(r, t)])
     with pytest.raises(NotImplementedError):
         lower(s.to_spec(MOLFiniteDifference({r: 0.1}, t)))
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_spherical_rule_on_a_nonuniform_grid(order):
+    """On a grid given as points the rule's first derivative and nonlinear Laplacian use the
+    per-point tables (centered_difference.jl:32-56, half_offset_weights.jl:72-150)."""
+    r, t = IV("r"), IV("t")
+    u = Field("u")
+    Dt, Dr = Differential(t), Differential(r)
+    s = PDESystem([Eq(Dt(u(r, t)), Dr(r ** 2 * (1.0 + u(r, t)) * Dr(u(r, t))) / r ** 2)],
+                  [Eq(u(r, 0.0), sin(r) / r), Eq(Dr(u(0.0, t)), 0.0), Eq(u(1.0, t), exp(-t) * math.sin(1.0))],
+                  [(t, Interval(0, 1)), (r, Interval(0.0, 1.0))], [t, r], [u(r, t)])
+    spec = s.to_spec(MOLFiniteDifference({r: problems.stretched_points(31)}, t, approx_order=order))
+    lw, orc = lower(spec), OracleProblem(spec)
+    assert any(o.rows is not None for o in lw.ops)
+    v = lw.u0 * 1.01
+    assert np.array_equal(orc.rhs(v, 0.3), DescInterp(lw).rhs(v, 0.3))
