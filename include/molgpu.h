@@ -263,13 +263,15 @@ int mol_rhs_f32state(mol_plan* plan, float* du, const float* u, const float* p, 
 int mol_step_ssprk33(mol_plan* plan, double* u, const double* p, double t0, double dt, int64_t nsteps);
 int mol_step_ssprk33_f32state(mol_plan* plan, float* u, const float* p, double t0, double dt, int64_t nsteps);
 /* Same steps as mol_step_ssprk33, for callers that cannot let the call allocate device
- * memory (inside a CUDA-graph stream capture, under a fixed device-memory budget, in a
- * host callback).  No counterpart in the reference.  The two stage buffers live in one
- * static device array sized for at most 2^20 unknowns (16 MiB, held by every GPU that
- * loads the library until exit); larger plans get MOL_ERR_INVALID.  u and p must be
- * device memory.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race. */
+ * memory (a device-memory budget fixed up front, e.g. a pool that must not grow or one
+ * GPU divided between several plans at start-up; host callbacks, where CUDA allocation
+ * calls are not allowed).  No counterpart in the reference.  The two stage buffers live
+ * in one static device array sized for at most 2^20 unknowns (16 MiB, held by every GPU
+ * that loads the library until exit); larger plans get MOL_ERR_INVALID, as do host
+ * arrays (u and p must be device memory) and non-finite t0 or dt.  The plan's kernels
+ * are loaded by mol_plan_create, so the call loads nothing.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) and should come before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU race. */
 int mol_step_ssprk33_noalloc(mol_plan* plan, double* u, const double* p, double t0, double dt, int64_t nsteps);
 
 /* solve(prob, Tsit5(); abstol, reltol) from t0 to t1, in place on u

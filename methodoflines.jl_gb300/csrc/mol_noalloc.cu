@@ -2,12 +2,11 @@
 //
 // mol_step_ssprk33 keeps its two stage buffers (u1, u2) in the plan and allocates
 // them on first use; it may also stage host arrays and instantiate a CUDA graph.
-// Some callers cannot let a call allocate device memory: code that runs while a
-// stream is being captured into a CUDA graph (cudaMalloc is not a capturable
-// operation), solver loops whose device memory budget is fixed up front (memory
-// pools that must not grow, several plans sharing one GPU), and host callbacks in
-// which CUDA allocation calls are not allowed.  For them this variant takes its
-// stage buffers from one file-scope device array instead.
+// Some callers cannot let a call allocate device memory: solver loops whose device
+// memory budget is fixed up front (memory pools that must not grow, several plans
+// sharing one GPU whose memory was divided between them at start-up), and host
+// callbacks in which CUDA allocation calls are not allowed.  For them this variant
+// takes its stage buffers from one file-scope device array instead.
 //
 // Limits and sharing:
 //  - the array holds the stage buffers of at most MOL_NOALLOC_MAX_UNKNOWNS unknowns
@@ -19,9 +18,14 @@
 //    nothing in the array has to start at zero and stale contents of an earlier call
 //    are never observed;
 //  - the state `u` and parameters `p` must already be device memory; host arrays are
-//    rejected because staging them would need a device buffer.
+//    rejected because staging them would need a device buffer;
+//  - the plan's generated FP64 kernels are compiled and loaded by mol_plan_create, so a
+//    call loads no module; a nonlinear-Laplacian face buffer is used only if an earlier
+//    mol_step_ssprk33 / mol_rhs call on the plan already made one (the kernels evaluate
+//    the faces in the cell otherwise, with bit-identical results).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <mutex>
 
 #include "mol_kernels.cuh"
@@ -67,7 +71,9 @@ int scratch_address(mol_plan* plan, int dev, double** out) {
 extern "C" {
 
 int mol_step_ssprk33_noalloc(mol_plan* plan, double* u, const double* p, double t0, double dt, int64_t nsteps) {
-    if (!plan || !u || nsteps < 0 || !(dt == dt) || !(t0 == t0)) return MOL_ERR_INVALID;
+    if (!plan || !u || nsteps < 0) return MOL_ERR_INVALID;
+    if (!std::isfinite(dt) || !std::isfinite(t0))
+        return mol::set_err(plan, MOL_ERR_INVALID, "mol_step_ssprk33_noalloc: t0 and dt must be finite");
     if (plan->nunk > MOL_NOALLOC_MAX_UNKNOWNS)
         return mol::set_err(plan, MOL_ERR_INVALID,
                             "mol_step_ssprk33_noalloc: " + std::to_string(plan->nunk) +
@@ -81,6 +87,9 @@ int mol_step_ssprk33_noalloc(mol_plan* plan, double* u, const double* p, double 
     if (prev != plan->dev) cudaSetDevice(plan->dev);
     double* scratch = nullptr;
     int st = scratch_address(plan, plan->dev, &scratch);
+    // the FP64 group is loaded at plan creation; this only confirms it (no module load here)
+    if (!st && plan->use_jit && !(plan->jit.loaded & (1u << mol::JIT_FWD64)))
+        st = mol::set_err(plan, MOL_ERR_CUDA, "mol_step_ssprk33_noalloc: the plan's generated kernels are not loaded");
     if (!st) {
         const double* pp = p ? p : (const double*)plan->a64.params;
         double* u1 = scratch;

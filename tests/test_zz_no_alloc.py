@@ -1,7 +1,8 @@
 """The allocation-free SSPRK33 entry point (mol_step_ssprk33_noalloc).
 
-Callers that cannot let a call allocate device memory (stream capture, fixed
-memory budgets, host callbacks) use it instead of mol_step_ssprk33.  This file
+Callers that cannot let a call allocate device memory (a device-memory budget
+fixed up front, host callbacks where CUDA allocation calls are not allowed) use
+it instead of mol_step_ssprk33.  This file
 is collected last so a run that stops at the first failure has already run
 every other test.
 """
@@ -51,6 +52,34 @@ def test_noalloc_matches_step_ssprk33_two_calls(gpu_lib, name, kw):
     b.close()
 
 
+@pytest.mark.parametrize("face_buffer_first", [False, True])
+def test_noalloc_nonlinear_laplacian(gpu_lib, face_buffer_first):
+    """A nonlinear-Laplacian plan above the face-pass size (198 x 198 cells): on a fresh plan
+    the allocation-free steps evaluate every face in the cell; after an ordinary step has
+    made the plan's face buffer they read it.  Both must match mol_step_ssprk33."""
+    torch = _torch()
+    sys_, disc, _ = problems.nonlinear_diffusion(200, 1.3, 1000)
+    lw = lower(sys_.to_spec(disc))
+    dx = 1.0 / 199
+    dt = 0.125 * dx * dx / float(np.max(lw.u0)) ** 2
+    a = Plan(lw)
+    b = Plan(lw)
+    p = torch.tensor(lw.param_values, device="cuda")
+    if face_buffer_first:
+        w = torch.tensor(lw.u0, device="cuda")
+        a.step_ssprk33(w, dt, 1, t0=0.0, p=p)       # makes plan a's face buffer
+    ua = torch.tensor(lw.u0, device="cuda")
+    ub = torch.tensor(lw.u0, device="cuda")
+    for t0, n in ((0.0, 6), (6 * dt, 4)):
+        a.step_ssprk33_noalloc(ua, dt, n, t0=t0, p=p)
+        b.step_ssprk33(ub, dt, n, t0=t0, p=p)
+        torch.cuda.synchronize()
+        x, y = ua.cpu().numpy(), ub.cpu().numpy()
+        assert np.linalg.norm(x - y) <= TOL * np.linalg.norm(y)
+    a.close()
+    b.close()
+
+
 def test_noalloc_rejects_oversized_and_host_arrays(gpu_lib):
     torch = _torch()
     sys_, disc, ex = problems.brusselator(N=1024)       # 2,097,152 unknowns > 2^20
@@ -65,4 +94,9 @@ def test_noalloc_rejects_oversized_and_host_arrays(gpu_lib):
     with pytest.raises(L.MolError) as e:
         small.step_ssprk33_noalloc(np.zeros(small.n), 1e-9, 1)
     assert e.value.status == -1 and "device memory" in str(e.value)
+    ud = torch.zeros(small.n, dtype=torch.float64, device="cuda")
+    for t0, dt in ((0.0, float("inf")), (float("-inf"), 1e-9), (float("nan"), 1e-9)):
+        with pytest.raises(L.MolError) as e:
+            small.step_ssprk33_noalloc(ud, dt, 1, t0=t0)
+        assert e.value.status == -1
     small.close()
