@@ -1,17 +1,20 @@
 """Benchmark of the method-of-lines hot path on GB300.
 
-Headline workload: the 2-D periodic Brusselator at 1024 x 1024 (2 fields, 2,097,152
-unknowns), Float64, one fixed SSPRK33 step per bench step (the fixed-step run of the
-Brusselator configuration).  Metric: Mcell-updates/s, a cell-update being one unknown
-advanced by one full step.  Inputs are synthetic (the reference's own initial
-condition and forcing), resident in HBM when timing starts; the 48 MB of state fit in
-L2, so L2 is flushed (a 256 MB write) between timed steps, outside the timed events.
+Headline workload: the 3-D advection-diffusion-reaction system at 256^3 unknowns
+(16,777,216), Float64, one fixed SSPRK33 step per bench step:
+    u_t = div(K grad u) + 0.3 u_xy - (1, 0.5, 0) . grad u - 0.5 u^2
+on [0,1]^3, x and y periodic, z Dirichlet 0, K a seeded log-normal field at the faces,
+second-order centered diffusion and mixed terms, first-order upwind advection.  Metric:
+Mcell-updates/s, a cell-update being one unknown advanced by one full step.  Inputs are
+synthetic (seeded), resident in HBM when timing starts; the state (134 MB) and the three
+face-diffusivity arrays (3 x 134 MB) are larger than L2, so no flush is needed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--full]
 
-`--impl reference` times the CPU restatement of the reference's discretisation
-(C/OpenMP, oracle/c, on every host core) on the same workload; the reference itself
-is Julia and cannot run on this machine.  `--full` adds the long runs of every configuration.
+`--impl reference` times the CPU restatement of the reference's discretisation of the same
+workload (C/OpenMP, oracle/c/adr_oracle.c, on every host core); the reference itself is
+Julia and cannot run on this machine.  Secondary workloads (every other configuration at
+its size) follow in `workloads`; `--full` lengthens the Tsit5 horizon.
 """
 from __future__ import annotations
 
@@ -31,7 +34,10 @@ for _p in (ROOT, os.path.join(ROOT, "methodoflines.jl_gb300")):
 
 METRIC = "Mcell-updates/s + %HBM roofline; batched & adjoint vs plain, 1 GPU, 1e-10 rel"
 UNIT = "Mcell-updates/s"
-HEADLINE_N = 1024
+HEADLINE = {"N": 256, "nz_pts": 258}
+# algorithmic bytes per unknown and SSPRK33 step: 64 (u -> u1 16, (u, u1) -> u2 24,
+# (u, u2) -> u' 24) plus the three face-diffusivity arrays read once per stage (3 x 3 x 8)
+ADR_BYTES_PER_UNKNOWN_STEP = 64 + 3 * 24
 
 
 def _peaks():
@@ -43,8 +49,13 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-# FP64 pipe peak measured on this machine's GB300 with an 8-chain DFMA probe (TFLOP/s).
-FP64_PEAK_TFLOPS = 1.2558
+def _profile_numbers():
+    """Per-step DRAM traffic and FP64 flop counts taken from ncu captures (profiles/)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
 
 
 def _dist():
@@ -105,11 +116,38 @@ class ClockSampler:
         return res
 
 
+def adr_problem():
+    from molgpu import lower, problems
+    sys_, disc, ex = problems.adr3d(**HEADLINE)
+    return lower(sys_.to_spec(disc)), ex
+
+
+def headline_config(lw, ex, world):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": "adr3d_256^3_ssprk33_step", "unknowns": int(lw.n_unknowns), "fields": 1,
+            "grid": [256, 256, 256], "dt": float(ex["dt"]), "integrator": "SSPRK33 (fixed step)",
+            "equation": "u_t = div(K grad u) + 0.3 u_xy - (1, 0.5, 0).grad u - 0.5 u^2",
+            "bcs": "x, y periodic; z Dirichlet 0",
+            "discretisation": "approx_order 2, nonlinear Laplacian with K at the faces, UpwindScheme(1)",
+            "l2": "no flush: state (134 MB) and face-diffusivity arrays (3 x 134 MB) exceed L2",
+            "parallelism": "replicas only" if world > 1 else "single GPU"}
+
+
 def brusselator_plan(N):
     from molgpu import Plan, lower, problems
     sys_, disc, ex = problems.brusselator(N=N)
     lw = lower(sys_.to_spec(disc))
     return Plan(lw), lw, ex
+
+
+def fp64_peak_live():
+    """FP64 pipe peak on this GPU, measured now (eight independent DFMA chains per thread)."""
+    import ctypes as C
+    from molgpu import _lib as L
+    w, t = C.c_double(), C.c_double()
+    if L.lib().mol_diag_fp64_rate(32, C.byref(w), C.byref(t)) != 0:
+        return None
+    return t.value
 
 
 # ---------------------------------------------------------------------------------------
@@ -119,6 +157,7 @@ def brusselator_plan(N):
 def run_ours(args, rank, world):
     import numpy as np
     import torch
+    from molgpu import Plan
     from molgpu import _lib as L
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
@@ -126,15 +165,18 @@ def run_ours(args, rank, world):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     hbm_peak, peak_kind = _peaks()
-    plan, lw, ex = brusselator_plan(HEADLINE_N)
+    t_setup = time.perf_counter()
+    lw, ex = adr_problem()
+    plan = Plan(lw)
     plan.set_stream(stream.cuda_stream)
+    setup_s = time.perf_counter() - t_setup
     n = lw.n_unknowns
-    dt = ex["dt_ssprk"]
+    dt = ex["dt"]
     p = torch.tensor(lw.param_values, device=dev)
     u = torch.tensor(lw.u0, device=dev)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    fp64_peak = fp64_peak_live()
     t = 0.0
-    for _ in range(args.warmup):
+    for _ in range(max(3, args.warmup)):
         plan.step_ssprk33(u, dt, 1, t0=t, p=p)
         t += dt
     torch.cuda.synchronize()
@@ -149,7 +191,6 @@ def run_ours(args, rank, world):
     wall0 = time.perf_counter()
     reps = max(1, args.steps)
     for _ in range(reps):
-        flush.fill_(1.0)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -158,13 +199,14 @@ def run_ours(args, rank, world):
         evs.append((e0, e1))
         t += dt
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     wall = time.perf_counter() - wall0
     launches = L.lib().mol_launch_count() - launches0
     # keep the GPU busy a little longer so the clock sampler sees the kernels under load
     tl = time.perf_counter()
     while time.perf_counter() - tl < 1.0:
-        for _ in range(50):
-            plan.step_ssprk33(u, dt, 1, t0=t, p=p)
+        plan.step_ssprk33(u, dt, 16, t0=t, p=p)
         torch.cuda.synchronize()
     clocks = sampler.stop()
     step_ms = [a.elapsed_time(b) for a, b in evs]
@@ -175,31 +217,20 @@ def run_ours(args, rank, world):
         ms_total = float(tt.item())
     ms_per_step = ms_total / reps
     value = world * n * reps / (ms_total * 1e-3) / 1e6
-    # roofline of the dominant kernel: the SSPRK33 stage kernel, 3 launches per step,
-    # 64 algorithmic bytes per unknown and step (16 + 24 + 24), FP64 state
-    bytes_per_step = 64.0 * n
+    prof = _profile_numbers()
+    bytes_per_step = float(ADR_BYTES_PER_UNKNOWN_STEP) * n
     achieved = bytes_per_step / (ms_per_step * 1e-3) / 1e9
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("brusselator_1024_ssprk33_step_bytes")
-        except Exception:
-            traffic = None
-    fp64_per_unknown = None
-    if os.path.exists(prof):
-        try:
-            fp64_per_unknown = json.load(open(prof)).get("brusselator_1024_fp64_flops_per_unknown_step")
-        except Exception:
-            pass
-    # e2e: the public C-ABI call with pinned host buffers (H2D + step + D2H each step)
+    traffic = prof.get("adr3d_256_ssprk33_step_bytes")
+    fp64_per_unknown = prof.get("adr3d_256_fp64_flops_per_unknown_step")
+    fp64_achieved = fp64_per_unknown * n / (ms_per_step * 1e-3) / 1e12 if fp64_per_unknown else None
+    # e2e: the public C-ABI call with pinned host buffers (H2D + step + D2H in every call)
     host = torch.empty(n, dtype=torch.float64, pin_memory=True)
     host.copy_(torch.from_numpy(lw.u0))
     hnp = host.numpy()
     pnp = lw.param_values.copy()
     for _ in range(2):
         plan.step_ssprk33(hnp, dt, 1, t0=0.0, p=pnp)
-    e2e_reps = max(3, min(reps, 50))
+    e2e_reps = max(3, min(reps, 30))
     te = time.perf_counter()
     for k in range(e2e_reps):
         plan.step_ssprk33(hnp, dt, 1, t0=k * dt, p=pnp)
@@ -211,70 +242,72 @@ def run_ours(args, rank, world):
         "unit": UNIT,
         "n_gpus": world,
         "steps": reps,
-        "warmup": args.warmup,
+        "warmup": max(3, args.warmup),
         "ms_per_step": ms_per_step,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic: the reference Brusselator test's initial condition and forcing "
-                "(test/Brusselator/brusselator_eq.jl), 1024x1024 periodic grid",
-        "config": {"workload": "brusselator2d_1024x1024_periodic_ssprk33_step", "unknowns": n,
-                   "fields": 2, "grid": [1024, 1024], "dt": dt, "integrator": "SSPRK33 (fixed step)",
-                   "l2": "flushed between timed steps (256 MB write, outside the timed events)",
-                   "parallelism": "replicas only" if world > 1 else "single GPU",
-                   "codegen": bool(plan.uses_codegen)},
+        "data": "synthetic: seeded log-normal diffusivity (64 random Fourier modes, correlation length 0.1) "
+                "and a Gaussian initial blob, 256^3 unknowns",
+        "config": headline_config(lw, ex, world),
+        "codegen": bool(plan.uses_codegen),
+        "setup_s": setup_s,
         "gpu_launches": int(launches),
         "wall_s_timed_loop": wall,
+        "step_ms_min_median": [min(step_ms), statistics.median(step_ms)],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "peak_source": peak_kind,
-                     "kernel": "k_ssprk_t (generated cell, 3 stage launches per step)",
-                     "algorithmic_bytes_per_unknown_step": 64,
+                     "kernel": "one SSPRK33 step: k_faces_t (faces of the three K terms) + k_ssprk_t, per stage",
+                     "algorithmic_bytes_per_unknown_step": ADR_BYTES_PER_UNKNOWN_STEP,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 128^3 step, x 8"
+                     if traffic else None,
                      "note": "FP64-pipe bound on GB300 (FP64 = 1/64 of FP32); see fp64"},
-        "fp64": {"peak_tflops": FP64_PEAK_TFLOPS,
+        "fp64": {"peak_tflops_measured_now": fp64_peak,
                  "flops_per_unknown_step": fp64_per_unknown,
-                 "achieved_tflops": (fp64_per_unknown * n / (ms_per_step * 1e-3) / 1e12) if fp64_per_unknown else None,
-                 "frac": (fp64_per_unknown * n / (ms_per_step * 1e-3) / 1e12 / FP64_PEAK_TFLOPS)
-                 if fp64_per_unknown else None},
+                 "achieved_tflops": fp64_achieved,
+                 "frac": fp64_achieved / fp64_peak if (fp64_achieved and fp64_peak) else None},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "path": "mol_step_ssprk33 with pinned host buffers, one step per call"},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(lw, ex, samples=1)
+        out["cpu_baseline"] = cpu_baseline(lw, ex)
     if rank == 0 and not args.headline_only:
-        out["workloads"] = workloads(args, dev, stream)
+        out["workloads"] = workloads(args, dev, stream, (plan, lw, ex))
+    plan.close()
     return out
 
 
-def cpu_baseline(lw, ex, samples=1):
+def cpu_baseline(lw, ex):
     """The C/OpenMP restatement of the reference discretisation and SSPRK33 (oracle/c) on the
-    host cores: SSPRK33 steps of the same 1024x1024 system, in chunks of 10 steps until at
-    least 10 s have passed, on every core, then 10 steps on one core."""
-    from oracle.c_port import Brusselator, max_threads
-    b = Brusselator(lw)
-    dt = ex["dt_ssprk"]
-    u = b.ssprk33(lw.u0, 0.0, dt, 1)      # warm (pages, threads)
+    host cores: SSPRK33 steps of the same 256^3 system on every core until at least 10 s have
+    passed (at most 400 steps), then one step on one core."""
+    import numpy as np
+    from oracle.c_port import ADR3D, max_threads
+    a = ADR3D(lw)
+    dt = ex["dt"]
+    s = np.array(lw.u0, copy=True)
+    a.ssprk33(s, dt, 1, out=s)                     # warm (pages, threads)
     steps, el = 0, 0.0
-    while el < 10.0 and steps < 4000:
+    while el < 10.0 and steps < 400:
         t0 = time.perf_counter()
-        u = b.ssprk33(u, steps * dt, dt, 10)
+        a.ssprk33(s, dt, 2, out=s)
         el += time.perf_counter() - t0
-        steps += 10
+        steps += 2
     cores = max_threads()
     t0 = time.perf_counter()
-    b.ssprk33(lw.u0, 0.0, dt, 10, 1)
-    one = lw.n_unknowns * 10 / (time.perf_counter() - t0) / 1e6
+    a.ssprk33(lw.u0, dt, 1, 1)
+    one = lw.n_unknowns / (time.perf_counter() - t0) / 1e6
     return {"value": lw.n_unknowns * steps / el / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{steps} SSPRK33 steps of the 1024x1024 Brusselator (2,097,152 unknowns) in "
-                      f"{el:.1f} s, C/OpenMP restatement of the reference discretisation on {cores} "
-                      f"threads; one thread: {one:.1f} Mcell-updates/s"}
+            "sample": f"{steps} SSPRK33 steps of the 256^3 ADR system (16,777,216 unknowns) in {el:.1f} s, "
+                      f"C/OpenMP restatement of the reference discretisation on {cores} threads; "
+                      f"one thread: {one:.1f} Mcell-updates/s"}
 
 
 # ---------------------------------------------------------------------------------------
-# secondary workloads (every configuration at its size; the ensemble runs 1000 steps and
-# Tsit5 a longer horizon with --full)
+# secondary workloads (every configuration at its size)
 # ---------------------------------------------------------------------------------------
 
 def _time(fn, stream, reps, warm=True):
@@ -292,10 +325,10 @@ def _time(fn, stream, reps, warm=True):
     return e0.elapsed_time(e1) / reps
 
 
-def workloads(args, dev, stream):
+def workloads(args, dev, stream, adr):
     import numpy as np
     import torch
-    from molgpu import Batch, Plan, lower, problems
+    from molgpu import Plan, lower, problems
     hbm_peak, _ = _peaks()
     res = {}
     full = args.full
@@ -326,10 +359,11 @@ def workloads(args, dev, stream):
         u32 = torch.tensor(lw.u0, device=dev, dtype=torch.float32)
         du32 = torch.zeros_like(u32)
         ms32 = _time(lambda: plan.rhs(du32, u32, None, 0.5), stream, 20)
-        res[f"brusselator_{N}"] = {"unknowns": n, "rhs_ms": ms, "rhs_Mcell_s": n / ms / 1e3,
-                                   "rhs_hbm_frac": 16 * n / (ms * 1e-3) / 1e9 / hbm_peak,
-                                   "ssprk33_step_ms": ms_step, "ssprk33_Mcell_s": n / ms_step / 1e3,
-                                   "f32state_rhs_ms": ms32, "f32state_rhs_hbm_frac": 8 * n / (ms32 * 1e-3) / 1e9 / hbm_peak}
+        row = {"unknowns": n, "rhs_ms": ms, "rhs_Mcell_s": n / ms / 1e3,
+               "rhs_hbm_frac": 16 * n / (ms * 1e-3) / 1e9 / hbm_peak,
+               "ssprk33_step_ms": ms_step, "ssprk33_Mcell_s": n / ms_step / 1e3,
+               "ssprk33_hbm_frac": 64 * n / (ms_step * 1e-3) / 1e9 / hbm_peak,
+               "f32state_rhs_ms": ms32, "f32state_rhs_hbm_frac": 8 * n / (ms32 * 1e-3) / 1e9 / hbm_peak}
         if N == 256:
             # explicit Tsit5 on this stiff system is step-size limited by diffusion (dt ~ 6.6e-7):
             # t = 11.5 needs ~1.7e7 steps, so the timed run covers a short horizon
@@ -337,8 +371,32 @@ def workloads(args, dev, stream):
             t_end = 0.02 if full else 0.002
             t0 = time.perf_counter()
             st = plan.solve_tsit5(uh, 0.0, t_end, 1e-8, 1e-8)
-            res[f"brusselator_{N}"]["tsit5"] = {"t_end": t_end, "wall_s": time.perf_counter() - t0,
-                                                "naccept": st["naccept"], "nreject": st["nreject"]}
+            row["tsit5"] = {"t_end": t_end, "wall_s": time.perf_counter() - t0,
+                            "naccept": st["naccept"], "nreject": st["nreject"]}
+        else:
+            # end to end through mol_step_ssprk33 on pinned host buffers, and the C/OpenMP
+            # restatement on the host cores, one step per call / per sample step
+            from oracle.c_port import Brusselator, max_threads
+            host = torch.empty(n, dtype=torch.float64, pin_memory=True)
+            host.copy_(torch.from_numpy(lw.u0))
+            hnp = host.numpy()
+            for _ in range(2):
+                plan.step_ssprk33(hnp, ex["dt_ssprk"], 1)
+            te = time.perf_counter()
+            for k in range(30):
+                plan.step_ssprk33(hnp, ex["dt_ssprk"], 1, t0=k * ex["dt_ssprk"])
+            row["e2e_Mcell_s"] = n * 30 / (time.perf_counter() - te) / 1e6
+            b = Brusselator(lw)
+            s = b.ssprk33(lw.u0, 0.0, ex["dt_ssprk"], 2)
+            steps, el = 0, 0.0
+            while el < 3.0:
+                t0 = time.perf_counter()
+                s = b.ssprk33(s, steps * ex["dt_ssprk"], ex["dt_ssprk"], 20)
+                el += time.perf_counter() - t0
+                steps += 20
+            row["cpu_port_Mcell_s"] = n * steps / el / 1e6
+            row["cpu_port_cores"] = max_threads()
+        res[f"brusselator_{N}"] = row
         plan.close()
 
     # config 3: Burgers WENO5, SSPRK33 for 20000 steps and the discrete adjoint
@@ -351,7 +409,6 @@ def workloads(args, dev, stream):
     ud = torch.tensor(lw.u0, device=dev)
     plan.step_ssprk33(ud, ex["dt"], 32)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     fwd_ms = _time(lambda: plan.step_ssprk33(ud, ex["dt"], nsteps), stream, 1, warm=False)
     tgt = torch.tensor(ex["target"], device=dev)
     g = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -376,18 +433,12 @@ def workloads(args, dev, stream):
                                   "loss": loss, "dLdnu": float(gp.item())}
     plan.close()
 
-    # config 5: 3-D ADR at 256^3 (RHS, SSPRK33, adjoint dL/dK over 500 steps)
-    t0 = time.perf_counter()
-    sys_, disc, ex = problems.adr3d(N=256, nz_pts=258)
-    lw = lower(sys_.to_spec(disc))
-    setup = time.perf_counter() - t0
-    plan = Plan(lw)
-    plan.set_stream(stream.cuda_stream)
+    # config 5 beyond the headline step: RHS, Float32 state, adjoint dL/dK over 500 steps
+    plan, lw, ex = adr
     n = lw.n_unknowns
     ud = torch.tensor(lw.u0, device=dev)
     du = torch.zeros_like(ud)
     ms = _time(lambda: plan.rhs(du, ud, None, 0.1), stream, 5)
-    ms_step = _time(lambda: plan.step_ssprk33(ud, ex["dt"], 16), stream, 1) / 16
     u32 = torch.tensor(lw.u0, device=dev, dtype=torch.float32)
     du32 = torch.zeros_like(u32)
     ms32 = _time(lambda: plan.rhs(du32, u32, None, 0.1), stream, 5)
@@ -406,19 +457,17 @@ def workloads(args, dev, stream):
     _, nfw0 = plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=0, dLdaux=gaux)
     torch.cuda.synchronize()
     adj_all_s = time.perf_counter() - ta
-    side = round(n ** (1 / 3))
-    res[f"adr3d_{side}^3"] = {"unknowns": n, "setup_s": setup, "rhs_ms": ms, "rhs_Mcell_s": n / ms / 1e3,
-                              "rhs_hbm_frac": (16 + 24) * n / (ms * 1e-3) / 1e9 / hbm_peak,
-                              "ssprk33_ms_per_step": ms_step, "ssprk33_Mcell_s": n / ms_step / 1e3,
-                              "f32state_rhs_ms": ms32,
-                              "f32state_rhs_hbm_frac": (8 + 12) * n / (ms32 * 1e-3) / 1e9 / hbm_peak,
-                              "adjoint_steps": adj_steps, "adjoint_dLdK_64_snapshots_s": adj_s,
-                              "adjoint_64_snapshots_vs_forward": adj_s / (fwd * 1e-3),
-                              "adjoint_64_snapshots_forward_steps": nfw64,
-                              "adjoint_dLdK_states_kept_s": adj_all_s,
-                              "adjoint_states_kept_vs_forward": adj_all_s / (fwd * 1e-3),
-                              "adjoint_states_kept_forward_steps": nfw0}
-    plan.close()
+    res["adr3d_256^3"] = {"unknowns": n, "rhs_ms": ms, "rhs_Mcell_s": n / ms / 1e3,
+                          "rhs_hbm_frac": (16 + 24) * n / (ms * 1e-3) / 1e9 / hbm_peak,
+                          "f32state_rhs_ms": ms32,
+                          "f32state_rhs_hbm_frac": (8 + 12) * n / (ms32 * 1e-3) / 1e9 / hbm_peak,
+                          "forward_500_steps_ms": fwd,
+                          "adjoint_steps": adj_steps, "adjoint_dLdK_64_snapshots_s": adj_s,
+                          "adjoint_64_snapshots_vs_forward": adj_s / (fwd * 1e-3),
+                          "adjoint_64_snapshots_forward_steps": nfw64,
+                          "adjoint_dLdK_states_kept_s": adj_all_s,
+                          "adjoint_states_kept_vs_forward": adj_all_s / (fwd * 1e-3),
+                          "adjoint_states_kept_forward_steps": nfw0}
 
     # config 4: batched ensemble of uneven nonlinear-diffusion problems vs sequential plain solves
     res["batched_nonlinear_diffusion"] = batched(args, dev, stream)
@@ -426,6 +475,9 @@ def workloads(args, dev, stream):
 
 
 def batched(args, dev, stream):
+    """The configuration's 4096 members for its 1000 SSPRK33 steps, FP64 and Float32 state
+    from the same initial states (the Float32 error is taken between the two runs), against
+    sequential plain solves of a stratified sample of the members for the same 1000 steps."""
     import numpy as np
     import torch
     from molgpu import Batch, Plan, lower, problems
@@ -444,23 +496,20 @@ def batched(args, dev, stream):
     batch.set_stream(stream.cuda_stream)
     setup = time.perf_counter() - t0
     total = int(batch.offsets[-1])
-    steps = 1000 if args.full else 20
-    u = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev)
-    batch.step_ssprk33(u, dts, 2)          # autotune + warm
+    steps = 1000
+    packed = batch.pack([lw.u0 for lw in lws])
+    w = torch.tensor(packed, device=dev)
+    batch.step_ssprk33(w, dts, 2)          # autotune + warm
+    w32 = w.float()
+    batch.step_ssprk33(w32, dts, 2)
+    del w, w32
+    u = torch.tensor(packed, device=dev)
+    u32 = u.float()
     torch.cuda.synchronize()
     ms = _time(lambda: batch.step_ssprk33(u, dts, steps), stream, 1, warm=False)
-    u32 = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev, dtype=torch.float32)
-    u64 = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev)
-    batch.step_ssprk33(u64, dts, steps)
-    batch.step_ssprk33(u32, dts, 2)
     ms32 = _time(lambda: batch.step_ssprk33(u32, dts, steps), stream, 1, warm=False)
-    # the f32-state error is measured on a fresh run of the same steps
-    a = torch.tensor(batch.pack([lw.u0 for lw in lws]), device=dev)
-    b = a.float()
-    batch.step_ssprk33(a, dts, steps)
-    batch.step_ssprk33(b, dts, steps)
-    torch.cuda.synchronize()
-    f32err = float(torch.linalg.norm(b.double() - a) / torch.linalg.norm(a))
+    batch.check()
+    f32err = float(torch.linalg.norm(u32.double() - u) / torch.linalg.norm(u))
     # sequential plain solves (one plan per instance, same steps) on a stratified sample
     idx = list(range(0, count, max(1, count // 64)))
     seq_ms = 0.0
@@ -479,7 +528,8 @@ def batched(args, dev, stream):
             "f32state_batched_ms": ms32, "f32state_rel_err_vs_f64": f32err,
             "schedule": sched,
             "sequential_plain_ms_estimated": seq_ms,
-            "sequential_sample": f"{len(idx)} of {count} instances, scaled by {count / len(idx):.1f}",
+            "sequential_sample": f"{len(idx)} of {count} instances ({steps} steps each), scaled by "
+                                 f"{count / len(idx):.1f}",
             "batched_vs_sequential": seq_ms / ms}
 
 
@@ -490,30 +540,35 @@ def batched(args, dev, stream):
 def run_reference(args, rank, world):
     """The reference's CPU path for the headline workload: the reference itself is Julia and
     cannot run on this machine, so its discretisation and SSPRK33 are timed through the
-    C/OpenMP restatement (oracle/c) on every host core, K steps after W warm-up steps."""
+    C/OpenMP restatement (oracle/c/adr_oracle.c) on every host core: W warm-up steps, then
+    at least K steps and at least one second."""
     if rank != 0:
         return None
-    from molgpu import lower, problems
-    from oracle.c_port import Brusselator, max_threads
-    sys_, disc, ex = problems.brusselator(N=HEADLINE_N)
-    lw = lower(sys_.to_spec(disc))
-    b = Brusselator(lw)
-    dt = ex["dt_ssprk"]
+    import numpy as np
+    from oracle.c_port import ADR3D, max_threads
+    lw, ex = adr_problem()
+    a = ADR3D(lw)
+    dt = ex["dt"]
     w = max(0, args.warmup)
-    u = b.ssprk33(lw.u0, 0.0, dt, w) if w else lw.u0.copy()
+    s = np.array(lw.u0, copy=True)
+    if w:
+        a.ssprk33(s, dt, w, out=s)
     reps = max(1, args.steps)
-    t0 = time.perf_counter()
-    b.ssprk33(u, w * dt, dt, reps)
-    el = time.perf_counter() - t0
-    value = lw.n_unknowns * reps / el / 1e6
+    steps, el = 0, 0.0
+    while steps < reps or el < 1.0:
+        t0 = time.perf_counter()
+        a.ssprk33(s, dt, 1, out=s)
+        el += time.perf_counter() - t0
+        steps += 1
+    value = lw.n_unknowns * steps / el / 1e6
     cores = max_threads()
-    sample = (f"{reps} SSPRK33 steps of the 1024x1024 Brusselator (2,097,152 unknowns) after {w} warm-up "
-              f"steps; C/OpenMP restatement of the reference discretisation on {cores} threads (the "
+    sample = (f"{steps} SSPRK33 steps of the 256^3 ADR system (16,777,216 unknowns) after {w} warm-up steps, "
+              f"{el:.2f} s; C/OpenMP restatement of the reference discretisation on {cores} threads (the "
               "reference is Julia and is not runnable here)")
-    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": reps, "warmup": w,
-            "ms_per_step": el / reps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": w,
+            "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "brusselator2d_1024x1024_periodic_ssprk33_step"},
+            "config": headline_config(lw, ex, world),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -544,6 +599,18 @@ def run_case(name, args):
         torch.cuda.synchronize()
         out.update(loss=loss, dLdnu=float(gp.item()))
         plan.close()
+    elif name == "burgers_steps":
+        # Burgers WENO5 (65,536 unknowns): 64 SSPRK33 steps
+        sys_, disc, ex = problems.burgers()
+        lw = lower(sys_.to_spec(disc))
+        plan = Plan(lw)
+        plan.set_stream(stream.cuda_stream)
+        u = torch.tensor(lw.u0, device=dev)
+        for _ in range(4):
+            plan.step_ssprk33(u, ex["dt"], 16)
+        torch.cuda.synchronize()
+        out.update(norm=float(torch.linalg.norm(u)))
+        plan.close()
     elif name == "ensemble":
         # the first 512 ensemble members, 5 steps of the tiled persistent kernel
         lws, dts = [], []
@@ -561,18 +628,22 @@ def run_case(name, args):
         batch.check()
         out.update(unknowns=int(batch.offsets[-1]), norm=float(torch.linalg.norm(u)))
         batch.close()
-    elif name in ("brusselator_rhs_generated", "brusselator_rhs_interpreted"):
-        # one RHS of the 1024^2 Brusselator through the generated cell or the interpreter
+    elif name in ("brusselator_rhs_generated", "brusselator_rhs_interpreted", "brusselator_steps"):
+        # one RHS (or SSPRK33 steps) of the 1024^2 Brusselator through the generated cell or
+        # the interpreter
         if name.endswith("interpreted"):
             os.environ["MOL_DISABLE_CODEGEN"] = "1"
-        sys_, disc, _ = problems.brusselator(N=1024)
+        sys_, disc, ex = problems.brusselator(N=1024)
         lw = lower(sys_.to_spec(disc))
         plan = Plan(lw)
         plan.set_stream(stream.cuda_stream)
         u = torch.tensor(lw.u0, device=dev)
         du = torch.zeros_like(u)
         for _ in range(5):
-            plan.rhs(du, u, None, 0.5)
+            if name == "brusselator_steps":
+                plan.step_ssprk33(u, ex["dt_ssprk"], 1)
+            else:
+                plan.rhs(du, u, None, 0.5)
         torch.cuda.synchronize()
         out.update(codegen=plan.uses_codegen, norm=float(torch.linalg.norm(du)))
         plan.close()
@@ -586,16 +657,19 @@ def run_case(name, args):
             L.check(L.lib().mol_diag_fp64_rate(act, C.byref(w), C.byref(t)))
             rows.append({"active_lanes": act, "warp_fma_G_per_s": w.value / 1e9, "lane_tflops": t.value})
         out.update(rows=rows)
-    elif name == "adr3d_rhs":
-        # one RHS of the 3-D ADR problem at 128^3
-        sys_, disc, _ = problems.adr3d(N=128, nz_pts=130)
+    elif name in ("adr3d_rhs", "adr3d_steps"):
+        # one RHS (or SSPRK33 steps) of the 3-D ADR problem at 128^3
+        sys_, disc, ex = problems.adr3d(N=128, nz_pts=130)
         lw = lower(sys_.to_spec(disc))
         plan = Plan(lw)
         plan.set_stream(stream.cuda_stream)
         u = torch.tensor(lw.u0, device=dev)
         du = torch.zeros_like(u)
         for _ in range(5):
-            plan.rhs(du, u, None, 0.1)
+            if name == "adr3d_steps":
+                plan.step_ssprk33(u, ex["dt"], 1)
+            else:
+                plan.rhs(du, u, None, 0.1)
         torch.cuda.synchronize()
         out.update(norm=float(torch.linalg.norm(du)))
         plan.close()
@@ -604,18 +678,20 @@ def run_case(name, args):
     print(json.dumps(out), flush=True)
 
 
+CASES = ["burgers_adjoint", "burgers_steps", "ensemble", "brusselator_rhs_generated", "brusselator_rhs_interpreted",
+         "brusselator_steps", "adr3d_rhs", "adr3d_steps", "fp64_lanes"]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--full", action="store_true", help="long runs of every configuration")
+    ap.add_argument("--full", action="store_true", help="longer Tsit5 horizon")
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", default=None,
-                    choices=["burgers_adjoint", "ensemble", "brusselator_rhs_generated",
-                             "brusselator_rhs_interpreted", "adr3d_rhs", "fp64_lanes"],
+    ap.add_argument("--case", default=None, choices=CASES,
                     help="run one small single-path case (for profiling) and exit")
     args = ap.parse_args()
     if args.case:

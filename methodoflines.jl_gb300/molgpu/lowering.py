@@ -179,6 +179,38 @@ def host_eval(t, coords: Dict[str, np.ndarray], functions, t_value=None):
     raise ValueError(f"cannot evaluate {k} on the host")
 
 
+def eval_on_mesh(t, axes, ivs, functions, shape) -> np.ndarray:
+    """host_eval of a coordinate-only expression at every point of the tensor grid `axes`
+    (one 1-D coordinate array per dimension), as an array of `shape`.  Every operation is
+    elementwise, so the grid is cut into slabs of its last dimension evaluated on a thread
+    pool (numpy releases the GIL inside its loops): the values are those of one evaluation
+    over the whole mesh, and a 256^3 face array takes seconds instead of a minute."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    total = int(np.prod(shape))
+    nlast = len(axes[-1]) if axes else 1
+    workers = max(1, min(os.cpu_count() or 1, 32, nlast))
+    if total < (1 << 18) or workers == 1 or len(axes) == 0:
+        mesh = np.meshgrid(*axes, indexing="ij")
+        v = host_eval(t, {x: g for x, g in zip(ivs, mesh)}, functions)
+        return np.broadcast_to(np.asarray(v, dtype=np.float64), shape).copy()
+    out = np.empty(shape, dtype=np.float64)
+    bounds = np.linspace(0, nlast, min(nlast, 4 * workers) + 1).astype(int)
+
+    def slab(k):
+        a, b = int(bounds[k]), int(bounds[k + 1])
+        if b <= a:
+            return
+        sub = list(axes[:-1]) + [axes[-1][a:b]]
+        mesh = np.meshgrid(*sub, indexing="ij")
+        v = host_eval(t, {x: g for x, g in zip(ivs, mesh)}, functions)
+        out[..., a:b] = np.broadcast_to(np.asarray(v, dtype=np.float64), shape[:-1] + (b - a,))
+
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        list(ex.map(slab, range(len(bounds) - 1)))
+    return out
+
+
 def _leaves(t):
     """Set of leaf kinds in t ('field', 'param', 'iv', 't', 'D', 'term', ...)."""
     k = t[0]
@@ -674,9 +706,8 @@ class _Lowerer:
         lw = self.lw
         key = ("cell", t)
         if key not in lw.aux_keys:
-            coords = lw.interior_coords()
-            v = host_eval(t, coords, lw.functions)
-            arr = np.broadcast_to(np.asarray(v, dtype=np.float64), lw.interior_shape)
+            axes = [lw.grids[j][lw.lower[j]:lw.npts[j] - lw.upper[j]] for j in range(len(lw.ivs))]
+            arr = eval_on_mesh(t, axes, lw.ivs, lw.functions, tuple(lw.interior_shape))
             lw.aux_keys[key] = len(lw.aux)
             lw.aux.append(np.ascontiguousarray(arr.reshape(-1, order="F")))
         return ("aux", lw.aux_keys[key])
@@ -769,9 +800,7 @@ class _Lowerer:
                 axes.append(xh)
             else:
                 axes.append(lw.grids[k])
-        mesh = np.meshgrid(*axes, indexing="ij")
-        coords = {lw.ivs[k]: mesh[k] for k in range(nd)}
-        v = np.broadcast_to(np.asarray(host_eval(t, coords, lw.functions), dtype=np.float64), tuple(ext)).copy()
+        v = eval_on_mesh(t, axes, lw.ivs, lw.functions, tuple(ext))
         sl = [slice(None)] * nd
         sl[j] = ~valid
         v[tuple(sl)] = 0.0

@@ -31,3 +31,31 @@ def test_c_port_ssprk33_matches_numpy_oracle(nthreads):
     got = b.ssprk33(lw.u0, 1.0, ex["dt_ssprk"], 25, nthreads)
     ref, _ = ssprk33(lambda v, t: orc.rhs(v, t), lw.u0, 1.0, ex["dt_ssprk"], 25)
     assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("N,nz", [(8, 10), (12, 11)])
+def test_c_port_adr_rhs_matches_numpy_oracle(N, nz):
+    """The 3-D advection-diffusion-reaction restatement (oracle/c/adr_oracle.c) against the
+    numpy oracle's general evaluation of the same system."""
+    from oracle.c_port import ADR3D
+    sys_, disc, _ = problems.adr3d(N=N, nz_pts=nz)
+    spec = sys_.to_spec(disc)
+    lw = lower(spec)
+    a, orc = ADR3D(lw), OracleProblem(spec)
+    u = lw.u0 + 0.05 * np.random.default_rng(N).standard_normal(lw.n_unknowns)
+    ref = orc.rhs(u, 0.1)
+    got = a.rhs(u)
+    assert np.linalg.norm(got - ref) <= 1e-13 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("nthreads", [1, 0])
+def test_c_port_adr_ssprk33_matches_numpy_oracle(nthreads):
+    from oracle.c_port import ADR3D
+    sys_, disc, ex = problems.adr3d(N=8, nz_pts=10)
+    spec = sys_.to_spec(disc)
+    lw = lower(spec)
+    a, orc = ADR3D(lw), OracleProblem(spec)
+    dt = ex["dt"]
+    got = a.ssprk33(lw.u0, dt, 12, nthreads)
+    ref, _ = ssprk33(lambda v, t: orc.rhs(v, t), lw.u0, 0.0, dt, 12)
+    assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
