@@ -259,9 +259,16 @@ int mol_rhs(mol_plan* plan, double* du, const double* u, const double* p, double
 int mol_rhs_f32state(mol_plan* plan, float* du, const float* u, const float* p, double t);
 
 /* solve(prob, SSPRK33(); dt, adaptive=false) for nsteps steps from t0, in place on u
- * (OrdinaryDiffEqSSPRK SSPRK33, used at benchmark/weno/suite.jl:291-295). */
+ * (OrdinaryDiffEqSSPRK SSPRK33, used at benchmark/weno/suite.jl:291-295).  Every step's
+ * result is tested for NaN and Inf on the GPU (OrdinaryDiffEq's default unstable_check,
+ * which ends such a solve with ReturnCode.Unstable).  On host state the call waits for the
+ * steps and returns MOL_ERR_NONFINITE when one produced such a value; on device state it
+ * stays asynchronous and mol_plan_check reports it. */
 int mol_step_ssprk33(mol_plan* plan, double* u, const double* p, double t0, double dt, int64_t nsteps);
 int mol_step_ssprk33_f32state(mol_plan* plan, float* u, const float* p, double t0, double dt, int64_t nsteps);
+/* Waits for the plan's stream and returns MOL_ERR_NONFINITE (then clears the condition) when
+ * an SSPRK33 step since the last check, on this plan, produced a NaN or Inf state value. */
+int mol_plan_check(mol_plan* plan);
 /* Same steps as mol_step_ssprk33, for callers that cannot let the call allocate device
  * memory (a device-memory budget fixed up front, e.g. a pool that must not grow or one
  * GPU divided between several plans at start-up; host callbacks, where CUDA allocation
@@ -285,7 +292,8 @@ int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, doubl
  *   MOL_LOSS_LAMBDA:  `target` is dL/du(T) supplied by the caller
  * Outputs (any may be NULL): uT, loss, dL/du0 (n_unknowns), dL/dp (nparams),
  * dL/daux (concatenated aux arrays in descriptor order).  nsnap checkpoints
- * (binomial/revolve schedule) bound the stored states. */
+ * (binomial/revolve schedule) bound the stored states.  MOL_ERR_NONFINITE when a forward
+ * step produced a NaN or Inf state value (as mol_plan_check) or the loss is not finite. */
 #define MOL_LOSS_MISFIT 0
 #define MOL_LOSS_LAMBDA 1
 int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, double t0, double dt,
@@ -318,8 +326,9 @@ int mol_batch_step_ssprk33_f32state(mol_batch* batch, float* u_packed, const dou
  * instance.  0 leaves a setting as it is; all three 0 autotune again on the next run. */
 int mol_batch_tune(mol_batch* batch, int32_t threads, int32_t ctas_per_sm, int64_t tile_cells);
 /* Waits for the batch's stream and reports a run that was abandoned because a stage
- * dependency wait ran out of its poll budget (MOL_ERR_CUDA; the flag is then cleared).
- * Steps on host arrays call it themselves. */
+ * dependency wait ran out of its poll budget (MOL_ERR_CUDA), or a step since the last check
+ * that produced a NaN or Inf state value in some instance (MOL_ERR_NONFINITE, OrdinaryDiffEq's
+ * unstable_check); the condition is then cleared.  Steps on host arrays call it themselves. */
 int mol_batch_check(mol_batch* batch);
 /* The schedule in use (after autotuning, once a step has run): threads per CTA, CTAs per SM,
  * tile cells (-1: one CTA per instance). */

@@ -564,6 +564,10 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
     if (!st && dLdp && plan->nparams > 0) st = dev_out(plan, dLdp, A.lam_p, plan->nparams);
     if (!st && dLdaux && plan->aux_total > 0) st = dev_out(plan, dLdaux, A.lam_aux, plan->aux_total);
     if (!st) st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "adjoint sync");
+    // a forward (re)computed step with a NaN or Inf state, or a non-finite misfit
+    if (!st) st = sync_and_check_finite(plan);
+    if (!st && !std::isfinite(A.loss))
+        st = set_err(plan, MOL_ERR_NONFINITE, "adjoint: the loss is NaN or Inf");
     if (loss) *loss = A.loss;
     if (nforward_steps) *nforward_steps = A.fwd_steps;
     release();

@@ -138,6 +138,7 @@ int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, 
     BatchSync sync;
     sync.ticket = b->d_sync;
     sync.status = (int*)(b->d_sync + 1);
+    sync.nonfinite = (int*)(b->d_sync + 1) + 1;
     sync.done = b->d_sync + 2;
     sync.spin_limit = MOL_BATCH_SPIN_LIMIT;
     // Host-side injection of a dependency that is never met, for tests of the bounded waits:
@@ -164,7 +165,7 @@ int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, 
         cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned), b->stream);
         if (e != cudaSuccess) return e;
         return launch_k(k, grid, threads, b->stream, probs, off, order, ninst, U, U1, U2, params,
-                        (const double*)b->d_dt, t0, nsteps, ticket);
+                        (const double*)b->d_dt, t0, nsteps, ticket, sync.nonfinite);
     };
     // one replayable graph: counter resets + persistent kernel
     const bool key_ok = b->graph && b->g_key[0] == (const void*)U && b->g_key[1] == (const void*)k &&
@@ -324,9 +325,15 @@ int mol_batch_create(const mol_problem_desc* const* descs, int32_t n, mol_batch*
             return berr(b, st, "instance " + std::to_string(i) + ": " + m);
         }
         b->plans.push_back(p);
-        if (i > 0 && (descs[i]->nparams != descs[0]->nparams || descs[i]->nfields != descs[0]->nfields)) {
+        if (i > 0 && (descs[i]->nparams != descs[0]->nparams || descs[i]->nfields != descs[0]->nfields ||
+                      descs[i]->nterms != descs[0]->nterms)) {
             return berr(b, MOL_ERR_INVALID, "instance " + std::to_string(i) + " differs in structure");
         }
+        // the shared module folds a nonlinear-Laplacian term only if every member's weights allow it
+        for (int k = 0; i > 0 && k < descs[0]->nterms; ++k)
+            if (nonlinlap_fold(descs[i], k) != nonlinlap_fold(descs[0], k))
+                return berr(b, MOL_ERR_INVALID, "instance " + std::to_string(i) + " differs in structure (term " +
+                                                    std::to_string(k) + " weights)");
         b->off[i + 1] = b->off[i] + p->nunk;
         b->max_cells = std::max(b->max_cells, p->ncell);
     }
@@ -431,13 +438,14 @@ int mol_batch_check(mol_batch* b) {
     if (!b) return MOL_ERR_INVALID;
     int st = bcheck(b, cudaStreamSynchronize(b->stream), "batch sync");
     if (st) return st;
-    int status = 0;
-    if ((st = bcheck(b, cudaMemcpy(&status, (int*)(b->d_sync + 1), sizeof(int), cudaMemcpyDeviceToHost), "status")))
+    int words[2] = {0, 0};  // status, nonfinite
+    if ((st = bcheck(b, cudaMemcpy(words, (int*)(b->d_sync + 1), sizeof(words), cudaMemcpyDeviceToHost), "status")))
         return st;
-    if (status) {
-        cudaMemset((int*)(b->d_sync + 1), 0, sizeof(int));
+    if (words[0] || words[1]) cudaMemset((int*)(b->d_sync + 1), 0, sizeof(words));
+    if (words[0])
         return berr(b, MOL_ERR_CUDA, "batch: a stage dependency wait ran out of its poll budget; the run was abandoned");
-    }
+    if (words[1])
+        return berr(b, MOL_ERR_NONFINITE, "batch: a step produced a NaN or Inf state value (unstable)");
     return MOL_OK;
 }
 

@@ -35,6 +35,21 @@
 
 namespace mol {
 
+bool nonlinlap_fold(const mol_problem_desc* d, int k) {
+    if (k < 0 || k >= d->nterms) return false;
+    const mol_term& tm = d->terms[k];
+    if (tm.kind != MOL_TERM_NONLINLAP) return false;
+    const char* env = getenv("MOL_JIT_FOLD");
+    if (env && env[0] == '0') return false;
+    const mol_op1d& oo = d->ops[tm.op];
+    const mol_op1d& oi = d->ops[tm.op2];
+    const mol_op1d& op = d->ops[tm.op3];
+    if (oo.nrows || oi.nrows || op.nrows || oo.L != 2 || oi.L != 2) return false;
+    const double* w = d->weights;
+    auto anti = [&](const mol_op1d& o) { return w[o.w_int] != 0.0 && w[o.w_int] == -w[o.w_int + 1]; };
+    return anti(oo) && anti(oi);
+}
+
 namespace {
 
 std::string lit(double v) {
@@ -550,6 +565,10 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
     for (int m = 0; m < op.L; ++m)
         if (!zero_w(d, op.w_int + m)) nzp.push_back(m);
     const std::string opi = std::to_string(tm.op2), opp = std::to_string(tm.op3), opo = std::to_string(tm.op);
+    // folded form (nonlinlap_fold): forward faces are a * (u[+] - u[-]), the cell scales the
+    // difference of its two faces by wo[1] wi[1] (P.w[reserved0]); 1 / wi[1] is at reserved0 + 1
+    const bool fold = nonlinlap_fold(d, k);
+    const std::string FOLDC = "P.w[P.terms[" + K + "].reserved0]", RWI = "P.w[P.terms[" + K + "].reserved0 + 1]";
 
     // face program (forward), given uf*/fa* variables named with `tag`, result in `tag`a
     auto face_forward = [&](const std::string& tag) {
@@ -625,14 +644,17 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
     // statements computing the face at relative half point r: tag du, tag uf<f>, the face
     // program; leaves tag a and tag du
     auto face_body = [&](int r, const std::string& tag, bool vjp) {
-        // inner derivative
-        for (size_t q = 0; q < nzi.size(); ++q) {
+        // inner derivative (folded: the plain difference, its weight wi[1] moves to the cell)
+        if (fold && !vjp)
+            e << "    const T " << tag << "du = bF[" << toff(r + oi.omin + 1) << "] - bF[" << toff(r + oi.omin + 0)
+              << "];\n";
+        for (size_t q = 0; q < nzi.size() && !(fold && !vjp); ++q) {
             const int t_ = nzi[q];
             const std::string tap = "bF[" + toff(r + oi.omin + t_) + "]";
             if (q == 0) e << "    T " << tag << "du = wi[" << t_ << "] * " << tap << ";\n";
             else e << "    " << tag << "du = fma(wi[" << t_ << "], " << tap << ", " << tag << "du);\n";
         }
-        if (nzi.empty()) e << "    T " << tag << "du = T(0);\n";
+        if (nzi.empty() && !(fold && !vjp)) e << "    T " << tag << "du = T(0);\n";
         for (int f : used_fields) {
             e << "    const T* __restrict__ bf" << f << " = u + (long long)" << f << " * P.ncell + c;\n";
             for (size_t q = 0; q < nzp.size(); ++q) {
@@ -664,7 +686,11 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
         const int r = oo.omin + m - 1;
         const std::string tag = "f" + std::to_string(m) + "_";
         e << "    {\n";
-        if (!vjp) {
+        if (!vjp && fold) {
+            // the two faces go to F0 / F1 declared by the caller
+            face_body(r, tag, false);
+            e << "    F" << m << " = " << tag << "a * " << tag << "du;\n";
+        } else if (!vjp) {
             face_body(r, tag, false);
             e << "    const T " << tag << "F = " << tag << "a * " << tag << "du;\n";
             e << "    acc = started ? fma(wo[" << m << "], " << tag << "F, acc) : wo[" << m << "] * " << tag << "F;\n"
@@ -725,21 +751,28 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
             for (int m : nzo) all_owned += " && " + from_pass(oo.omin + m - 1);
             e << "    if (warp_all(" << all_owned << ")) {\n"
               << "    const T* __restrict__ fq = P.faces + (long long)" << FQ << " * P.ncell + c;\n";
-            bool first = true;
-            for (int m : nzo) {
-                const int r = oo.omin + m - 1;
-                const std::string Fv = "fq[(long long)(" + std::to_string(r + 1) + ") * s]";
-                if (first) e << "    T acc = wo[" << m << "] * " << Fv << ";\n";
-                else e << "    acc = fma(wo[" << m << "], " << Fv << ", acc);\n";
-                first = false;
+            if (fold) {
+                e << "    return " << FOLDC << " * (fq[(long long)(" << (oo.omin + 1) << ") * s] - fq[(long long)("
+                  << oo.omin << ") * s]);\n    }\n";
+                e << "    T F0, F1;\n";
+            } else {
+                bool first = true;
+                for (int m : nzo) {
+                    const int r = oo.omin + m - 1;
+                    const std::string Fv = "fq[(long long)(" + std::to_string(r + 1) + ") * s]";
+                    if (first) e << "    T acc = wo[" << m << "] * " << Fv << ";\n";
+                    else e << "    acc = fma(wo[" << m << "], " << Fv << ", acc);\n";
+                    first = false;
+                }
+                e << "    return " << (nzo.empty() ? "T(0)" : "acc") << ";\n    }\n";
+                e << "    T acc = T(0);\n    bool started = false;\n";
             }
-            e << "    return " << (nzo.empty() ? "T(0)" : "acc") << ";\n    }\n";
-            e << "    T acc = T(0);\n    bool started = false;\n";
         } else {
             e << "    T* lF = lam_u + (long long)" << F << " * P.ncell + c;\n";
         }
         for (int m : nzo) fast_face(m, vjp);
-        if (!vjp) e << "    return acc;\n    }\n";
+        if (!vjp && fold) e << "    return " << FOLDC << " * (F1 - F0);\n    }\n";
+        else if (!vjp) e << "    return acc;\n    }\n";
         else e << "    return;\n    }\n";
         // generic path: runtime outer taps
         e << "    const bool per = (P.permask[" << F << "] >> " << D << ") & 1;\n"
@@ -753,7 +786,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
               << "        T F_;\n"
               << "        if (P.faces && Ih + 1 > P.lo[" << D << "] && Ih + 1 <= P.n[" << D << "] - P.up[" << D << "])\n"
               << "            F_ = P.faces[(long long)" << FQ << " * P.ncell + c + (long long)(Ih + 1 - I[" << D
-              << "]) * gstride(P, " << D << ")];\n"
+              << "]) * gstride(P, " << D << ")]" << (fold ? " * P.w[P.ops[" + opi + "].w_int + 1]" : "") << ";\n"
               << "        else\n"
               << "            F_ = gface" << K << "<T>(P, u, c, I, Ih, t, p);\n"
               << "        acc = started ? fma(w_, F_, acc) : w_ * F_;\n        started = true;\n    }\n    return acc;\n";
@@ -785,7 +818,8 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
       << "    const long long s = gstride(P, " << D << ");\n";
     face_body(-1, "fl_", false);
     e << "    return fl_a * fl_du;\n    }\n"
-      << "    return gface" << K << "<T>(P, u, c, I, I[" << D << "] - 1, t, p);\n}\n";
+      << "    return gface" << K << "<T>(P, u, c, I, I[" << D << "] - 1, t, p)" << (fold ? " * " + RWI : "")
+      << ";\n}\n";
 }
 
 }  // namespace

@@ -28,6 +28,13 @@ struct JitKernels {
 };
 
 std::string generate_source(const mol_problem_desc* d, std::string& why);
+// True when the generated code evaluates nonlinear-Laplacian term k in its folded form: the
+// outer and inner operators are two-point antisymmetric stencils (w[0] == -w[1], the
+// second-order half-offset first derivative), so a face is stored as a * (u[I+1] - u[I])
+// and the cell forms (wo[1] wi[1]) * (F'(I+1/2) - F'(I-1/2)).  The library then appends
+// wo[1] * wi[1] and 1 / wi[1] to the weight pool at the term's reserved0 offset.
+// MOL_JIT_FOLD=0 turns the folded form off.
+bool nonlinlap_fold(const mol_problem_desc* d, int k);
 std::vector<std::string> jit_kernel_names(int nparams, int group);
 // Generates, compiles (NVRTC, sm_103a) and loads the module of a problem structure;
 // modules are cached per generated source for the life of the process.

@@ -44,7 +44,8 @@ struct SolverState {
     double dtb[8];      // dt * btilde_j
     double sums[4];
     long long naccept, nreject, nf, iter, maxiters;
-    int done, status, accepted, pad;
+    int done, status, accepted;
+    int nonfinite;      // set by the last SSPRK33 stage when a state value is NaN or Inf (sticky)
     unsigned int blocks_done, pad2;
 };
 

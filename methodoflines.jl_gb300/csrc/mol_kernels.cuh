@@ -31,6 +31,21 @@ __device__ __forceinline__ double div3m(double x) {
 }
 __device__ __forceinline__ float div3m(float x) { return x / 3.0f; }
 
+// Finite test on the exponent bits (integer instructions: no FP64 pipe time).  The last
+// SSPRK33 stage ORs it over its outputs, the counterpart of OrdinaryDiffEq's unstable_check
+// (any NaN in u ends the solve): a NaN or Inf anywhere in a stage reaches the step's result.
+__device__ __forceinline__ bool nonfinite_bits(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool nonfinite_bits(float x) {
+    return ((unsigned)__float_as_int(x) & 0x7f800000u) == 0x7f800000u;
+}
+
+// One flag per warp that saw a non-finite value (every lane of the warp must call it).
+__device__ __forceinline__ void flag_nonfinite(bool bad, int* flag) {
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
 struct InterpCell {
     static constexpr int kFields = 0;  // field count known only at run time
     static constexpr int kFaceTerms = 0;  // the interpreter evaluates every face in the cell
@@ -131,6 +146,7 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_ssprk_t(const __gr
     T out[MOL_MAX_FIELDS];
     typename G::template Uniform<T> U;
     G::uniform(P, T(ts), p, U);
+    bool bad = false;
     for (long long c = cbeg + blockIdx.x * (long long)blockDim.x + threadIdx.x; c < cend;
          c += (long long)gridDim.x * blockDim.x) {
         int I[3];
@@ -139,9 +155,12 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_ssprk_t(const __gr
         #pragma unroll
         for (int f = 0; f < nfields_of<G>(P); ++f) {
             const long long g = (long long)f * P.ncell + c;
-            uout[g] = ssprk_combine<T, STAGE>(u0[g], uin[g], out[f], T(dt), T(2 * dt));
+            const T r = ssprk_combine<T, STAGE>(u0[g], uin[g], out[f], T(dt), T(2 * dt));
+            if (STAGE == 3) bad |= nonfinite_bits(r);
+            uout[g] = r;
         }
     }
+    if (STAGE == 3) flag_nonfinite(bad, &S->nonfinite);
     if (STAGE == 3 && from_state) last_block_advance(S, t0 + dt);
 }
 
@@ -214,7 +233,7 @@ __global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_ssprk_
                                                             const int* __restrict__ order, int ninst, T* U, T* U1,
                                                             T* U2, const T* const* __restrict__ params,
                                                             const double* __restrict__ dts, double t0,
-                                                            long long nsteps, unsigned* ticket) {
+                                                            long long nsteps, unsigned* ticket, int* nonfinite) {
     __shared__ int slot;
     T out[MOL_MAX_FIELDS];
     typename G::template Uniform<T> UN;
@@ -258,6 +277,7 @@ __global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_ssprk_
             }
             __syncthreads();
             G::uniform(P, T(t + dt / 2), p, UN);
+            bool bad = false;
             for (long long c = threadIdx.x; c < nc; c += blockDim.x) {
                 int I[3];
                 cell_index(P, c, I);
@@ -265,9 +285,12 @@ __global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_ssprk_
                 #pragma unroll
                 for (int f = 0; f < nfields_of<G>(P); ++f) {
                     const long long g = (long long)f * nc + c;
-                    u[g] = ssprk_combine<T, 3>(u[g], u2[g], out[f], T(dt), T(2 * dt));
+                    const T r = ssprk_combine<T, 3>(u[g], u2[g], out[f], T(dt), T(2 * dt));
+                    bad |= nonfinite_bits(r);
+                    u[g] = r;
                 }
             }
+            flag_nonfinite(bad, nonfinite);
             __syncthreads();
             t = t + dt;
         }
@@ -296,6 +319,7 @@ struct BatchSync {
     unsigned long long* done;     // [instance] tiles finished, all rounds so far
     int* status;                  // 0 ok, 1 a wait ran out of budget
     long long spin_limit;         // polls before a wait gives up (MOL_BATCH_SPIN_LIMIT by default)
+    int* nonfinite;               // set when a step's result holds a NaN or Inf (sticky)
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
@@ -402,6 +426,7 @@ __global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_tiles_
             }
         } else {
             G::uniform(P, T(t + dt / 2), p, UN);
+            bool bad = false;
             for (long long c = j * tile_cells + threadIdx.x; c < c_end; c += blockDim.x) {
                 int I[3];
                 cell_index(P, c, I);
@@ -409,9 +434,12 @@ __global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_tiles_
                 #pragma unroll
                 for (int f = 0; f < nfields_of<G>(P); ++f) {
                     const long long q = (long long)f * nc + c;
-                    u[q] = ssprk_combine<T, 3>(u[q], u2[q], out[f], T(dt), T(2 * dt));
+                    const T r = ssprk_combine<T, 3>(u[q], u2[q], out[f], T(dt), T(2 * dt));
+                    bad |= nonfinite_bits(r);
+                    u[q] = r;
                 }
             }
+            flag_nonfinite(bad, sync.nonfinite);
         }
         __syncthreads();
         if (threadIdx.x == 0) red_release_add_u64(sync.done + i, 1ull);

@@ -984,6 +984,12 @@ int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member
             tm.reserved0 = (int32_t)weights.size();
             for (int x = 0; x < o1.L; ++x)
                 for (int y = 0; y < o2.L; ++y) weights.push_back(d->weights[o1.w_int + x] * d->weights[o2.w_int + y]);
+        } else if (nonlinlap_fold(d, k)) {
+            // folded nonlinear Laplacian: the cell's scale wo[1] wi[1] and the face's 1 / wi[1]
+            const double wo1 = d->weights[d->ops[tm.op].w_int + 1], wi1 = d->weights[d->ops[tm.op2].w_int + 1];
+            tm.reserved0 = (int32_t)weights.size();
+            weights.push_back(wo1 * wi1);
+            weights.push_back(1.0 / wi1);
         }
     }
     mol_problem_desc dd = *d;
@@ -1155,6 +1161,24 @@ int rhs_impl(mol_plan* plan, T* du, const T* u, const T* p, double t) {
     return MOL_OK;
 }
 
+}  // namespace
+
+// Waits for the plan's stream, then reports (and clears) the flag the last SSPRK33 stage sets
+// when a step produced a NaN or Inf: OrdinaryDiffEq's unstable_check ending a solve.
+int mol::sync_and_check_finite(mol_plan* plan) {
+    int st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+    if (st) return st;
+    int bad = 0;
+    if ((st = cuda_check(plan, cudaMemcpy(&bad, &plan->d_state->nonfinite, sizeof(int), cudaMemcpyDeviceToHost),
+                         "status")))
+        return st;
+    if (!bad) return MOL_OK;
+    cudaMemset(&plan->d_state->nonfinite, 0, sizeof(int));
+    return set_err(plan, MOL_ERR_NONFINITE, "a step produced a NaN or Inf state value (unstable)");
+}
+
+namespace {
+
 template <class T>
 int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t nsteps) {
     if (!plan || !u || nsteps < 0 || !std::isfinite(dt) || !std::isfinite(t0)) return MOL_ERR_INVALID;
@@ -1203,7 +1227,7 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
         T* out1 = (nsteps == 1 && hz) ? hz : ud;
         if ((st = launch_ssprk_step_io<T>(plan, ud, out1, u1, u2, pp, dt, true))) return st;
         --nsteps;
-        if (nsteps == 0 && hz) return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+        if (nsteps == 0 && hz) return sync_and_check_finite(plan);
     }
     if (nsteps == 0) hz = nullptr;  // nothing left to step: the state goes back by copy below
     const int64_t nmid = hz ? nsteps - 1 : nsteps;  // steps that stay in the device buffer ud
@@ -1248,14 +1272,15 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
         if ((st = launch_ssprk_step<T>(plan, ud, u1, u2, pp, dt))) return st;
     if (hz) {
         if ((st = launch_ssprk_step_io<T>(plan, ud, hz, u1, u2, pp, dt))) return st;
-        return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+        return sync_and_check_finite(plan);
     }
     if (host) {
         if ((st = cuda_check(plan, cudaMemcpyAsync(u, ud, sizeof(T) * (size_t)plan->nunk, cudaMemcpyDeviceToHost,
                                                    plan->stream), "D2H")))
             return st;
-        return cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync");
+        return sync_and_check_finite(plan);
     }
+    // device state: the call stays asynchronous; mol_plan_check reports a non-finite result
     return cuda_check(plan, cudaGetLastError(), "ssprk33");
 }
 
@@ -1309,6 +1334,11 @@ int mol_step_ssprk33(mol_plan* plan, double* u, const double* p, double t0, doub
 }
 int mol_step_ssprk33_f32state(mol_plan* plan, float* u, const float* p, double t0, double dt, int64_t nsteps) {
     return ssprk_impl<float>(plan, u, p, t0, dt, nsteps);
+}
+int mol_plan_check(mol_plan* plan) {
+    if (!plan) return MOL_ERR_INVALID;
+    DeviceGuard g(plan->dev);
+    return sync_and_check_finite(plan);
 }
 
 int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, double t1, double abstol, double reltol,

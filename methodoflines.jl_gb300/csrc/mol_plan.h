@@ -108,6 +108,9 @@ int plan_grid(const mol_plan* plan);
 int grid_for(long long ncell, int sms, int blocks_per_sm);
 int threads_for(long long ncell, int sms, int blocks_per_sm);
 int plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member);
+// Synchronises the plan's stream and returns MOL_ERR_NONFINITE (clearing the flag) when an
+// SSPRK33 step since the last check produced a NaN or Inf state value.
+int sync_and_check_finite(mol_plan* plan);
 
 template <class T>
 DevProb<T>& prob(mol_plan* plan);

@@ -106,6 +106,7 @@ _PROTOS = {
     "mol_step_ssprk33_f32state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                             C.c_int64]),
     "mol_step_ssprk33_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64]),
+    "mol_plan_check": (C.c_int, [C.c_void_p]),
     "mol_solve_tsit5": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                   C.c_double, C.c_double, C.c_int64, C.POINTER(mol_stats)]),
     "mol_adjoint_ssprk33": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64,

@@ -207,6 +207,11 @@ class Plan:
         L.check(fn(self._h, pu, pp, float(t0), float(dt), int(nsteps)), self._h)
         return u
 
+    def check(self):
+        """Waits for the plan's stream; raises MolError (MOL_ERR_NONFINITE) if an SSPRK33 step
+        since the last check produced a NaN or Inf (steps on host arrays check themselves)."""
+        L.check(L.lib().mol_plan_check(self._h), self._h)
+
     def step_ssprk33_noalloc(self, u, dt: float, nsteps: int, t0: float = 0.0, p=None):
         """SSPRK33 steps that allocate nothing (device arrays only, at most 2^20 unknowns)."""
         pu, _ = _ptr(u, self.n, "u", False, out=True)
