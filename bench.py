@@ -658,8 +658,9 @@ def run_case(name, args):
             rows.append({"active_lanes": act, "warp_fma_G_per_s": w.value / 1e9, "lane_tflops": t.value})
         out.update(rows=rows)
     elif name in ("adr3d_rhs", "adr3d_steps"):
-        # one RHS (or SSPRK33 steps) of the 3-D ADR problem at 128^3
-        sys_, disc, ex = problems.adr3d(N=128, nz_pts=130)
+        # five RHS evaluations (or SSPRK33 steps) of the 3-D ADR problem at N^3 (--case-n, 128 by default)
+        N = args.case_n or 128
+        sys_, disc, ex = problems.adr3d(N=N, nz_pts=N + 2)
         lw = lower(sys_.to_spec(disc))
         plan = Plan(lw)
         plan.set_stream(stream.cuda_stream)
@@ -693,6 +694,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None, choices=CASES,
                     help="run one small single-path case (for profiling) and exit")
+    ap.add_argument("--case-n", type=int, default=0, help="grid side of the adr3d cases")
     args = ap.parse_args()
     if args.case:
         run_case(args.case, args)

@@ -56,6 +56,7 @@ struct mol_batch {
     float* s32[3] = {nullptr, nullptr, nullptr};
     int threads = 256, ctas_per_sm = 2, sms = 152;
     int tile_cells = 2048;   // > 0 tiled schedule, 0 one CTA per instance
+    int nface = 0;           // nonlinear-Laplacian terms (faces shared through shared memory)
     bool tuned = false;
     std::vector<void*> allocs;
     cudaGraphExec_t graph = nullptr;
@@ -85,6 +86,21 @@ int balloc(mol_batch* b, void** p, size_t bytes) {
     if (e != cudaSuccess) return bcheck(b, e, "cudaMalloc");
     b->allocs.push_back(*p);
     return MOL_OK;
+}
+
+// Shared-memory face window of the tiled kernel for state type T: bytes per CTA (0: off) and
+// cells per face term.  MOL_BATCH_FACE_BYTES sets the bytes (0 turns the window off).
+template <class T>
+void face_window(const mol_batch* b, size_t* bytes, long long* cells) {
+    *bytes = 0;
+    *cells = 0;
+    if (b->nface <= 0) return;
+    long long want = 45056;
+    if (const char* e = getenv("MOL_BATCH_FACE_BYTES")) want = std::max(0ll, std::min(atoll(e), 48ll * 1024));
+    const long long w = want / ((long long)b->nface * (long long)sizeof(T));
+    if (w < 64) return;
+    *cells = w;
+    *bytes = (size_t)w * b->nface * sizeof(T);
 }
 
 // The tile table of one round for a tile size: tiles of the instances in slot order
@@ -150,6 +166,9 @@ int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, 
     if (tiled && getenv("MOL_BATCH_INJECT_SKIP_ROUND") && getenv("MOL_BATCH_INJECT_SKIP_ROUND")[0] == '1')
         first_ticket = (unsigned long long)b->tiles_total;
     const size_t sync_bytes = sizeof(unsigned long long) * (2 + (size_t)b->n);
+    size_t fbytes = 0;
+    long long fcells = 0;
+    if (tiled) face_window<T>(b, &fbytes, &fcells);
     auto enqueue = [&]() -> cudaError_t {
         if (tiled) {
             // the status word survives replays so a failed run stays visible to mol_batch_check
@@ -159,8 +178,9 @@ int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, 
             if (e == cudaSuccess)
                 e = cudaMemsetAsync(b->d_sync + 2, 0, sync_bytes - 2 * sizeof(unsigned long long), b->stream);
             if (e != cudaSuccess) return e;
-            return launch_k(k, grid, threads, b->stream, probs, off, (const TileRef*)b->d_tiles, b->tiles_total,
-                            tile_cells, U, U1, U2, params, (const double*)b->d_dt, t0, nsteps, sync);
+            return launch_ks(k, grid, threads, fbytes, b->stream, probs, off, (const TileRef*)b->d_tiles,
+                             b->tiles_total, tile_cells, U, U1, U2, params, (const double*)b->d_dt, t0, nsteps, sync,
+                             fcells);
         }
         cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned), b->stream);
         if (e != cudaSuccess) return e;
@@ -202,9 +222,9 @@ int run(mol_batch* b, T* U, double t0, long long nsteps, int threads, int ctas, 
 }
 
 // CTAs of `k` that fit on one SM at `threads` per CTA (0 if the query fails).
-int resident_ctas(cudaKernel_t k, int threads) {
+int resident_ctas(cudaKernel_t k, int threads, size_t smem = 0) {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k, threads, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k, threads, smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -220,8 +240,11 @@ int tune(mol_batch* b, T* U, long long probe_steps) {
     std::vector<Cand> cand;
     for (int tiled = 0; tiled < 2; ++tiled) {
         cudaKernel_t k = tiled ? (is64 ? b->jit.tiles64 : b->jit.tiles32) : (is64 ? b->jit.batch64 : b->jit.batch32);
+        size_t fbytes = 0;
+        long long fcells = 0;
+        if (tiled) face_window<T>(b, &fbytes, &fcells);
         for (int th : {128, 256}) {
-            const int maxc = resident_ctas(k, th);
+            const int maxc = resident_ctas(k, th, fbytes);
             for (int c : {1, 2, 3, 4, 6, 8}) {
                 if (c > maxc) continue;
                 if (!tiled) cand.push_back({th, c, 0});
@@ -315,6 +338,8 @@ int mol_batch_create(const mol_problem_desc* const* descs, int32_t n, mol_batch*
     std::string why;
     b->src = generate_source(descs[0], why);
     if (b->src.empty()) return berr(b, MOL_ERR_UNSUPPORTED, "codegen: " + why);
+    for (int k = 0; k < descs[0]->nterms; ++k)
+        if (descs[0]->terms[k].kind == MOL_TERM_NONLINLAP) ++b->nface;
     b->off.assign(n + 1, 0);
     for (int i = 0; i < n; ++i) {
         mol_plan* p = nullptr;

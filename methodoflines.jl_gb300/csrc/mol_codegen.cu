@@ -679,8 +679,10 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
     // cell is an unknown reached without a wrap
     const std::string FQ = std::to_string(face_slot);
     auto from_pass = [&](int r) {
+        const std::string cf = "c + (long long)(" + std::to_string(r + 1) + ") * s";
         return "P.faces && I[" + D + "] + (" + std::to_string(r + 1) + ") > P.lo[" + D + "] && I[" + D + "] + (" +
-               std::to_string(r + 1) + ") <= P.n[" + D + "] - P.up[" + D + "]";
+               std::to_string(r + 1) + ") <= P.n[" + D + "] - P.up[" + D + "] && " + cf + " >= P.fbeg && " + cf +
+               " < P.fend";
     };
     auto fast_face = [&](int m, bool vjp) {
         const int r = oo.omin + m - 1;
@@ -750,7 +752,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
             std::string all_owned = "P.faces";
             for (int m : nzo) all_owned += " && " + from_pass(oo.omin + m - 1);
             e << "    if (warp_all(" << all_owned << ")) {\n"
-              << "    const T* __restrict__ fq = P.faces + (long long)" << FQ << " * P.ncell + c;\n";
+              << "    const T* __restrict__ fq = P.faces + (long long)" << FQ << " * P.fstride + c;\n";
             if (fold) {
                 e << "    return " << FOLDC << " * (fq[(long long)(" << (oo.omin + 1) << ") * s] - fq[(long long)("
                   << oo.omin << ") * s]);\n    }\n";
@@ -784,9 +786,11 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
         if (!vjp)
             e << "        const int Ih = so.first + q;\n"
               << "        T F_;\n"
-              << "        if (P.faces && Ih + 1 > P.lo[" << D << "] && Ih + 1 <= P.n[" << D << "] - P.up[" << D << "])\n"
-              << "            F_ = P.faces[(long long)" << FQ << " * P.ncell + c + (long long)(Ih + 1 - I[" << D
-              << "]) * gstride(P, " << D << ")]" << (fold ? " * P.w[P.ops[" + opi + "].w_int + 1]" : "") << ";\n"
+              << "        const long long cf_ = c + (long long)(Ih + 1 - I[" << D << "]) * gstride(P, " << D << ");\n"
+              << "        if (P.faces && Ih + 1 > P.lo[" << D << "] && Ih + 1 <= P.n[" << D << "] - P.up[" << D
+              << "] && cf_ >= P.fbeg && cf_ < P.fend)\n"
+              << "            F_ = P.faces[(long long)" << FQ << " * P.fstride + cf_]"
+              << (fold ? " * P.w[P.ops[" + opi + "].w_int + 1]" : "") << ";\n"
               << "        else\n"
               << "            F_ = gface" << K << "<T>(P, u, c, I, Ih, t, p);\n"
               << "        acc = started ? fma(w_, F_, acc) : w_ * F_;\n        started = true;\n    }\n    return acc;\n";

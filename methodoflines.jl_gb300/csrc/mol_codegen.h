@@ -50,5 +50,11 @@ cudaError_t launch_k(cudaKernel_t k, int grid, int block, cudaStream_t s, A... a
     void* pa[] = {(void*)&args...};
     return cudaLaunchKernel((const void*)k, dim3(grid), dim3(block), pa, 0, s);
 }
+// The same with `smem` bytes of dynamic shared memory per CTA.
+template <class... A>
+cudaError_t launch_ks(cudaKernel_t k, int grid, int block, size_t smem, cudaStream_t s, A... args) {
+    void* pa[] = {(void*)&args...};
+    return cudaLaunchKernel((const void*)k, dim3(grid), dim3(block), pa, smem, s);
+}
 
 }  // namespace mol

@@ -83,8 +83,12 @@ struct DevProb {
     const T* aux;
     const long long* aux_off;     // naux + 1 offsets into aux
     int naux;
-    // left faces of the nonlinear-Laplacian terms from the face pass ([slot][cell]), or null
+    // left faces of the nonlinear-Laplacian terms from the face pass ([slot][cell]), or null;
+    // slot q of cell c at faces[q * fstride + c] (fstride = ncell for the face pass over the
+    // whole grid; the ensemble kernel points faces at a shared-memory window of fstride cells)
     const T* faces;
+    long long fstride;
+    long long fbeg, fend;   // cells whose faces `faces` holds: [fbeg, fend)
 };
 
 __device__ __forceinline__ int wrap_periodic(int i, int l) {

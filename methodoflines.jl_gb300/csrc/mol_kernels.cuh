@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_faces_t(const __gr
         cell_index(P, c, I);
         G::faces(P, u, c, I, T(t), p, out);
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) faces[(long long)q * P.ncell + c] = out[q];
+        for (int q = 0; q < NQ; ++q) faces[(long long)q * P.fstride + c] = out[q];
     }
 }
 
@@ -338,6 +338,72 @@ struct TileRef {
     int inst, tile, ntiles, pad;
 };
 
+// One SSPRK33 stage of cells [cb, ce) of an instance (the CTA's threads stride over them);
+// returns whether a last-stage result of this thread was NaN or Inf.
+template <class T, class G, int STAGE>
+__device__ __forceinline__ bool batch_cells(const DevProb<T>& P, const T* __restrict__ uin, const T* u0, T* uout,
+                                            const T* __restrict__ p, double ts, double dt, long long cb,
+                                            long long ce, const typename G::template Uniform<T>& UN) {
+    T out[MOL_MAX_FIELDS];
+    bool bad = false;
+    const long long nc = P.ncell;
+    for (long long c = cb + threadIdx.x; c < ce; c += blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        G::cell(P, uin, c, I, T(ts), p, UN, out);
+#pragma unroll
+        for (int f = 0; f < nfields_of<G>(P); ++f) {
+            const long long q = (long long)f * nc + c;
+            const T r = ssprk_combine<T, STAGE>(u0[q], uin[q], out[f], T(dt), T(2 * dt));
+            if (STAGE == 3) bad |= nonfinite_bits(r);
+            uout[q] = r;
+        }
+    }
+    return bad;
+}
+
+// The same stage with the nonlinear-Laplacian faces computed once: cells [cb, ce) go in chunks;
+// for each chunk the CTA first writes the left face of every cell the chunk's cells read
+// (the chunk plus one line of the slowest face dimension) into a shared-memory window of W
+// cells per face term, then runs the cells on a copy of the problem view (sP, in shared
+// memory) whose faces point at the window.  Each face is then evaluated once per chunk
+// instead of once for each of the two cells that share it; the values are the ones the
+// cells would compute themselves (the same generated code), so results are unchanged.
+// Instances whose face line does not fit the window run without it.
+template <class T, class G, int STAGE>
+__device__ bool batch_cells_faces(const DevProb<T>& Pg, DevProb<T>& sP, T* win, long long W, const T* __restrict__ uin,
+                                  const T* u0, T* uout, const T* __restrict__ p, double ts, double dt, long long cb,
+                                  long long ce, const typename G::template Uniform<T>& UN) {
+    constexpr int NQ = G::kFaceTerms > 0 ? G::kFaceTerms : 1;
+    const long long nc = Pg.ncell;
+    const long long line = gstride(Pg, Pg.ndim - 1);   // cells between neighbours along the slowest dimension
+    const long long chunk = W - line;
+    if (G::kFaceTerms == 0 || W <= 0 || chunk < (long long)blockDim.x)
+        return batch_cells<T, G, STAGE>(Pg, uin, u0, uout, p, ts, dt, cb, ce, UN);
+    bool bad = false;
+    for (long long a = cb; a < ce; a += chunk) {
+        const long long b = min(ce, a + chunk);
+        const long long fe = min(nc, b + line);
+        for (long long c = a + threadIdx.x; c < fe; c += blockDim.x) {
+            int I[3];
+            cell_index(Pg, c, I);
+            T fo[NQ];
+            G::faces(Pg, uin, c, I, T(ts), p, fo);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) win[(long long)q * W + (c - a)] = fo[q];
+        }
+        if (threadIdx.x == 0) {
+            sP.faces = win - a;   // faces[q * W + c] is the window's entry of cell c, for c in [a, fe)
+            sP.fbeg = a;
+            sP.fend = fe;
+        }
+        __syncthreads();
+        bad |= batch_cells<T, G, STAGE>(sP, uin, u0, uout, p, ts, dt, a, b, UN);
+        __syncthreads();
+    }
+    return bad;
+}
+
 template <class T, class G>
 __global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_tiles_t(const DevProb<T>* __restrict__ probs,
                                                             const long long* __restrict__ off,
@@ -345,12 +411,16 @@ __global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_tiles_
                                                             long long ntiles, int tile_cells, T* U, T* U1, T* U2,
                                                             const T* const* __restrict__ params,
                                                             const double* __restrict__ dts, double t0,
-                                                            long long nsteps, BatchSync sync) {
+                                                            long long nsteps, BatchSync sync, long long face_window) {
     __shared__ long long s_item;
     __shared__ TileRef s_ref;
     __shared__ int s_ok;
+    // the face window (dynamic shared memory, face_window cells per face term) and the
+    // problem view that points at it
+    extern __shared__ __align__(16) unsigned char mol_batch_smem[];
+    __shared__ DevProb<T> sP;
+    T* win = reinterpret_cast<T*>(mol_batch_smem);
     const long long nitems = 3 * nsteps * ntiles;
-    T out[MOL_MAX_FIELDS];
     typename G::template Uniform<T> UN;
     // thread 0 takes the next ticket while the CTA works on the current tile; the held ticket
     // is larger than the one being worked on, so the lowest unfinished unit still always runs
@@ -399,46 +469,22 @@ __global__ void __launch_bounds__(kThreads, MOL_BATCH_MIN_BLOCKS) k_batch_tiles_
         const long long nc = P.ncell;
         const int stage = (int)(r % 3);
         const double t = t0 + (double)(r / 3) * dt;
+        const long long c_beg = j * (long long)tile_cells;
         const long long c_end = min(nc, (j + 1) * (long long)tile_cells);
+        if (G::kFaceTerms > 0 && face_window > 0 && threadIdx.x == 0) {
+            sP = P;
+            sP.fstride = face_window;
+        }
         if (stage == 0) {
             G::uniform(P, T(t), p, UN);
-            for (long long c = j * tile_cells + threadIdx.x; c < c_end; c += blockDim.x) {
-                int I[3];
-                cell_index(P, c, I);
-                G::cell(P, u, c, I, T(t), p, UN, out);
-                #pragma unroll
-                for (int f = 0; f < nfields_of<G>(P); ++f) {
-                    const long long q = (long long)f * nc + c;
-                    u1[q] = ssprk_combine<T, 1>(u[q], u[q], out[f], T(dt), T(2 * dt));
-                }
-            }
+            batch_cells_faces<T, G, 1>(P, sP, win, face_window, u, u, u1, p, t, dt, c_beg, c_end, UN);
         } else if (stage == 1) {
             G::uniform(P, T(t + dt), p, UN);
-            for (long long c = j * tile_cells + threadIdx.x; c < c_end; c += blockDim.x) {
-                int I[3];
-                cell_index(P, c, I);
-                G::cell(P, u1, c, I, T(t + dt), p, UN, out);
-                #pragma unroll
-                for (int f = 0; f < nfields_of<G>(P); ++f) {
-                    const long long q = (long long)f * nc + c;
-                    u2[q] = ssprk_combine<T, 2>(u[q], u1[q], out[f], T(dt), T(2 * dt));
-                }
-            }
+            batch_cells_faces<T, G, 2>(P, sP, win, face_window, u1, u, u2, p, t + dt, dt, c_beg, c_end, UN);
         } else {
             G::uniform(P, T(t + dt / 2), p, UN);
-            bool bad = false;
-            for (long long c = j * tile_cells + threadIdx.x; c < c_end; c += blockDim.x) {
-                int I[3];
-                cell_index(P, c, I);
-                G::cell(P, u2, c, I, T(t + dt / 2), p, UN, out);
-                #pragma unroll
-                for (int f = 0; f < nfields_of<G>(P); ++f) {
-                    const long long q = (long long)f * nc + c;
-                    const T r = ssprk_combine<T, 3>(u[q], u2[q], out[f], T(dt), T(2 * dt));
-                    bad |= nonfinite_bits(r);
-                    u[q] = r;
-                }
-            }
+            const bool bad =
+                batch_cells_faces<T, G, 3>(P, sP, win, face_window, u2, u, u, p, t + dt / 2, dt, c_beg, c_end, UN);
             flag_nonfinite(bad, sync.nonfinite);
         }
         __syncthreads();

@@ -798,6 +798,10 @@ static int build_prec(mol_plan* plan, const mol_problem_desc* d, PlanArrays& A, 
         P.permask[f] = m;
     }
     P.ncell = plan->ncell;
+    P.faces = nullptr;
+    P.fstride = plan->ncell;
+    P.fbeg = 0;
+    P.fend = plan->ncell;
     P.bc = (const DevBC<T>*)A.bc;
     P.ops = plan->d_ops;
     P.w = (const T*)A.w;

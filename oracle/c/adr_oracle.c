@@ -158,13 +158,19 @@ int adr_ssprk33(const int64_t* n, const double* wi, const double* wo, const doub
     adr_grid g;
     fill(&g, n, wi, wo, wm, wb, coef, Kx, Ky, Kz);
 #ifdef _OPENMP
+    const int prev_threads = omp_get_max_threads();   /* restored on return */
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
     (void)nthreads;
 #endif
     const int64_t m = n[0] * n[1] * n[2];
     double* k = scratch(3 * (size_t)m);
-    if (!k) return -1;
+    if (!k) {
+#ifdef _OPENMP
+        omp_set_num_threads(prev_threads);
+#endif
+        return -1;
+    }
     double* u1 = k + m;
     double* u2 = u1 + m;
     for (int64_t step = 0; step < nsteps; ++step) {
@@ -179,5 +185,8 @@ int adr_ssprk33(const int64_t* n, const double* wi, const double* wo, const doub
 #pragma omp parallel for schedule(static)
         for (int64_t q = 0; q < m; ++q) s[q] = ((s[q] + 2.0 * u2[q]) + dt2 * k[q]) / 3.0;
     }
+#ifdef _OPENMP
+    omp_set_num_threads(prev_threads);
+#endif
     return 0;
 }

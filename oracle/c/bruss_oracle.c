@@ -101,13 +101,19 @@ int bruss_ssprk33(int64_t nx, int64_t ny, const double* wx, const double* wy, do
     g.x = x;
     g.y = y;
 #ifdef _OPENMP
+    const int prev_threads = omp_get_max_threads();   /* restored on return */
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
     (void)nthreads;
 #endif
     const int64_t n2 = 2 * nx * ny;
     double* k = scratch(3 * (size_t)n2);
-    if (!k) return -1;
+    if (!k) {
+#ifdef _OPENMP
+        omp_set_num_threads(prev_threads);
+#endif
+        return -1;
+    }
     double* u1 = k + n2;
     double* u2 = u1 + n2;
     double t = t0;
@@ -124,6 +130,9 @@ int bruss_ssprk33(int64_t nx, int64_t ny, const double* wx, const double* wy, do
         for (int64_t q = 0; q < n2; ++q) s[q] = ((s[q] + 2.0 * u2[q]) + dt2 * k[q]) / 3.0;
         t = t + dt;
     }
+#ifdef _OPENMP
+    omp_set_num_threads(prev_threads);
+#endif
     return 0;
 }
 
