@@ -8,6 +8,8 @@ as text from its test files and generated documentation:
 * ``test/Components/utils_test.jl:129-137``        periodic index wrap
 * ``docs/src/generated/bruss_ode_eqs.md``          the generated Brusselator ODE system
   at dx = dy = 1/4 (the reference's own discretisation, after ModelingToolkit)
+* ``docs/src/generated/bruss_code.md``             the compiled f! of the same system: its
+  argument order and each output's expression with the folded coefficients
 
 Usage: ``python tests/golden/make_golden.py [REFERENCE_ROOT]``.  The JSON files are
 committed so the tests never need the reference checkout.
@@ -119,6 +121,54 @@ def brusselator_equations(root):
     return {"dx": 0.25, "alpha": 10.0, "source": "docs/src/generated/bruss_ode_eqs.md", "equations": eqs}
 
 
+def _parse_prefix(s: str, pos: int):
+    """One Julia prefix-call expression of the generated code: ``(+)(a, b)``, ``(*)(a, b)``,
+    ``(^)(x, 2)``, a number or ``var"u[i, j](t)"``; returns (tree, next position)."""
+    while s[pos] == " ":
+        pos += 1
+    if s.startswith('var"', pos):
+        end = s.index('"', pos + 4)
+        m = re.match(r"([uv])\[(\d+), (\d+)\]\(t\)", s[pos + 4:end])
+        return ["var", m.group(1), int(m.group(2)), int(m.group(3))], end + 1
+    if s[pos] == "(" and s[pos + 2] == ")" and s[pos + 1] in "+*^":
+        op = s[pos + 1]
+        pos += 3
+        assert s[pos] == "("
+        pos += 1
+        args = []
+        while True:
+            a, pos = _parse_prefix(s, pos)
+            args.append(a)
+            while s[pos] == " ":
+                pos += 1
+            if s[pos] == ",":
+                pos += 1
+                continue
+            assert s[pos] == ")", s[pos:pos + 20]
+            return [op] + args, pos + 1
+    m = re.match(r"-?[\d.]+(e-?\d+)?", s[pos:])
+    return ["num", float(m.group(0))], pos + m.end()
+
+
+def brusselator_compiled(root):
+    """The compiled f! at dx = dy = 1/4 (docs/src/generated/bruss_code.md): the unknown order
+    of its argument vector and, for every output, the expression tree with its folded
+    coefficients (alpha/dx^2 in every tap, centre coefficients merged) in the printed order."""
+    txt = open(os.path.join(root, "docs/src/generated/bruss_code.md")).read()
+    start = txt.index("function (ˍ₋out, ˍ₋arg1, ˍ₋arg2, t)")
+    body = txt[start:]
+    unknowns = []
+    for m in re.finditer(r'var"([uv])\[(\d+), (\d+)\]\(t\)" = @inbounds\(ˍ₋arg1\[(\d+)\]\)', body):
+        assert int(m.group(4)) == len(unknowns) + 1
+        unknowns.append([m.group(1), int(m.group(2)), int(m.group(3))])
+    outs = {}
+    for m in re.finditer(r"ˍ₋out\[(\d+)\] = ", body):
+        tree, _ = _parse_prefix(body, m.end())
+        outs[int(m.group(1))] = tree
+    return {"dx": 0.25, "alpha": 10.0, "source": "docs/src/generated/bruss_code.md",
+            "unknowns": unknowns, "outputs": [outs[k] for k in range(1, len(outs) + 1)]}
+
+
 def main(root="/root/reference"):
     golden = {
         "fornberg": fornberg_cases(root),
@@ -129,6 +179,8 @@ def main(root="/root/reference"):
         json.dump(golden, fh, indent=1)
     with open(os.path.join(HERE, "brusselator_dx025_equations.json"), "w") as fh:
         json.dump(brusselator_equations(root), fh, indent=1)
+    with open(os.path.join(HERE, "brusselator_dx025_compiled.json"), "w") as fh:
+        json.dump(brusselator_compiled(root), fh)
     print("fornberg", len(golden["fornberg"]), "stencils", len(golden["centered_stencils"]),
           "wrap", len(golden["periodic_wrap"]))
 
