@@ -341,6 +341,7 @@ int mol_batch_create(const mol_problem_desc* const* descs, int32_t n, mol_batch*
     for (int k = 0; k < descs[0]->nterms; ++k)
         if (descs[0]->terms[k].kind == MOL_TERM_NONLINLAP) ++b->nface;
     b->off.assign(n + 1, 0);
+    std::vector<int> cfold_shape;
     for (int i = 0; i < n; ++i) {
         mol_plan* p = nullptr;
         st = plan_create_impl(descs[i], &p, true);
@@ -359,6 +360,15 @@ int mol_batch_create(const mol_problem_desc* const* descs, int32_t n, mol_batch*
             if (nonlinlap_fold(descs[i], k) != nonlinlap_fold(descs[0], k))
                 return berr(b, MOL_ERR_INVALID, "instance " + std::to_string(i) + " differs in structure (term " +
                                                     std::to_string(k) + " weights)");
+        // and fuses the same constant-coefficient stencils (same taps) in every member
+        if (i == 0) {
+            for (const FoldGroup& g : const_linear_groups(descs[0])) cfold_shape.push_back((int)g.taps.size());
+        } else {
+            std::vector<int> shp;
+            for (const FoldGroup& g : const_linear_groups(descs[i])) shp.push_back((int)g.taps.size());
+            if (shp != cfold_shape)
+                return berr(b, MOL_ERR_INVALID, "instance " + std::to_string(i) + " differs in structure (fused stencils)");
+        }
         b->off[i + 1] = b->off[i] + p->nunk;
         b->max_cells = std::max(b->max_cells, p->ncell);
     }

@@ -23,8 +23,10 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
+#include <set>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -111,6 +113,212 @@ SSA to_ssa(const mol_problem_desc* d, int prog) {
     }
     return s;
 }
+
+// Value of a node built from constants only (CONST, NEG, ADD, SUB, MUL, DIV), or false.
+bool const_value(const mol_problem_desc* d, const SSA& s, int pc, double* out) {
+    if (pc < 0) return false;
+    const mol_instr& in = s.ins[pc];
+    double a = 0, b = 0;
+    switch (in.op) {
+        case MOL_OP_CONST: *out = d->consts[in.imm]; return std::isfinite(*out);
+        case MOL_OP_NEG:
+            if (!const_value(d, s, s.ia[pc], &a)) return false;
+            *out = -a;
+            return true;
+        case MOL_OP_ADD: case MOL_OP_SUB: case MOL_OP_MUL: case MOL_OP_DIV:
+            if (!const_value(d, s, s.ia[pc], &a) || !const_value(d, s, s.ib[pc], &b)) return false;
+            *out = in.op == MOL_OP_ADD ? a + b : in.op == MOL_OP_SUB ? a - b : in.op == MOL_OP_MUL ? a * b : a / b;
+            return std::isfinite(*out);
+        default: return false;
+    }
+}
+
+}  // namespace
+
+std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d) {
+    std::vector<FoldGroup> groups;
+    const char* env = getenv("MOL_JIT_CFOLD");
+    if ((env && env[0] == '0') || d->cell_prog < 0) return groups;
+    const SSA s = to_ssa(d, d->cell_prog);
+    if (!s.ok) return groups;
+    const int n = (int)s.ins.size();
+    std::vector<int> uses(n, 0);
+    for (int pc = 0; pc < n; ++pc)
+        for (int x : {s.ia[pc], s.ib[pc], s.ic[pc]})
+            if (x >= 0) uses[x]++;
+    auto nz = [&](long long off) { return d->weights[off] != 0.0; };
+    // a first-derivative stencil term of compile-time weights
+    auto first_deriv = [&](int k) {
+        if (k < 0 || k >= d->nterms) return false;
+        const mol_term& tm = d->terms[k];
+        if (tm.kind == MOL_TERM_MIXED) return d->ops[tm.op].nrows == 0 && d->ops[tm.op2].nrows == 0;
+        if (tm.kind != MOL_TERM_LINEAR) return false;
+        const mol_op1d& o = d->ops[tm.op];
+        if (o.nrows) return false;
+        for (int m = 0; m < o.L; ++m)
+            if (d->weights[o.w_int + m] != -d->weights[o.w_int + o.L - 1 - m]) return false;
+        return true;
+    };
+    auto is_uniform_const = [&](int pc, double* c) { return const_value(d, s, pc, c); };
+    // a foldable leaf: (term, coefficient, subtree pcs)
+    struct Leaf {
+        int term;
+        double coef;
+        std::vector<int> nodes;
+    };
+    std::function<bool(int, Leaf*)> leaf = [&](int pc, Leaf* L) -> bool {
+        const mol_instr& in = s.ins[pc];
+        if (uses[pc] != 1) return false;
+        if (in.op == MOL_OP_TERM && first_deriv(in.imm)) {
+            *L = Leaf{in.imm, 1.0, {pc}};
+            return true;
+        }
+        if (in.op == MOL_OP_UPWIND) {
+            double c;
+            if (!is_uniform_const(s.ia[pc], &c)) return false;
+            const int k = c < 0 ? in.b : in.c;
+            if (k < 0 || k >= d->nterms || d->terms[k].kind != MOL_TERM_LINEAR || d->ops[d->terms[k].op].nrows)
+                return false;
+            *L = Leaf{k, c, {pc}};
+            return true;
+        }
+        if (in.op == MOL_OP_MUL) {
+            double c;
+            for (int side = 0; side < 2; ++side) {
+                const int cp = side ? s.ib[pc] : s.ia[pc], xp = side ? s.ia[pc] : s.ib[pc];
+                if (!is_uniform_const(cp, &c)) continue;
+                Leaf inner;
+                if (xp >= 0 && leaf(xp, &inner)) {
+                    inner.coef *= c;
+                    inner.nodes.push_back(pc);
+                    *L = inner;
+                    return true;
+                }
+            }
+        }
+        return false;
+    };
+    for (int pc = 0; pc < n; ++pc) {
+        if (s.ins[pc].op != MOL_OP_OUT || s.ia[pc] < 0) continue;
+        FoldGroup g;
+        g.out_pc = pc;
+        // flatten the output's sum: ADD / SUB / NEG nodes used once (the root included)
+        std::vector<std::pair<double, int>> adds;
+        std::vector<int> chain;
+        std::function<void(int, double, bool)> flat = [&](int q, double sg, bool root) {
+            const mol_instr& in = s.ins[q];
+            double cv;
+            const bool varying = !is_uniform_const(q, &cv);
+            if (varying && (root || uses[q] == 1) && (in.op == MOL_OP_ADD || in.op == MOL_OP_SUB)) {
+                chain.push_back(q);
+                flat(s.ia[q], sg, false);
+                flat(s.ib[q], in.op == MOL_OP_SUB ? -sg : sg, false);
+                return;
+            }
+            if (varying && (root || uses[q] == 1) && in.op == MOL_OP_NEG) {
+                chain.push_back(q);
+                flat(s.ia[q], -sg, false);
+                return;
+            }
+            adds.push_back({sg, q});
+        };
+        flat(s.ia[pc], 1.0, true);
+        std::vector<Leaf> leaves;
+        for (auto& a : adds) {
+            Leaf L;
+            if (leaf(a.second, &L) && (g.field < 0 || d->terms[L.term].field == g.field)) {
+                g.field = d->terms[L.term].field;
+                L.coef *= a.first;
+                g.folded.push_back(a);
+                leaves.push_back(L);
+            } else {
+                g.rest.push_back(a);
+            }
+        }
+        // worth it: two or more stencils, or one with a coefficient to fold
+        if (leaves.empty() || (leaves.size() == 1 && leaves[0].nodes.size() == 1 && std::fabs(leaves[0].coef) == 1.0))
+            continue;
+        g.absorbed = chain;
+        for (auto& L : leaves)
+            for (int q : L.nodes) {
+                g.absorbed.push_back(q);
+                g.leaf_nodes.push_back(q);
+            }
+        std::sort(g.leaf_nodes.begin(), g.leaf_nodes.end());
+        // the term whose reserved2 holds the weights' offset: one not already keying a group
+        g.key_term = -1;
+        for (auto& L : leaves) {
+            bool taken = false;
+            for (auto& h : groups) taken |= h.key_term == L.term;
+            if (!taken && (g.key_term < 0 || L.term < g.key_term)) g.key_term = L.term;
+        }
+        if (g.key_term < 0) continue;
+        auto add_part = [&](int o0, int o1, int o2, const FoldPart& p) {
+            for (auto& t : g.taps)
+                if (t.o[0] == o0 && t.o[1] == o1 && t.o[2] == o2) {
+                    t.parts.push_back(p);
+                    return;
+                }
+            FoldTap t;
+            t.o[0] = o0;
+            t.o[1] = o1;
+            t.o[2] = o2;
+            t.parts.push_back(p);
+            g.taps.push_back(t);
+        };
+        for (auto& L : leaves) {
+            const mol_term& tm = d->terms[L.term];
+            if (tm.kind == MOL_TERM_LINEAR) {
+                const mol_op1d& o = d->ops[tm.op];
+                for (int m = 0; m < o.L; ++m) {
+                    if (!nz(o.w_int + m)) continue;
+                    int off[3] = {0, 0, 0};
+                    off[tm.dim] = o.omin + m;
+                    add_part(off[0], off[1], off[2], FoldPart{L.term, m, L.coef});
+                }
+            } else {
+                const mol_op1d& o1 = d->ops[tm.op];
+                const mol_op1d& o2 = d->ops[tm.op2];
+                for (int x = 0; x < o1.L; ++x)
+                    for (int y = 0; y < o2.L; ++y) {
+                        if (!nz(o1.w_int + x) || !nz(o2.w_int + y)) continue;
+                        int off[3] = {0, 0, 0};
+                        off[tm.dim] += o1.omin + x;
+                        off[tm.dim2] += o2.omin + y;
+                        add_part(off[0], off[1], off[2], FoldPart{L.term, x * o2.L + y, L.coef});
+                    }
+            }
+        }
+        groups.push_back(g);
+    }
+    return groups;
+}
+
+// The fused weights of `g`: per tap the sum over its parts of coefficient * weight (MIXED:
+// the product of the two interior weights), in part order.
+std::vector<double> fold_weights(const mol_problem_desc* d, const FoldGroup& g) {
+    std::vector<double> w;
+    for (const FoldTap& t : g.taps) {
+        double acc = 0.0;
+        bool first = true;
+        for (const FoldPart& p : t.parts) {
+            const mol_term& tm = d->terms[p.term];
+            double wk;
+            if (tm.kind == MOL_TERM_LINEAR) {
+                wk = d->weights[d->ops[tm.op].w_int + p.m];
+            } else {
+                const mol_op1d& o2 = d->ops[tm.op2];
+                wk = d->weights[d->ops[tm.op].w_int + p.m / o2.L] * d->weights[o2.w_int + p.m % o2.L];
+            }
+            acc = first ? p.coef * wk : acc + p.coef * wk;
+            first = false;
+        }
+        w.push_back(acc);
+    }
+    return w;
+}
+
+namespace {
 
 // How leaves of a program are read and how their adjoints are written.
 struct Leaves {
@@ -866,6 +1074,15 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
         }
     }
     auto name = [&](int pc) { return uni[pc] ? "U.u" + std::to_string(pc) : v(pc); };
+    // constant-coefficient fusion of first-derivative stencils (const_linear_groups): the
+    // nodes a group absorbs are emitted on its fallback path only
+    const std::vector<FoldGroup> cgroups = const_linear_groups(d);
+    std::vector<char> cabs(n, 0);
+    std::map<int, int> cgroup_at;
+    for (size_t gi = 0; gi < cgroups.size(); ++gi) {
+        for (int q : cgroups[gi].absorbed) cabs[q] = 1;
+        cgroup_at[cgroups[gi].out_pc] = (int)gi;
+    }
     // linear analysis
     std::vector<LinInfo> lin(n);
     for (int pc = 0; pc < n; ++pc) {
@@ -920,7 +1137,7 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
     // Off by default: on GB300 the fused stencil's extra live weights cost more occupancy than
     // the FP64 operations it saves (measured); MOL_JIT_FUSE=1 turns it on.
     const char* fz = getenv("MOL_JIT_FUSE");
-    const bool fuse = fz && fz[0] == '1';
+    const bool fuse = fz && fz[0] == '1' && cgroups.empty();
     for (int pc = n - 1; pc >= 0 && fuse; --pc) {
         if (!lin[pc].ok || absorbed[pc]) continue;
         if (s.ins[pc].op == MOL_OP_TERM) continue;  // a lone term gains nothing
@@ -1074,13 +1291,77 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
             default: return "";
         }
     };
+    // one constant-coefficient group: the fused stencil where every member is on its interior
+    // (or wrapped periodic) path, the original terms elsewhere, then the output's other addends
+    auto emit_cgroup = [&](int gi, int out_field) {
+        const FoldGroup& g = cgroups[gi];
+        const std::string G = "fg" + std::to_string(gi), F = std::to_string(g.field);
+        std::set<int> members;
+        int reach[3] = {0, 0, 0};
+        for (const FoldTap& t : g.taps) {
+            for (const FoldPart& p : t.parts) members.insert(p.term);
+            for (int q = 0; q < 3; ++q) reach[q] = std::max(reach[q], std::abs(t.o[q]));
+        }
+        std::string cond_u, cond_w;   // uniform (periodic wrap) and per-cell (interior) parts
+        for (int q = 0; q < 3; ++q) {
+            if (!reach[q]) continue;
+            if (periodic_dim(d, g.field, q)) {
+                cond_u += (cond_u.empty() ? "" : " && ") + std::string("wrap_line_ok(P, ") + F + ", " +
+                          std::to_string(q) + ", " + std::to_string(reach[q]) + ")";
+                continue;
+            }
+            for (int k : members) {
+                const mol_term& tm = d->terms[k];
+                const int op = tm.dim == q ? tm.op : (tm.kind == MOL_TERM_MIXED && tm.dim2 == q ? tm.op2 : -1);
+                if (op < 0) continue;
+                cond_w += (cond_w.empty() ? "" : " && ") + std::string("fast_line(P, P.ops[") + std::to_string(op) +
+                          "], " + F + ", " + std::to_string(q) + ", I[" + std::to_string(q) + "])";
+            }
+        }
+        std::string cond = cond_u.empty() ? "true" : cond_u;
+        if (!cond_w.empty()) cond += " && warp_all(" + cond_w + ")";
+        e << "    T " << G << ";\n    if (" << cond << ") {\n"
+          << "        const T* __restrict__ fw = P.w + P.terms[" << g.key_term << "].reserved2;\n"
+          << "        const T* __restrict__ fb = u + (long long)" << F << " * P.ncell + c;\n";
+        for (size_t i = 0; i < g.taps.size(); ++i) {
+            std::string off;
+            for (int q = 0; q < 3; ++q) {
+                if (!g.taps[i].o[q]) continue;
+                const std::string oq = std::to_string(g.taps[i].o[q]);
+                const std::string term = periodic_dim(d, g.field, q)
+                                             ? "(long long)wrap_off(I[" + std::to_string(q) + "], " + oq + ", P.n[" +
+                                                   std::to_string(q) + "]) * gstride(P, " + std::to_string(q) + ")"
+                                             : "(long long)(" + oq + ") * gstride(P, " + std::to_string(q) + ")";
+                off += (off.empty() ? "" : " + ") + term;
+            }
+            if (off.empty()) off = "0";
+            if (i == 0) e << "        T acc = fw[0] * fb[" << off << "];\n";
+            else e << "        acc = fma(fw[" << i << "], fb[" << off << "], acc);\n";
+        }
+        e << "        " << G << " = " << (g.taps.empty() ? "T(0)" : "acc") << ";\n    } else {\n";
+        for (int q : g.leaf_nodes) e << "        " << stmt(q) << "\n";
+        std::string fsum;
+        for (auto& a : g.folded) {
+            const std::string x = name(a.second);
+            fsum = fsum.empty() ? (a.first < 0 ? "-" + x : x) : fsum + (a.first < 0 ? " - " : " + ") + x;
+        }
+        e << "        " << G << " = " << fsum << ";\n    }\n";
+        std::string sum;
+        for (auto& a : g.rest) {
+            const std::string x = name(a.second);
+            sum = sum.empty() ? (a.first < 0 ? "-" + x : x) : sum + (a.first < 0 ? " - " : " + ") + x;
+        }
+        e << "    out[" << out_field << "] = " << (sum.empty() ? G : "(" + sum + ") + " + G) << ";\n";
+    };
     for (int pc = 0; pc < n; ++pc) {
         const mol_instr& in = s.ins[pc];
         if (in.op == MOL_OP_OUT) {
-            e << "    out[" << in.imm << "] = " << name(s.ia[pc]) << ";\n";
+            auto it = cgroup_at.find(pc);
+            if (it != cgroup_at.end()) emit_cgroup(it->second, in.imm);
+            else e << "    out[" << in.imm << "] = " << name(s.ia[pc]) << ";\n";
             continue;
         }
-        if (uni[pc] || absorbed[pc]) continue;
+        if (uni[pc] || absorbed[pc] || cabs[pc]) continue;
         if (!root[pc]) {
             e << "    " << stmt(pc) << "\n";
             continue;

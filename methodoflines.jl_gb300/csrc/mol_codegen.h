@@ -35,6 +35,37 @@ std::string generate_source(const mol_problem_desc* d, std::string& why);
 // wo[1] * wi[1] and 1 / wi[1] to the weight pool at the term's reserved0 offset.
 // MOL_JIT_FOLD=0 turns the folded form off.
 bool nonlinlap_fold(const mol_problem_desc* d, int k);
+
+// Constant-coefficient fusion of first-derivative stencils.  In the sum that forms one
+// output of the cell program, the addends c * T with c a compile-time constant and T a
+// first-derivative stencil of one field (a LINEAR term with antisymmetric interior weights,
+// a MIXED term, or the stencil an UPWIND select picks for the constant's sign) are evaluated
+// as one stencil over the union of their taps, with weights sum(c * w) precomputed per plan
+// (appended to the weight pool; the offset is stored in terms[key_term].reserved2).  Second
+// derivatives are left alone: folding a constant into a 1/dx^2 stencil changes the rounding
+// of its cancelling sum by far more than the 1e-12 parity bar.  MOL_JIT_CFOLD=0 turns it off.
+struct FoldPart {
+    int term;      // member term
+    int m;         // interior weight index (MIXED: x * L2 + y)
+    double coef;   // the constant, sign included
+};
+struct FoldTap {
+    int o[3];
+    std::vector<FoldPart> parts;
+};
+struct FoldGroup {
+    int out_pc = -1;                        // OUT instruction of the cell program
+    int field = -1;
+    int key_term = -1;
+    std::vector<std::pair<double, int>> folded;   // (sign, leaf pc) in addend order
+    std::vector<std::pair<double, int>> rest;     // the other addends, in order
+    std::vector<int> absorbed;              // pcs emitted only on the fallback path (or not at all)
+    std::vector<int> leaf_nodes;            // pcs of the folded leaves' subtrees (fallback path)
+    std::vector<FoldTap> taps;
+};
+std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d);
+// The fused weights of a group, one per tap (sum over its parts of coefficient * weight).
+std::vector<double> fold_weights(const mol_problem_desc* d, const FoldGroup& g);
 std::vector<std::string> jit_kernel_names(int nparams, int group);
 // Generates, compiles (NVRTC, sm_103a) and loads the module of a problem structure;
 // modules are cached per generated source for the life of the process.

@@ -996,6 +996,13 @@ int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member
             weights.push_back(1.0 / wi1);
         }
     }
+    // fused weights of the constant-coefficient first-derivative groups (at reserved2 of
+    // each group's key term)
+    for (const FoldGroup& g : const_linear_groups(d)) {
+        const std::vector<double> fw = fold_weights(d, g);
+        terms[g.key_term].reserved2 = (int32_t)weights.size();
+        weights.insert(weights.end(), fw.begin(), fw.end());
+    }
     mol_problem_desc dd = *d;
     dd.weights = weights.data();
     dd.nweights = (int64_t)weights.size();
