@@ -94,7 +94,9 @@ template <class T>
 void face_window(const mol_batch* b, size_t* bytes, long long* cells) {
     *bytes = 0;
     *cells = 0;
-    if (b->nface <= 0) return;
+    // FP64 state only: the Float32-state ensemble is not bound by its face arithmetic, and the
+    // window's barriers made it slower (1000 steps of the 4096 members: 25.5 s -> 33.5 s)
+    if (b->nface <= 0 || sizeof(T) != sizeof(double)) return;
     long long want = 45056;
     if (const char* e = getenv("MOL_BATCH_FACE_BYTES")) want = std::max(0ll, std::min(atoll(e), 48ll * 1024));
     const long long w = want / ((long long)b->nface * (long long)sizeof(T));

@@ -285,7 +285,9 @@ DevProb<T> with_faces(mol_plan* plan, const T* u, const T* p, double toff, doubl
     cudaKernel_t k = std::is_same<T, double>::value ? plan->jit.faces64 : plan->jit.faces32;
     // FP32 arithmetic is not the bound of the Float32-state kernels: no face pass there
     if (!std::is_same<T, double>::value || !plan->face_pass || !plan->use_jit || !fb || !k) return P;
-    *e = launch_k(k, plan->nblocks, plan->nthreads, plan->stream, P, u, p, (const SolverState*)plan->d_state, toff,
+    *e = launch_k(k, plan->face_blocks > 0 ? plan->face_blocks : plan->nblocks,
+                  plan->face_blocks > 0 ? plan->face_threads : plan->nthreads, plan->stream, P, u, p,
+                  (const SolverState*)plan->d_state, toff,
                   tfix, fb);
     ++g_launches;
     P.faces = fb;
@@ -1064,6 +1066,21 @@ int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member
                 if (d->terms[k].kind == MOL_TERM_NONLINLAP) ++plan->nface;
             const char* fp = getenv("MOL_FACE_PASS");
             plan->face_pass = plan->nface > 0 && (fp && fp[0] ? fp[0] == '1' : ncell >= 32768);
+            if (plan->face_pass && plan->jit.faces64) {
+                // as many resident CTAs per SM as the face kernel's registers allow (MOL_FACE_CTAS
+                // caps it): its loads and stores need the warps to hide their latency
+                int bps = 0;
+                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)plan->jit.faces64, 256, 0) !=
+                    cudaSuccess)
+                    cudaGetLastError();
+                if (const char* fc = getenv("MOL_FACE_CTAS"))
+                    if (atoi(fc) > 0) bps = std::min(bps, atoi(fc));
+                if (bps > 0) {
+                    plan->face_threads = 256;
+                    plan->face_blocks = (int)std::max<long long>(
+                        1, std::min<long long>((long long)sms * bps, (ncell + 255) / 256));
+                }
+            }
         }
         if (!plan->use_jit) {
             const char* req = getenv("MOL_REQUIRE_CODEGEN");

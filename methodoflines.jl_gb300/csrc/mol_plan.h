@@ -62,6 +62,9 @@ struct mol_plan {
     mol::SolverState* d_state = nullptr;
     double* d_partials = nullptr;
     int nblocks = 0;
+    // grid of the face pass: it moves more bytes per FP64 operation than the stage kernels
+    // and needs more warps in flight, so it runs at its own (higher) occupancy
+    int face_blocks = 0, face_threads = 256;
     int sms = 152;
     int nthreads = 256;
     // adjoint workspaces

@@ -33,6 +33,13 @@ def _torch():
     return torch
 
 
+def _on_stream(obj, torch):
+    """Run a plan or batch on torch's current stream, so its asynchronous work on device
+    tensors is ordered with the torch operations that produce and read them."""
+    obj.set_stream(torch.cuda.current_stream().cuda_stream)
+    return obj
+
+
 @pytest.fixture(scope="module")
 def bruss1024():
     sys_, disc, ex = problems.brusselator(N=1024)
@@ -50,7 +57,7 @@ def adr256():
 def test_brusselator_1024_rhs_and_steps(gpu_lib, bruss1024):
     torch = _torch()
     lw, dt, cref = bruss1024
-    plan = Plan(lw)
+    plan = _on_stream(Plan(lw), torch)
     u = torch.tensor(lw.u0, device="cuda")
     du = torch.zeros_like(u)
     for t in (0.5, 1.2):                       # before and after the forcing switches on
@@ -84,7 +91,7 @@ def test_adr3d_256_rhs_and_steps(gpu_lib, adr256):
     """The headline workload: RHS through the face pass, SSPRK33 steps, device state."""
     torch = _torch()
     lw, dt, cref = adr256
-    plan = Plan(lw)
+    plan = _on_stream(Plan(lw), torch)
     u = torch.tensor(lw.u0, device="cuda")
     du = torch.zeros_like(u)
     plan.rhs(du, u, None, 0.1)
@@ -136,7 +143,7 @@ def test_ensemble_4096_members(gpu_lib):
         specs.append(spec)
         dts.append(0.125 / (n - 1) ** 2 / float(np.max(lw.u0)) ** 2)
     dts = np.array(dts)
-    batch = Batch(lws)
+    batch = _on_stream(Batch(lws), torch)
     u = torch.tensor(batch.pack([lw.u0 for lw in lws]), device="cuda")
     batch.step_ssprk33(u, dts, 3)
     batch.check()
@@ -158,7 +165,7 @@ def test_burgers_65536_gradient_64_snapshots(gpu_lib):
     torch = _torch()
     sys_, disc, ex = problems.burgers()
     lw = lower(sys_.to_spec(disc))
-    plan = Plan(lw)
+    plan = _on_stream(Plan(lw), torch)
     n, dt, steps = lw.n_unknowns, ex["dt"], 200
     tgt = torch.tensor(ex["target"], device="cuda")
     u0 = torch.tensor(lw.u0, device="cuda")
