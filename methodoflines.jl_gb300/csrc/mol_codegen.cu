@@ -848,6 +848,51 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
         return per ? "(long long)wrap_off(I[" + D + "], " + std::to_string(x) + ", P.n[" + D + "]) * s"
                    : "(long long)(" + std::to_string(x) + ") * s";
     };
+    // Folded form: the stored face value F' of half point Ih from runtime positions, with the
+    // fast paths' arithmetic where the face's stencils are interior (so the face pass, the
+    // ensemble's window and the cells' own evaluation agree bit for bit), else the generic
+    // face divided by wi[1].  The edge path of the cell reads faces through it.
+    int reach_l = 0;
+    for (int t_ : nzi) reach_l = std::max(reach_l, std::abs(-1 + oi.omin + t_));
+    for (int t_ : nzp) reach_l = std::max(reach_l, std::abs(-1 + op.omin + t_));
+    if (fold) {
+        std::string gc;
+        if (per) {
+            gc = "wrap_line_ok(P, " + F + ", " + D + ", " + std::to_string(reach_l) + ")";
+            for (int f : used_fields)
+                if (f != tm.field)
+                    gc += " && wrap_line_ok(P, " + std::to_string(f) + ", " + D + ", " + std::to_string(reach_l) + ")";
+        } else {
+            gc = "fast_line(P, P.ops[" + opi + "], " + F + ", " + D + ", Ih) && fast_line(P, P.ops[" + opp + "], " + F +
+                 ", " + D + ", Ih)";
+        }
+        auto lp = [&](int f, const std::string& pos) {
+            return "line_pt<T, " + D + ", " + dyn_bc(d, f, tm.dim) + ">(P, u, " + std::to_string(f) + ", I, c, " + pos +
+                   ", t, p)";
+        };
+        e << "template <class T>\n__device__ __forceinline__ T gfacef" << K
+          << "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, int Ih, T t, const T* "
+             "__restrict__ p) {\n"
+          << "    if (" << gc << ") {\n"
+          << "    const T* __restrict__ wp = P.w + P.ops[" << opp << "].w_int;\n"
+          << "    const T gf_du = " << lp(tm.field, "Ih + (" + std::to_string(oi.omin + 1) + ")") << " - "
+          << lp(tm.field, "Ih + (" + std::to_string(oi.omin) + ")") << ";\n";
+        for (int f : used_fields) {
+            for (size_t q = 0; q < nzp.size(); ++q) {
+                const int t_ = nzp[q];
+                const std::string tap = lp(f, "Ih + (" + std::to_string(op.omin + t_) + ")");
+                if (q == 0) e << "    T gf_uf" << f << " = wp[" << t_ << "] * " << tap << ";\n";
+                else e << "    gf_uf" << f << " = fma(wp[" << t_ << "], " << tap << ", gf_uf" << f << ");\n";
+            }
+            if (nzp.empty()) e << "    T gf_uf" << f << " = T(0);\n";
+        }
+        for (int j : used_aux)
+            e << "    const T gf_fa" << j << " = P.aux[P.aux_off[P.terms[" << K << "].aux0 + " << j
+              << "] + face_index(P, " << D << ", Ih, I)];\n";
+        face_forward("gf_");
+        e << "    return gf_a * gf_du;\n    }\n"
+          << "    return gface" << K << "<T>(P, u, c, I, Ih, t, p) * " << RWI << ";\n}\n";
+    }
     // fast path helpers: relative face offsets r = omin_outer + m - 1 (outer stencil sits at II - 1)
     // statements computing the face at relative half point r: tag du, tag uf<f>, the face
     // program; leaves tag a and tag du
@@ -1000,7 +1045,9 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
               << "            F_ = P.faces[(long long)" << FQ << " * P.fstride + cf_]"
               << (fold ? " * P.w[P.ops[" + opi + "].w_int + 1]" : "") << ";\n"
               << "        else\n"
-              << "            F_ = gface" << K << "<T>(P, u, c, I, Ih, t, p);\n"
+              << (fold ? "            F_ = gfacef" + K + "<T>(P, u, c, I, Ih, t, p) * P.w[P.ops[" + opi +
+                             "].w_int + 1];\n"
+                       : "            F_ = gface" + K + "<T>(P, u, c, I, Ih, t, p);\n")
               << "        acc = started ? fma(w_, F_, acc) : w_ * F_;\n        started = true;\n    }\n    return acc;\n";
         else
             e << "        gface" << K << "_vjp<T>(P, u, c, I, so.first + q, t, p, g * w_, lam_u, lp, lam_aux);\n    }\n";
@@ -1030,8 +1077,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
       << "    const long long s = gstride(P, " << D << ");\n";
     face_body(-1, "fl_", false);
     e << "    return fl_a * fl_du;\n    }\n"
-      << "    return gface" << K << "<T>(P, u, c, I, I[" << D << "] - 1, t, p)" << (fold ? " * " + RWI : "")
-      << ";\n}\n";
+      << "    return " << (fold ? "gfacef" : "gface") << K << "<T>(P, u, c, I, I[" << D << "] - 1, t, p);\n}\n";
 }
 
 }  // namespace
@@ -1584,6 +1630,12 @@ std::vector<std::string> jit_options(int min_blocks) {
     const char* mb = getenv("MOL_JIT_MIN_BLOCKS");
     const int minb = (mb && atoi(mb) > 0) ? atoi(mb) : (min_blocks > 0 ? min_blocks : kDefaultMinBlocks);
     o.push_back("-DMOL_MIN_BLOCKS=" + std::to_string(minb));
+    // the face pass at one resident CTA per SM more than the stage kernels (ptxas: the ADR
+    // face kernel fits 64 registers with 28 bytes of spills; at 40 it spills 260 bytes);
+    // MOL_FACE_MIN_BLOCKS overrides
+    const char* fmb = getenv("MOL_FACE_MIN_BLOCKS");
+    const int fminb = (fmb && atoi(fmb) > 0) ? atoi(fmb) : std::min(8, minb + 1);
+    o.push_back("-DMOL_FACE_MIN_BLOCKS=" + std::to_string(fminb));
     // MOL_BATCH_MIN_BLOCKS: the same bound for the ensemble kernels (default 1: no cap)
     const char* bmb = getenv("MOL_BATCH_MIN_BLOCKS");
     if (bmb && atoi(bmb) > 0) o.push_back("-DMOL_BATCH_MIN_BLOCKS=" + std::to_string(atoi(bmb)));

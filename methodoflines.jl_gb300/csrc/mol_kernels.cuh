@@ -19,6 +19,11 @@ constexpr int kThreads = 256;
 #ifndef MOL_MIN_BLOCKS
 #define MOL_MIN_BLOCKS 1
 #endif
+// The face pass moves ~7 bytes per FP64 instruction: it needs more warps in flight than the
+// stage kernels, so its register budget allows more resident CTAs (set for generated modules).
+#ifndef MOL_FACE_MIN_BLOCKS
+#define MOL_FACE_MIN_BLOCKS MOL_MIN_BLOCKS
+#endif
 
 // Correctly rounded x/3 with one multiply and two FMAs (Markstein's theorem:
 // with c = RN(1/3) and q0 within an ulp of x/3, q0 + (x - 3 q0) c rounds to
@@ -91,7 +96,7 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_rhs_t(const __grid
 // computed once instead of evaluating it for both cells that share it.  The time is
 // S->t (tfix NaN) or tfix, plus toff, exactly as the stage kernel forms its stage time.
 template <class T, class G>
-__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_faces_t(const __grid_constant__ DevProb<T> P,
+__global__ void __launch_bounds__(kThreads, MOL_FACE_MIN_BLOCKS) k_faces_t(const __grid_constant__ DevProb<T> P,
                                                                       const T* __restrict__ u,
                                                                       const T* __restrict__ p, const SolverState* S,
                                                                       double toff, double tfix, T* __restrict__ faces) {
