@@ -89,7 +89,25 @@ struct DevProb {
     const T* faces;
     long long fstride;
     long long fbeg, fend;   // cells whose faces `faces` holds: [fbeg, fend)
+    // cell index -> grid position by multiplication (divmagic) when ncell < 2^31: the magic
+    // multipliers and shifts of ni[0] and ni[1]
+    unsigned dm[2], ds[2];
+    int fastdiv;
 };
+
+// Division of n < 2^31 by an invariant divisor d with a precomputed multiplier m and shift l
+// (Granlund and Montgomery, "Division by invariant integers using multiplication", PLDI
+// 1994, Fig. 4.1 with N = 32): l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, and
+// floor(n / d) = (umulhi(m, n) + n) >> l, the sum below 2^32 for n < 2^31.  Grid positions
+// are taken from cell indices in every kernel; the hardware has no integer divide, and the
+// generic 64-bit division costs ~100 instructions per cell, as much as a face pass's FP64 work.
+__host__ __device__ inline void divmagic(unsigned d, unsigned* m, unsigned* l) {
+    unsigned s = 0;
+    while (s < 32 && (1ull << s) < (unsigned long long)d) ++s;
+    *l = s;
+    *m = (unsigned)((((1ull << s) - d) << 32) / d + 1);
+}
+__device__ __forceinline__ unsigned divq(unsigned n, unsigned m, unsigned l) { return (__umulhi(m, n) + n) >> l; }
 
 __device__ __forceinline__ int wrap_periodic(int i, int l) {
     // _wrapperiodic (interface_boundary.jl:33-42): u[1] == u[l]
@@ -901,6 +919,15 @@ __device__ __noinline__ T eval_term(const DevProb<T>& P, int k, const T* u, cons
 // Full-grid index of interior cell `c` (flat, first dimension fastest).
 template <class T>
 __device__ __forceinline__ void cell_index(const DevProb<T>& P, long long c, int* I) {
+    if (P.fastdiv) {
+        const unsigned cc = (unsigned)c;
+        const unsigned r = divq(cc, P.dm[0], P.ds[0]);
+        const unsigned c2 = divq(r, P.dm[1], P.ds[1]);
+        I[0] = (int)(cc - r * (unsigned)P.ni[0]) + 1 + P.lo[0];
+        I[1] = (int)(r - c2 * (unsigned)P.ni[1]) + 1 + P.lo[1];
+        I[2] = (int)c2 + 1 + P.lo[2];
+        return;
+    }
     const long long c0 = c % P.ni[0];
     const long long r = c / P.ni[0];
     const long long c1 = r % P.ni[1];

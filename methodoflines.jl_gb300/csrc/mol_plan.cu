@@ -792,6 +792,8 @@ static int build_prec(mol_plan* plan, const mol_problem_desc* d, PlanArrays& A, 
         P.ni[q] = P.n[q] - P.lo[q] - P.up[q];
         P.coords[q] = (const T*)A.coords[q];
     }
+    P.fastdiv = plan->ncell < (1ll << 31) && P.ni[0] >= 1 && P.ni[1] >= 1;
+    for (int q = 0; q < 2; ++q) divmagic((unsigned)std::max(1, P.ni[q]), &P.dm[q], &P.ds[q]);
     for (int f = 0; f < MOL_MAX_FIELDS; ++f) {
         int m = 0;
         if (f < d->nfields)
