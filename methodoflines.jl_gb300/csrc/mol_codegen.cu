@@ -890,7 +890,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
             e << "    const T gf_fa" << j << " = P.aux[P.aux_off[P.terms[" << K << "].aux0 + " << j
               << "] + face_index(P, " << D << ", Ih, I)];\n";
         face_forward("gf_");
-        e << "    return gf_a * gf_du;\n    }\n"
+        e << "    return mulrn(gf_a, gf_du);\n    }\n"
           << "    return gface" << K << "<T>(P, u, c, I, Ih, t, p) * " << RWI << ";\n}\n";
     }
     // fast path helpers: relative face offsets r = omin_outer + m - 1 (outer stencil sits at II - 1)
@@ -944,7 +944,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
         if (!vjp && fold) {
             // the two faces go to F0 / F1 declared by the caller
             face_body(r, tag, false);
-            e << "    F" << m << " = " << tag << "a * " << tag << "du;\n";
+            e << "    F" << m << " = mulrn(" << tag << "a, " << tag << "du);\n";
         } else if (!vjp) {
             face_body(r, tag, false);
             e << "    const T " << tag << "F = " << tag << "a * " << tag << "du;\n";
@@ -1076,7 +1076,7 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
       << "    const T* __restrict__ bF = u + (long long)" << F << " * P.ncell + c;\n"
       << "    const long long s = gstride(P, " << D << ");\n";
     face_body(-1, "fl_", false);
-    e << "    return fl_a * fl_du;\n    }\n"
+    e << "    return " << (fold ? "mulrn(fl_a, fl_du)" : "fl_a * fl_du") << ";\n    }\n"
       << "    return " << (fold ? "gfacef" : "gface") << K << "<T>(P, u, c, I, I[" << D << "] - 1, t, p);\n}\n";
 }
 

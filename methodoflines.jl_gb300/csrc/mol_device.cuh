@@ -120,6 +120,12 @@ __device__ __forceinline__ int wrap_periodic(int i, int l) {
 // result) instead of both paths one after the other.
 __device__ __forceinline__ bool warp_all(bool p) { return __all_sync(__activemask(), p); }
 
+// A product rounded on its own, never contracted into an FMA with the addition that uses it:
+// the folded nonlinear-Laplacian faces are stored by the face pass (rounded) and subtracted
+// in the cell, so the cells' own evaluation must round them the same way to agree bit for bit.
+__device__ __forceinline__ double mulrn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mulrn(float a, float b) { return __fmul_rn(a, b); }
+
 // Offset, along a periodic line of n points, of the tap at i + off after the same single
 // wrap (the unknowns being points 2..n).  Valid while |off| <= n - 2.
 __device__ __forceinline__ int wrap_off(int i, int off, int n) {
