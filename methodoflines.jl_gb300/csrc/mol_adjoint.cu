@@ -182,7 +182,7 @@ struct Adj {
         if (err) return;
         const DevProb<double>& P = plan->P64;
         cap_begin();
-        cudaError_t e = launch_k(plan->jit.vjp64, plan->nblocks, plan->nthreads, plan->stream, P, in, scale, u, p, t,
+        cudaError_t e = launch_k(plan->jit.vjp64, plan->vjp_blocks > 0 ? plan->vjp_blocks : plan->nblocks, plan->nthreads, plan->stream, P, in, scale, u, p, t,
                                  out, lam_p, lam_aux);
         ++g_launches;
         ck(e, "vjp launch");
@@ -344,6 +344,16 @@ int need_vjp(mol_plan* plan) {
     if (st) return set_err(plan, st, plan->jit_err);
     st = jit_ensure(&plan->jit, JIT_FWD64, plan->jit_err);
     if (st) return set_err(plan, st, plan->jit_err);
+    if (!plan->vjp_blocks) {
+        // SMs x the VJP kernel's resident CTAs (a grid-stride loop: one wave)
+        int bps = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)plan->jit.vjp64, plan->nthreads, 0) !=
+            cudaSuccess)
+            cudaGetLastError();
+        plan->vjp_blocks = bps > 0 ? (int)std::max<long long>(1, std::min<long long>((long long)plan->sms * bps,
+                                                                   (plan->ncell + plan->nthreads - 1) / plan->nthreads))
+                                   : plan->nblocks;
+    }
     return MOL_OK;
 }
 
@@ -414,7 +424,7 @@ int mol_rhs_vjp(mol_plan* plan, const double* lambda, const double* u, const dou
     VjpSeed<double> in = {};
     in.x[0] = dl;
     in.a[0] = 1.0;
-    cudaError_t e = launch_k(plan->jit.vjp64, plan->nblocks, plan->nthreads, plan->stream, P, in, 1.0, du, pp, t, ou,
+    cudaError_t e = launch_k(plan->jit.vjp64, plan->vjp_blocks > 0 ? plan->vjp_blocks : plan->nblocks, plan->nthreads, plan->stream, P, in, 1.0, du, pp, t, ou,
                              lam_p ? op : (double*)nullptr, oa);
     ++g_launches;
     if ((st = cuda_check(plan, e, "vjp"))) return st;

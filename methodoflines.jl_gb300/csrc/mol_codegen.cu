@@ -1636,6 +1636,11 @@ std::vector<std::string> jit_options(int min_blocks) {
     const char* fmb = getenv("MOL_FACE_MIN_BLOCKS");
     const int fminb = (fmb && atoi(fmb) > 0) ? atoi(fmb) : std::min(8, minb + 1);
     o.push_back("-DMOL_FACE_MIN_BLOCKS=" + std::to_string(fminb));
+    // the VJP at no more than two resident CTAs (128 registers: 44 bytes of spills for the ADR
+    // cell instead of 2.2 KB at 80); MOL_VJP_MIN_BLOCKS overrides
+    const char* vmb = getenv("MOL_VJP_MIN_BLOCKS");
+    const int vminb = (vmb && atoi(vmb) > 0) ? atoi(vmb) : std::min(minb, 2);
+    o.push_back("-DMOL_VJP_MIN_BLOCKS=" + std::to_string(vminb));
     // MOL_BATCH_MIN_BLOCKS: the same bound for the ensemble kernels (default 1: no cap)
     const char* bmb = getenv("MOL_BATCH_MIN_BLOCKS");
     if (bmb && atoi(bmb) > 0) o.push_back("-DMOL_BATCH_MIN_BLOCKS=" + std::to_string(atoi(bmb)));

@@ -28,6 +28,11 @@ constexpr int kThreads = 256;
 #ifndef MOL_FACE_MIN_BLOCKS
 #define MOL_FACE_MIN_BLOCKS MOL_MIN_BLOCKS
 #endif
+// The vector-Jacobian product holds the forward values and partials of a whole cell: at the
+// stage kernels' 80-register budget it spilled 2.2 KB per thread (ptxas), so it gets its own.
+#ifndef MOL_VJP_MIN_BLOCKS
+#define MOL_VJP_MIN_BLOCKS MOL_MIN_BLOCKS
+#endif
 
 // Correctly rounded x/3 with one multiply and two FMAs (Markstein's theorem:
 // with c = RN(1/3) and q0 within an ulp of x/3, q0 + (x - 3 q0) c rounds to
@@ -189,7 +194,7 @@ struct VjpSeed {
 };
 
 template <class T, class G, int NP>
-__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_vjp_t(const __grid_constant__ DevProb<T> P,
+__global__ void __launch_bounds__(kThreads, MOL_VJP_MIN_BLOCKS) k_vjp_t(const __grid_constant__ DevProb<T> P,
                                                                     const VjpSeed<T> in, T scale,
                                                                     const T* __restrict__ u, const T* __restrict__ p,
                                                                     double t, T* lam_u, T* lam_p, T* lam_aux) {

@@ -65,6 +65,7 @@ struct mol_plan {
     // grid of the face pass: it moves more bytes per FP64 operation than the stage kernels
     // and needs more warps in flight, so it runs at its own (higher) occupancy
     int face_blocks = 0, face_threads = 256;
+    int vjp_blocks = 0;   // grid of the vector-Jacobian product (its own register budget)
     int sms = 152;
     int nthreads = 256;
     // adjoint workspaces
