@@ -14,11 +14,11 @@ constexpr int kThreads = 256;
 // Minimum resident CTAs per SM requested from the register allocator for the kernels that
 // evaluate the right-hand side (set for generated modules, MOL_JIT_MIN_BLOCKS).
 #ifndef MOL_BATCH_MIN_BLOCKS
-// ensemble kernels: CTAs of kThreads per SM the register budget must allow.  2 keeps the tiled
-// kernel at 128 registers (no spills for the nonlinear-diffusion members), so four CTAs of
-// 128 threads fit an SM; uncapped it took 134 and the autotuner fell back to one CTA per
-// instance (48 s -> 79 s for the 4096 members' 1000 steps)
-#define MOL_BATCH_MIN_BLOCKS 2
+// ensemble kernels: CTAs of kThreads per SM the register budget must allow.  Uncapped the tiled
+// kernel took 134 registers and the autotuner fell back to one CTA per instance (48 s -> 79 s
+// for the 4096 members' 1000 steps); at 2 (128 registers, no spills) 1024 members' 200 steps
+// took 2.65 s, at 3 (85 registers, some spills, 24 warps per SM) 2.42 s
+#define MOL_BATCH_MIN_BLOCKS 3
 #endif
 #ifndef MOL_MIN_BLOCKS
 #define MOL_MIN_BLOCKS 1
