@@ -261,7 +261,8 @@ def run_ours(args, rank, world):
                      "peak_source": peak_kind,
                      "kernel": "one SSPRK33 step: k_faces_t (faces of the three K terms) + k_ssprk_t, per stage",
                      "algorithmic_bytes_per_unknown_step": ADR_BYTES_PER_UNKNOWN_STEP,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 128^3 step, x 8"
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the six launches of "
+                                       "one 200^3 step (profiles/adr3d_256_ssprk33.md), scaled to 256^3 by unknowns"
                      if traffic else None,
                      "note": "FP64-pipe bound on GB300 (FP64 = 1/64 of FP32); see fp64"},
         "fp64": {"peak_tflops_measured_now": fp64_peak,

@@ -1630,11 +1630,11 @@ std::vector<std::string> jit_options(int min_blocks) {
     const char* mb = getenv("MOL_JIT_MIN_BLOCKS");
     const int minb = (mb && atoi(mb) > 0) ? atoi(mb) : (min_blocks > 0 ? min_blocks : kDefaultMinBlocks);
     o.push_back("-DMOL_MIN_BLOCKS=" + std::to_string(minb));
-    // the face pass at two resident CTAs per SM more than the stage kernels: the 256^3 ADR step
-    // measured 3.18 / 3.00 / 2.91 ms with the face kernel at 3 / 4 / 5 CTAs per SM (80 / 64 / 51
-    // registers; it spills some at 51, but needs the warps); MOL_FACE_MIN_BLOCKS overrides
+    // the face pass at three resident CTAs per SM more than the stage kernels: the 256^3 ADR
+    // step measured 3.18 / 3.00 / 2.91 / 2.86 / 2.93 ms with the face kernel at 3 / 4 / 5 / 6 / 8
+    // CTAs per SM (it spills some from 5 on, but needs the warps); MOL_FACE_MIN_BLOCKS overrides
     const char* fmb = getenv("MOL_FACE_MIN_BLOCKS");
-    const int fminb = (fmb && atoi(fmb) > 0) ? atoi(fmb) : std::min(8, minb + 2);
+    const int fminb = (fmb && atoi(fmb) > 0) ? atoi(fmb) : std::min(8, minb + 3);
     o.push_back("-DMOL_FACE_MIN_BLOCKS=" + std::to_string(fminb));
     // the VJP at no more than two resident CTAs (128 registers: 44 bytes of spills for the ADR
     // cell instead of 2.2 KB at 80); MOL_VJP_MIN_BLOCKS overrides
