@@ -659,8 +659,10 @@ def run_case(name, args):
             L.check(L.lib().mol_diag_fp64_rate(act, C.byref(w), C.byref(t)))
             rows.append({"active_lanes": act, "warp_fma_G_per_s": w.value / 1e9, "lane_tflops": t.value})
         out.update(rows=rows)
-    elif name in ("adr3d_rhs", "adr3d_steps"):
-        # five RHS evaluations (or SSPRK33 steps) of the 3-D ADR problem at N^3 (--case-n, 128 by default)
+    elif name in ("adr3d_rhs", "adr3d_steps", "adr3d_vjp"):
+        # five RHS evaluations, SSPRK33 steps or vector-Jacobian products (into dL/du and
+        # dL/daux, as the adjoint accumulates them) of the 3-D ADR problem at N^3 (--case-n,
+        # 128 by default)
         N = args.case_n or 128
         sys_, disc, ex = problems.adr3d(N=N, nz_pts=N + 2)
         lw = lower(sys_.to_spec(disc))
@@ -668,9 +670,13 @@ def run_case(name, args):
         plan.set_stream(stream.cuda_stream)
         u = torch.tensor(lw.u0, device=dev)
         du = torch.zeros_like(u)
+        lam = torch.tensor(np.random.default_rng(3).standard_normal(u.numel()), device=dev)
+        gaux = torch.zeros(sum(a.size for a in lw.aux), dtype=torch.float64, device=dev)
         for _ in range(5):
             if name == "adr3d_steps":
                 plan.step_ssprk33(u, ex["dt"], 1)
+            elif name == "adr3d_vjp":
+                plan.vjp(lam, u, None, 0.1, lam_u=du, lam_aux=gaux)
             else:
                 plan.rhs(du, u, None, 0.1)
         torch.cuda.synchronize()
@@ -682,7 +688,7 @@ def run_case(name, args):
 
 
 CASES = ["burgers_adjoint", "burgers_steps", "ensemble", "brusselator_rhs_generated", "brusselator_rhs_interpreted",
-         "brusselator_steps", "adr3d_rhs", "adr3d_steps", "fp64_lanes"]
+         "brusselator_steps", "adr3d_rhs", "adr3d_steps", "adr3d_vjp", "fp64_lanes"]
 
 
 def main():
