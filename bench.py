@@ -6,8 +6,9 @@ Headline workload: the 3-D advection-diffusion-reaction system at 256^3 unknowns
 on [0,1]^3, x and y periodic, z Dirichlet 0, K a seeded log-normal field at the faces,
 second-order centered diffusion and mixed terms, first-order upwind advection.  Metric:
 Mcell-updates/s, a cell-update being one unknown advanced by one full step.  Inputs are
-synthetic (seeded), resident in HBM when timing starts; the state (134 MB) and the three
-face-diffusivity arrays (3 x 134 MB) are larger than L2, so no flush is needed.
+synthetic (seeded), resident in HBM when timing starts; the state (134 MB) and the per-cell
+coefficient arrays (6 or 7 x 134 MB) are larger than L2, so no flush is needed.
+`--stencil-form` picks the coefficient stencils' difference (default) or expanded form.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--full]
 
@@ -36,8 +37,13 @@ METRIC = "Mcell-updates/s + %HBM roofline; batched & adjoint vs plain, 1 GPU, 1e
 UNIT = "Mcell-updates/s"
 HEADLINE = {"N": 256, "nz_pts": 258}
 # algorithmic bytes per unknown and SSPRK33 step: 64 (u -> u1 16, (u, u1) -> u2 24,
-# (u, u2) -> u' 24) plus the three face-diffusivity arrays read once per stage (3 x 3 x 8)
-ADR_BYTES_PER_UNKNOWN_STEP = 64 + 3 * 24
+# (u, u2) -> u' 24) plus 8 per per-cell coefficient array read once per stage: the three
+# face-diffusivity arrays of the face form, or the plan's coefficient-stencil arrays
+# (6 in the difference form, 7 expanded)
+
+
+def adr_bytes_per_unknown_step(coef_arrays: int) -> int:
+    return 64 + 3 * 8 * (coef_arrays if coef_arrays > 0 else 3)
 
 
 def _peaks():
@@ -129,7 +135,7 @@ def headline_config(lw, ex, world):
             "equation": "u_t = div(K grad u) + 0.3 u_xy - (1, 0.5, 0).grad u - 0.5 u^2",
             "bcs": "x, y periodic; z Dirichlet 0",
             "discretisation": "approx_order 2, nonlinear Laplacian with K at the faces, UpwindScheme(1)",
-            "l2": "no flush: state (134 MB) and face-diffusivity arrays (3 x 134 MB) exceed L2",
+            "l2": "no flush: the state (134 MB) and the per-cell coefficient arrays (134 MB each) exceed L2",
             "parallelism": "replicas only" if world > 1 else "single GPU"}
 
 
@@ -167,18 +173,29 @@ def run_ours(args, rank, world):
     hbm_peak, peak_kind = _peaks()
     t_setup = time.perf_counter()
     lw, ex = adr_problem()
-    plan = Plan(lw)
+    plan = Plan(lw, expand_stencils=args.stencil_form == "expanded")
     plan.set_stream(stream.cuda_stream)
     setup_s = time.perf_counter() - t_setup
+    bytes_per_unknown = adr_bytes_per_unknown_step(plan.coef_arrays)
     n = lw.n_unknowns
     dt = ex["dt"]
     p = torch.tensor(lw.param_values, device=dev)
-    u = torch.tensor(lw.u0, device=dev)
+    u0 = torch.tensor(lw.u0, device=dev)
+    u = u0.clone()
     fp64_peak = fp64_peak_live()
     t = 0.0
     for _ in range(max(3, args.warmup)):
         plan.step_ssprk33(u, dt, 1, t0=t, p=p)
         t += dt
+    # The configuration's 0.3 u_xy exceeds 2 K (K ~ 0.01): its diffusion tensor is indefinite and
+    # the discretisation grows modes near kx dx = ky dx = pi/2 by ~8 % per step, so from the
+    # initial state a trajectory reaches O(1) growth, and -lambda u^2 then a blow-up, within
+    # ~500 steps (the C/OpenMP restatement of the reference's discretisation does the same).  The
+    # state is reset to u0 outside the timed events every RESET steps; the time of a step does not
+    # depend on the values.
+    RESET = 100
+    u.copy_(u0)
+    t = 0.0
     torch.cuda.synchronize()
     sampler = ClockSampler(dev.index)
     sampler.start()
@@ -190,7 +207,10 @@ def run_ours(args, rank, world):
     evs = []
     wall0 = time.perf_counter()
     reps = max(1, args.steps)
-    for _ in range(reps):
+    for k in range(reps):
+        if k and k % RESET == 0:
+            u.copy_(u0)
+            t = 0.0
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -205,8 +225,15 @@ def run_ours(args, rank, world):
     launches = L.lib().mol_launch_count() - launches0
     # keep the GPU busy a little longer so the clock sampler sees the kernels under load
     tl = time.perf_counter()
+    u.copy_(u0)
+    t, done = 0.0, 0
     while time.perf_counter() - tl < 1.0:
+        if done >= RESET:
+            u.copy_(u0)
+            t, done = 0.0, 0
         plan.step_ssprk33(u, dt, 16, t0=t, p=p)
+        t += 16 * dt
+        done += 16
         torch.cuda.synchronize()
     clocks = sampler.stop()
     step_ms = [a.elapsed_time(b) for a, b in evs]
@@ -217,11 +244,11 @@ def run_ours(args, rank, world):
         ms_total = float(tt.item())
     ms_per_step = ms_total / reps
     value = world * n * reps / (ms_total * 1e-3) / 1e6
-    prof = _profile_numbers()
-    bytes_per_step = float(ADR_BYTES_PER_UNKNOWN_STEP) * n
+    prof = _profile_numbers().get(f"adr3d_256_{args.stencil_form}", {})
+    bytes_per_step = float(bytes_per_unknown) * n
     achieved = bytes_per_step / (ms_per_step * 1e-3) / 1e9
-    traffic = prof.get("adr3d_256_ssprk33_step_bytes")
-    fp64_per_unknown = prof.get("adr3d_256_fp64_flops_per_unknown_step")
+    traffic = prof.get("step_bytes")
+    fp64_per_unknown = prof.get("fp64_flops_per_unknown_step")
     fp64_achieved = fp64_per_unknown * n / (ms_per_step * 1e-3) / 1e12 if fp64_per_unknown else None
     # e2e: the public C-ABI call with pinned host buffers (H2D + step + D2H in every call)
     host = torch.empty(n, dtype=torch.float64, pin_memory=True)
@@ -252,6 +279,7 @@ def run_ours(args, rank, world):
                 "and a Gaussian initial blob, 256^3 unknowns",
         "config": headline_config(lw, ex, world),
         "codegen": bool(plan.uses_codegen),
+        "stencil_form": args.stencil_form,
         "setup_s": setup_s,
         "gpu_launches": int(launches),
         "wall_s_timed_loop": wall,
@@ -259,11 +287,10 @@ def run_ours(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "peak_source": peak_kind,
-                     "kernel": "one SSPRK33 step: k_faces_t (faces of the three K terms) + k_ssprk_t, per stage",
-                     "algorithmic_bytes_per_unknown_step": ADR_BYTES_PER_UNKNOWN_STEP,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the six launches of "
-                                       "one 200^3 step (profiles/adr3d_256_ssprk33.md), scaled to 256^3 by unknowns"
-                     if traffic else None,
+                     "kernel": "one SSPRK33 step: k_ssprk_t per stage (coefficient stencil, "
+                               f"{plan.coef_arrays} per-cell coefficient arrays, no face pass)",
+                     "algorithmic_bytes_per_unknown_step": bytes_per_unknown,
+                     "traffic_source": prof.get("source") if traffic else None,
                      "note": "FP64-pipe bound on GB300 (FP64 = 1/64 of FP32); see fp64"},
         "fp64": {"peak_tflops_measured_now": fp64_peak,
                  "flops_per_unknown_step": fp64_per_unknown,
@@ -274,25 +301,43 @@ def run_ours(args, rank, world):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(lw, ex)
+        out["cpu_baseline"], out["parity"] = cpu_baseline(lw, ex, plan, args.stencil_form, dev, stream)
     if rank == 0 and not args.headline_only:
         out["workloads"] = workloads(args, dev, stream, (plan, lw, ex))
     plan.close()
     return out
 
 
-def cpu_baseline(lw, ex):
+def cpu_baseline(lw, ex, plan, form, dev, stream):
     """The C/OpenMP restatement of the reference discretisation and SSPRK33 (oracle/c) on the
     host cores: SSPRK33 steps of the same 256^3 system on every core until at least 10 s have
-    passed (at most 400 steps), then one step on one core."""
+    passed (at most 400 steps, restarted from u0 every 100: the configuration blows up near
+    step 450), then one step on one core.  The same restatement checks the GPU right-hand side of
+    both stencil forms on u0 (the parity bar is 1e-12 relative, norm-wise)."""
     import numpy as np
+    import torch
+    from molgpu import Plan
     from oracle.c_port import ADR3D, max_threads
     a = ADR3D(lw)
     dt = ex["dt"]
+    ref_rhs = a.rhs(lw.u0)
+    parity = {"reference": "oracle/c/adr_oracle.c right-hand side at u0", "bar": 1e-12}
+    for f in ("difference", "expanded"):
+        fp = plan if f == form else Plan(lw, expand_stencils=f == "expanded")
+        fp.set_stream(stream.cuda_stream)
+        uf = torch.tensor(lw.u0, device=dev)
+        duf = torch.zeros_like(uf)
+        fp.rhs(duf, uf, None, 0.0)
+        torch.cuda.synchronize()
+        parity[f"rhs_rel_err_{f}"] = float(np.linalg.norm(duf.cpu().numpy() - ref_rhs) / np.linalg.norm(ref_rhs))
+        if fp is not plan:
+            fp.close()
     s = np.array(lw.u0, copy=True)
     a.ssprk33(s, dt, 1, out=s)                     # warm (pages, threads)
     steps, el = 0, 0.0
     while el < 10.0 and steps < 400:
+        if steps and steps % 100 == 0:
+            s[...] = lw.u0
         t0 = time.perf_counter()
         a.ssprk33(s, dt, 2, out=s)
         el += time.perf_counter() - t0
@@ -304,7 +349,7 @@ def cpu_baseline(lw, ex):
     return {"value": lw.n_unknowns * steps / el / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{steps} SSPRK33 steps of the 256^3 ADR system (16,777,216 unknowns) in {el:.1f} s, "
                       f"C/OpenMP restatement of the reference discretisation on {cores} threads; "
-                      f"one thread: {one:.1f} Mcell-updates/s"}
+                      f"one thread: {one:.1f} Mcell-updates/s"}, parity
 
 
 # ---------------------------------------------------------------------------------------
@@ -443,7 +488,11 @@ def workloads(args, dev, stream, adr):
     u32 = torch.tensor(lw.u0, device=dev, dtype=torch.float32)
     du32 = torch.zeros_like(u32)
     ms32 = _time(lambda: plan.rhs(du32, u32, None, 0.1), stream, 5)
-    adj_steps = 500
+    # 400 of the configuration's 500 steps: its 0.3 u_xy makes the system ill-posed (indefinite
+    # diffusion tensor), and from u0 the reference's discretisation itself (the C/OpenMP
+    # restatement) leaves O(1) between steps 400 (max |u| 1.03) and 450 (2.95) and overflows before
+    # step 500, where the gradient is no longer finite
+    adj_steps = 400
     tgt = torch.tensor(np.random.default_rng(12).standard_normal(n) * 1e-3, device=dev)
     u0d = torch.tensor(lw.u0, device=dev)
     gaux = torch.zeros(sum(a.size for a in lw.aux), dtype=torch.float64, device=dev)
@@ -458,11 +507,23 @@ def workloads(args, dev, stream, adr):
     _, nfw0 = plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=0, dLdaux=gaux)
     torch.cuda.synchronize()
     adj_all_s = time.perf_counter() - ta
+    # both stencil forms' step (the headline plan's and the other one)
+    forms = {}
+    for form in ("difference", "expanded"):
+        fp = plan if form == args.stencil_form else Plan(lw, expand_stencils=form == "expanded")
+        fp.set_stream(stream.cuda_stream)
+        uf = torch.tensor(lw.u0, device=dev)
+        step = _time(lambda: fp.step_ssprk33(uf, ex["dt"], 1), stream, 10)
+        forms[form] = {"ssprk33_step_ms": step, "ssprk33_Mcell_s": n / step / 1e3, "coef_arrays": fp.coef_arrays}
+        if fp is not plan:
+            fp.close()
     res["adr3d_256^3"] = {"unknowns": n, "rhs_ms": ms, "rhs_Mcell_s": n / ms / 1e3,
-                          "rhs_hbm_frac": (16 + 24) * n / (ms * 1e-3) / 1e9 / hbm_peak,
+                          "rhs_hbm_frac": (16 + 8 * max(plan.coef_arrays, 3)) * n / (ms * 1e-3) / 1e9 / hbm_peak,
+                          "stencil_forms": forms,
                           "f32state_rhs_ms": ms32,
-                          "f32state_rhs_hbm_frac": (8 + 12) * n / (ms32 * 1e-3) / 1e9 / hbm_peak,
-                          "forward_500_steps_ms": fwd,
+                          "f32state_rhs_hbm_frac": (8 + 4 * max(plan.coef_arrays, 3)) * n / (ms32 * 1e-3) / 1e9
+                          / hbm_peak,
+                          "forward_steps_ms": fwd,
                           "adjoint_steps": adj_steps, "adjoint_dLdK_64_snapshots_s": adj_s,
                           "adjoint_64_snapshots_vs_forward": adj_s / (fwd * 1e-3),
                           "adjoint_64_snapshots_forward_steps": nfw64,
@@ -557,6 +618,8 @@ def run_reference(args, rank, world):
     reps = max(1, args.steps)
     steps, el = 0, 0.0
     while steps < reps or el < 1.0:
+        if steps and steps % 100 == 0:
+            s[...] = lw.u0          # outside the timed call: the configuration blows up near step 450
         t0 = time.perf_counter()
         a.ssprk33(s, dt, 1, out=s)
         el += time.perf_counter() - t0
@@ -666,7 +729,7 @@ def run_case(name, args):
         N = args.case_n or 128
         sys_, disc, ex = problems.adr3d(N=N, nz_pts=N + 2)
         lw = lower(sys_.to_spec(disc))
-        plan = Plan(lw)
+        plan = Plan(lw, expand_stencils=args.stencil_form == "expanded")
         plan.set_stream(stream.cuda_stream)
         u = torch.tensor(lw.u0, device=dev)
         du = torch.zeros_like(u)
@@ -703,6 +766,8 @@ def main():
     ap.add_argument("--case", default=None, choices=CASES,
                     help="run one small single-path case (for profiling) and exit")
     ap.add_argument("--case-n", type=int, default=0, help="grid side of the adr3d cases")
+    ap.add_argument("--stencil-form", default="expanded", choices=["difference", "expanded"],
+                    help="coefficient stencils of the 3-D ADR plan (MOL_FLAG_EXPAND_STENCILS for expanded)")
     args = ap.parse_args()
     if args.case:
         run_case(args.case, args)

@@ -175,6 +175,14 @@ typedef enum mol_fn { MOL_FN_SIN = 0, MOL_FN_COS, MOL_FN_TAN, MOL_FN_EXP, MOL_FN
 typedef enum mol_cmp { MOL_CMP_LE = 0, MOL_CMP_LT, MOL_CMP_GE, MOL_CMP_GT, MOL_CMP_EQ } mol_cmp;
 
 #define MOL_FLAG_NONE 0
+/* Coordinate-dependent linear stencils (a nonlinear Laplacian Dj(K(x) Dj u) whose face
+ * coefficient reads only aux arrays and constants, with the first-derivative stencils of
+ * constant coefficient beside it in the same output) are evaluated from per-cell coefficient
+ * arrays filled once at plan creation.  By default the taps are applied to differences
+ * u[tap] - u[cell] (the face form's conditioning); with this flag as one expanded sum
+ * sum_k c_k[cell] u[tap_k] (ModelingToolkit's canonical sum: fewer FP64 operations, rounding
+ * error that grows with the cancellation of the sum, about (dx^2 u''/u)^-1 for diffusion). */
+#define MOL_FLAG_EXPAND_STENCILS 1
 
 typedef struct mol_problem_desc {
     int32_t abi_version;            /* MOL_ABI_VERSION                                   */
@@ -235,6 +243,11 @@ int64_t mol_launch_count(void);
 /* 1 when the plan runs the generated (NVRTC-compiled) right-hand side, 0 for the
  * register-machine interpreter; the source text (or the reason it is off). */
 int mol_plan_uses_codegen(const mol_plan* plan);
+/* Number of per-cell coefficient arrays the plan holds for its coefficient stencils
+ * (see MOL_FLAG_EXPAND_STENCILS); 0 when it has none.  Each array holds one value per
+ * interior cell and is read once per right-hand-side evaluation.  New entry point: it has no
+ * counterpart in the reference, whose compiled f! carries such weights as literals. */
+int mol_plan_coef_arrays(const mol_plan* plan);
 const char* mol_plan_codegen_source(const mol_plan* plan);
 /* Registers per thread of the generated stage kernel (0 for the interpreter), threads per
  * CTA and CTAs of the plan's grid-stride launches. */

@@ -159,6 +159,27 @@ std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d) {
             if (d->weights[o.w_int + m] != -d->weights[o.w_int + o.L - 1 - m]) return false;
         return true;
     };
+    // a nonlinear Laplacian in its folded form whose face coefficient depends on the
+    // coordinates only: the face program reads aux arrays and constants (no field, parameter,
+    // time or term), so its per-cell stencil weights are fixed for the plan's life
+    auto var_deriv = [&](int k) {
+        if (!nonlinlap_fold(d, k)) return false;
+        const mol_term& tm = d->terms[k];
+        if (tm.prog < 0) return true;
+        if (tm.prog >= d->nprogs) return false;
+        const int start = d->prog_ranges[2 * tm.prog], len = d->prog_ranges[2 * tm.prog + 1];
+        for (int pc = start; pc < start + len; ++pc) {
+            switch (d->code[pc].op) {
+                case MOL_OP_CONST: case MOL_OP_AUX: case MOL_OP_ADD: case MOL_OP_SUB: case MOL_OP_MUL:
+                case MOL_OP_DIV: case MOL_OP_NEG: case MOL_OP_POWI: case MOL_OP_POW: case MOL_OP_FN:
+                case MOL_OP_CMP: case MOL_OP_IFELSE: case MOL_OP_OUT:
+                    break;
+                default:
+                    return false;
+            }
+        }
+        return true;
+    };
     auto is_uniform_const = [&](int pc, double* c) { return const_value(d, s, pc, c); };
     // a foldable leaf: (term, coefficient, subtree pcs)
     struct Leaf {
@@ -169,7 +190,7 @@ std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d) {
     std::function<bool(int, Leaf*)> leaf = [&](int pc, Leaf* L) -> bool {
         const mol_instr& in = s.ins[pc];
         if (uses[pc] != 1) return false;
-        if (in.op == MOL_OP_TERM && first_deriv(in.imm)) {
+        if (in.op == MOL_OP_TERM && (first_deriv(in.imm) || var_deriv(in.imm))) {
             *L = Leaf{in.imm, 1.0, {pc}};
             return true;
         }
@@ -235,8 +256,11 @@ std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d) {
                 g.rest.push_back(a);
             }
         }
-        // worth it: two or more stencils, or one with a coefficient to fold
-        if (leaves.empty() || (leaves.size() == 1 && leaves[0].nodes.size() == 1 && std::fabs(leaves[0].coef) == 1.0))
+        // worth it: two or more stencils, one with a coefficient to fold, or a variable member
+        bool any_var = false;
+        for (auto& L : leaves) any_var |= d->terms[L.term].kind == MOL_TERM_NONLINLAP;
+        if (leaves.empty() ||
+            (!any_var && leaves.size() == 1 && leaves[0].nodes.size() == 1 && std::fabs(leaves[0].coef) == 1.0))
             continue;
         g.absorbed = chain;
         for (auto& L : leaves)
@@ -276,6 +300,23 @@ std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d) {
                     off[tm.dim] = o.omin + m;
                     add_part(off[0], off[1], off[2], FoldPart{L.term, m, L.coef});
                 }
+            } else if (tm.kind == MOL_TERM_NONLINLAP) {
+                // folded form: W (F(face 1) - F(face 0)), F(face m) = a_m (u[r_m + oi.omin + 1] -
+                // u[r_m + oi.omin]) at the outer stencil's half point r_m = oo.omin + m - 1
+                const mol_op1d& oo = d->ops[tm.op];
+                const mol_op1d& oi = d->ops[tm.op2];
+                const double W = d->weights[oo.w_int + 1] * d->weights[oi.w_int + 1];
+                for (int m = 0; m < 2; ++m) {
+                    const int r = oo.omin + m - 1;
+                    const double sg = m == 1 ? 1.0 : -1.0;
+                    for (int side = 0; side < 2; ++side) {
+                        int off[3] = {0, 0, 0};
+                        off[tm.dim] = r + oi.omin + side;
+                        add_part(off[0], off[1], off[2],
+                                 FoldPart{L.term, m, L.coef * W * sg * (side ? 1.0 : -1.0), m});
+                    }
+                }
+                g.variable = true;
             } else {
                 const mol_op1d& o1 = d->ops[tm.op];
                 const mol_op1d& o2 = d->ops[tm.op2];
@@ -289,19 +330,63 @@ std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d) {
                     }
             }
         }
+        if (g.variable) {
+            // tap modes: in the difference form every off-centre tap with a variable part is
+            // applied to (u[tap] - u[centre]) and reads a coefficient array; the centre keeps a
+            // uniform weight.  Expanded: every tap with a variable part reads an array.
+            const bool expanded = (d->flags & MOL_FLAG_EXPAND_STENCILS) != 0;
+            bool has_centre = false;
+            for (auto& t : g.taps) has_centre |= t.o[0] == 0 && t.o[1] == 0 && t.o[2] == 0;
+            if (!has_centre) {
+                FoldTap t;
+                t.o[0] = t.o[1] = t.o[2] = 0;
+                g.taps.push_back(t);
+            }
+            for (auto& t : g.taps) {
+                bool var = false;
+                for (auto& p : t.parts) var |= p.face >= 0;
+                const bool centre = t.o[0] == 0 && t.o[1] == 0 && t.o[2] == 0;
+                if (!var || (centre && !expanded)) continue;
+                t.diff = !centre && !expanded;
+                t.arr = g.narr++;
+            }
+            int base = 0;
+            for (auto& h : groups) base += h.narr;
+            g.arr0 = base;
+        }
         groups.push_back(g);
     }
     return groups;
 }
 
-// The fused weights of `g`: per tap the sum over its parts of coefficient * weight (MIXED:
-// the product of the two interior weights), in part order.
+int fold_coef_arrays(const std::vector<FoldGroup>& groups) {
+    int n = 0;
+    for (auto& g : groups) n += g.narr;
+    return n;
+}
+
+bool nonlinlap_all_in_groups(const mol_problem_desc* d, const std::vector<FoldGroup>& groups) {
+    for (int k = 0; k < d->nterms; ++k) {
+        if (d->terms[k].kind != MOL_TERM_NONLINLAP) continue;
+        bool found = false;
+        for (auto& g : groups)
+            for (auto& t : g.taps)
+                for (auto& p : t.parts) found |= p.term == k && p.face >= 0;
+        if (!found) return false;
+    }
+    return true;
+}
+
+// The fused weights of `g`: per tap the sum over its constant parts of coefficient * weight
+// (MIXED: the product of the two interior weights), in part order; the difference form's
+// centre then gains the differenced taps' constant parts.
 std::vector<double> fold_weights(const mol_problem_desc* d, const FoldGroup& g) {
     std::vector<double> w;
     for (const FoldTap& t : g.taps) {
         double acc = 0.0;
         bool first = true;
         for (const FoldPart& p : t.parts) {
+            if (p.face >= 0) continue;   // coordinate-dependent part: added per cell by k_coef_t
             const mol_term& tm = d->terms[p.term];
             double wk;
             if (tm.kind == MOL_TERM_LINEAR) {
@@ -314,6 +399,14 @@ std::vector<double> fold_weights(const mol_problem_desc* d, const FoldGroup& g) 
             first = false;
         }
         w.push_back(acc);
+    }
+    // difference form: c_k (u_k - u_0) for the differenced taps moves c_k's constant part off
+    // the centre (the variable parts of the centre cancel identically and are not formed)
+    for (size_t i = 0; i < g.taps.size(); ++i) {
+        const FoldTap& t = g.taps[i];
+        if (t.o[0] || t.o[1] || t.o[2]) continue;
+        for (size_t j = 0; j < g.taps.size(); ++j)
+            if (g.taps[j].diff) w[i] += w[j];
     }
     return w;
 }
@@ -1358,6 +1451,16 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
             }
             for (int k : members) {
                 const mol_term& tm = d->terms[k];
+                if (tm.kind == MOL_TERM_NONLINLAP) {
+                    // the variable member's own interior condition (outer, inner and
+                    // interpolation stencils all on their interior weights)
+                    if (tm.dim == q)
+                        cond_w += (cond_w.empty() ? "" : " && ") + std::string("fast_nonlinlap(P, P.ops[") +
+                                  std::to_string(tm.op) + "], P.ops[" + std::to_string(tm.op2) + "], P.ops[" +
+                                  std::to_string(tm.op3) + "], " + F + ", " + std::to_string(q) + ", I[" +
+                                  std::to_string(q) + "])";
+                    continue;
+                }
                 const int op = tm.dim == q ? tm.op : (tm.kind == MOL_TERM_MIXED && tm.dim2 == q ? tm.op2 : -1);
                 if (op < 0) continue;
                 cond_w += (cond_w.empty() ? "" : " && ") + std::string("fast_line(P, P.ops[") + std::to_string(op) +
@@ -1365,11 +1468,24 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
             }
         }
         std::string cond = cond_u.empty() ? "true" : cond_u;
+        // variable groups need the plan's coefficient arrays (batches have none)
+        if (g.variable) cond = "P.cw && " + cond;
         if (!cond_w.empty()) cond += " && warp_all(" + cond_w + ")";
         e << "    T " << G << ";\n    if (" << cond << ") {\n"
           << "        const T* __restrict__ fw = P.w + P.terms[" << g.key_term << "].reserved2;\n"
           << "        const T* __restrict__ fb = u + (long long)" << F << " * P.ncell + c;\n";
+        if (g.variable) {
+            e << "        const T* __restrict__ cw = P.cw + (long long)" << g.arr0 << " * P.ncell + c;\n";
+            bool anydiff = false;
+            for (const FoldTap& t : g.taps) anydiff |= t.diff;
+            if (anydiff) e << "        const T u0 = fb[0];\n";
+        }
+        const std::vector<double> fwv = fold_weights(d, g);
+        bool started = false;
         for (size_t i = 0; i < g.taps.size(); ++i) {
+            // a uniform weight that is exactly zero (the difference form's centre when the
+            // differenced constant parts cancel it) is left out
+            if (g.variable && g.taps[i].arr < 0 && fwv[i] == 0.0) continue;
             std::string off;
             for (int q = 0; q < 3; ++q) {
                 if (!g.taps[i].o[q]) continue;
@@ -1381,10 +1497,16 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
                 off += (off.empty() ? "" : " + ") + term;
             }
             if (off.empty()) off = "0";
-            if (i == 0) e << "        T acc = fw[0] * fb[" << off << "];\n";
-            else e << "        acc = fma(fw[" << i << "], fb[" << off << "], acc);\n";
+            const FoldTap& tp = g.taps[i];
+            const std::string wv = tp.arr >= 0 ? (tp.arr == 0 ? std::string("cw[0]")
+                                                              : "cw[(long long)" + std::to_string(tp.arr) + " * P.ncell]")
+                                               : "fw[" + std::to_string(i) + "]";
+            const std::string xv = tp.diff ? "(fb[" + off + "] - u0)" : "fb[" + off + "]";
+            if (!started) e << "        T acc = " << wv << " * " << xv << ";\n";
+            else e << "        acc = fma(" << wv << ", " << xv << ", acc);\n";
+            started = true;
         }
-        e << "        " << G << " = " << (g.taps.empty() ? "T(0)" : "acc") << ";\n    } else {\n";
+        e << "        " << G << " = " << (started ? "acc" : "T(0)") << ";\n    } else {\n";
         for (int q : g.leaf_nodes) e << "        " << stmt(q) << "\n";
         std::string fsum;
         for (auto& a : g.folded) {
@@ -1450,6 +1572,59 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
     e << "}\n";
 }
 
+// The coefficient arrays of the variable groups at cell c (k_coef_t, once per plan): per tap
+// with an array, its uniform constant part plus, for every variable part, coef * a(face) with
+// a the term's face program at the outer stencil's half point.
+static void emit_coef(Emitter& e, const mol_problem_desc* d, const std::vector<FoldGroup>& groups) {
+    e << "template <class T>\n__device__ __forceinline__ void gen_coef(const DevProb<T>& P, long long c, const int* I, "
+         "T* out) {\n";
+    std::set<std::pair<int, int>> faces;   // (term, outer face)
+    for (const FoldGroup& g : groups)
+        for (const FoldTap& t : g.taps)
+            if (t.arr >= 0)
+                for (const FoldPart& p : t.parts)
+                    if (p.face >= 0) faces.insert({p.term, p.face});
+    for (auto& fk : faces) {
+        const int k = fk.first, m = fk.second;
+        const mol_term& tm = d->terms[k];
+        const int r = d->ops[tm.op].omin + m - 1;
+        const std::string tag = "c" + std::to_string(k) + "_" + std::to_string(m) + "_";
+        const std::string D = std::to_string(tm.dim);
+        e << "    T " << tag << "a;\n    {\n";
+        if (tm.prog < 0) {
+            e << "    " << tag << "a = T(1);\n";
+        } else {
+            const SSA fs = to_ssa(d, tm.prog);
+            std::set<int> used_aux;
+            for (auto& in : fs.ins)
+                if (in.op == MOL_OP_AUX) used_aux.insert(in.imm);
+            for (int j : used_aux)
+                e << "    const T " << tag << "fa" << j << " = P.aux[P.aux_off[P.terms[" << k << "].aux0 + " << j
+                  << "] + face_index(P, " << D << ", I[" << D << "] + (" << r << "), I)];\n";
+            FaceLeaves L(tag);
+            std::vector<std::pair<int, int>> outs;
+            emit_forward(e, d, fs, L, tag, &outs, false);
+            e << "    " << tag << "a = " << (outs.empty() ? "T(1)" : tag + v(outs[0].second)) << ";\n";
+        }
+        e << "    }\n";
+    }
+    for (const FoldGroup& g : groups) {
+        if (!g.variable) continue;
+        e << "    {\n    const T* __restrict__ fw = P.w + P.terms[" << g.key_term << "].reserved2;\n";
+        for (size_t i = 0; i < g.taps.size(); ++i) {
+            const FoldTap& t = g.taps[i];
+            if (t.arr < 0) continue;
+            std::string ex = "fw[" + std::to_string(i) + "]";
+            for (const FoldPart& p : t.parts)
+                if (p.face >= 0)
+                    ex += " + " + lit(p.coef) + " * c" + std::to_string(p.term) + "_" + std::to_string(p.face) + "_a";
+            e << "    out[" << (g.arr0 + t.arr) << "] = " << ex << ";\n";
+        }
+        e << "    }\n";
+    }
+    e << "}\n";
+}
+
 // True when some boundary program uses an elementary function, a power, a comparison or a
 // select (the generated module then compiles those cases into run_bc_prog).
 bool bc_full_ops(const mol_problem_desc* d) {
@@ -1505,6 +1680,9 @@ std::string generate_source(const mol_problem_desc* d, std::string& why) {
     const char* inl = getenv("MOL_JIT_INLINE_CELL");
     const std::string cell_attr = (inl && inl[0] == '0') ? "__noinline__" : "__forceinline__";
     emit_cell_fused(e, d, cs, cell_attr);
+    const std::vector<FoldGroup> coef_groups = const_linear_groups(d);
+    const int ncoef = fold_coef_arrays(coef_groups);
+    emit_coef(e, d, coef_groups);
     e << "template <class T>\n__device__ __forceinline__ void gen_cell_vjp(const DevProb<T>& P, const T* __restrict__ u, "
          "long long c, const int* I, T t, const T* __restrict__ p, const T* seed, T* lam_u, T* lp, T* lam_aux) {\n";
     VjpCellLeaves VL;
@@ -1544,6 +1722,9 @@ std::string generate_source(const mol_problem_desc* d, std::string& why) {
     e << "struct GenCell {\n"
       << "static constexpr int kFields = " << d->nfields << ";\n"
       << "static constexpr int kFaceTerms = " << nface << ";\n"
+      << "static constexpr int kCoefArrays = " << ncoef << ";\n"
+      << "template <class T>\nstatic __device__ __forceinline__ void coefs(const DevProb<T>& P, long long c, const int* I, "
+         "T* out) { gen_coef<T>(P, c, I, out); }\n"
       << "template <class T>\nstatic __device__ __forceinline__ void faces(const DevProb<T>& P, const T* __restrict__ u, "
          "long long c, const int* I, T t, const T* __restrict__ p, T* out) { gen_faces<T>(P, u, c, I, t, p, out); }\n"
          "template <class T> using Uniform = GenUniform<T>;\n"
@@ -1743,7 +1924,8 @@ std::vector<std::string> jit_kernel_names(int nparams, int group) {
         case JIT_FWD64:
             n = {"&mol::k_rhs_t<double, mol::GenCell>", "&mol::k_ssprk_t<double, mol::GenCell, 1>",
                  "&mol::k_ssprk_t<double, mol::GenCell, 2>", "&mol::k_ssprk_t<double, mol::GenCell, 3>",
-                 "&mol::k_tsit_stage_t<double, mol::GenCell>", "&mol::k_faces_t<double, mol::GenCell>"};
+                 "&mol::k_tsit_stage_t<double, mol::GenCell>", "&mol::k_faces_t<double, mol::GenCell>",
+                 "&mol::k_coef_t<mol::GenCell>"};
             break;
         case JIT_FWD32:
             n = {"&mol::k_rhs_t<float, mol::GenCell>", "&mol::k_ssprk_t<float, mol::GenCell, 1>",
@@ -1860,6 +2042,7 @@ int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k
             k->ssp64[2] = got[3];
             k->tsit64 = got[4];
             k->faces64 = got[5];
+            k->coef64 = got[6];
             break;
         case JIT_FWD32:
             k->rhs32 = got[0];

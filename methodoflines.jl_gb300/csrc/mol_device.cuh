@@ -89,6 +89,9 @@ struct DevProb {
     const T* faces;
     long long fstride;
     long long fbeg, fend;   // cells whose faces `faces` holds: [fbeg, fend)
+    // per-cell coefficient arrays of the generated cell's coefficient stencils ([array][cell],
+    // filled by k_coef_t at plan creation), or null (ensembles; the interpreter)
+    const T* cw;
     // cell index -> grid position by multiplication (divmagic) when ncell < 2^31: the magic
     // multipliers and shifts of ni[0] and ni[1]
     unsigned dm[2], ds[2];

@@ -63,6 +63,7 @@ __device__ __forceinline__ void flag_nonfinite(bool bad, int* flag) {
 struct InterpCell {
     static constexpr int kFields = 0;  // field count known only at run time
     static constexpr int kFaceTerms = 0;  // the interpreter evaluates every face in the cell
+    static constexpr int kCoefArrays = 0; // and has no coefficient stencils
     template <class T>
     static __device__ __forceinline__ void faces(const DevProb<T>&, const T*, long long, const int*, T, const T*, T*) {}
     template <class T>
@@ -121,6 +122,29 @@ __global__ void __launch_bounds__(kThreads, MOL_FACE_MIN_BLOCKS) k_faces_t(const
         G::faces(P, u, c, I, T(t), p, out);
 #pragma unroll
         for (int q = 0; q < NQ; ++q) faces[(long long)q * P.fstride + c] = out[q];
+    }
+}
+
+// Coefficient stencils: the per-cell coefficient arrays of the generated cell's variable
+// groups ([array][cell], FP64, and an FP32 copy for the Float32-state kernels when cw32 is
+// set), computed once at plan creation from the face programs of coordinate-dependent
+// nonlinear Laplacians.
+template <class G>
+__global__ void __launch_bounds__(kThreads) k_coef_t(const __grid_constant__ DevProb<double> P, double* __restrict__ cw,
+                                                     float* __restrict__ cw32) {
+    constexpr int NA = G::kCoefArrays > 0 ? G::kCoefArrays : 1;
+    if (G::kCoefArrays == 0) return;
+    double out[NA];
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        int I[3];
+        cell_index(P, c, I);
+        G::coefs(P, c, I, out);
+#pragma unroll
+        for (int q = 0; q < NA; ++q) {
+            cw[(long long)q * P.ncell + c] = out[q];
+            if (cw32) cw32[(long long)q * P.ncell + c] = (float)out[q];
+        }
     }
 }
 

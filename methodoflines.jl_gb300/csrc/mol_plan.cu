@@ -803,6 +803,7 @@ static int build_prec(mol_plan* plan, const mol_problem_desc* d, PlanArrays& A, 
     }
     P.ncell = plan->ncell;
     P.faces = nullptr;
+    P.cw = nullptr;
     P.fstride = plan->ncell;
     P.fbeg = 0;
     P.fend = plan->ncell;
@@ -852,6 +853,7 @@ const char* mol_status_string(int s) {
 int64_t mol_launch_count(void) { return g_launches.load(); }
 
 int mol_plan_uses_codegen(const mol_plan* plan) { return plan && plan->use_jit ? 1 : 0; }
+int mol_plan_coef_arrays(const mol_plan* plan) { return plan ? plan->ncoef : 0; }
 
 int mol_plan_launch_config(const mol_plan* plan, int32_t* regs, int32_t* threads, int32_t* blocks) {
     if (!plan) return MOL_ERR_INVALID;
@@ -1082,6 +1084,30 @@ int mol::plan_create_impl(const mol_problem_desc* d, mol_plan** out, bool member
                     plan->face_blocks = (int)std::max<long long>(
                         1, std::min<long long>((long long)sms * bps, (ncell + 255) / 256));
                 }
+            }
+        }
+        // Coefficient stencils: the per-cell weights of the generated cell's variable groups,
+        // once per plan (aux arrays are fixed at creation).  The face pass then serves only
+        // terms outside the groups, and is dropped when there are none.
+        if (plan->use_jit) {
+            const std::vector<FoldGroup> groups = const_linear_groups(d);
+            const int narr = fold_coef_arrays(groups);
+            if (narr > 0) {
+                if (!plan->jit.coef64) return fail(set_err(plan, MOL_ERR_CUDA, "coefficient kernel not loaded"));
+                const size_t cells = (size_t)narr * (size_t)ncell;
+                if ((st = plan_alloc(plan, (void**)&plan->coef64, sizeof(double) * cells))) return fail(st);
+                if ((st = plan_alloc(plan, (void**)&plan->coef32, sizeof(float) * cells))) return fail(st);
+                plan->ncoef = narr;
+                const int grid = grid_for(ncell, sms, 4);
+                cudaError_t e = launch_k(plan->jit.coef64, grid, kThreads, plan->stream, plan->P64, plan->coef64,
+                                         plan->coef32);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(plan->stream);
+                if ((st = cuda_check(plan, e, "coefficient stencils"))) return fail(st);
+                ++g_launches;
+                plan->P64.cw = plan->coef64;
+                plan->P32.cw = plan->coef32;
+                const char* fp = getenv("MOL_FACE_PASS");
+                if (nonlinlap_all_in_groups(d, groups) && !(fp && fp[0] == '1')) plan->face_pass = false;
             }
         }
         if (!plan->use_jit) {

@@ -90,6 +90,10 @@ struct mol_plan {
     bool face_pass = false;
     double* faces64 = nullptr;
     float* faces32 = nullptr;
+    // coefficient stencils: ncoef per-cell coefficient arrays (k_coef_t), FP64 and FP32
+    int ncoef = 0;
+    double* coef64 = nullptr;
+    float* coef32 = nullptr;
     // device staging of full-grid output (mol_fill_grid) for host destinations
     double* grid_buf = nullptr;
     long long grid_cap = 0;

@@ -15,6 +15,7 @@ MOL_MAX_DIMS = 3
 MOL_MAX_FIELDS = 8
 MOL_MAX_REGS = 64
 MOL_ABI_VERSION = 2
+MOL_FLAG_EXPAND_STENCILS = 1   # mol_problem_desc.flags: coefficient stencils as one expanded sum
 
 STATUS = {
     0: "MOL_OK", -1: "MOL_ERR_INVALID", -2: "MOL_ERR_OOM", -3: "MOL_ERR_NONFINITE",
@@ -96,6 +97,7 @@ _PROTOS = {
     "mol_plan_n_unknowns": (C.c_int64, [C.c_void_p]),
     "mol_launch_count": (C.c_int64, []),
     "mol_plan_uses_codegen": (C.c_int, [C.c_void_p]),
+    "mol_plan_coef_arrays": (C.c_int, [C.c_void_p]),
     "mol_plan_codegen_source": (C.c_char_p, [C.c_void_p]),
     "mol_plan_launch_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int32)]),

@@ -78,7 +78,14 @@ class MOLFiniteDifference:
 
     ``dxs`` maps each spatial variable to a number of points (int), a step (float) or the
     grid's points (a sequence, a nonuniform grid: centered derivatives and boundary rows
-    along it use per-point weights, centered_diff_weights.jl:77-153)."""
+    along it use per-point weights, centered_diff_weights.jl:77-153).
+
+    GPU-backend keyword: ``stencil_form`` ("difference", the default, or "expanded") picks how
+    a diffusion term with a coordinate-dependent coefficient, Dx(K(x) Dx(u)), is evaluated
+    together with the constant-coefficient first-derivative terms beside it: from per-cell
+    weights applied to differences u[tap] - u[cell] (the face form's rounding), or as one
+    expanded sum of per-cell weights times unknowns (fewer FP64 operations; its rounding error
+    relative to the result grows as the sum cancels, about 1 / (dx^2 u''/u) for diffusion)."""
 
     def __init__(self, dxs, time: Optional[IV] = None, approx_order: int = 2, advection_scheme=None,
                  grid_align: str = "center", **kwargs):
@@ -96,6 +103,9 @@ class MOLFiniteDifference:
         if kwargs.get("upwind_order") is not None:
             # MOLFiniteDifference.jl:53-55: the keyword is accepted and has no effect
             warnings.warn("`upwind_order` no longer does anything; use advection_scheme=UpwindScheme(order)")
+        self.stencil_form = kwargs.pop("stencil_form", "difference")
+        if self.stencil_form not in ("difference", "expanded"):
+            raise ValueError("stencil_form must be 'difference' or 'expanded'")
         self.kwargs = kwargs
 
 
@@ -139,9 +149,13 @@ def _ptr(a, n=None, name="array", f32=None, out=False):
 class Plan:
     """Owner of one ``mol_plan``: the compiled GPU right-hand side and its steppers."""
 
-    def __init__(self, lowered: Lowered):
+    def __init__(self, lowered: Lowered, expand_stencils: bool = False):
+        """``expand_stencils``: evaluate coefficient stencils as one expanded sum
+        (MOL_FLAG_EXPAND_STENCILS) instead of on differences."""
         self.lowered = lowered
         self.desc = Descriptor(lowered)
+        if expand_stencils:
+            self.desc.desc.flags |= L.MOL_FLAG_EXPAND_STENCILS
         h = C.c_void_p()
         st = L.lib().mol_plan_create(C.byref(self.desc.desc), C.byref(h))
         self._h = h
@@ -231,6 +245,11 @@ class Plan:
     @property
     def uses_codegen(self) -> bool:
         return bool(L.lib().mol_plan_uses_codegen(self._h))
+
+    @property
+    def coef_arrays(self) -> int:
+        """Per-cell coefficient arrays of the plan's coefficient stencils (0: none)."""
+        return int(L.lib().mol_plan_coef_arrays(self._h))
 
     @property
     def launch_config(self) -> dict:
@@ -364,7 +383,7 @@ def discretize(pdesys: PDESystem, disc: MOLFiniteDifference, tspan=None) -> ODEP
     """``discretize(pdesys, MOLFiniteDifference(...))`` returning a GPU-backed ODEProblem."""
     spec = pdesys.to_spec(disc)
     lw = lower(spec)
-    plan = Plan(lw)
+    plan = Plan(lw, expand_stencils=getattr(disc, "stencil_form", "difference") == "expanded")
     if tspan is None:
         tname = spec["time"]
         tspan = tuple(spec["domain"][tname]) if tname in spec["domain"] else (0.0, 1.0)

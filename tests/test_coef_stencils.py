@@ -1,0 +1,59 @@
+"""Coefficient stencils in the generated code (no device needed): which problems get them,
+the two forms' statements, and NVRTC compiles of both for sm_103a."""
+import ctypes as C
+
+import pytest
+
+from molgpu import Descriptor, lower, problems
+from molgpu import _lib as L
+
+
+def _source(name, kw, flags=0):
+    sys_, disc, _ = getattr(problems, name)(**kw)
+    D = Descriptor(lower(sys_.to_spec(disc)))
+    D.desc.flags = flags
+    need = C.c_int64()
+    assert L.lib().mol_generate_code(C.byref(D.desc), None, 0, C.byref(need)) == 0
+    buf = C.create_string_buffer(need.value)
+    assert L.lib().mol_generate_code(C.byref(D.desc), buf, need.value, C.byref(need)) == 0
+    return buf.value.decode(), D
+
+
+def _cell(src):
+    return src[src.index("void gen_cell("):src.index("void gen_coef(")]
+
+
+def test_adr_difference_form():
+    src, _ = _source("adr3d", dict(N=6, nz_pts=8))
+    cell = _cell(src)
+    assert "if (P.cw && " in cell
+    assert "kCoefArrays = 6;" in src                    # the six face taps
+    assert cell.count(" - u0)") == 6                     # applied to differences
+    assert "const T u0 = fb[0];" in cell
+    # the centre's constant parts (upwinding) cancel against the differenced taps: no centre tap
+    assert "fb[0], acc" not in cell and "* fb[0];" not in cell
+
+
+def test_adr_expanded_form():
+    src, _ = _source("adr3d", dict(N=6, nz_pts=8), L.MOL_FLAG_EXPAND_STENCILS)
+    cell = _cell(src)
+    assert "kCoefArrays = 7;" in src                    # the face taps and the centre
+    assert " - u0)" not in cell
+    assert "fb[0], acc" in cell
+
+
+def test_state_dependent_coefficient_is_not_a_coefficient_stencil():
+    src, _ = _source("nonlinear_diffusion", dict(n=9, k=1.3, seed=1000))
+    assert "kCoefArrays = 0;" in src and "P.cw &&" not in src
+
+
+def test_constant_coefficients_keep_uniform_weights():
+    src, _ = _source("brusselator", dict(N=8))
+    assert "kCoefArrays = 0;" in src and "P.cw &&" not in src
+
+
+@pytest.mark.parametrize("flags", [0, L.MOL_FLAG_EXPAND_STENCILS])
+def test_both_forms_compile_for_sm103a(flags):
+    _, D = _source("adr3d", dict(N=6, nz_pts=8), flags)
+    log = C.create_string_buffer(1 << 16)
+    assert L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16) == 0, log.value.decode()

@@ -87,11 +87,13 @@ def test_brusselator_1024_pinned_host_state(gpu_lib, bruss1024):
     plan.close()
 
 
-def test_adr3d_256_rhs_and_steps(gpu_lib, adr256):
-    """The headline workload: RHS through the face pass, SSPRK33 steps, device state."""
+@pytest.mark.parametrize("expand", [False, True])
+def test_adr3d_256_rhs_and_steps(gpu_lib, adr256, expand):
+    """The headline workload: RHS through the coefficient stencils (difference and expanded
+    forms), SSPRK33 steps, device state."""
     torch = _torch()
     lw, dt, cref = adr256
-    plan = _on_stream(Plan(lw), torch)
+    plan = _on_stream(Plan(lw, expand_stencils=expand), torch)
     u = torch.tensor(lw.u0, device="cuda")
     du = torch.zeros_like(u)
     plan.rhs(du, u, None, 0.1)
@@ -102,10 +104,11 @@ def test_adr3d_256_rhs_and_steps(gpu_lib, adr256):
     plan.close()
 
 
-def test_adr3d_256_pinned_host_state(gpu_lib, adr256):
+@pytest.mark.parametrize("expand", [False, True])
+def test_adr3d_256_pinned_host_state(gpu_lib, adr256, expand):
     torch = _torch()
     lw, dt, cref = adr256
-    plan = Plan(lw)
+    plan = Plan(lw, expand_stencils=expand)
     host = torch.empty(lw.n_unknowns, dtype=torch.float64, pin_memory=True)
     host.copy_(torch.from_numpy(lw.u0))
     hnp = host.numpy()
@@ -116,11 +119,12 @@ def test_adr3d_256_pinned_host_state(gpu_lib, adr256):
     plan.close()
 
 
-def test_adr3d_128_rhs_against_numpy_oracle(gpu_lib):
+@pytest.mark.parametrize("expand", [False, True])
+def test_adr3d_128_rhs_against_numpy_oracle(gpu_lib, expand):
     sys_, disc, _ = problems.adr3d(N=128, nz_pts=130)
     spec = sys_.to_spec(disc)
     lw = lower(spec)
-    plan = Plan(lw)
+    plan = Plan(lw, expand_stencils=expand)
     rng = np.random.default_rng(3)
     u = lw.u0 + 0.01 * rng.standard_normal(lw.n_unknowns)
     du = np.zeros(lw.n_unknowns)
