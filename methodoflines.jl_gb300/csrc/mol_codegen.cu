@@ -609,6 +609,10 @@ struct CellLeaves : Leaves {
 // their split forward/backward pair, which share the partials in fwK/gwK.
 struct VjpCellLeaves : CellLeaves {
     std::vector<int> split;
+    // members of coefficient-stencil groups (term -> group): on the group path their adjoints
+    // are scattered by the group (emit_group_vjp), so their own statements are left out
+    std::map<int, int> var_member;
+    bool omit_members = false;
     bool is_split(int k) const { return std::find(split.begin(), split.end(), k) != split.end(); }
     std::string term(int k) const override {
         if (!is_split(k)) return CellLeaves::term(k);
@@ -616,6 +620,7 @@ struct VjpCellLeaves : CellLeaves {
         return "gt" + K + "_fg<T>(P, u, c, I, t, p, fw" + K + ", gw" + K + ")";
     }
     std::string term_adj(int k, const std::string& g) const override {
+        if (omit_members && var_member.count(k)) return "";
         if (!is_split(k)) return CellLeaves::term_adj(k, g);
         const std::string K = std::to_string(k);
         return "    gt" + K + "_bg<T>(P, u, c, I, t, p, " + g + ", fw" + K + ", gw" + K + ", lam_u, lp, lam_aux, own" +
@@ -1187,6 +1192,63 @@ void emit_nonlinlap(Emitter& e, const mol_problem_desc* d, int k, int face_slot)
 // operations, the binding resource.
 // ----------------------------------------------------------------------------
 
+// Where a group's fused stencil applies: every member on its interior (or wrapped periodic)
+// path; a variable group also needs the plan's coefficient arrays (batches have none).
+static std::string group_cond(const mol_problem_desc* d, const FoldGroup& g) {
+    const std::string F = std::to_string(g.field);
+    std::set<int> members;
+    int reach[3] = {0, 0, 0};
+    for (const FoldTap& t : g.taps) {
+        for (const FoldPart& p : t.parts) members.insert(p.term);
+        for (int q = 0; q < 3; ++q) reach[q] = std::max(reach[q], std::abs(t.o[q]));
+    }
+    std::string cond_u, cond_w;   // uniform (periodic wrap) and per-cell (interior) parts
+    for (int q = 0; q < 3; ++q) {
+        if (!reach[q]) continue;
+        if (periodic_dim(d, g.field, q)) {
+            cond_u += (cond_u.empty() ? "" : " && ") + std::string("wrap_line_ok(P, ") + F + ", " + std::to_string(q) +
+                      ", " + std::to_string(reach[q]) + ")";
+            continue;
+        }
+        for (int k : members) {
+            const mol_term& tm = d->terms[k];
+            if (tm.kind == MOL_TERM_NONLINLAP) {
+                // the variable member's own interior condition (outer, inner and interpolation
+                // stencils all on their interior weights)
+                if (tm.dim == q)
+                    cond_w += (cond_w.empty() ? "" : " && ") + std::string("fast_nonlinlap(P, P.ops[") +
+                              std::to_string(tm.op) + "], P.ops[" + std::to_string(tm.op2) + "], P.ops[" +
+                              std::to_string(tm.op3) + "], " + F + ", " + std::to_string(q) + ", I[" +
+                              std::to_string(q) + "])";
+                continue;
+            }
+            const int op = tm.dim == q ? tm.op : (tm.kind == MOL_TERM_MIXED && tm.dim2 == q ? tm.op2 : -1);
+            if (op < 0) continue;
+            cond_w += (cond_w.empty() ? "" : " && ") + std::string("fast_line(P, P.ops[") + std::to_string(op) + "], " +
+                      F + ", " + std::to_string(q) + ", I[" + std::to_string(q) + "])";
+        }
+    }
+    std::string cond = cond_u.empty() ? "true" : cond_u;
+    if (g.variable) cond = "P.cw && " + cond;
+    if (!cond_w.empty()) cond += " && warp_all(" + cond_w + ")";
+    return cond;
+}
+
+// Offset of a group tap from the cell (wrapped along periodic dimensions).
+static std::string group_tap_off(const mol_problem_desc* d, const FoldGroup& g, const FoldTap& t) {
+    std::string off;
+    for (int q = 0; q < 3; ++q) {
+        if (!t.o[q]) continue;
+        const std::string oq = std::to_string(t.o[q]);
+        const std::string term = periodic_dim(d, g.field, q)
+                                     ? "(long long)wrap_off(I[" + std::to_string(q) + "], " + oq + ", P.n[" +
+                                           std::to_string(q) + "]) * gstride(P, " + std::to_string(q) + ")"
+                                     : "(long long)(" + oq + ") * gstride(P, " + std::to_string(q) + ")";
+        off += (off.empty() ? "" : " + ") + term;
+    }
+    return off.empty() ? "0" : off;
+}
+
 struct LinInfo {
     bool ok = false;
     int field = -1;
@@ -1435,42 +1497,7 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
     auto emit_cgroup = [&](int gi, int out_field) {
         const FoldGroup& g = cgroups[gi];
         const std::string G = "fg" + std::to_string(gi), F = std::to_string(g.field);
-        std::set<int> members;
-        int reach[3] = {0, 0, 0};
-        for (const FoldTap& t : g.taps) {
-            for (const FoldPart& p : t.parts) members.insert(p.term);
-            for (int q = 0; q < 3; ++q) reach[q] = std::max(reach[q], std::abs(t.o[q]));
-        }
-        std::string cond_u, cond_w;   // uniform (periodic wrap) and per-cell (interior) parts
-        for (int q = 0; q < 3; ++q) {
-            if (!reach[q]) continue;
-            if (periodic_dim(d, g.field, q)) {
-                cond_u += (cond_u.empty() ? "" : " && ") + std::string("wrap_line_ok(P, ") + F + ", " +
-                          std::to_string(q) + ", " + std::to_string(reach[q]) + ")";
-                continue;
-            }
-            for (int k : members) {
-                const mol_term& tm = d->terms[k];
-                if (tm.kind == MOL_TERM_NONLINLAP) {
-                    // the variable member's own interior condition (outer, inner and
-                    // interpolation stencils all on their interior weights)
-                    if (tm.dim == q)
-                        cond_w += (cond_w.empty() ? "" : " && ") + std::string("fast_nonlinlap(P, P.ops[") +
-                                  std::to_string(tm.op) + "], P.ops[" + std::to_string(tm.op2) + "], P.ops[" +
-                                  std::to_string(tm.op3) + "], " + F + ", " + std::to_string(q) + ", I[" +
-                                  std::to_string(q) + "])";
-                    continue;
-                }
-                const int op = tm.dim == q ? tm.op : (tm.kind == MOL_TERM_MIXED && tm.dim2 == q ? tm.op2 : -1);
-                if (op < 0) continue;
-                cond_w += (cond_w.empty() ? "" : " && ") + std::string("fast_line(P, P.ops[") + std::to_string(op) +
-                          "], " + F + ", " + std::to_string(q) + ", I[" + std::to_string(q) + "])";
-            }
-        }
-        std::string cond = cond_u.empty() ? "true" : cond_u;
-        // variable groups need the plan's coefficient arrays (batches have none)
-        if (g.variable) cond = "P.cw && " + cond;
-        if (!cond_w.empty()) cond += " && warp_all(" + cond_w + ")";
+        const std::string cond = group_cond(d, g);
         e << "    T " << G << ";\n    if (" << cond << ") {\n"
           << "        const T* __restrict__ fw = P.w + P.terms[" << g.key_term << "].reserved2;\n"
           << "        const T* __restrict__ fb = u + (long long)" << F << " * P.ncell + c;\n";
@@ -1486,17 +1513,7 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
             // a uniform weight that is exactly zero (the difference form's centre when the
             // differenced constant parts cancel it) is left out
             if (g.variable && g.taps[i].arr < 0 && fwv[i] == 0.0) continue;
-            std::string off;
-            for (int q = 0; q < 3; ++q) {
-                if (!g.taps[i].o[q]) continue;
-                const std::string oq = std::to_string(g.taps[i].o[q]);
-                const std::string term = periodic_dim(d, g.field, q)
-                                             ? "(long long)wrap_off(I[" + std::to_string(q) + "], " + oq + ", P.n[" +
-                                                   std::to_string(q) + "]) * gstride(P, " + std::to_string(q) + ")"
-                                             : "(long long)(" + oq + ") * gstride(P, " + std::to_string(q) + ")";
-                off += (off.empty() ? "" : " + ") + term;
-            }
-            if (off.empty()) off = "0";
+            const std::string off = group_tap_off(d, g, g.taps[i]);
             const FoldTap& tp = g.taps[i];
             const std::string wv = tp.arr >= 0 ? (tp.arr == 0 ? std::string("cw[0]")
                                                               : "cw[(long long)" + std::to_string(tp.arr) + " * P.ncell]")
@@ -1625,6 +1642,74 @@ static void emit_coef(Emitter& e, const mol_problem_desc* d, const std::vector<F
     e << "}\n";
 }
 
+// Vector-Jacobian product of a coefficient-stencil group where its stencil applies: the
+// output's seed g times each tap's weight scattered to the tap (the difference form's taps
+// also take it off the cell itself), and for each variable member's face the derivative of the
+// output with respect to its coefficient a, g * sum(coef * u[tap]), through the face program
+// into the aux arrays it reads.
+static void emit_group_vjp(Emitter& e, const mol_problem_desc* d, const FoldGroup& g, int gi, int out_field) {
+    const std::string F = std::to_string(g.field);
+    e << "    if (cgv" << gi << ") {\n"
+      << "        const T g = seed[" << out_field << "];\n"
+      << "        const T* __restrict__ fw = P.w + P.terms[" << g.key_term << "].reserved2;\n"
+      << "        const T* __restrict__ cw = P.cw + (long long)" << g.arr0 << " * P.ncell + c;\n"
+      << "        const T* __restrict__ fb = u + (long long)" << F << " * P.ncell + c;\n"
+      << "        T* lb = lam_u + (long long)" << F << " * P.ncell + c;\n";
+    const std::vector<double> fwv = fold_weights(d, g);
+    for (size_t i = 0; i < g.taps.size(); ++i) {
+        const FoldTap& t = g.taps[i];
+        if (t.arr < 0 && fwv[i] == 0.0) continue;
+        const std::string wv = t.arr >= 0 ? (t.arr == 0 ? std::string("cw[0]")
+                                                        : "cw[(long long)" + std::to_string(t.arr) + " * P.ncell]")
+                                          : "fw[" + std::to_string(i) + "]";
+        const std::string off = group_tap_off(d, g, t);
+        e << "        {\n        const T gw = g * " << wv << ";\n";
+        if (off == "0") {
+            e << "        own" << F << " += gw;\n";
+        } else {
+            e << "        atomicAdd(lb + " << off << ", gw);\n";
+            if (t.diff) e << "        own" << F << " -= gw;\n";
+        }
+        e << "        }\n";
+    }
+    std::map<std::pair<int, int>, std::vector<std::pair<const FoldTap*, double>>> faces;
+    for (const FoldTap& t : g.taps)
+        for (const FoldPart& p : t.parts)
+            if (p.face >= 0) faces[{p.term, p.face}].push_back({&t, p.coef});
+    if (!faces.empty()) e << "        if (lam_aux) {\n";
+    for (auto& fk : faces) {
+        const int k = fk.first.first, m = fk.first.second;
+        const mol_term& tm = d->terms[k];
+        if (tm.prog < 0) continue;   // a = 1: no coefficient to differentiate
+        const std::string D = std::to_string(tm.dim);
+        const int r = d->ops[tm.op].omin + m - 1;
+        const std::string tag = "va" + std::to_string(k) + "_" + std::to_string(m) + "_";
+        e << "        {\n        T " << tag << "s = T(0);\n";
+        for (auto& tc : fk.second)
+            e << "        " << tag << "s = fma(" << lit(tc.second) << ", fb[" << group_tap_off(d, g, *tc.first) << "], "
+              << tag << "s);\n";
+        e << "        const T " << tag << "ga = g * " << tag << "s;\n";
+        const SSA fs = to_ssa(d, tm.prog);
+        std::set<int> used_aux;
+        for (auto& in : fs.ins)
+            if (in.op == MOL_OP_AUX) used_aux.insert(in.imm);
+        for (int j : used_aux)
+            e << "        const long long " << tag << "fi" << j << " = P.aux_off[P.terms[" << k << "].aux0 + " << j
+              << "] + face_index(P, " << D << ", I[" << D << "] + (" << r << "), I);\n"
+              << "        const T " << tag << "fa" << j << " = P.aux[" << tag << "fi" << j << "];\n"
+              << "        T " << tag << "gfa" << j << " = T(0);\n";
+        FaceLeaves L(tag);
+        std::vector<std::pair<int, int>> outs;
+        emit_forward(e, d, fs, L, tag, &outs, false);
+        emit_reverse(e, fs, L, tag, [&](int) { return tag + "ga"; });
+        for (int j : used_aux)
+            e << "        atomicAdd(lam_aux + " << tag << "fi" << j << ", " << tag << "gfa" << j << ");\n";
+        e << "        }\n";
+    }
+    if (!faces.empty()) e << "        }\n";
+    e << "    }\n";
+}
+
 // True when some boundary program uses an elementary function, a power, a comparison or a
 // select (the generated module then compiles those cases into run_bc_prog).
 bool bc_full_ops(const mol_problem_desc* d) {
@@ -1683,31 +1768,69 @@ std::string generate_source(const mol_problem_desc* d, std::string& why) {
     const std::vector<FoldGroup> coef_groups = const_linear_groups(d);
     const int ncoef = fold_coef_arrays(coef_groups);
     emit_coef(e, d, coef_groups);
-    e << "template <class T>\n__device__ __forceinline__ void gen_cell_vjp(const DevProb<T>& P, const T* __restrict__ u, "
-         "long long c, const int* I, T t, const T* __restrict__ p, const T* seed, T* lam_u, T* lp, T* lam_aux) {\n";
-    VjpCellLeaves VL;
-    VL.d = d;
-    for (int f = 0; f < d->nfields; ++f) e << "    T own" << f << " = T(0);\n";
-    {
-        // WENO terms read by exactly one TERM instruction (and by no upwind select)
-        std::vector<int> refs(d->nterms, 0);
-        for (auto& in : cs.ins) {
-            if (in.op == MOL_OP_TERM && in.imm >= 0 && in.imm < d->nterms) refs[in.imm] += 1;
-            if (in.op == MOL_OP_UPWIND) {
-                if (in.b < d->nterms) refs[in.b] += 2;
-                if (in.c < d->nterms) refs[in.c] += 2;
+    // The cell VJP.  With coefficient stencils it is two functions: the group path (the members'
+    // adjoints scattered by the groups, emit_group_vjp) inline, for warps where every group's
+    // stencil applies, and the full reverse sweep out of line (__noinline__) for the others (the
+    // boundary planes), so the rarely taken sweep does not set the register budget of the kernel.
+    bool any_var = false;
+    for (auto& g : coef_groups) any_var |= g.variable;
+    const std::string vjp_sig = "(const DevProb<T>& P, const T* __restrict__ u, long long c, const int* I, T t, "
+                                "const T* __restrict__ p, const T* seed, T* lam_u, T* lp, T* lam_aux)";
+    auto vjp_body = [&](bool fast) {
+        VjpCellLeaves VL;
+        VL.d = d;
+        VL.omit_members = fast;
+        for (int f = 0; f < d->nfields; ++f) e << "    T own" << f << " = T(0);\n";
+        if (fast)
+            for (size_t gi = 0; gi < coef_groups.size(); ++gi) {
+                const FoldGroup& g = coef_groups[gi];
+                if (!g.variable) continue;
+                for (const FoldTap& t : g.taps)
+                    for (const FoldPart& pp : t.parts) VL.var_member[pp.term] = (int)gi;
             }
+        {
+            // WENO terms read by exactly one TERM instruction (and by no upwind select)
+            std::vector<int> refs(d->nterms, 0);
+            for (auto& in : cs.ins) {
+                if (in.op == MOL_OP_TERM && in.imm >= 0 && in.imm < d->nterms) refs[in.imm] += 1;
+                if (in.op == MOL_OP_UPWIND) {
+                    if (in.b < d->nterms) refs[in.b] += 2;
+                    if (in.c < d->nterms) refs[in.c] += 2;
+                }
+            }
+            for (int k = 0; k < d->nterms; ++k)
+                if (d->terms[k].kind == MOL_TERM_WENO && d->terms[k].variant == 0 && refs[k] == 1) {
+                    VL.split.push_back(k);
+                    e << "    bool fw" << k << " = false;\n    T gw" << k << "[5];\n";
+                }
         }
-        for (int k = 0; k < d->nterms; ++k)
-            if (d->terms[k].kind == MOL_TERM_WENO && d->terms[k].variant == 0 && refs[k] == 1) {
-                VL.split.push_back(k);
-                e << "    bool fw" << k << " = false;\n    T gw" << k << "[5];\n";
-            }
+        emit_forward(e, d, cs, VL, "", nullptr, true);
+        emit_reverse(e, cs, VL, "", [&](int k) { return "seed[" + std::to_string(k) + "]"; });
+        if (fast)
+            for (size_t gi = 0; gi < coef_groups.size(); ++gi)
+                if (coef_groups[gi].variable)
+                    emit_group_vjp(e, d, coef_groups[gi], (int)gi, cs.ins[coef_groups[gi].out_pc].imm);
+        for (int f = 0; f < d->nfields; ++f)
+            e << "    atomicAdd(lam_u + (long long)" << f << " * P.ncell + c, own" << f << ");\n";
+    };
+    if (any_var) {
+        e << "template <class T>\n__device__ __noinline__ void gen_cell_vjp_full" << vjp_sig << " {\n";
+        vjp_body(false);
+        e << "}\n";
     }
-    emit_forward(e, d, cs, VL, "", nullptr, true);
-    emit_reverse(e, cs, VL, "", [&](int k) { return "seed[" + std::to_string(k) + "]"; });
-    for (int f = 0; f < d->nfields; ++f)
-        e << "    atomicAdd(lam_u + (long long)" << f << " * P.ncell + c, own" << f << ");\n";
+    e << "template <class T>\n__device__ __forceinline__ void gen_cell_vjp" << vjp_sig << " {\n";
+    if (any_var) {
+        std::string all;
+        for (size_t gi = 0; gi < coef_groups.size(); ++gi) {
+            const FoldGroup& g = coef_groups[gi];
+            if (!g.variable) continue;
+            e << "    const bool cgv" << gi << " = " << group_cond(d, g) << ";\n";
+            all += (all.empty() ? "" : " && ") + std::string("cgv") + std::to_string(gi);
+        }
+        e << "    if (!(" << all << ")) {\n        gen_cell_vjp_full<T>(P, u, c, I, t, p, seed, lam_u, lp, lam_aux);\n"
+          << "        return;\n    }\n";
+    }
+    vjp_body(any_var);
     e << "}\n";
     // the face pass: left faces of every nonlinear-Laplacian term, slot order = term order
     e << "template <class T>\n__device__ __forceinline__ void gen_faces(const DevProb<T>& P, const T* __restrict__ u, "
@@ -1803,7 +1926,15 @@ std::map<std::string, CacheEntry> g_cache;
 // NVRTC options.  MOL_JIT_MIN_BLOCKS sets the CTAs per SM the register allocator must allow
 // for the right-hand-side kernels; MOL_JIT_MAXRREG caps registers per thread.
 constexpr int kDefaultMinBlocks = 2;
-std::vector<std::string> jit_options(int min_blocks) {
+// Resident CTAs per SM for the VJP of a module whose cell VJP has a coefficient-stencil path
+// (the full reverse sweep out of line): its group path holds few values, and the 256^3 ADR VJP
+// measured 1.708 / 1.374 / 1.364 ms at 2 / 3 / 4 CTAs per SM (long-scoreboard bound at 2).
+constexpr int kCoefVjpMinBlocks = 3;
+int vjp_min_blocks_of(const std::string& src) {
+    return src.find("gen_cell_vjp_full") != std::string::npos ? kCoefVjpMinBlocks : 0;
+}
+
+std::vector<std::string> jit_options(int min_blocks, int vjp_min_blocks) {
     std::vector<std::string> o = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
                                   "-default-device", "-DMOL_JIT=1"};
     const char* r = getenv("MOL_JIT_MAXRREG");
@@ -1817,10 +1948,11 @@ std::vector<std::string> jit_options(int min_blocks) {
     const char* fmb = getenv("MOL_FACE_MIN_BLOCKS");
     const int fminb = (fmb && atoi(fmb) > 0) ? atoi(fmb) : std::min(8, minb + 3);
     o.push_back("-DMOL_FACE_MIN_BLOCKS=" + std::to_string(fminb));
-    // the VJP at no more than two resident CTAs (128 registers: 44 bytes of spills for the ADR
-    // cell instead of 2.2 KB at 80); MOL_VJP_MIN_BLOCKS overrides
+    // the VJP at no more than two resident CTAs (the face-form ADR cell VJP took 128 registers:
+    // 44 bytes of spills instead of 2.2 KB at 80), or the coefficient-stencil budget above;
+    // MOL_VJP_MIN_BLOCKS overrides
     const char* vmb = getenv("MOL_VJP_MIN_BLOCKS");
-    const int vminb = (vmb && atoi(vmb) > 0) ? atoi(vmb) : std::min(minb, 2);
+    const int vminb = (vmb && atoi(vmb) > 0) ? atoi(vmb) : (vjp_min_blocks > 0 ? vjp_min_blocks : std::min(minb, 2));
     o.push_back("-DMOL_VJP_MIN_BLOCKS=" + std::to_string(vminb));
     // MOL_BATCH_MIN_BLOCKS: the same bound for the ensemble kernels (default 1: no cap)
     const char* bmb = getenv("MOL_BATCH_MIN_BLOCKS");
@@ -1859,7 +1991,7 @@ std::string disk_cache_path(const std::string& src, int nparams, int min_blocks)
         }
     };
     mix(src);
-    for (auto& o : jit_options(min_blocks)) mix(o);
+    for (auto& o : jit_options(min_blocks, vjp_min_blocks_of(src))) mix(o);
     mix("v4|" + std::to_string(nparams));
     for (int i = 0; i < (int)(sizeof(kEmbedTexts) / sizeof(kEmbedTexts[0])); ++i) mix(kEmbedTexts[i]);
     char name[64];
@@ -1958,7 +2090,7 @@ int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<ch
         return MOL_ERR_CUDA;
     }
     for (auto& n : names) N.addname(prog, n.c_str());
-    std::vector<std::string> ostr = jit_options(min_blocks);
+    std::vector<std::string> ostr = jit_options(min_blocks, vjp_min_blocks_of(src));
     std::vector<const char*> opts;
     for (auto& o : ostr) opts.push_back(o.c_str());
     const int rc = N.compile(prog, (int)opts.size(), opts.data());

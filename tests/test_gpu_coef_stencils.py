@@ -116,3 +116,75 @@ def test_nonlinear_diffusion_keeps_face_pass(gpu_lib):
     assert L.lib().mol_launch_count() - before == 2
     assert _rel(dd.cpu().numpy(), OracleProblem(spec).rhs(lw.u0, 0.0)) < RHS_TOL
     plan.close()
+
+
+@pytest.mark.parametrize("expand", [False, True])
+def test_adr_vjp_both_forms_against_finite_differences(gpu_lib, expand):
+    """The coefficient stencil's own VJP (per-tap scatter of the seed times the cell's weights,
+    and the derivative with respect to each face's K) against central differences of the RHS
+    along seeded directions, in u and in the face-diffusivity arrays."""
+    import copy
+    lw, _, _ = _adr(12)
+    plan = Plan(lw, expand_stencils=expand)
+    assert plan.coef_arrays == (7 if expand else 6)
+    rng = np.random.default_rng(23)
+    u = lw.u0 + 0.05 * rng.standard_normal(lw.n_unknowns)
+    lam = rng.standard_normal(lw.n_unknowns)
+    v = rng.standard_normal(lw.n_unknowns)
+    lam_u = np.zeros(lw.n_unknowns)
+    lam_aux = np.zeros(sum(a.size for a in lw.aux))
+    plan.vjp(lam, u, None, 0.1, lam_u=lam_u, lam_aux=lam_aux)
+
+    def rhs(pl, x):
+        du = np.zeros_like(x)
+        pl.rhs(du, x, None, 0.1)
+        return du
+
+    h = 1e-6
+    fd = lam @ (rhs(plan, u + h * v) - rhs(plan, u - h * v)) / (2 * h)
+    assert abs(lam_u @ v - fd) <= 1e-6 * abs(fd), (lam_u @ v, fd)
+    dirs = [rng.standard_normal(a.size) * (a != 0) for a in lw.aux]
+    ha = 1e-7
+
+    def with_aux(sign):
+        lw2 = copy.copy(lw)
+        lw2.aux = [a + sign * ha * d for a, d in zip(lw.aux, dirs)]
+        p2 = Plan(lw2, expand_stencils=expand)
+        out = rhs(p2, u)
+        p2.close()
+        return out
+
+    fda = lam @ (with_aux(+1) - with_aux(-1)) / (2 * ha)
+    got = lam_aux @ np.concatenate(dirs)
+    assert abs(got - fda) <= 1e-6 * abs(fda), (got, fda)
+    plan.close()
+
+
+@pytest.mark.parametrize("expand", [False, True])
+def test_adr_adjoint_dLdK_both_forms(gpu_lib, expand):
+    """dL/dK of a 6-step SSPRK33 misfit through the checkpointed adjoint, against a central
+    difference of the loss along a seeded direction of the face arrays."""
+    import copy
+    lw, _, ex = _adr(12)
+    rng = np.random.default_rng(24)
+    target = rng.standard_normal(lw.n_unknowns) * 1e-3
+    dt, n = ex["dt"], 6
+    plan = Plan(lw, expand_stencils=expand)
+    gaux = np.zeros(sum(a.size for a in lw.aux))
+    loss, _ = plan.adjoint_ssprk33(lw.u0, dt, n, target, nsnap=2, dLdaux=gaux)
+    plan.close()
+    dirs = [rng.standard_normal(a.size) * (a != 0) for a in lw.aux]
+    h = 1e-7
+
+    def L(sign):
+        lw2 = copy.copy(lw)
+        lw2.aux = [a + sign * h * d for a, d in zip(lw.aux, dirs)]
+        p2 = Plan(lw2, expand_stencils=expand)
+        w = lw.u0.copy()
+        p2.step_ssprk33(w, dt, n)
+        p2.close()
+        return 0.5 * float(np.sum((w - target) ** 2))
+
+    fd = (L(+1) - L(-1)) / (2 * h)
+    got = gaux @ np.concatenate(dirs)
+    assert abs(got - fd) <= 1e-6 * abs(fd), (got, fd)
