@@ -462,10 +462,16 @@ def workloads(args, dev, stream, adr):
     u0d = torch.tensor(lw.u0, device=dev)
     plan.adjoint_ssprk33(u0d, ex["dt"], 2, tgt, nsnap=2, dLdu0=g, dLdp=gp)   # warm: compiles the VJP
     torch.cuda.synchronize()
+    # each schedule once untimed first: its checkpoint storage (31 GB with every state kept) is
+    # allocated by the first call and reused by later ones
+    plan.adjoint_ssprk33(u0d, ex["dt"], nsteps, tgt, nsnap=64, dLdu0=g, dLdp=gp)
+    torch.cuda.synchronize()
     ta = time.perf_counter()
     loss, nfw = plan.adjoint_ssprk33(u0d, ex["dt"], nsteps, tgt, nsnap=64, dLdu0=g, dLdp=gp)
     torch.cuda.synchronize()
     adj_s = time.perf_counter() - ta
+    plan.adjoint_ssprk33(u0d, ex["dt"], nsteps, tgt, nsnap=0, dLdu0=g, dLdp=gp)
+    torch.cuda.synchronize()
     ta = time.perf_counter()
     plan.adjoint_ssprk33(u0d, ex["dt"], nsteps, tgt, nsnap=0, dLdu0=g, dLdp=gp)
     torch.cuda.synchronize()
@@ -499,10 +505,14 @@ def workloads(args, dev, stream, adr):
     fwd = _time(lambda: plan.step_ssprk33(u0d.clone(), ex["dt"], adj_steps), stream, 1)
     plan.adjoint_ssprk33(u0d, ex["dt"], 2, tgt, nsnap=2, dLdaux=gaux)   # warm: compiles the VJP
     torch.cuda.synchronize()
+    plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=64, dLdaux=gaux)   # allocates the slots
+    torch.cuda.synchronize()
     ta = time.perf_counter()
     _, nfw64 = plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=64, dLdaux=gaux)
     torch.cuda.synchronize()
     adj_s = time.perf_counter() - ta
+    plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=0, dLdaux=gaux)    # allocates 54 GB of states
+    torch.cuda.synchronize()
     ta = time.perf_counter()
     _, nfw0 = plan.adjoint_ssprk33(u0d, ex["dt"], adj_steps, tgt, nsnap=0, dLdaux=gaux)
     torch.cuda.synchronize()

@@ -76,14 +76,28 @@ int grid_for(long long ncell, int sms, int blocks_per_sm) {
     return (int)std::max<long long>(1, std::min<long long>(want, full));
 }
 
-// Threads per block: kThreads, or fewer for problems smaller than one full wave so
-// that every SM gets the same number of cells (a multiple of 32, at least 64).
+// Threads per block: kThreads, or fewer for problems smaller than one full wave so that
+// every SM gets about the same number of cells (a multiple of 32, at least 64).  Below one
+// wave the busiest SM sets the time of an FP64-bound stage, and it issues every warp it holds
+// whatever the warp's active lanes: among b = blocks_per_sm .. 1 CTAs per SM the shape whose
+// busiest SM holds the fewest warps is taken (65,536 cells on 152 SMs: 293 CTAs of 224 threads,
+// 14 warps on the busiest SM, instead of 410 of 160, 15 warps).
 int threads_for(long long ncell, int sms, int blocks_per_sm) {
     const long long slots = (long long)sms * blocks_per_sm;
     if (ncell >= slots * kThreads) return kThreads;
-    long long t = (ncell + slots - 1) / slots;
-    t = (t + 31) / 32 * 32;
-    return (int)std::max<long long>(64, std::min<long long>(kThreads, t));
+    long long best_t = 0, best_w = 0;
+    for (int b = blocks_per_sm; b >= 1; --b) {
+        const long long sl = (long long)sms * b;
+        long long t = (ncell + sl - 1) / sl;
+        t = std::max<long long>(64, std::min<long long>(kThreads, (t + 31) / 32 * 32));
+        const long long blocks = (ncell + t - 1) / t;
+        const long long w = (blocks + sms - 1) / sms * (t / 32);
+        if (!best_t || w < best_w) {
+            best_t = t;
+            best_w = w;
+        }
+    }
+    return (int)best_t;
 }
 
 template <class T>

@@ -188,3 +188,24 @@ def test_adr_adjoint_dLdK_both_forms(gpu_lib, expand):
     fd = (L(+1) - L(-1)) / (2 * h)
     got = gaux @ np.concatenate(dirs)
     assert abs(got - fd) <= 1e-6 * abs(fd), (got, fd)
+
+
+@pytest.mark.parametrize("expand", [False, True])
+def test_adr_f32state_reads_float_coefficients(gpu_lib, expand):
+    """The Float32-state kernels read the FP32 copy of the coefficient arrays: their RHS and
+    20 SSPRK33 steps stay at FP32 distance from the FP64 ones."""
+    lw, _, ex = _adr(32)
+    plan = Plan(lw, expand_stencils=expand)
+    u64 = lw.u0.copy()
+    du64 = np.zeros_like(u64)
+    plan.rhs(du64, u64, None, 0.0)
+    u32 = u64.astype(np.float32)
+    du32 = np.zeros_like(u32)
+    plan.rhs(du32, u32, None, 0.0)
+    assert _rel(du32.astype(np.float64), du64) < 1e-4
+    a = u64.copy()
+    plan.step_ssprk33(a, ex["dt"], 20)
+    b = u32.copy()
+    plan.step_ssprk33(b, ex["dt"], 20)
+    assert _rel(b.astype(np.float64), a) < 1e-5
+    plan.close()
