@@ -305,7 +305,9 @@ int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, doubl
  *   MOL_LOSS_LAMBDA:  `target` is dL/du(T) supplied by the caller
  * Outputs (any may be NULL): uT, loss, dL/du0 (n_unknowns), dL/dp (nparams),
  * dL/daux (concatenated aux arrays in descriptor order).  nsnap checkpoints
- * (binomial/revolve schedule) bound the stored states.  MOL_ERR_NONFINITE when a forward
+ * (binomial/revolve schedule) bound the stored states; nsnap <= 0 keeps every state (and both
+ * stage values of every step) that fits in three quarters of the free device memory, for the
+ * duration of the call.  MOL_ERR_NONFINITE when a forward
  * step produced a NaN or Inf state value (as mol_plan_check) or the loss is not finite. */
 #define MOL_LOSS_MISFIT 0
 #define MOL_LOSS_LAMBDA 1

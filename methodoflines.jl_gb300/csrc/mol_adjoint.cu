@@ -460,15 +460,19 @@ int mol_adjoint_ssprk33(mol_plan* plan, const double* u0, const double* p, doubl
         for (void* q : mine) cudaFree(q);
     };
     // checkpoint slots.  nsnap <= 0: keep every state and both stage values of every step
-    // when they fit in half of the free memory (no recomputation at all), else as many
-    // states as fit (binomial schedule over them).
+    // when they fit in three quarters of the free memory (no recomputation at all), else as
+    // many states as fit (binomial schedule over them).  The buffers live for the call only;
+    // the quarter left is for the caller (the 400-step 256^3 ADR adjoint keeps 161 GB of its
+    // 280 GB device this way instead of recomputing two stages per reverse step).
+    constexpr double kAdjointMemFraction = 0.75;
     int64_t slots = nsnap;
     bool keep_stages = false;
     if (slots <= 0) {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
-        keep_stages = nsteps > 0 && (3.0 * nsteps + 1.0) * 8.0 * n <= 0.5 * fr;
-        slots = (int64_t)std::max<double>(2.0, std::min<double>((double)nsteps + 1, 0.5 * fr / (8.0 * n)));
+        keep_stages = nsteps > 0 && (3.0 * nsteps + 1.0) * 8.0 * n <= kAdjointMemFraction * fr;
+        slots = (int64_t)std::max<double>(
+            2.0, std::min<double>((double)nsteps + 1, kAdjointMemFraction * fr / (8.0 * n)));
     }
     slots = std::max<int64_t>(1, std::min<int64_t>(slots, nsteps + 1));
     Adj A;
