@@ -741,7 +741,8 @@ def run_case(name, args):
         lw = lower(sys_.to_spec(disc))
         plan = Plan(lw, expand_stencils=args.stencil_form == "expanded")
         plan.set_stream(stream.cuda_stream)
-        u = torch.tensor(lw.u0, device=dev)
+        # --state f32: the Float32-state kernels (RHS and steps)
+        u = torch.tensor(lw.u0, device=dev, dtype=torch.float32 if args.state == "f32" else torch.float64)
         du = torch.zeros_like(u)
         lam = torch.tensor(np.random.default_rng(3).standard_normal(u.numel()), device=dev)
         gaux = torch.zeros(sum(a.size for a in lw.aux), dtype=torch.float64, device=dev)
@@ -776,6 +777,7 @@ def main():
     ap.add_argument("--case", default=None, choices=CASES,
                     help="run one small single-path case (for profiling) and exit")
     ap.add_argument("--case-n", type=int, default=0, help="grid side of the adr3d cases")
+    ap.add_argument("--state", default="f64", choices=["f64", "f32"], help="state precision of the adr3d cases")
     ap.add_argument("--stencil-form", default="expanded", choices=["difference", "expanded"],
                     help="coefficient stencils of the 3-D ADR plan (MOL_FLAG_EXPAND_STENCILS for expanded)")
     args = ap.parse_args()

@@ -1934,13 +1934,20 @@ int vjp_min_blocks_of(const std::string& src) {
     return src.find("gen_cell_vjp_full") != std::string::npos ? kCoefVjpMinBlocks : 0;
 }
 
-std::vector<std::string> jit_options(int min_blocks, int vjp_min_blocks) {
+// Resident CTAs per SM for the Float32-state group: its cells hold half-width values, its
+// kernels are bound by memory latency rather than the FP64 pipe, and the 256^3 ADR FP32 step
+// measured 1.028 / 0.828 / 0.675 / 0.728 ms at 3 / 4 / 6 / 8 CTAs per SM.
+constexpr int kF32MinBlocks = 6;
+
+std::vector<std::string> jit_options(int min_blocks, int vjp_min_blocks, int group) {
     std::vector<std::string> o = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
                                   "-default-device", "-DMOL_JIT=1"};
     const char* r = getenv("MOL_JIT_MAXRREG");
     if (r && atoi(r) > 0) o.push_back(std::string("--maxrregcount=") + std::to_string(atoi(r)));
     const char* mb = getenv("MOL_JIT_MIN_BLOCKS");
-    const int minb = (mb && atoi(mb) > 0) ? atoi(mb) : (min_blocks > 0 ? min_blocks : kDefaultMinBlocks);
+    const int minb = (mb && atoi(mb) > 0) ? atoi(mb)
+                     : group == JIT_FWD32 ? kF32MinBlocks
+                                         : (min_blocks > 0 ? min_blocks : kDefaultMinBlocks);
     o.push_back("-DMOL_MIN_BLOCKS=" + std::to_string(minb));
     // the face pass at three resident CTAs per SM more than the stage kernels: the 256^3 ADR
     // step measured 3.18 / 3.00 / 2.91 / 2.86 / 2.93 ms with the face kernel at 3 / 4 / 5 / 6 / 8
@@ -1976,7 +1983,7 @@ std::vector<std::string> jit_options(int min_blocks, int vjp_min_blocks) {
 
 // Compiled modules are kept on disk (MOL_CACHE_DIR, else $HOME/.cache/molgpu) keyed by a
 // hash of the generated source, the compile options and the kernel list.
-std::string disk_cache_path(const std::string& src, int nparams, int min_blocks) {
+std::string disk_cache_path(const std::string& src, int nparams, int min_blocks, int group) {
     const char* dir = getenv("MOL_CACHE_DIR");
     std::string base;
     if (dir && dir[0]) base = dir;
@@ -1991,7 +1998,7 @@ std::string disk_cache_path(const std::string& src, int nparams, int min_blocks)
         }
     };
     mix(src);
-    for (auto& o : jit_options(min_blocks, vjp_min_blocks_of(src))) mix(o);
+    for (auto& o : jit_options(min_blocks, vjp_min_blocks_of(src), group)) mix(o);
     mix("v4|" + std::to_string(nparams));
     for (int i = 0; i < (int)(sizeof(kEmbedTexts) / sizeof(kEmbedTexts[0])); ++i) mix(kEmbedTexts[i]);
     char name[64];
@@ -2090,7 +2097,7 @@ int nvrtc_compile(const std::string& src, int nparams, int group, std::vector<ch
         return MOL_ERR_CUDA;
     }
     for (auto& n : names) N.addname(prog, n.c_str());
-    std::vector<std::string> ostr = jit_options(min_blocks, vjp_min_blocks_of(src));
+    std::vector<std::string> ostr = jit_options(min_blocks, vjp_min_blocks_of(src), group);
     std::vector<const char*> opts;
     for (auto& o : ostr) opts.push_back(o.c_str());
     const int rc = N.compile(prog, (int)opts.size(), opts.data());
@@ -2140,7 +2147,7 @@ int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k
     if (got.empty()) {
         std::vector<char> cubin;
         std::vector<std::string> lowered;
-        const std::string cache_path = disk_cache_path(key, nparams, k->min_blocks);
+        const std::string cache_path = disk_cache_path(key, nparams, k->min_blocks, group);
         if (!(cache_path.size() && disk_cache_load(cache_path, names.size(), &cubin, &lowered))) {
             int st = nvrtc_compile(src, nparams, group, &cubin, &lowered, err, k->min_blocks);
             if (st) return st;

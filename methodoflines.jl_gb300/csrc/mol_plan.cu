@@ -313,18 +313,53 @@ template int ensure_faces<float>(mol_plan*);
 template DevProb<double> with_faces<double>(mol_plan*, const double*, const double*, double, double, cudaError_t*);
 template DevProb<float> with_faces<float>(mol_plan*, const float*, const float*, double, double, cudaError_t*);
 
+// The generated forward group of precision T, loaded on first use.  The FP32 group is compiled
+// for more resident CTAs per SM than the FP64 one, so its grid is shaped from its own register
+// count the first time it is loaded.
+template <class T>
+int ensure_fwd(mol_plan* plan) {
+    const bool is64 = std::is_same<T, double>::value;
+    int st = jit_ensure(&plan->jit, is64 ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
+    if (st) return set_err(plan, st, plan->jit_err);
+    if (!is64 && plan->nblocks32 == 0) {
+        plan->nblocks32 = plan->nblocks;
+        plan->nthreads32 = plan->nthreads;
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, (const void*)plan->jit.ssp32[0]) == cudaSuccess && fa.numRegs > 0) {
+            const int bps = std::max(1, std::min(8, 65536 / (fa.numRegs * kThreads)));
+            plan->nthreads32 = threads_for(plan->ncell, plan->sms, bps);
+            const long long slots = (long long)plan->sms * bps;
+            plan->nblocks32 = (int)std::max<long long>(
+                1, std::min<long long>(slots, (plan->ncell + plan->nthreads32 - 1) / plan->nthreads32));
+        } else {
+            cudaGetLastError();
+        }
+    }
+    return MOL_OK;
+}
+
+// Grid of the generated kernels of precision T.
+template <class T>
+int blocks_of(const mol_plan* plan) {
+    return (!std::is_same<T, double>::value && plan->nblocks32 > 0) ? plan->nblocks32 : plan->nblocks;
+}
+template <class T>
+int threads_of(const mol_plan* plan) {
+    return (!std::is_same<T, double>::value && plan->nthreads32 > 0) ? plan->nthreads32 : plan->nthreads;
+}
+
 template <class T>
 int launch_rhs(mol_plan* plan, T* du, const T* u, const T* p, double t) {
     const bool is64 = std::is_same<T, double>::value;
     if (plan->use_jit) {
-        int st = jit_ensure(&plan->jit, is64 ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
-        if (st) return set_err(plan, st, plan->jit_err);
+        int st = ensure_fwd<T>(plan);
+        if (st) return st;
         cudaError_t e;
         const DevProb<T> Pf = with_faces<T>(plan, u, p, 0.0, t, &e);
         if (e != cudaSuccess) return cuda_check(plan, e, "face pass launch");
         ++g_launches;
-        return cuda_check(plan, launch_k(is64 ? plan->jit.rhs64 : plan->jit.rhs32, plan->nblocks, plan->nthreads,
-                                         plan->stream, Pf, u, du, p, t), "rhs launch");
+        return cuda_check(plan, launch_k(is64 ? plan->jit.rhs64 : plan->jit.rhs32, blocks_of<T>(plan),
+                                         threads_of<T>(plan), plan->stream, Pf, u, du, p, t), "rhs launch");
     }
     k_rhs_t<T, InterpCell><<<plan->nblocks, kThreads, 0, plan->stream>>>(prob<T>(plan), u, du, p, t);
     ++g_launches;
@@ -348,8 +383,9 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
     g_launches += 3;
     if (plan->use_jit) {
         const bool is64 = std::is_same<T, double>::value;
-        int st = jit_ensure(&plan->jit, is64 ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
-        if (st) return set_err(plan, st, plan->jit_err);
+        int st = ensure_fwd<T>(plan);
+        if (st) return st;
+        const int nb = blocks_of<T>(plan), nt = threads_of<T>(plan);
         cudaKernel_t* k = is64 ? plan->jit.ssp64 : plan->jit.ssp32;
         const T* cu = u;
         const T* cu1 = u1;
@@ -359,15 +395,15 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
         DevProb<T> Pf = with_faces<T>(plan, cu, p, 0.0, nan, &e);
         const long long c0 = 0, c1 = plan->ncell;
         if (e == cudaSuccess && !skip1)
-            e = launch_k(k[0], plan->nblocks, plan->nthreads, plan->stream, Pf, cu, cu, u1, p, plan->d_state, dt, nan,
+            e = launch_k(k[0], nb, nt, plan->stream, Pf, cu, cu, u1, p, plan->d_state, dt, nan,
                          c0, c1);
         if (e == cudaSuccess) Pf = with_faces<T>(plan, cu1, p, dt, nan, &e);
         if (e == cudaSuccess)
-            e = launch_k(k[1], plan->nblocks, plan->nthreads, plan->stream, Pf, cu1, cu, u2, p, plan->d_state, dt, nan,
+            e = launch_k(k[1], nb, nt, plan->stream, Pf, cu1, cu, u2, p, plan->d_state, dt, nan,
                          c0, c1);
         if (e == cudaSuccess) Pf = with_faces<T>(plan, cu2, p, dt / 2, nan, &e);
         if (e == cudaSuccess)
-            e = launch_k(k[2], plan->nblocks, plan->nthreads, plan->stream, Pf, cu2, cu, uout, p, plan->d_state, dt, nan,
+            e = launch_k(k[2], nb, nt, plan->stream, Pf, cu2, cu, uout, p, plan->d_state, dt, nan,
                          c0, c1);
         return cuda_check(plan, e, "ssprk launch");
     }
@@ -419,12 +455,12 @@ int launch_stage1_streamed(mol_plan* plan, const T* host, T* ud, T* u1, const T*
     const bool is64 = std::is_same<T, double>::value;
     auto stage1 = [&](long long c0, long long c1) -> int {
         if (c1 <= c0) return MOL_OK;
-        const int thr = plan->use_jit ? plan->nthreads : kThreads;
-        const int blocks = (int)std::min<long long>(plan->nblocks, (c1 - c0 + thr - 1) / thr);
+        const int thr = plan->use_jit ? threads_of<T>(plan) : kThreads;
+        const int blocks = (int)std::min<long long>(blocks_of<T>(plan), (c1 - c0 + thr - 1) / thr);
         ++g_launches;
         if (plan->use_jit) {
             cudaKernel_t kk = is64 ? plan->jit.ssp64[0] : plan->jit.ssp32[0];
-            return cuda_check(plan, launch_k(kk, blocks, plan->nthreads, plan->stream, P, (const T*)ud, (const T*)ud, u1,
+            return cuda_check(plan, launch_k(kk, blocks, thr, plan->stream, P, (const T*)ud, (const T*)ud, u1,
                                              p, plan->d_state, dt, nan, c0, c1), "stage-1 slab");
         }
         k_ssprk_t<T, InterpCell, 1><<<blocks, kThreads, 0, plan->stream>>>(P, ud, ud, u1, p, plan->d_state, dt, nan,
@@ -1285,8 +1321,8 @@ int ssprk_impl(mol_plan* plan, T* u, const T* p, double t0, double dt, int64_t n
     const T* pp = params_ptr<T>(plan, p, &st);
     if (st) return st;
     if (plan->use_jit) {  // modules are loaded before any stream capture begins
-        st = jit_ensure(&plan->jit, std::is_same<T, double>::value ? JIT_FWD64 : JIT_FWD32, plan->jit_err);
-        if (st) return set_err(plan, st, plan->jit_err);
+        st = ensure_fwd<T>(plan);
+        if (st) return st;
     }
     k_set_time<<<1, 1, 0, plan->stream>>>(plan->d_state, t0);
     ++g_launches;

@@ -62,6 +62,7 @@ struct mol_plan {
     mol::SolverState* d_state = nullptr;
     double* d_partials = nullptr;
     int nblocks = 0;
+    int nblocks32 = 0, nthreads32 = 0;   // grid of the Float32-state kernels (own register budget)
     // grid of the face pass: it moves more bytes per FP64 operation than the stage kernels
     // and needs more warps in flight, so it runs at its own (higher) occupancy
     int face_blocks = 0, face_threads = 256;
