@@ -160,6 +160,36 @@ def nonlinear_diffusion(n: int, k: float, seed: int):
     return sys, disc, {}
 
 
+def coefficient_system(n: int = 24):
+    """Two coupled fields on [0,1]^2 with coordinate-dependent diffusivities beside constant
+    first-derivative terms, one diffusivity scaled by a parameter, and Dirichlet, Neumann and
+    Robin rows:
+        u_t = Dx(K1 Dx u) + Dy(kp K2 Dy u) + 0.7 Dx(u) - v
+        v_t = Dx(K2 Dx v) + Dy(K1 Dy v) - 0.4 Dy(v) + u v
+    K1 = 0.5 + 0.3 sin(2 pi x) cos(pi y), K2 = 1 + 0.2 x y (registered functions of the
+    coordinates, evaluated on the host at the faces)."""
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u, v = Field("u"), Field("v")
+    Dt, Dx, Dy = Differential(t), Differential(x), Differential(y)
+    K1 = register("K1", lambda X, Y: 0.5 + 0.3 * np.sin(2 * math.pi * X) * np.cos(math.pi * Y))
+    K2 = register("K2", lambda X, Y: 1.0 + 0.2 * X * Y)
+    kp = Param("kp", 0.8)
+    U, V = u(x, y, t), v(x, y, t)
+    eq1 = Eq(Dt(U), Dx(K1(x, y) * Dx(U)) + Dy(kp * K2(x, y) * Dy(U)) + 0.7 * Dx(U) - V)
+    eq2 = Eq(Dt(V), Dx(K2(x, y) * Dx(V)) + Dy(K1(x, y) * Dy(V)) - 0.4 * Dy(V) + U * V)
+    bcs = [Eq(u(x, y, 0.0), 1.0 + 0.2 * y + 0.1 * sin(math.pi * x) * sin(math.pi * y)),
+           Eq(v(x, y, 0.0), 0.5 + 0.1 * cos(math.pi * x) * cos(2 * math.pi * y)),
+           Eq(u(0.0, y, t), 1.0 + 0.2 * y), Eq(Dx(u(1.0, y, t)), 0.0),
+           Eq(u(x, 0.0, t) + 0.5 * Dy(u(x, 0.0, t)), 1.0), Eq(u(x, 1.0, t), 1.2),
+           Eq(Dx(v(0.0, y, t)), 0.0), Eq(Dx(v(1.0, y, t)), 0.0), Eq(Dy(v(x, 0.0, t)), 0.0),
+           Eq(Dy(v(x, 1.0, t)), 0.0)]
+    sys = PDESystem([eq1, eq2], bcs, [(x, Interval(0.0, 1.0)), (y, Interval(0.0, 1.0)), (t, Interval(0.0, 1.0))],
+                    [x, y, t], [U, V], [kp])
+    disc = MOLFiniteDifference({x: n, y: n}, t, approx_order=2)
+    h = 1.0 / (n - 1)
+    return sys, disc, {"dt": 0.1 * h * h}
+
+
 def ensemble_members(count: int = 4096, seed_n: int = 7, seed_k: int = 8, nmin: int = 32, nmax: int = 512):
     """(n_i, k_i, ic seed) of the ensemble: n log-uniform on [nmin, nmax], k uniform on [0, 2]."""
     rn = _rng(seed_n)

@@ -209,3 +209,84 @@ def test_adr_f32state_reads_float_coefficients(gpu_lib, expand):
     plan.step_ssprk33(b, ex["dt"], 20)
     assert _rel(b.astype(np.float64), a) < 1e-5
     plan.close()
+
+
+def _system(n):
+    sys_, disc, ex = problems.coefficient_system(n)
+    spec = sys_.to_spec(disc)
+    return lower(spec), OracleProblem(spec), ex
+
+
+@pytest.mark.parametrize("expand", [False, True])
+def test_two_field_system_rhs_and_trajectory(gpu_lib, expand):
+    """Two fields, each with its own coefficient stencil (arrays at different offsets), a
+    parameter-scaled diffusivity left on the face form beside them, and Dirichlet, Neumann and
+    Robin rows on every side (edge cells on the original statements)."""
+    lw, orc, ex = _system(24)
+    plan = Plan(lw, expand_stencils=expand)
+    assert plan.coef_arrays == (2 + 4 if not expand else 3 + 5)
+    rng = np.random.default_rng(25)
+    u = lw.u0 * (1 + 0.05 * rng.standard_normal(lw.n_unknowns))
+    for t in (0.0, 0.4):
+        du = np.zeros(lw.n_unknowns)
+        plan.rhs(du, u, None, t)
+        assert _rel(du, orc.rhs(u, t)) < RHS_TOL
+    w = lw.u0.copy()
+    plan.step_ssprk33(w, ex["dt"], 20, t0=0.0)
+    ref, _ = ssprk33(lambda q, t: orc.rhs(q, t), lw.u0, 0.0, ex["dt"], 20)
+    assert _rel(w, ref) < TRAJ_TOL
+    plan.close()
+
+
+@pytest.mark.parametrize("expand", [False, True])
+def test_two_field_system_vjp(gpu_lib, expand):
+    import copy
+    lw, _, _ = _system(24)
+    plan = Plan(lw, expand_stencils=expand)
+    rng = np.random.default_rng(26)
+    u = lw.u0 * (1 + 0.05 * rng.standard_normal(lw.n_unknowns))
+    lam = rng.standard_normal(lw.n_unknowns)
+    v = rng.standard_normal(lw.n_unknowns)
+    lam_u = np.zeros(lw.n_unknowns)
+    lam_p = np.zeros(1)
+    lam_aux = np.zeros(sum(a.size for a in lw.aux))
+    plan.vjp(lam, u, None, 0.2, lam_u=lam_u, lam_p=lam_p, lam_aux=lam_aux)
+
+    def rhs(pl, x, p=None):
+        du = np.zeros_like(x)
+        pl.rhs(du, x, p, 0.2)
+        return du
+
+    h = 1e-6
+    fd = lam @ (rhs(plan, u + h * v) - rhs(plan, u - h * v)) / (2 * h)
+    assert abs(lam_u @ v - fd) <= 1e-6 * abs(fd), (lam_u @ v, fd)
+    p0 = lw.param_values.copy()
+    fdp = lam @ (rhs(plan, u, p0 + h) - rhs(plan, u, p0 - h)) / (2 * h)
+    assert abs(lam_p[0] - fdp) <= 1e-6 * abs(fdp), (lam_p[0], fdp)
+    dirs = [rng.standard_normal(a.size) * (a != 0) for a in lw.aux]
+
+    def with_aux(sign):
+        lw2 = copy.copy(lw)
+        lw2.aux = [a + sign * 1e-7 * d for a, d in zip(lw.aux, dirs)]
+        p2 = Plan(lw2, expand_stencils=expand)
+        out = rhs(p2, u)
+        p2.close()
+        return out
+
+    fda = lam @ (with_aux(+1) - with_aux(-1)) / 2e-7
+    got = lam_aux @ np.concatenate(dirs)
+    assert abs(got - fda) <= 1e-6 * abs(fda), (got, fda)
+    plan.close()
+
+
+def test_two_field_system_with_face_pass(gpu_lib):
+    """At 200^2 cells per field the parameter-scaled term goes through the face pass while the
+    other three diffusion terms are coefficient stencils; RHS against the oracle."""
+    lw, orc, _ = _system(202)
+    plan = Plan(lw)
+    rng = np.random.default_rng(27)
+    u = lw.u0 * (1 + 0.05 * rng.standard_normal(lw.n_unknowns))
+    du = np.zeros(lw.n_unknowns)
+    plan.rhs(du, u, None, 0.1)
+    assert _rel(du, orc.rhs(u, 0.1)) < RHS_TOL
+    plan.close()
