@@ -353,6 +353,56 @@ std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d) {
             int base = 0;
             for (auto& h : groups) base += h.narr;
             g.arr0 = base;
+            // a reaction k u^2 in the cell's own unknown joins the expanded centre tap:
+            // (c_0 + k u) u is one FMA fewer than c_0 u + k (u u)
+            bool centre_arr = false;
+            for (auto& t : g.taps) centre_arr |= t.arr >= 0 && !t.o[0] && !t.o[1] && !t.o[2];
+            std::function<bool(int)> uniform = [&](int q) -> bool {
+                if (q < 0) return false;
+                const mol_instr& in = s.ins[q];
+                switch (in.op) {
+                    case MOL_OP_CONST: case MOL_OP_PARAM: case MOL_OP_TIME: return true;
+                    case MOL_OP_ADD: case MOL_OP_SUB: case MOL_OP_MUL: case MOL_OP_DIV: case MOL_OP_POW:
+                    case MOL_OP_CMP:
+                        return uniform(s.ia[q]) && uniform(s.ib[q]);
+                    case MOL_OP_NEG: case MOL_OP_POWI: case MOL_OP_FN: return uniform(s.ia[q]);
+                    case MOL_OP_IFELSE: return uniform(s.ia[q]) && uniform(s.ib[q]) && uniform(s.ic[q]);
+                    default: return false;
+                }
+            };
+            // the square of the group's field at the cell: POWI(F, 2) or MUL(F, F) of one FIELD
+            // node used by nothing else
+            auto square = [&](int q, std::vector<int>* nodes) -> bool {
+                if (q < 0 || uses[q] != 1) return false;
+                const mol_instr& in = s.ins[q];
+                int f = -1;
+                if (in.op == MOL_OP_POWI && in.imm == 2) f = s.ia[q];
+                else if (in.op == MOL_OP_MUL && s.ia[q] == s.ib[q]) f = s.ia[q];
+                if (f < 0 || s.ins[f].op != MOL_OP_FIELD || s.ins[f].imm != g.field) return false;
+                if (uses[f] != (in.op == MOL_OP_MUL ? 2 : 1)) return false;
+                *nodes = {f, q};
+                return true;
+            };
+            for (size_t i = 0; expanded && centre_arr && i < g.rest.size(); ++i) {
+                const int q = g.rest[i].second;
+                if (s.ins[q].op != MOL_OP_MUL || uses[q] != 1) continue;
+                std::vector<int> nodes;
+                int k = -1;
+                if (uniform(s.ia[q]) && square(s.ib[q], &nodes)) k = s.ia[q];
+                else if (uniform(s.ib[q]) && square(s.ia[q], &nodes)) k = s.ib[q];
+                if (k < 0) continue;
+                g.quad_coef = k;
+                g.quad_sign = g.rest[i].first;
+                nodes.push_back(q);
+                for (int x : nodes) {
+                    g.absorbed.push_back(x);
+                    g.leaf_nodes.push_back(x);
+                }
+                std::sort(g.leaf_nodes.begin(), g.leaf_nodes.end());
+                g.folded.push_back(g.rest[i]);
+                g.rest.erase(g.rest.begin() + i);
+                break;
+            }
         }
         groups.push_back(g);
     }
@@ -1503,7 +1553,7 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
           << "        const T* __restrict__ fb = u + (long long)" << F << " * P.ncell + c;\n";
         if (g.variable) {
             e << "        const T* __restrict__ cw = P.cw + (long long)" << g.arr0 << " * P.ncell + c;\n";
-            bool anydiff = false;
+            bool anydiff = g.quad_coef >= 0;
             for (const FoldTap& t : g.taps) anydiff |= t.diff;
             if (anydiff) e << "        const T u0 = fb[0];\n";
         }
@@ -1518,9 +1568,15 @@ static void emit_cell_fused(Emitter& e, const mol_problem_desc* d, const SSA& s,
             const std::string wv = tp.arr >= 0 ? (tp.arr == 0 ? std::string("cw[0]")
                                                               : "cw[(long long)" + std::to_string(tp.arr) + " * P.ncell]")
                                                : "fw[" + std::to_string(i) + "]";
-            const std::string xv = tp.diff ? "(fb[" + off + "] - u0)" : "fb[" + off + "]";
-            if (!started) e << "        T acc = " << wv << " * " << xv << ";\n";
-            else e << "        acc = fma(" << wv << ", " << xv << ", acc);\n";
+            std::string xv = tp.diff ? "(fb[" + off + "] - u0)" : "fb[" + off + "]";
+            std::string wq = wv;
+            if (g.quad_coef >= 0 && tp.arr >= 0 && !tp.o[0] && !tp.o[1] && !tp.o[2]) {
+                // the reaction k u^2 on the centre tap: (c_0 + k u) u
+                wq = "fma(" + std::string(g.quad_sign < 0 ? "-" : "") + name(g.quad_coef) + ", u0, " + wv + ")";
+                xv = "u0";
+            }
+            if (!started) e << "        T acc = " << wq << " * " << xv << ";\n";
+            else e << "        acc = fma(" << wq << ", " << xv << ", acc);\n";
             started = true;
         }
         e << "        " << G << " = " << (started ? "acc" : "T(0)") << ";\n    } else {\n";

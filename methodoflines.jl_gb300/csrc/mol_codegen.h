@@ -88,6 +88,10 @@ struct FoldGroup {
     bool variable = false;                  // has coordinate-dependent (nonlinear-Laplacian) members
     int arr0 = 0;                           // first coefficient array of the group (plan-wide index)
     int narr = 0;                           // coefficient arrays of the group
+    // expanded form: an addend quad_sign * k * u^2 of the output (k uniform, u the group's field
+    // at the cell) joins the centre tap as (c_0 + quad_sign * k * u) * u; quad_coef is k's pc
+    int quad_coef = -1;
+    double quad_sign = 0.0;
 };
 std::vector<FoldGroup> const_linear_groups(const mol_problem_desc* d);
 // The fused weights of a group, one per tap: the sum over its constant parts of coefficient *
