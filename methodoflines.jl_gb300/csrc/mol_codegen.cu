@@ -1733,6 +1733,20 @@ static void emit_group_vjp(Emitter& e, const mol_problem_desc* d, const FoldGrou
         for (const FoldPart& p : t.parts)
             if (p.face >= 0) faces[{p.term, p.face}].push_back({&t, p.coef});
     if (!faces.empty()) e << "        if (lam_aux) {\n";
+    // a face whose two parts are c (u[a] - u[b]) with c > 0 (the folded nonlinear Laplacian's
+    // faces): g * c is computed once for every face with that c
+    auto paired = [&](const std::vector<std::pair<const FoldTap*, double>>& pr) {
+        return pr.size() == 2 && pr[0].second == -pr[1].second && pr[0].second != 0.0;
+    };
+    std::map<double, std::string> scales;
+    for (auto& fk : faces) {
+        if (d->terms[fk.first.first].prog < 0 || !paired(fk.second)) continue;
+        const double c = std::fabs(fk.second[0].second);
+        if (scales.count(c)) continue;
+        const std::string nm = "gs" + std::to_string(scales.size());
+        e << "        const T " << nm << " = g * " << lit(c) << ";\n";
+        scales[c] = nm;
+    }
     for (auto& fk : faces) {
         const int k = fk.first.first, m = fk.first.second;
         const mol_term& tm = d->terms[k];
@@ -1740,11 +1754,20 @@ static void emit_group_vjp(Emitter& e, const mol_problem_desc* d, const FoldGrou
         const std::string D = std::to_string(tm.dim);
         const int r = d->ops[tm.op].omin + m - 1;
         const std::string tag = "va" + std::to_string(k) + "_" + std::to_string(m) + "_";
-        e << "        {\n        T " << tag << "s = T(0);\n";
-        for (auto& tc : fk.second)
-            e << "        " << tag << "s = fma(" << lit(tc.second) << ", fb[" << group_tap_off(d, g, *tc.first) << "], "
-              << tag << "s);\n";
-        e << "        const T " << tag << "ga = g * " << tag << "s;\n";
+        e << "        {\n";
+        const auto& pr = fk.second;
+        if (paired(pr)) {
+            const int ia = pr[0].second > 0 ? 0 : 1;
+            e << "        const T " << tag << "ga = " << scales.at(std::fabs(pr[0].second)) << " * (fb["
+              << group_tap_off(d, g, *pr[ia].first) << "] - fb[" << group_tap_off(d, g, *pr[1 - ia].first)
+              << "]);\n";
+        } else {
+            e << "        T " << tag << "s = T(0);\n";
+            for (auto& tc : pr)
+                e << "        " << tag << "s = fma(" << lit(tc.second) << ", fb[" << group_tap_off(d, g, *tc.first)
+                  << "], " << tag << "s);\n";
+            e << "        const T " << tag << "ga = g * " << tag << "s;\n";
+        }
         const SSA fs = to_ssa(d, tm.prog);
         std::set<int> used_aux;
         for (auto& in : fs.ins)
