@@ -39,7 +39,9 @@ def test_adr_expanded_form():
     cell = _cell(src)
     assert "kCoefArrays = 7;" in src                    # the face taps and the centre
     assert " - u0)" not in cell
-    assert "fb[0], acc" in cell
+    # -lambda u^2 joins the centre tap: (c_0 - lambda u) u
+    assert "fma(fma(-U." in cell and "u0, acc)" in cell
+    assert "out[0] = fg0;" in cell
 
 
 def test_state_dependent_coefficient_is_not_a_coefficient_stencil():
