@@ -1,6 +1,6 @@
 """Discrete adjoint on the GPU: VJP and checkpointed reverse sweep against finite differences.
 
-Bar (the benchmark spec): gradients match central finite differences to 1e-6 relative.
+Bar: gradients match central finite differences to 1e-6 relative.
 """
 import numpy as np
 import pytest

@@ -1,6 +1,6 @@
 """GPU parity: libmolgpu against the oracle, through the C ABI.
 
-Bars (the benchmark spec): RHS within 1e-12 relative (norm-wise) of the reference's
+Bars: RHS within 1e-12 relative (norm-wise) of the reference's
 discretisation; fixed-step SSPRK33 trajectories within 1e-10 relative.
 """
 import math
