@@ -670,6 +670,30 @@ __device__ T apply_mixed(const DevProb<T>& P, const mol_term& tm, const T* u, co
 template <class T>
 __device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps, T inv_dx) {
     const T c13_12 = T(13) / T(12);
+    if (sizeof(T) == 8) {
+        // FP64 issue is the bound: beta_1 and beta_3 take their second square as (b/2)^2 with b/2
+        // formed directly (1.5 u - 2 u' + 0.5 u''), bit for bit 0.25 b^2 since scaling by 1/2
+        // commutes with rounding; the ideal weights (0.1, 0.6, 0.3) ride on the candidate
+        // reconstructions' coefficients instead of six products with the P_k
+        const T a1 = u0 - T(2) * up1 + up2, h1 = T(1.5) * u0 - T(2) * up1 + T(0.5) * up2;
+        const T a2 = um1 - T(2) * u0 + up1, b2 = um1 - up1;
+        const T a3 = um2 - T(2) * um1 + u0, h3 = T(0.5) * um2 - T(2) * um1 + T(1.5) * u0;
+        const T e1 = eps + fma(c13_12 * a1, a1, h1 * h1);
+        const T e2 = eps + fma(c13_12 * a2, a2, T(0.25) * (b2 * b2));
+        const T e3 = eps + fma(c13_12 * a3, a3, h3 * h3);
+        const T s1 = e1 * e1, s2 = e2 * e2, s3 = e3 * e3;
+        const T P1 = s2 * s3, P2 = s1 * s3, P3 = s1 * s2;   // P_k = prod_{j != k} (eps + beta_j)^2
+        // gamma_k times the candidates (scaled by 6, the 1/6 folded into inv_dx below)
+        const T gm1 = T(1.1) * u0 - T(0.7) * up1 + T(0.2) * up2;   // 0.1 (11 u0 - 7 up1 + 2 up2)
+        const T gm2 = T(3.0) * u0 - T(0.6) * up1 + T(1.2) * um1;   // 0.6 (5 u0 - up1 + 2 um1)
+        const T gm3 = T(0.6) * u0 + T(1.5) * um1 - T(0.3) * um2;   // 0.3 (2 u0 + 5 um1 - um2)
+        const T gp1 = T(0.6) * u0 + T(1.5) * up1 - T(0.3) * up2;   // 0.3 (2 u0 + 5 up1 - up2)
+        const T gp2 = T(3.0) * u0 + T(1.2) * up1 - T(0.6) * um1;   // 0.6 (5 u0 + 2 up1 - um1)
+        const T gp3 = T(1.1) * u0 - T(0.7) * um1 + T(0.2) * um2;   // 0.1 (11 u0 - 7 um1 + 2 um2)
+        const T Np = fma(P1, gp1, fma(P2, gp2, P3 * gp3)), Dp = fma(T(0.3), P1, fma(T(0.6), P2, T(0.1) * P3));
+        const T Nm = fma(P1, gm1, fma(P2, gm2, P3 * gm3)), Dm = fma(T(0.1), P1, fma(T(0.6), P2, T(0.3) * P3));
+        return fma(Np, Dm, -Nm * Dp) / (Dp * Dm) * (inv_dx * T(1.0 / 6.0));
+    }
     const T a1 = u0 - T(2) * up1 + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
     const T a2 = um1 - T(2) * u0 + up1, b2 = um1 - up1;
     const T a3 = um2 - T(2) * um1 + u0, b3 = um2 - T(4) * um1 + T(3) * u0;
@@ -683,15 +707,6 @@ __device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps
     const T hp1 = T(2) * u0 + T(5) * up1 - up2;
     const T hp2 = T(5) * u0 + T(2) * up1 - um1;
     const T hp3 = T(11) * u0 - T(7) * um1 + T(2) * um2;
-    if (sizeof(T) == 8) {
-        const T s1 = e1 * e1, s2 = e2 * e2, s3 = e3 * e3;
-        const T P1 = s2 * s3, P2 = s1 * s3, P3 = s1 * s2;   // P_k = prod_{j != k} (eps + beta_j)^2
-        const T wm1 = T(0.1) * P1, wm2 = T(0.6) * P2, wm3 = T(0.3) * P3;
-        const T wp1 = T(0.3) * P1, wp2 = T(0.6) * P2, wp3 = T(0.1) * P3;
-        const T Np = fma(wp1, hp1, fma(wp2, hp2, wp3 * hp3)), Dp = wp1 + wp2 + wp3;
-        const T Nm = fma(wm1, hm1, fma(wm2, hm2, wm3 * hm3)), Dm = wm1 + wm2 + wm3;
-        return fma(Np, Dm, -Nm * Dp) / (Dp * Dm) * (inv_dx * T(1.0 / 6.0));
-    }
     const T q1 = T(1) / (e1 * e1), q2 = T(1) / (e2 * e2), q3 = T(1) / (e3 * e3);
     const T wm1 = T(0.1) * q1, wm2 = T(0.6) * q2, wm3 = T(0.3) * q3;
     const T wp1 = T(0.3) * q1, wp2 = T(0.6) * q2, wp3 = T(0.1) * q3;
