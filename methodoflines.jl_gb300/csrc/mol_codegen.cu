@@ -2143,7 +2143,7 @@ std::vector<std::string> jit_kernel_names(int nparams, int group) {
             n = {"&mol::k_rhs_t<double, mol::GenCell>", "&mol::k_ssprk_t<double, mol::GenCell, 1>",
                  "&mol::k_ssprk_t<double, mol::GenCell, 2>", "&mol::k_ssprk_t<double, mol::GenCell, 3>",
                  "&mol::k_tsit_stage_t<double, mol::GenCell>", "&mol::k_faces_t<double, mol::GenCell>",
-                 "&mol::k_coef_t<mol::GenCell>"};
+                 "&mol::k_coef_t<mol::GenCell>", "&mol::k_tsit_small_t<double, mol::GenCell>"};
             break;
         case JIT_FWD32:
             n = {"&mol::k_rhs_t<float, mol::GenCell>", "&mol::k_ssprk_t<float, mol::GenCell, 1>",
@@ -2261,6 +2261,7 @@ int jit_load_group(const std::string& src, int nparams, int group, JitKernels* k
             k->tsit64 = got[4];
             k->faces64 = got[5];
             k->coef64 = got[6];
+            k->tsitsmall64 = got[7];
             break;
         case JIT_FWD32:
             k->rhs32 = got[0];

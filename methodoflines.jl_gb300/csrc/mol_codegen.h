@@ -26,6 +26,7 @@ struct JitKernels {
     cudaKernel_t tiles64 = nullptr, tiles32 = nullptr;
     cudaKernel_t faces64 = nullptr, faces32 = nullptr;  // face pass (nonlinear Laplacian)
     cudaKernel_t coef64 = nullptr;                      // coefficient stencils (k_coef_t)
+    cudaKernel_t tsitsmall64 = nullptr;                 // one-CTA Tsit5 for small problems
 };
 
 std::string generate_source(const mol_problem_desc* d, std::string& why);

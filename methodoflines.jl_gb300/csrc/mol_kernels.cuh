@@ -541,23 +541,38 @@ __device__ __forceinline__ double tsit_c(int i) {
     }
 }
 
-// Stage i (2..7): k_i = f(y_i, t + c_i dt); the epilogue writes y_{i+1} = u + sum_j (dt a_{i+1,j}) k_j.
-// Stage 7 accumulates the scaled error sum_j (dt btilde_j) k_j; the last block to finish
-// reduces it deterministically and runs the PI step-size controller.
+// Row updates of the controller's dt-scaled tableau (Tsitouras 2011 a_ij and btilde_j); one thread.
+__device__ __forceinline__ void tsit_scale(SolverState* S) {
+    const double A[8][8] = {
+        {0}, {0},
+        {0, 0.161},
+        {0, -0.008480655492356989, 0.335480655492357},
+        {0, 2.897153057105493, -6.359448489975075, 4.3622954328695815},
+        {0, 5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525},
+        {0, 5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383},
+        {0, 0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081,
+         2.324710524099774}};
+    const double B[8] = {0, -0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+                         -0.1447110071732629, 0.5823571654525552, -0.45808210592918697, 0.015151515151515152};
+    const double dt = S->dt;
+    for (int i = 0; i < 8; ++i)
+        for (int j = 0; j < 8; ++j) S->dta[i][j] = dt * A[i][j];
+    for (int j = 0; j < 8; ++j) S->dtb[j] = dt * B[j];
+}
+
+// Stage i (2..7) on cells c_beg, c_beg + c_step, ...: k_i = f(y_i, t), and y_{i+1} = u +
+// sum_j (dt a_{i+1,j}) k_j, or at stage 7 the scaled error sum_j (dt btilde_j) k_j, whose
+// squared norm terms are returned.
 template <class T, class G>
-__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_tsit_stage_t(const __grid_constant__ DevProb<T> P, int stage, const T* __restrict__ y,
-                                                           T* ynext, const T* __restrict__ u, T* const* k,
-                                                           const T* __restrict__ p, SolverState* S,
-                                                           double* partials) {
-    if (S->done) return;
-    const double t = S->t + tsit_c(stage) * S->dt;
+__device__ __forceinline__ double tsit_stage_cells(const DevProb<T>& P, int stage, const T* __restrict__ y, T* ynext,
+                                                   const T* __restrict__ u, T* const* k, const T* __restrict__ p,
+                                                   const SolverState* S, double t, long long c_beg, long long c_step) {
     T out[MOL_MAX_FIELDS];
     double errsq = 0.0;
     const double abstol = S->abstol, reltol = S->reltol;
     typename G::template Uniform<T> U;
     G::uniform(P, T(t), p, U);
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P.ncell;
-         c += (long long)gridDim.x * blockDim.x) {
+    for (long long c = c_beg; c < P.ncell; c += c_step) {
         int I[3];
         cell_index(P, c, I);
         G::cell(P, y, c, I, T(t), p, U, out);
@@ -584,27 +599,12 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_tsit_stage_t(const
             }
         }
     }
-    if (stage < 7) return;
-    __shared__ double red[kThreads / 32];
-    for (int o = 16; o > 0; o >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = errsq;
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
-        partials[blockIdx.x] = s;
-        __threadfence();
-        const unsigned v = atomicAdd(&S->blocks_done, 1u);
-        last = (v == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!last || threadIdx.x != 0) return;
-    __threadfence();
-    double s = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[b];
-    S->blocks_done = 0;
-    const double N = (double)P.ncell * P.nfields;
+    return errsq;
+}
+
+// The PI step-size controller (OrdinaryDiffEq's for Tsit5) given the error norm's sum of squares
+// over N values; one thread.
+__device__ __forceinline__ void tsit_control(SolverState* S, double s, double N, double qold_pow = -1.0) {
     const double EEst = sqrt(s / N);
     S->EEst = EEst;
     S->nf += 6;
@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_tsit_stage_t(const
     const double dt = S->dt;
     double dtnew;
     if (EEst <= 1.0) {
-        double q = q11 / pow(S->qold, beta2);
+        double q = q11 / (qold_pow >= 0.0 ? qold_pow : pow(S->qold, beta2));
         q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gamma));
         S->t = S->t + dt;
         S->qold = fmax(EEst, qoldinit);
@@ -648,6 +648,136 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_tsit_stage_t(const
     }
     S->dt = dtnew;
     __threadfence();
+}
+
+// Stage i (2..7) over the grid; at stage 7 the last block to finish reduces the error norm
+// deterministically (block order) and runs the controller.
+template <class T, class G>
+__global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_tsit_stage_t(const __grid_constant__ DevProb<T> P, int stage, const T* __restrict__ y,
+                                                           T* ynext, const T* __restrict__ u, T* const* k,
+                                                           const T* __restrict__ p, SolverState* S,
+                                                           double* partials) {
+    if (S->done) return;
+    const double t = S->t + tsit_c(stage) * S->dt;
+    double errsq = tsit_stage_cells<T, G>(P, stage, y, ynext, u, k, p, S, t,
+                                          blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                                          (long long)gridDim.x * blockDim.x);
+    if (stage < 7) return;
+    __shared__ double red[kThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = errsq;
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
+        partials[blockIdx.x] = s;
+        __threadfence();
+        const unsigned v = atomicAdd(&S->blocks_done, 1u);
+        last = (v == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double s = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[b];
+    S->blocks_done = 0;
+    tsit_control(S, s, (double)P.ncell * P.nfields);
+}
+
+// Tsit5 for small problems: one CTA owns the whole state and runs up to `attempts` attempts
+// (stages 2..7, the error norm, the controller and the commit) in one launch, with block
+// barriers between the phases instead of kernel boundaries; the host checks S->done between
+// launches.  With `smem` set (dynamic shared memory of 10 state arrays) the state, the seven
+// stage values and the two stage inputs live in shared memory for the launch, and the solver
+// state is worked on in a shared copy.  For a few hundred unknowns the seven launches of an
+// attempt, and its loads from L2, cost more than its arithmetic.  y2 must be formed before
+// the first launch (k_tsit_commit, first).
+template <class T, class G>
+__global__ void __launch_bounds__(kThreads) k_tsit_small_t(const __grid_constant__ DevProb<T> P, T* u,
+                                                          T* const* k, T* yb0, T* yb1, const T* __restrict__ p,
+                                                          SolverState* S, int attempts, int smem) {
+    extern __shared__ __align__(16) unsigned char tsit_smem[];
+    __shared__ SolverState Ss;
+    __shared__ double red[kThreads / 32];
+    __shared__ double qpow;
+    __shared__ int stop;
+    const long long n = P.ncell * nfields_of<G>(P);
+    T* su = u;
+    T* sy0 = yb0;
+    T* sy1 = yb1;
+    T* sk[7];
+    for (int j = 0; j < 7; ++j) sk[j] = k[j];
+    if (smem) {
+        T* base = (T*)tsit_smem;
+        su = base;
+        sy0 = base + n;
+        sy1 = base + 2 * n;
+        for (int j = 0; j < 7; ++j) sk[j] = base + (3 + j) * n;
+        for (long long g = threadIdx.x; g < n; g += blockDim.x) {
+            su[g] = u[g];
+            sy0[g] = yb0[g];
+            sk[0][g] = k[0][g];
+        }
+    }
+    if (threadIdx.x == 0) Ss = *S;
+    __syncthreads();
+    const double beta2 = 0.08;
+    for (int a = 0; a < attempts; ++a) {
+        if (threadIdx.x == 0) stop = Ss.done;
+        // the controller's pow(qold, beta2) on another warp, off the critical path
+        if (threadIdx.x == 32 || (blockDim.x <= 32 && threadIdx.x == 0)) qpow = pow(Ss.qold, beta2);
+        __syncthreads();
+        if (stop) break;
+        double errsq = 0.0;
+        for (int stage = 2; stage <= 7; ++stage) {
+            const T* yin = (stage % 2 == 0) ? sy0 : sy1;
+            T* yout = (stage % 2 == 0) ? sy1 : sy0;
+            const double t = Ss.t + tsit_c(stage) * Ss.dt;
+            const double e = tsit_stage_cells<T, G>(P, stage, yin, yout, su, sk, p, &Ss, t, threadIdx.x, blockDim.x);
+            if (stage == 7) errsq = e;
+            __syncthreads();
+        }
+        for (int o = 16; o > 0; o >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = errsq;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int w = 0; w < (int)((blockDim.x + 31) / 32); ++w) s += red[w];
+            tsit_control(&Ss, s, (double)n, qpow);
+        }
+        __syncthreads();
+        // commit an accepted step (u <- y7, k1 <- k7) and form y2 = u + dt a21 k1 for the next
+        const bool acc = Ss.accepted, done = Ss.done;
+        const T a21 = T(Ss.dt * 0.161);
+        for (long long g = threadIdx.x; g < n; g += blockDim.x) {
+            T uu, kk;
+            if (acc) {
+                uu = sy1[g];
+                kk = sk[6][g];
+                su[g] = uu;
+                sk[0][g] = kk;
+            } else {
+                uu = su[g];
+                kk = sk[0][g];
+            }
+            if (!done) sy0[g] = fma(a21, kk, uu);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) tsit_scale(&Ss);
+        __syncthreads();
+    }
+    if (smem) {
+        for (long long g = threadIdx.x; g < n; g += blockDim.x) {
+            u[g] = su[g];
+            yb0[g] = sy0[g];
+            k[0][g] = sk[0][g];
+        }
+    }
+    if (threadIdx.x == 0) {
+        *S = Ss;
+        __threadfence();
+    }
 }
 
 }  // namespace mol

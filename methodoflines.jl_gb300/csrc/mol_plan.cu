@@ -132,24 +132,7 @@ static int ensure_slot(mol_plan* plan, int slot) {
 // kernels that do not evaluate the right-hand side (the others are in mol_kernels.cuh)
 // ----------------------------------------------------------------------------
 
-// Row updates of the controller's dt-scaled tableau; one thread.
-__device__ void tsit_scale(SolverState* S) {
-    const double A[8][8] = {
-        {0}, {0},
-        {0, 0.161},
-        {0, -0.008480655492356989, 0.335480655492357},
-        {0, 2.897153057105493, -6.359448489975075, 4.3622954328695815},
-        {0, 5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525},
-        {0, 5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383},
-        {0, 0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081,
-         2.324710524099774}};
-    const double B[8] = {0, -0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
-                         -0.1447110071732629, 0.5823571654525552, -0.45808210592918697, 0.015151515151515152};
-    const double dt = S->dt;
-    for (int i = 0; i < 8; ++i)
-        for (int j = 0; j < 8; ++j) S->dta[i][j] = dt * A[i][j];
-    for (int j = 0; j < 8; ++j) S->dtb[j] = dt * B[j];
-}
+
 
 // After the controller: commit an accepted step (u <- y7, k1 <- k7), rescale the
 // tableau for the new dt and form y2 = u + dt a21 k1 for the next attempt.
@@ -1447,6 +1430,34 @@ int mol_plan_check(mol_plan* plan) {
     return sync_and_check_finite(plan);
 }
 
+}  // extern "C"
+
+namespace {
+
+// End of a Tsit5 solve: statistics, the state back to host memory, the controller's status.
+int tsit_finish(mol_plan* plan, double* u, const double* ud, bool host, const SolverState& hs, mol_stats* stats) {
+    int st;
+    if (stats) {
+        stats->naccept = hs.naccept;
+        stats->nreject = hs.nreject;
+        stats->nf = hs.nf + 1;
+        stats->t = hs.t;
+        stats->dt = hs.dt;
+    }
+    if (host) {
+        if ((st = cuda_check(plan, cudaMemcpyAsync(u, ud, sizeof(double) * (size_t)plan->nunk, cudaMemcpyDeviceToHost,
+                                                   plan->stream), "D2H")))
+            return st;
+        if ((st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync"))) return st;
+    }
+    if (hs.status) return set_err(plan, hs.status, "tsit5 stopped early");
+    return MOL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, double t1, double abstol, double reltol,
                     double dt0, int64_t maxiters, mol_stats* stats) {
     if (!plan || !u || !std::isfinite(t0) || !std::isfinite(t1) || !(t1 >= t0) || !(abstol > 0) ||
@@ -1514,6 +1525,29 @@ int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, doubl
     ++g_launches;
     k_tsit_commit<double><<<nb, kThreads, 0, plan->stream>>>(plan->P64, ud, k1, k7, yb1, yb0, plan->d_state, 1);
     ++g_launches;
+    // Small problems: one CTA runs whole attempts (k_tsit_small_t), kSmallAttempts per launch,
+    // instead of seven launches per attempt.  Measured threshold: below about a thousand
+    // unknowns an attempt's launches cost more than its arithmetic on one SM.
+    constexpr long long kSmallTsit = 1024;
+    constexpr long long kSmallTsitShared = 512;   // 10 arrays of 8 bytes in 40 KB of shared memory
+    constexpr int kSmallAttempts = 256;
+    if (plan->use_jit && plan->jit.tsitsmall64 && n <= kSmallTsit && !getenv("MOL_TSIT_NO_SMALL")) {
+        SolverState hs;
+        const int smem = n <= kSmallTsitShared ? 1 : 0;
+        const size_t bytes = smem ? sizeof(double) * 10 * (size_t)n : 0;
+        for (;;) {
+            if ((st = cuda_check(plan, launch_ks(plan->jit.tsitsmall64, 1, kThreads, bytes, plan->stream, plan->P64,
+                                                 ud, (double* const*)d_k, yb0, yb1, pp, plan->d_state,
+                                                 kSmallAttempts, smem),
+                                 "tsit5 small launch")))
+                return st;
+            ++g_launches;
+            cudaMemcpyAsync(&hs, plan->d_state, sizeof(SolverState), cudaMemcpyDeviceToHost, plan->stream);
+            if ((st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "tsit5 sync"))) return st;
+            if (hs.done) break;
+        }
+        return tsit_finish(plan, u, ud, host, hs, stats);
+    }
     // one attempt = stages 2..7 + commit; M attempts per captured graph
     auto attempt = [&]() {
         for (int s = 2; s <= 7; ++s) {
@@ -1557,21 +1591,7 @@ int mol_solve_tsit5(mol_plan* plan, double* u, const double* p, double t0, doubl
     }
     if (gx) cudaGraphExecDestroy(gx);
     if (st) return st;
-    if (stats) {
-        stats->naccept = hs.naccept;
-        stats->nreject = hs.nreject;
-        stats->nf = hs.nf + 1;
-        stats->t = hs.t;
-        stats->dt = hs.dt;
-    }
-    if (host) {
-        if ((st = cuda_check(plan, cudaMemcpyAsync(u, ud, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost,
-                                                   plan->stream), "D2H")))
-            return st;
-        if ((st = cuda_check(plan, cudaStreamSynchronize(plan->stream), "sync"))) return st;
-    }
-    if (hs.status) return set_err(plan, hs.status, "tsit5 stopped early");
-    return MOL_OK;
+    return tsit_finish(plan, u, ud, host, hs, stats);
 }
 
 }  // extern "C"

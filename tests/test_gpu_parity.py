@@ -272,3 +272,18 @@ def test_readme_example_heat_equation(gpu_lib):
     assert np.max(np.abs(sol.u - exact)) < 1e-3 * np.max(np.abs(exact))
     assert sol[u].shape == (6, 101) and np.array_equal(sol[u][-1, 1:-1], sol.u)
     assert np.array_equal(sol[x], np.arange(101) * 0.01) or np.allclose(sol[x], np.arange(101) * 0.01, atol=1e-15)
+
+
+def test_tsit5_small_problem_one_cta_matches_launch_per_stage(gpu_lib, monkeypatch):
+    """Problems of at most 1024 unknowns run whole Tsit5 attempts in one CTA; the same solve
+    through the launch-per-stage path takes the same steps (the error norm is summed in a
+    different order, so accept/reject decisions may differ at the margin) to the same result."""
+    plan, orc, lw, _ = _setup("heat1d", n=101)
+    a = lw.u0.copy()
+    sa = plan.solve_tsit5(a, 0.0, 0.1, 1e-10, 1e-10)
+    monkeypatch.setenv("MOL_TSIT_NO_SMALL", "1")
+    b = lw.u0.copy()
+    sb = plan.solve_tsit5(b, 0.0, 0.1, 1e-10, 1e-10)
+    assert abs(sa["naccept"] - sb["naccept"]) <= 2 and abs(sa["t"] - 0.1) < 1e-15
+    assert _rel(a, b) < 1e-12
+    plan.close()
