@@ -59,3 +59,44 @@ def test_both_forms_compile_for_sm103a(flags):
     _, D = _source("adr3d", dict(N=6, nz_pts=8), flags)
     log = C.create_string_buffer(1 << 16)
     assert L.lib().mol_codegen_compile_check(C.byref(D.desc), log, 1 << 16) == 0, log.value.decode()
+
+
+def _source_of(sys_disc, flags=0):
+    sys_, disc, _ = sys_disc
+    D = Descriptor(lower(sys_.to_spec(disc)))
+    D.desc.flags = flags
+    need = C.c_int64()
+    assert L.lib().mol_generate_code(C.byref(D.desc), None, 0, C.byref(need)) == 0
+    buf = C.create_string_buffer(need.value)
+    assert L.lib().mol_generate_code(C.byref(D.desc), buf, need.value, C.byref(need)) == 0
+    return buf.value.decode()
+
+
+def test_two_field_system_groups():
+    """One group per output field; the parameter-scaled diffusivity (its face program reads a
+    parameter) stays outside its field's group on its own statements."""
+    diff = _source_of(problems.coefficient_system(12))
+    exp = _source_of(problems.coefficient_system(12), L.MOL_FLAG_EXPAND_STENCILS)
+    assert "kCoefArrays = 6;" in diff and "kCoefArrays = 8;" in exp
+    for src in (diff, exp):
+        cell = _cell(src)
+        assert cell.count("if (P.cw && ") == 2
+        assert "P.cw + (long long)0 * P.ncell" in cell and "P.cw + (long long)" in cell
+        # the parameter-scaled term (term 1) is evaluated in the cell's main flow
+        before_group = cell[:cell.index("if (P.cw && ")]
+        assert "gt1<T>(" in before_group
+
+
+def test_reaction_joins_the_centre_only_in_expanded_form():
+    diff = _cell(_source("adr3d", dict(N=6, nz_pts=8))[0])
+    exp = _cell(_source("adr3d", dict(N=6, nz_pts=8), L.MOL_FLAG_EXPAND_STENCILS)[0])
+    assert "fma(fma(-U." not in diff and "v20" in diff.split("if (P.cw")[0]
+    assert "fma(fma(-U." in exp
+
+
+def test_coefficient_stencils_off(monkeypatch):
+    """MOL_JIT_CFOLD=0 turns the stencil groups off: the terms' own statements (and the face
+    pass) serve every cell."""
+    monkeypatch.setenv("MOL_JIT_CFOLD", "0")
+    src, _ = _source("adr3d", dict(N=6, nz_pts=8))
+    assert "kCoefArrays = 0;" in src and "P.cw &&" not in src
