@@ -132,8 +132,6 @@ static int ensure_slot(mol_plan* plan, int slot) {
 // kernels that do not evaluate the right-hand side (the others are in mol_kernels.cuh)
 // ----------------------------------------------------------------------------
 
-
-
 // After the controller: commit an accepted step (u <- y7, k1 <- k7), rescale the
 // tableau for the new dt and form y2 = u + dt a21 k1 for the next attempt.
 template <class T>
