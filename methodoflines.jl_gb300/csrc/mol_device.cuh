@@ -674,13 +674,16 @@ __device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps
         // FP64 issue is the bound: beta_1 and beta_3 take their second square as (b/2)^2 with b/2
         // formed directly (1.5 u - 2 u' + 0.5 u''), bit for bit 0.25 b^2 since scaling by 1/2
         // commutes with rounding; the ideal weights (0.1, 0.6, 0.3) ride on the candidate
-        // reconstructions' coefficients instead of six products with the P_k
-        const T a1 = u0 - T(2) * up1 + up2, h1 = T(1.5) * u0 - T(2) * up1 + T(0.5) * up2;
-        const T a2 = um1 - T(2) * u0 + up1, b2 = um1 - up1;
-        const T a3 = um2 - T(2) * um1 + u0, h3 = T(0.5) * um2 - T(2) * um1 + T(1.5) * u0;
-        const T e1 = eps + fma(c13_12 * a1, a1, h1 * h1);
-        const T e2 = eps + fma(c13_12 * a2, a2, T(0.25) * (b2 * b2));
-        const T e3 = eps + fma(c13_12 * a3, a3, h3 * h3);
+        // reconstructions' coefficients instead of six products with the P_k.  u - 2 u' is an
+        // explicit FMA (2 u' is exact: the same rounded difference; x + x would not contract),
+        // and eps enters through the FMA of the second square instead of a separate addition
+        // (eps + beta_k rounded in another order: one instruction fewer per indicator)
+        const T a1 = fma(T(-2), up1, u0) + up2, h1 = T(1.5) * u0 - T(2) * up1 + T(0.5) * up2;
+        const T a2 = fma(T(-2), u0, um1) + up1, b2 = um1 - up1;
+        const T a3 = fma(T(-2), um1, um2) + u0, h3 = T(0.5) * um2 - T(2) * um1 + T(1.5) * u0;
+        const T e1 = fma(c13_12 * a1, a1, fma(h1, h1, eps));
+        const T e2 = fma(c13_12 * a2, a2, fma(T(0.25) * b2, b2, eps));
+        const T e3 = fma(c13_12 * a3, a3, fma(h3, h3, eps));
         const T s1 = e1 * e1, s2 = e2 * e2, s3 = e3 * e3;
         const T P1 = s2 * s3, P2 = s1 * s3, P3 = s1 * s2;   // P_k = prod_{j != k} (eps + beta_j)^2
         // gamma_k times the candidates (scaled by 6, the 1/6 folded into inv_dx below)
@@ -694,9 +697,9 @@ __device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps
         const T Nm = fma(P1, gm1, fma(P2, gm2, P3 * gm3)), Dm = fma(T(0.1), P1, fma(T(0.6), P2, T(0.3) * P3));
         return fma(Np, Dm, -Nm * Dp) / (Dp * Dm) * (inv_dx * T(1.0 / 6.0));
     }
-    const T a1 = u0 - T(2) * up1 + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
-    const T a2 = um1 - T(2) * u0 + up1, b2 = um1 - up1;
-    const T a3 = um2 - T(2) * um1 + u0, b3 = um2 - T(4) * um1 + T(3) * u0;
+    const T a1 = fma(T(-2), up1, u0) + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
+    const T a2 = fma(T(-2), u0, um1) + up1, b2 = um1 - up1;
+    const T a3 = fma(T(-2), um1, um2) + u0, b3 = um2 - T(4) * um1 + T(3) * u0;
     const T e1 = eps + fma(c13_12 * a1, a1, T(0.25) * (b1 * b1));
     const T e2 = eps + fma(c13_12 * a2, a2, T(0.25) * (b2 * b2));
     const T e3 = eps + fma(c13_12 * a3, a3, T(0.25) * (b3 * b3));

@@ -358,19 +358,22 @@ __device__ __forceinline__ void scatter_taps_wrap(T* base, long long c, int i, i
 template <class T>
 __device__ __forceinline__ T weno5_valgrad(T um2, T um1, T u0, T up1, T up2, T eps, T inv_dx, T gr[5]) {
     const T c13_12 = T(13) / T(12);
-    const T a1 = u0 - T(2) * up1 + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
-    const T a2 = um1 - T(2) * u0 + up1, b2 = um1 - up1;
-    const T a3 = um2 - T(2) * um1 + u0, b3 = um2 - T(4) * um1 + T(3) * u0;
-    const T e1 = eps + fma(c13_12 * a1, a1, T(0.25) * (b1 * b1));
-    const T e2 = eps + fma(c13_12 * a2, a2, T(0.25) * (b2 * b2));
-    const T e3 = eps + fma(c13_12 * a3, a3, T(0.25) * (b3 * b3));
+    // products with 2 that join a sum are explicit FMAs (2 x is exact: the same rounded sums;
+    // 2 x may be rewritten as x + x, which then does not contract)
+    const T a1 = fma(T(-2), up1, u0) + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
+    const T a2 = fma(T(-2), u0, um1) + up1, b2 = um1 - up1;
+    const T a3 = fma(T(-2), um1, um2) + u0, b3 = um2 - T(4) * um1 + T(3) * u0;
+    // eps + beta_k with eps inside the FMA of the second square (0.25 b is exact)
+    const T e1 = fma(c13_12 * a1, a1, fma(T(0.25) * b1, b1, eps));
+    const T e2 = fma(c13_12 * a2, a2, fma(T(0.25) * b2, b2, eps));
+    const T e3 = fma(c13_12 * a3, a3, fma(T(0.25) * b3, b3, eps));
     // candidate reconstructions scaled by 6 (1/6 folded into c below)
-    const T hm1 = T(11) * u0 - T(7) * up1 + T(2) * up2;
-    const T hm2 = T(5) * u0 - up1 + T(2) * um1;
+    const T hm1 = fma(T(2), up2, T(11) * u0 - T(7) * up1);
+    const T hm2 = fma(T(2), um1, T(5) * u0 - up1);
     const T hm3 = T(2) * u0 + T(5) * um1 - um2;
     const T hp1 = T(2) * u0 + T(5) * up1 - up2;
     const T hp2 = T(5) * u0 + T(2) * up1 - um1;
-    const T hp3 = T(11) * u0 - T(7) * um1 + T(2) * um2;
+    const T hp3 = fma(T(2), um2, T(11) * u0 - T(7) * um1);
     const T c = inv_dx * T(1.0 / 6.0);
     T gwp1, gwp2, gwp3, gwm1, gwm2, gwm3, ghp1, ghp2, ghp3, ghm1, ghm2, ghm3, ge1, ge2, ge3, val;
     if (sizeof(T) == 8) {
@@ -416,16 +419,19 @@ __device__ __forceinline__ T weno5_valgrad(T um2, T um1, T u0, T up1, T up2, T e
         const T gq3 = T(0.3) * gwm3 + T(0.1) * gwp3;
         ge1 = -T(2) * q1 / e1 * gq1; ge2 = -T(2) * q2 / e2 * gq2; ge3 = -T(2) * q3 / e3 * gq3;
     }
-    const T ga1 = ge1 * T(2) * c13_12 * a1, gb1 = ge1 * T(0.5) * b1;
-    const T ga2 = ge2 * T(2) * c13_12 * a2, gb2 = ge2 * T(0.5) * b2;
-    const T ga3 = ge3 * T(2) * c13_12 * a3, gb3 = ge3 * T(0.5) * b3;
+    // (ge 2) c13_12 = ge (2 c13_12): doubling is exact, one product fewer
+    const T c13_6 = T(2) * c13_12;
+    const T ga1 = ge1 * c13_6 * a1, gb1 = ge1 * T(0.5) * b1;
+    const T ga2 = ge2 * c13_6 * a2, gb2 = ge2 * T(0.5) * b2;
+    const T ga3 = ge3 * c13_6 * a3, gb3 = ge3 * T(0.5) * b3;
     // linear maps to (um2, um1, u0, up1, up2); the h's are unscaled here
-    gr[0] = ga3 + gb3 - ghm3 + T(2) * ghp3;
-    gr[1] = ga2 + gb2 - T(2) * ga3 - T(4) * gb3 + T(2) * ghm2 + T(5) * ghm3 - ghp2 - T(7) * ghp3;
-    gr[2] = ga1 + T(3) * gb1 - T(2) * ga2 + ga3 + T(3) * gb3 + T(11) * ghm1 + T(5) * ghm2 + T(2) * ghm3 +
-            T(2) * ghp1 + T(5) * ghp2 + T(11) * ghp3;
-    gr[3] = -T(2) * ga1 - T(4) * gb1 + ga2 - gb2 - T(7) * ghm1 - ghm2 + T(5) * ghp1 + T(2) * ghp2;
-    gr[4] = ga1 + gb1 + T(2) * ghm1 - ghp1;
+    gr[0] = fma(T(2), ghp3, ga3 + gb3 - ghm3);
+    gr[1] = fma(T(2), ghm2, fma(T(-2), ga3, ga2 + gb2) - T(4) * gb3) + T(5) * ghm3 - ghp2 - T(7) * ghp3;
+    gr[2] = fma(T(2), ghp1, fma(T(2), ghm3, fma(T(-2), ga2, ga1 + T(3) * gb1) + ga3 + T(3) * gb3 + T(11) * ghm1 +
+                                                T(5) * ghm2)) +
+            T(5) * ghp2 + T(11) * ghp3;
+    gr[3] = fma(T(2), ghp2, -T(2) * ga1 - T(4) * gb1 + ga2 - gb2 - T(7) * ghm1 - ghm2 + T(5) * ghp1);
+    gr[4] = fma(T(2), ghm1, ga1 + gb1) - ghp1;
     return val;
 }
 
