@@ -674,10 +674,10 @@ __device__ __forceinline__ T weno5_point(T um2, T um1, T u0, T up1, T up2, T eps
         // FP64 issue is the bound: beta_1 and beta_3 take their second square as (b/2)^2 with b/2
         // formed directly (1.5 u - 2 u' + 0.5 u''), bit for bit 0.25 b^2 since scaling by 1/2
         // commutes with rounding; the ideal weights (0.1, 0.6, 0.3) ride on the candidate
-        // reconstructions' coefficients instead of six products with the P_k.  u - 2 u' is an
-        // explicit FMA (2 u' is exact: the same rounded difference; x + x would not contract),
-        // and eps enters through the FMA of the second square instead of a separate addition
-        // (eps + beta_k rounded in another order: one instruction fewer per indicator)
+        // reconstructions' coefficients instead of six products with the P_k.  u - 2 u' is
+        // fma(-2, u', u) (2 u' is exact: the same rounded difference), and eps enters through
+        // the FMA of the second square instead of a separate addition (eps + beta_k rounded in
+        // another order: one instruction fewer per indicator)
         const T a1 = fma(T(-2), up1, u0) + up2, h1 = T(1.5) * u0 - T(2) * up1 + T(0.5) * up2;
         const T a2 = fma(T(-2), u0, um1) + up1, b2 = um1 - up1;
         const T a3 = fma(T(-2), um1, um2) + u0, h3 = T(0.5) * um2 - T(2) * um1 + T(1.5) * u0;

@@ -150,9 +150,8 @@ __global__ void __launch_bounds__(kThreads) k_coef_t(const __grid_constant__ Dev
 
 // SSPRK33 stage epilogue with OrdinaryDiffEq's evaluation order:
 //   1: u1 = u0 + dt k     2: u2 = (3 u0 + u1 + dt k)/4     3: u = (u0 + 2 u2 + 2 dt k)/3
-// u0 + 2 u2 is an explicit FMA: 2 x may be rewritten as x + x, which then does not contract
-// with the sum; 2 x is exact, so fma(2, u2, u0) is the same correctly rounded sum in one
-// instruction.
+// u0 + 2 u2 is written as fma(2, u2, u0): 2 u2 is exact, so it is the same correctly rounded
+// sum, in one instruction whatever the compiler's contraction choices.
 template <class T, int STAGE>
 __device__ __forceinline__ T ssprk_combine(T u0, T uin, T k, T dt, T dt2) {
     if (STAGE == 1) return u0 + dt * k;

@@ -358,8 +358,7 @@ __device__ __forceinline__ void scatter_taps_wrap(T* base, long long c, int i, i
 template <class T>
 __device__ __forceinline__ T weno5_valgrad(T um2, T um1, T u0, T up1, T up2, T eps, T inv_dx, T gr[5]) {
     const T c13_12 = T(13) / T(12);
-    // products with 2 that join a sum are explicit FMAs (2 x is exact: the same rounded sums;
-    // 2 x may be rewritten as x + x, which then does not contract)
+    // products with 2 that join a sum are written as FMAs (2 x is exact: the same rounded sums)
     const T a1 = fma(T(-2), up1, u0) + up2, b1 = T(3) * u0 - T(4) * up1 + up2;
     const T a2 = fma(T(-2), u0, um1) + up1, b2 = um1 - up1;
     const T a3 = fma(T(-2), um1, um2) + u0, b3 = um2 - T(4) * um1 + T(3) * u0;
