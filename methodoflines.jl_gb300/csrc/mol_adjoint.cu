@@ -152,7 +152,7 @@ struct Adj {
         const DevProb<double> P = with_faces<double>(plan, cu, p, toff, t, &e);
         if (e == cudaSuccess)
             e = launch_k(plan->jit.ssp64[which - 1], plan->nblocks, plan->nthreads, plan->stream, P, cu, u0, uout, p,
-                         plan->d_state, dt, t, 0ll, (long long)plan->ncell);
+                         plan->d_state, which == 3 ? 2 * dt : dt, t, 0ll, (long long)plan->ncell);
         ++g_launches;
         ck(e, "stage launch");
         counted();

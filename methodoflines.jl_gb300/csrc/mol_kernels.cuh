@@ -175,11 +175,14 @@ __device__ __forceinline__ void last_block_advance(SolverState* S, double t_new)
 // `tfix` (when not NaN) is the step's start time, used instead of S->t and leaving S alone:
 // the adjoint recomputes single stages at known times without touching the solver state.
 // Cells [cbeg, cend) are processed (stage 1 runs in slabs while the state arrives from the
-// host; every other launch covers all cells).
+// host; every other launch covers all cells).  Stages 1 and 2 take the step in `dts`, stage 3
+// takes 2 dt, the coefficient of its combination, so that the cell loop reads it from the
+// kernel's parameters instead of forming 2 dt again per cell.
 template <class T, class G, int STAGE>
 __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_ssprk_t(const __grid_constant__ DevProb<T> P, const T* __restrict__ uin, const T* u0, T* uout,
-                                                      const T* __restrict__ p, SolverState* S, double dt,
+                                                      const T* __restrict__ p, SolverState* S, double dts,
                                                       double tfix, long long cbeg, long long cend) {
+    const double dt = STAGE == 3 ? 0.5 * dts : dts;
     const bool from_state = !(tfix == tfix);
     const double t0 = from_state ? S->t : tfix;
     const double ts = STAGE == 1 ? t0 : (STAGE == 2 ? t0 + dt : t0 + dt / 2);
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(kThreads, MOL_MIN_BLOCKS) k_ssprk_t(const __gr
         #pragma unroll
         for (int f = 0; f < nfields_of<G>(P); ++f) {
             const long long g = (long long)f * P.ncell + c;
-            const T r = ssprk_combine<T, STAGE>(u0[g], uin[g], out[f], T(dt), T(2 * dt));
+            const T r = ssprk_combine<T, STAGE>(u0[g], uin[g], out[f], T(dt), T(dts));
             if (STAGE == 3) bad |= nonfinite_bits(r);
             uout[g] = r;
         }

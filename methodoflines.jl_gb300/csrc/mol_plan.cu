@@ -384,7 +384,7 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
                          c0, c1);
         if (e == cudaSuccess) Pf = with_faces<T>(plan, cu2, p, dt / 2, nan, &e);
         if (e == cudaSuccess)
-            e = launch_k(k[2], nb, nt, plan->stream, Pf, cu2, cu, uout, p, plan->d_state, dt, nan,
+            e = launch_k(k[2], nb, nt, plan->stream, Pf, cu2, cu, uout, p, plan->d_state, 2 * dt, nan,
                          c0, c1);
         return cuda_check(plan, e, "ssprk launch");
     }
@@ -395,8 +395,8 @@ int launch_ssprk_step_io(mol_plan* plan, const T* uin, T* uout, T* u1, T* u2, co
                                                                                    0ll, c1);
     k_ssprk_t<T, InterpCell, 2><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u1, u, u2, p, plan->d_state, dt, nan,
                                                                                0ll, c1);
-    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, uout, p, plan->d_state, dt, nan,
-                                                                               0ll, c1);
+    k_ssprk_t<T, InterpCell, 3><<<plan->nblocks, kThreads, 0, plan->stream>>>(P, u2, u, uout, p, plan->d_state, 2 * dt,
+                                                                               nan, 0ll, c1);
     return cuda_check(plan, cudaGetLastError(), "k_ssprk launch");
 }
 
