@@ -149,3 +149,46 @@ def test_06_time_dependent_robin_order_6():
     sys_, x, t = _system(bcs, -1.0, 1.0)
     orc = OracleProblem(sys_.to_spec(MOLFiniteDifference({x: 0.01}, t, approx_order=6)))
     _check(orc, _implicit(orc, 1e-6), lambda xs, s: math.exp(-s) * np.sin(xs), 0.06)
+
+
+def _nonlinear(coef, exact, order=2, dirichlet=True, deriv=None):
+    """u_t = Dx(a(u) Dx(u)) on [0, 2], dx = 0.01, data from the exact solution (Dirichlet, or
+    Neumann with its derivative), integrated implicitly to t = 2 (the reference uses
+    Rosenbrock32); returns the oracle's sol[u] at t = 2 and the exact values on the grid."""
+    x, t = IV("x"), IV("t")
+    u = Field("u")
+    Dx = Differential(x)
+    U = u(x, t)
+    eq = Eq(Differential(t)(U), Dx(coef(U) * Dx(U)))
+    if dirichlet:
+        bcs = [Eq(u(x, 0.0), exact(0.0, x)), Eq(u(0.0, t), exact(t, 0.0)), Eq(u(2.0, t), exact(t, 2.0))]
+    else:
+        bcs = [Eq(u(x, 0.0), exact(0.0, x)), Eq(Dx(u(0.0, t)), deriv(0.0)), Eq(Dx(u(2.0, t)), deriv(2.0))]
+    sys_ = PDESystem([eq], bcs, [(t, Interval(0.0, 2.0)), (x, Interval(0.0, 2.0))], [t, x], [U], [])
+    orc = OracleProblem(sys_.to_spec(MOLFiniteDifference({x: 0.01}, t, approx_order=order)))
+    integ = pytest.importorskip("scipy.integrate")
+    sparse = pytest.importorskip("scipy.sparse")
+    n = orc.n_unknowns
+    band = sparse.diags([np.ones(n - abs(k)) for k in range(-12, 13)], list(range(-12, 13)), shape=(n, n))
+    r = integ.solve_ivp(lambda s, v: orc.rhs(v, s), (0.0, 2.0), orc.initial_condition(), method="Radau",
+                        t_eval=[2.0], rtol=1e-6, atol=1e-8, jac_sparsity=band)
+    assert r.success
+    got = orc.solution_arrays(r.y[:, -1], 2.0, orc.param_values)["u"]
+    xs = orc.grid[0]
+    return got, np.array([exact(2.0, float(v)) for v in xs])
+
+
+def test_nonlinear_00_inverse_coefficient():
+    """Nonlinear_Diffusion/MOL_1D_NonLinear_Diffusion.jl:12-69: a(u) = u^-1, exact
+    2 (1 + t) / (1 + x)^2, Dirichlet; the reference's isapprox on the arrays at t = 2 (2-norm of
+    the difference within atol 0.1)."""
+    got, want = _nonlinear(lambda U: U ** (-1), lambda t, x: 2.0 * (1.0 + t) / (1.0 + x) ** 2)
+    assert np.linalg.norm(got - want) <= 0.1
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_nonlinear_01_square_coefficient(order):
+    """MOL_1D_NonLinear_Diffusion.jl:127-254 (Tests 01a and 01b): a(u) = u^2, exact
+    0.5 (x + 0.5) / sqrt(50 - t), Dirichlet, approx_order 2 and 4; 2-norm within 0.1 at t = 2."""
+    got, want = _nonlinear(lambda U: U ** 2, lambda t, x: 0.5 * (x + 0.5) / (50.0 - t) ** 0.5, order=order)
+    assert np.linalg.norm(got - want) <= 0.1
