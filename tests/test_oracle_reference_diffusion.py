@@ -192,3 +192,47 @@ def test_nonlinear_01_square_coefficient(order):
     0.5 (x + 0.5) / sqrt(50 - t), Dirichlet, approx_order 2 and 4; 2-norm within 0.1 at t = 2."""
     got, want = _nonlinear(lambda U: U ** 2, lambda t, x: 0.5 * (x + 0.5) / (50.0 - t) ** 0.5, order=order)
     assert np.linalg.norm(got - want) <= 0.1
+
+
+def _two_d(rhs_of, order):
+    """2-D/MOL_2D_Diffusion.jl: u on [0, 2]^2, dx = 0.1, dy = 0.2, Dirichlet data from
+    exp(x + y) cos(x + y + 4t) on every side; sol[u] at t = 2 by an implicit solve through the
+    oracle's right-hand side, and the exact values with the corners set to 0 as the test does."""
+    x, y, t = IV("x"), IV("y"), IV("t")
+    u = Field("u")
+    U = u(x, y, t)
+    ex = lambda T, X, Y: exp(X + Y) * cos(X + Y + 4.0 * T)
+    bcs = [Eq(u(x, y, 0.0), ex(0.0, x, y)), Eq(u(0.0, y, t), ex(t, 0.0, y)), Eq(u(2.0, y, t), ex(t, 2.0, y)),
+           Eq(u(x, 0.0, t), ex(t, x, 0.0)), Eq(u(x, 2.0, t), ex(t, x, 2.0))]
+    sys_ = PDESystem([Eq(Differential(t)(U), rhs_of(U, x, y, t))], bcs,
+                     [(t, Interval(0.0, 2.0)), (x, Interval(0.0, 2.0)), (y, Interval(0.0, 2.0))], [t, x, y], [U], [])
+    orc = OracleProblem(sys_.to_spec(MOLFiniteDifference({x: 0.1, y: 0.2}, t, approx_order=order)))
+    integ = pytest.importorskip("scipy.integrate")
+    r = integ.solve_ivp(lambda s, v: orc.rhs(v, s), (0.0, 2.0), orc.initial_condition(), method="Radau",
+                        t_eval=[2.0], rtol=1e-6, atol=1e-8)
+    assert r.success
+    got = orc.solution_arrays(r.y[:, -1], 2.0, orc.param_values)["u"]
+    X, Y = np.meshgrid(orc.grid[0], orc.grid[1], indexing="ij")
+    want = np.exp(X + Y) * np.cos(X + Y + 8.0)
+    want[0, 0] = want[0, -1] = want[-1, 0] = want[-1, -1] = 0.0
+    assert got.shape == want.shape
+    return got, want
+
+
+def test_2d_00_heat_order_4():
+    """MOL_2D_Diffusion.jl:8-73: u_t = u_xx + u_yy, approx_order 4; 2-norm of the difference
+    at t = 2 within 0.4."""
+    got, want = _two_d(lambda U, x, y, t: (Differential(x) ** 2)(U) + (Differential(y) ** 2)(U), 4)
+    assert np.linalg.norm(got - want) <= 0.4
+
+
+def test_2d_01_nonlinear_coefficient_of_coordinates_time_and_state():
+    """MOL_2D_Diffusion.jl:75-149: a(x, y, t, u) = (u^2 / exp(x + y)^2 + sin(x + y + 4t)^2)^0.5
+    (1 on the exact solution) in both nonlinear Laplacians; both sides scaled by the exact
+    maximum, 2-norm within 0.4."""
+    def rhs(U, x, y, t):
+        a = (U ** 2 / exp(x + y) ** 2 + sin(x + y + 4.0 * t) ** 2) ** 0.5
+        return Differential(x)(a * Differential(x)(U)) + Differential(y)(a * Differential(y)(U))
+    got, want = _two_d(rhs, 2)
+    m = np.max(want)
+    assert np.linalg.norm(want / m - got / m) <= 0.4
