@@ -136,3 +136,45 @@ def test_julia_shim_structs_match_the_ctypes_layout():
         assert offs == [getattr(S, f).offset for f, _ in S._fields_], jname
         kinds = [_julia_kind(ty) for _, ty in structs[jname]]
         assert kinds == [_ctypes_kind(t) for _, t in S._fields_], (jname, kinds)
+
+
+def _jl_class(ty):
+    ty = ty.strip()
+    if ty in ("Cint", "Int32"):
+        return "i32"
+    if ty == "Int64":
+        return "i64"
+    if ty == "Float64":
+        return "f64"
+    if ty == "Cstring" or ty.startswith(("Ptr{", "Ref{")):
+        return "ptr"
+    raise AssertionError(f"unmapped Julia type {ty}")
+
+
+def _ct_class(t):
+    if t in (C.c_int, C.c_int32):
+        return "i32"
+    if t == C.c_int64:
+        return "i64"
+    if t == C.c_double:
+        return "f64"
+    if t in (C.c_void_p, C.c_char_p) or hasattr(t, "contents"):
+        return "ptr"
+    raise AssertionError(f"unmapped ctypes type {t}")
+
+
+def test_julia_shim_ccalls_match_the_prototypes():
+    """Every ccall of the Julia shim names an exported entry point with the return type and the
+    argument types (32/64-bit integer, double, pointer) of its prototype."""
+    import re
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = text[text.index("```julia"):]
+    block = block[:block.index("\n```\n")]
+    calls = re.findall(r"ccall\(\(:(\w+),\s*lib\),\s*(\w+),\s*\((.*?)\),", block, re.S)
+    assert len(calls) >= 10
+    for name, ret, args in calls:
+        assert name in L._PROTOS, name
+        cret, cargs = L._PROTOS[name]
+        types = [a for a in (s.strip() for s in args.split(",")) if a]
+        assert _jl_class(ret) == _ct_class(cret), (name, ret)
+        assert [_jl_class(a) for a in types] == [_ct_class(a) for a in cargs], (name, types)
