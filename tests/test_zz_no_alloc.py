@@ -80,6 +80,44 @@ def test_noalloc_nonlinear_laplacian(gpu_lib, face_buffer_first):
     b.close()
 
 
+def test_noalloc_allocates_nothing_and_replays_from_a_cuda_graph(gpu_lib):
+    """After one warm-up call (the scratch address lookup) the allocation-free steps leave the
+    device's free memory unchanged, and they capture into a CUDA graph on the plan's stream:
+    two replays (each restarting at t0) give what two mol_step_ssprk33 calls give."""
+    torch = _torch()
+    sys_, disc, ex = problems.brusselator(N=64)
+    lw = lower(sys_.to_spec(disc))
+    dt = ex["dt_ssprk"]
+    s = torch.cuda.Stream()
+    a = Plan(lw)
+    a.set_stream(s.cuda_stream)
+    b = Plan(lw)
+    ua = torch.tensor(lw.u0, device="cuda")
+    ub = torch.tensor(lw.u0, device="cuda")
+    u0 = torch.tensor(lw.u0, device="cuda")
+    a.step_ssprk33_noalloc(ua, dt, 1)                     # warm-up
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    a.step_ssprk33_noalloc(ua, dt, 3, t0=dt)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    ua.copy_(u0)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+        a.step_ssprk33_noalloc(ua, dt, 4, t0=0.0)
+    for _ in range(2):
+        g.replay()
+        b.step_ssprk33(ub, dt, 4, t0=0.0)
+    torch.cuda.synchronize()
+    x, y = ua.cpu().numpy(), ub.cpu().numpy()
+    assert np.linalg.norm(x - y) <= TOL * np.linalg.norm(y)
+    assert np.linalg.norm(x - lw.u0) > 0
+    del g
+    a.close()
+    b.close()
+
+
 def test_noalloc_rejects_oversized_and_host_arrays(gpu_lib):
     torch = _torch()
     sys_, disc, ex = problems.brusselator(N=1024)       # 2,097,152 unknowns > 2^20
