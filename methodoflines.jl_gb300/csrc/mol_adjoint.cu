@@ -22,7 +22,7 @@
 // C alternates between two buffers so the launch accumulating the new C never
 // shares a buffer with the one it folds.
 // States between checkpoints are recomputed; checkpoint positions follow the
-// binomial (revolve) schedule of Griewank & Walther for `nsnap` slots.
+// binomial (revolve) schedule of Griewank & Walther for `nsnap` slots (mol_schedule.h).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,6 +32,7 @@
 
 #include "mol_kernels.cuh"
 #include "mol_plan.h"
+#include "mol_schedule.h"
 
 namespace mol {
 
@@ -279,15 +280,6 @@ struct Adj {
         ck(cudaGetLastError(), "adjoint combine");
     }
 
-    static double beta(int s, int t) {  // C(s + t, t), saturating
-        double b = 1.0;
-        for (int i = 1; i <= t; ++i) {
-            b = b * (s + i) / i;
-            if (b > 1e18) return 1e18;
-        }
-        return b;
-    }
-
     // Reverse steps [l, r) with the state u_l in slot `sl`; `free` are spare slots.
     void rev(int64_t l, int64_t r, double* sl, std::vector<double*>& free) {
         if (err || r <= l) return;
@@ -306,13 +298,7 @@ struct Adj {
             }
             return;
         }
-        const int s = (int)free.size();
-        const int64_t nn = r - l;
-        int t = 1;
-        while (beta(s, t) < (double)nn) ++t;
-        int64_t left = (int64_t)std::min<double>(beta(s, t - 1), (double)(nn - 1));
-        left = std::max<int64_t>(1, left);
-        const int64_t m = l + left;
+        const int64_t m = l + checkpoint_split(r - l, (int)free.size());
         double* sm = free.back();
         free.pop_back();
         advance(sl, sm, l, m - l);
