@@ -298,6 +298,20 @@ struct Adj {
             }
             return;
         }
+        if ((int64_t)free.size() >= r - l - 1) {
+            // every state of [l, r) has a slot: store them walking forward and reverse walking
+            // back (the recursion would peel one step per level, as deep as the horizon)
+            std::vector<double*> st(1, sl);
+            for (int64_t k = l + 1; k < r && !err; ++k) {
+                double* q = free.back();
+                free.pop_back();
+                advance(st.back(), q, k - 1, 1);
+                st.push_back(q);
+            }
+            for (int64_t m = r - 1; m >= l && !err; --m) reverse_step(st[m - l], m);
+            for (size_t i = 1; i < st.size(); ++i) free.push_back(st[i]);
+            return;
+        }
         const int64_t m = l + checkpoint_split(r - l, (int)free.size());
         double* sm = free.back();
         free.pop_back();

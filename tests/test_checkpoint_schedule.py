@@ -3,7 +3,9 @@
 ``csrc/mol_adjoint.cu`` (``Adj::rev``) reverses steps [l, r) from the state u_l in its slot
 with s spare slots: it advances ``checkpoint_split(r - l, s)`` steps (``csrc/mol_schedule.h``),
 stores that state in a spare slot, reverses the right part with one spare slot fewer and then
-the left part; with no spare slot it recomputes every state from l.  A probe compiled with g++
+the left part; with no spare slot it recomputes every state from l, and when every state of
+[l, r) has a slot it stores them in one forward walk (r - l - 1 steps, what the split gives
+there: one step per level).  A probe compiled with g++
 against mol_schedule.h counts the forward steps of that recursion; they must equal the minimum
 over all splits (a dynamic program here, for small cases) and Griewank's closed form
 r n - C(c + r, r - 1) for the configurations' 64-snapshot adjoints.
